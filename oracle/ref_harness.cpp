@@ -1,0 +1,239 @@
+// Reference harness -- TEST INFRASTRUCTURE ONLY (the checker, never shipped).
+//
+// Compiles matt-42/cuimg's own CPU tracker
+// `tracker<tracking_strategies::bc2s_fast_gradient_cpu>`
+// (cuimg/tracking2/tracker.hpp, cuimg/tracking2/tracking_strategies.hpp) unchanged,
+// from the reference sources where they lie, with the self-written compat
+// shim in oracle/shim (Boost / Eigen stand-ins), and exposes it through a
+// small C ABI so the Python tests can drive it with ctypes and read every
+// intermediate stage back.  Built by oracle/Makefile into oracle/_ref/.
+//
+// Build flags mirror the reference's CPU configuration: -DNO_CUDA -DNDEBUG,
+// no WITH_OPENCV (so bc2s_feature<cpu>::update takes the integer binomial
+// blur branch, cuimg/tracking2/bc2s_feature.hpp:248-251), OpenMP enabled but
+// run with one thread (the reference's parallel matcher and merge are racy,
+// so the single-threaded order is the deterministic semantics).
+//
+// Uninitialised memory: the reference allocates images with `new char[]`
+// (cuimg/cpu/host_image2d.hpp:97) and never writes the outer ring of the
+// binomial blur outputs (cuimg/cpu/gaussian_blur.h:17,30).  This harness
+// replaces the global allocation operators with zero-filling ones, which
+// pins those never-written pixels to 0.  The CUDA path reproduces exactly
+// that.
+
+#include <cassert>
+#include <cstdlib>
+#include <cstring>
+#include <cstdint>
+#include <new>
+
+void* operator new(std::size_t n) {
+  void* p = std::calloc(1, n ? n : 1);
+  if (!p) throw std::bad_alloc();
+  return p;
+}
+void* operator new[](std::size_t n) {
+  void* p = std::calloc(1, n ? n : 1);
+  if (!p) throw std::bad_alloc();
+  return p;
+}
+void operator delete(void* p) noexcept { std::free(p); }
+void operator delete[](void* p) noexcept { std::free(p); }
+void operator delete(void* p, std::size_t) noexcept { std::free(p); }
+void operator delete[](void* p, std::size_t) noexcept { std::free(p); }
+
+#include <cuimg/profiler.h>
+#include <cuimg/dsl/all.h>
+#include <cuimg/cpu/host_image2d.h>
+#include <cuimg/cpu/fill.h>
+#include <cuimg/tracking2/tracker.h>
+
+using namespace cuimg;
+
+typedef tracking_strategies::bc2s_fast_gradient_cpu S;
+typedef tracker<S> T;
+typedef S::super G;  // generic_strategy<...>
+
+// Legal access to the strategy's protected stage buffers: a pointer to a
+// protected base member may be formed inside a derived class.
+struct peek : public S {
+  static host_image2d<unsigned int> G::*contrast() { return &peek::contrast_; }
+  static host_image2d<gl8u> G::*mask() { return &peek::mask_; }
+  static host_image2d<i_float2> G::*flow() { return &peek::flow_; }
+  static host_image2d<unsigned int> G::*mscount() { return &peek::multiscale_count_; }
+  static host_image2d<std::pair<int, i_int2> > G::*stats() { return &peek::flow_stats_; }
+  static int G::*frame() { return &peek::frame_cpt_; }
+};
+
+struct ref_ctx {
+  T* tr;
+  int nscales;
+  obox2d dom;
+};
+
+// Copy rows [-b, nrows+b) x cols [-b, ncols+b) of an image into `out`.
+template <typename V, typename O>
+static void dump(const host_image2d<V>& img, int b, O* out) {
+  int nr = img.nrows(), nc = img.ncols();
+  size_t k = 0;
+  for (int r = -b; r < nr + b; r++)
+    for (int cc = -b; cc < nc + b; cc++)
+      out[k++] = (O)img(r, cc).x;
+}
+
+extern "C" {
+
+void* ref_create(int rows, int cols, int nscales, int threshold,
+                 int detector_frequency, int filtering_frequency) {
+  ref_ctx* c = new ref_ctx;
+  c->dom = obox2d(rows, cols);
+  c->nscales = nscales;
+  c->tr = new T(c->dom, nscales);
+  c->tr->strategy().set_detector_frequency(detector_frequency);
+  c->tr->strategy().set_filtering_frequency(filtering_frequency);
+  for (int s = 0; s < nscales; s++)
+    c->tr->scale(s).strategy().detector().set_n(9).set_fast_threshold(threshold);
+  return c;
+}
+
+void ref_destroy(void* h) {
+  ref_ctx* c = (ref_ctx*)h;
+  delete c->tr;
+  delete c;
+}
+
+void ref_run(void* h, const uint8_t* frame) {
+  ref_ctx* c = (ref_ctx*)h;
+  host_image2d<gl8u> in(c->dom);
+  for (int r = 0; r < c->dom.nrows(); r++)
+    std::memcpy(&in(r, 0), frame + (size_t)r * c->dom.ncols(), c->dom.ncols());
+  c->tr->run(in);
+}
+
+void ref_dims(void* h, int scale, int* rows, int* cols) {
+  ref_ctx* c = (ref_ctx*)h;
+  const obox2d& d = c->tr->scale(scale).domain();
+  *rows = d.nrows();
+  *cols = d.ncols();
+}
+
+// Pyramid level (tracker input) with `b` border pixels.
+void ref_get_input(void* h, int scale, int b, uint8_t* out) {
+  ref_ctx* c = (ref_ctx*)h;
+  dump(c->tr->scale(scale).input(), b, out);
+}
+
+void ref_get_s1(void* h, int scale, int b, uint8_t* out) {
+  ref_ctx* c = (ref_ctx*)h;
+  dump(c->tr->scale(scale).strategy().feature().s1(), b, out);
+}
+
+void ref_get_s2(void* h, int scale, int b, uint8_t* out) {
+  ref_ctx* c = (ref_ctx*)h;
+  dump(c->tr->scale(scale).strategy().feature().s2(), b, out);
+}
+
+void ref_get_saliency(void* h, int scale, uint8_t* out) {
+  ref_ctx* c = (ref_ctx*)h;
+  dump(c->tr->scale(scale).strategy().detector().saliency(), 0, out);
+}
+
+void ref_get_contrast(void* h, int scale, uint32_t* out) {
+  ref_ctx* c = (ref_ctx*)h;
+  G& g = c->tr->scale(scale).strategy();
+  const host_image2d<unsigned int>& img = g.*peek::contrast();
+  for (int r = 0; r < img.nrows(); r++)
+    for (int cc = 0; cc < img.ncols(); cc++)
+      out[(size_t)r * img.ncols() + cc] = img(r, cc);
+}
+
+void ref_get_mask(void* h, int scale, uint8_t* out) {
+  ref_ctx* c = (ref_ctx*)h;
+  G& g = c->tr->scale(scale).strategy();
+  dump(g.*peek::mask(), 0, out);
+}
+
+// Flow-bin images: flow (float2), multiscale count, stats (count, last speed).
+void ref_bins(void* h, int scale, int* rows, int* cols) {
+  ref_ctx* c = (ref_ctx*)h;
+  G& g = c->tr->scale(scale).strategy();
+  *rows = (g.*peek::flow()).nrows();
+  *cols = (g.*peek::flow()).ncols();
+}
+
+void ref_get_bins(void* h, int scale, float* flow, uint32_t* count,
+                  int32_t* stat_n, int32_t* stat_speed) {
+  ref_ctx* c = (ref_ctx*)h;
+  G& g = c->tr->scale(scale).strategy();
+  const host_image2d<i_float2>& f = g.*peek::flow();
+  const host_image2d<unsigned int>& m = g.*peek::mscount();
+  const host_image2d<std::pair<int, i_int2> >& st = g.*peek::stats();
+  size_t k = 0;
+  for (int r = 0; r < f.nrows(); r++)
+    for (int cc = 0; cc < f.ncols(); cc++, k++) {
+      flow[2 * k] = f(r, cc).x;
+      flow[2 * k + 1] = f(r, cc).y;
+      count[k] = m(r, cc);
+      stat_n[k] = st(r, cc).first;
+      stat_speed[2 * k] = st(r, cc).second.x;
+      stat_speed[2 * k + 1] = st(r, cc).second.y;
+    }
+}
+
+int ref_frame_count(void* h, int scale) {
+  ref_ctx* c = (ref_ctx*)h;
+  G& g = c->tr->scale(scale).strategy();
+  return g.*peek::frame();
+}
+
+int ref_nparticles(void* h, int scale) {
+  ref_ctx* c = (ref_ctx*)h;
+  return c->tr->scale(scale).pset().size();
+}
+
+int ref_total_particles(void* h) {
+  ref_ctx* c = (ref_ctx*)h;
+  return c->tr->nparticles();
+}
+
+int ref_compact_has_run(void* h, int scale) {
+  ref_ctx* c = (ref_ctx*)h;
+  return c->tr->scale(scale).pset().compact_has_run();
+}
+
+// Particle state: speed (2 floats), pos (2 int16: row, col), age (uint16).
+// Features: 16 distances + 16 weights (uint8).  Matches: int32 per slot.
+void ref_get_particles(void* h, int scale, float* speed, int16_t* pos,
+                       uint16_t* age, uint8_t* feat, int32_t* matches,
+                       int* nmatches) {
+  ref_ctx* c = (ref_ctx*)h;
+  auto& ps = c->tr->scale(scale).pset();
+  const auto& P = ps.dense_particles();
+  const auto& F = ps.features();
+  for (size_t i = 0; i < P.size(); i++) {
+    speed[2 * i] = P[i].speed.x;
+    speed[2 * i + 1] = P[i].speed.y;
+    pos[2 * i] = P[i].pos.x;
+    pos[2 * i + 1] = P[i].pos.y;
+    age[i] = P[i].age;
+    for (int j = 0; j < 16; j++) {
+      feat[32 * i + j] = F[i].distances[j];
+      feat[32 * i + 16 + j] = F[i].weights[j];
+    }
+  }
+  const auto& M = ps.matches();
+  *nmatches = (int)M.size();
+  if (matches)
+    for (size_t i = 0; i < M.size(); i++) matches[i] = (int32_t)M[i];
+}
+
+// Sparse index image over the domain (uint32, 0xFFFFFFFF = empty).
+void ref_get_sparse(void* h, int scale, uint32_t* out) {
+  ref_ctx* c = (ref_ctx*)h;
+  const auto& sp = c->tr->scale(scale).pset().sparse_particles();
+  for (int r = 0; r < sp.nrows(); r++)
+    for (int cc = 0; cc < sp.ncols(); cc++)
+      out[(size_t)r * sp.ncols() + cc] = sp(r, cc);
+}
+
+}  // extern "C"
