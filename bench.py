@@ -1,0 +1,369 @@
+"""Benchmark: cuimg semi-dense tracker at 1920x1080 on GB300.
+
+Workload (one "step" = one frame of every stream): B independent 1920x1080
+uint8 gray video streams from the seeded generator, 4 scales, FAST threshold
+20, detector every 10 frames, filtering every frame (~100k live particles per
+stream), advanced by one launch per stage replayed as a CUDA graph.
+
+Prints one JSON line:
+  value      tracked frames/s over all streams (batched), frames resident in HBM
+  e2e        same metric through the C ABI from pinned host frames: H2D copy of
+             every frame and a D2H read of every stream's particle counts inside
+             the timed region
+  plain      frames/s of the single-stream (B = 1) path, and the speed-up
+  roofline   the dominant kernel's algorithmic bytes / its CUDA-event time
+  cpu_baseline  the oracle port (C restatement of the reference CPU tracker)
+             on the host cores, bounded sample
+`--impl reference` times that CPU implementation alone on the same workload.
+"""
+import argparse
+import concurrent.futures as cf
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+ROWS, COLS, NSCALES = 1080, 1920, 4
+DET_FREQ, FILT_FREQ, THRESHOLD = 10, 1, 20
+METRIC = "tracked_frames_per_s_1080p"
+UNIT = "frames/s"
+PER_PARTICLE_BYTES = 84  # state read/write, template read/write, sparse index
+
+
+def level_pixels():
+    return [(ROWS >> l) * (COLS >> l) for l in range(NSCALES)]
+
+
+def frame_bytes_model(live_particles):
+    """Algorithmic HBM bytes of one tracked frame (one stream)."""
+    P = level_pixels()
+    Pt = sum(P)
+    return P[0] + sum(P[1:]) + 2 * Pt + Pt + 2 * Pt + Pt / 8 + PER_PARTICLE_BYTES * live_particles
+
+
+def kernel_bytes_model(name, live_particles, nstreams):
+    P = level_pixels()
+    Pt = sum(P)
+    per = {
+        "k_blur": 3 * Pt,
+        "k_match": PER_PARTICLE_BYTES * live_particles,
+        "k_pyramid": P[0] + sum(P[1:]),
+        "k_detect": Pt + Pt / 4 + Pt / 9,
+    }.get(name)
+    return None if per is None else per * nstreams
+
+
+def gen_streams(nstreams, nframes, seed0=1000):
+    from cuimg_gb300 import synth
+
+    def one(i):
+        return synth.frames(seed0 + i, ROWS, COLS, nframes)
+
+    with cf.ThreadPoolExecutor(max_workers=min(16, os.cpu_count() or 4)) as ex:
+        return list(ex.map(one, range(nstreams)))
+
+
+class ClockSampler:
+    FIELDS = "clocks.sm,clocks.max.sm,clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown," \
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap"
+
+    def __init__(self, device):
+        self.device = device
+        self.samples = []
+        self._stop = threading.Event()
+        self._t = threading.Thread(target=self._run, daemon=True)
+
+    def _run(self):
+        while not self._stop.is_set():
+            try:
+                out = subprocess.run(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.FIELDS,
+                                      "--format=csv,noheader,nounits"], capture_output=True, text=True, timeout=5)
+                parts = [p.strip() for p in out.stdout.strip().split(",")]
+                if len(parts) == 6:
+                    self.samples.append(parts)
+            except Exception:
+                pass
+            self._stop.wait(0.2)
+
+    def __enter__(self):
+        self._t.start()
+        return self
+
+    def __exit__(self, *a):
+        self._stop.set()
+        self._t.join(timeout=10)
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for s in self.samples for k in range(4) if s[2 + k].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.samples)}
+
+
+def run_cpu_port(frames, steps, warmup, threads=None):
+    """Times the oracle port (C restatement of the reference CPU tracker)."""
+    if threads:
+        os.environ["OMP_NUM_THREADS"] = str(threads)
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    subprocess.check_call(["make", "-s", "-C", os.path.join(ROOT, "oracle")])
+    from oracle_lib import tracker_oracle
+    o = tracker_oracle(ROWS, COLS, NSCALES, THRESHOLD, DET_FREQ, FILT_FREQ)
+    for t in range(warmup):
+        o.run(frames[t % len(frames)])
+    t0 = time.perf_counter()
+    for t in range(steps):
+        o.run(frames[(warmup + t) % len(frames)])
+    dt = time.perf_counter() - t0
+    n = sum(o.nparticles(s) for s in range(NSCALES))
+    o.destroy()
+    return steps / dt, dt, n
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+        backend = os.environ.get("BENCH_BACKEND", "nccl")
+        dist.init_process_group(backend=backend)
+        pg = dist
+    return world, rank, local, pg
+
+
+def bench_reference(args):
+    world, rank, local, pg = dist_setup()
+    if rank != 0:
+        return
+    frames = gen_streams(1, min(args.warmup + args.steps, 40))[0]
+    threads = os.cpu_count() or 1
+    fps, dt, n = run_cpu_port(frames, args.steps, args.warmup, threads=threads)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": round(fps, 3), "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1000 * dt / args.steps, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8", "data": "synthetic",
+        "config": {"workload": "1920x1080 gray, 4 scales, FAST th 20, detector every 10 frames, filter every frame; "
+                               "1 stream, one frame per step", "streams": 1, "live_particles": n},
+        "cpu_baseline": {"value": round(fps, 3), "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": "%d frames of one 1080p stream after %d warm-up frames" % (args.steps, args.warmup)},
+        "e2e": {"value": round(fps, 3), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def bench_ours(args):
+    import numpy as np
+    import torch
+
+    from cuimg_gb300 import BatchTracker
+    from cuimg_gb300._native import check, cuda_lib
+
+    world, rank, local, pg = dist_setup()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    lib = cuda_lib()
+    B = args.streams
+    nfr = args.warmup + args.steps
+    frames = gen_streams(B, nfr, seed0=1000 + rank * B)
+    cfg = [dict(rows=ROWS, cols=COLS, nscales=NSCALES, detector_threshold=THRESHOLD, detector_frequency=DET_FREQ,
+                filtering_frequency=FILT_FREQ) for _ in range(B)]
+
+    def make(nstreams):
+        bt = BatchTracker(cfg[:nstreams], device=local, graphs=True)
+        bt._ensure()
+        return bt
+
+    dev_frames = [torch.from_numpy(f).to(dev) for f in frames]  # resident in HBM
+    torch.cuda.synchronize()
+
+    def timed_resident(bt, nstreams, steps, warmup, offset=0):
+        stream = torch.cuda.ExternalStream(bt.cuda_stream(), device=dev)
+        ptrs = (ctypes.c_void_p * nstreams)()
+        pitches = (ctypes.c_int64 * nstreams)(*([COLS] * nstreams))
+
+        def step(t):
+            for s in range(nstreams):
+                ptrs[s] = dev_frames[s][t % nfr].data_ptr()
+            check(lib.gbt_run(bt._ctx, ptrs, pitches, 1), bt._ctx)
+
+        for t in range(warmup):
+            step(offset + t)
+        bt.sync()
+        if pg:
+            pg.barrier()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for t in range(steps):
+            step(offset + warmup + t)
+        e1.record(stream)
+        e1.synchronize()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        if pg:
+            tt = torch.tensor([ms], device=dev)
+            pg.all_reduce(tt, op=pg.ReduceOp.MAX)
+            ms = float(tt.item())
+        return ms
+
+    # Batched, resident.
+    bt = make(B)
+    with ClockSampler(local) as clk:
+        ms = timed_resident(bt, B, args.steps, args.warmup)
+    clocks = clk.summary()
+    value = B * world * args.steps / (ms / 1000.0)
+    live = []
+    for s in range(B):
+        p = [bt._particles(s, l) for l in range(NSCALES)]
+        live.append(sum(int((q["age"] > 0).sum()) for q in p))
+    live_mean = float(np.mean(live))
+    kernels_per_frame = bt.kernels_per_frame()
+    bt.close()
+
+    # Plain single stream, resident.
+    bt1 = make(1)
+    ms1 = timed_resident(bt1, 1, args.steps, args.warmup)
+    plain = args.steps / (ms1 / 1000.0)
+    bt1.close()
+
+    # Per-kernel device time (eager, CUDA events on the context stream).
+    btp = BatchTracker(cfg, device=local, graphs=False)
+    btp._ensure()
+    nprof = max(args.steps, DET_FREQ)
+    for t in range(args.warmup):
+        btp.run([frames[s][t % nfr] for s in range(B)])
+    lib.gbt_profile_enable(btp._ctx, 1)
+    ptrs = (ctypes.c_void_p * B)()
+    pitches = (ctypes.c_int64 * B)(*([COLS] * B))
+    for t in range(nprof):
+        for s in range(B):
+            ptrs[s] = dev_frames[s][(args.warmup + t) % nfr].data_ptr()
+        check(lib.gbt_run(btp._ctx, ptrs, pitches, 1), btp._ctx)
+    btp.sync()
+    prof = {}
+    nameb = ctypes.create_string_buffer(64)
+    tot = ctypes.c_double()
+    cnt = ctypes.c_int32()
+    k = 0
+    while True:
+        nent = lib.gbt_profile_read(btp._ctx, k, nameb, 64, ctypes.byref(tot), ctypes.byref(cnt))
+        if k >= nent:
+            break
+        prof[nameb.value.decode()] = (tot.value, cnt.value)
+        k += 1
+    btp.close()
+    total_ms = sum(v[0] for v in prof.values())
+    shares = {n: round(v[0] / total_ms, 4) for n, v in sorted(prof.items(), key=lambda kv: -kv[1][0])}
+    modeled = [(n, v) for n, v in prof.items() if kernel_bytes_model(n, live_mean, B) is not None]
+    dom, (dom_ms, dom_launches) = max(modeled, key=lambda kv: kv[1][0])
+    dom_avg_s = dom_ms / dom_launches / 1000.0
+    dom_bytes = kernel_bytes_model(dom, live_mean, B)
+    peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
+        os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}
+    peak = peaks.get("hbm_gbs", 6800.0)
+    achieved = dom_bytes / dom_avg_s / 1e9
+    frame_bytes = frame_bytes_model(live_mean) * B
+    frame_gbs = frame_bytes * args.steps / (ms / 1000.0) / 1e9
+
+    # End to end through the C ABI: pinned host frames, H2D + D2H inside.
+    bte = make(B)
+    host = [torch.from_numpy(f).pin_memory() for f in frames]
+    hptrs = (ctypes.c_void_p * B)()
+    hpitch = (ctypes.c_int64 * B)(*([COLS] * B))
+    nunits = B * NSCALES
+    counts = np.zeros(nunits, np.int32)
+
+    def estep(t):
+        for s in range(B):
+            hptrs[s] = host[s][t % nfr].data_ptr()
+        check(lib.gbt_run(bte._ctx, hptrs, hpitch, 0), bte._ctx)
+        check(lib.gbt_read_counts(bte._ctx, counts.ctypes.data, nunits), bte._ctx)
+
+    for t in range(args.warmup):
+        estep(t)
+    if pg:
+        pg.barrier()
+    t0 = time.perf_counter()
+    for t in range(args.steps):
+        estep(args.warmup + t)
+    e2e_s = time.perf_counter() - t0
+    if pg:
+        tt = torch.tensor([e2e_s], device=dev)
+        pg.all_reduce(tt, op=pg.ReduceOp.MAX)
+        e2e_s = float(tt.item())
+    e2e = B * world * args.steps / e2e_s
+    bte.close()
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        threads = os.cpu_count() or 1
+        nsample = args.cpu_frames
+        fps_cpu, dt_cpu, _ = run_cpu_port(frames[0], nsample, 2, threads=threads)
+        cpu = {"value": round(fps_cpu, 3), "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": "%d frames of one 1080p stream (%.1f s), OpenMP over pixels/particles" % (nsample, dt_cpu)}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": round(value, 2), "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 4), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "u8", "data": "synthetic",
+            "config": {"workload": "%d streams x 1920x1080 gray, 4 scales, FAST th 20, detector every 10 frames, "
+                                   "filter every frame, CUDA-graph replay" % B,
+                       "streams_per_gpu": B, "live_particles_per_stream": round(live_mean),
+                       "l2": "working set per step > L2 (inputs larger than L2)",
+                       "parallelism": "replicas only (independent streams per GPU)"},
+            "plain": {"value": round(plain, 2), "unit": UNIT, "streams": 1, "ms_per_frame": round(ms1 / args.steps, 4),
+                      "batched_speedup": round(value / world / plain, 2)},
+            "mpix_per_s": round(value * ROWS * COLS / 1e6, 1),
+            "frame_roofline": {"achieved": round(frame_gbs, 1), "peak": peak, "unit": "GB/s",
+                               "frac": round(frame_gbs / peak, 4),
+                               "bytes_per_frame_model": round(frame_bytes / B)},
+            "roofline": {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                         "frac": round(achieved / peak, 4), "traffic": None,
+                         "avg_launch_ms": round(dom_avg_s * 1000, 5), "peak_source": "measured (MEASURED_PEAKS.json)"},
+            "kernel_time_shares": shares,
+            "gpu_launches": kernels_per_frame * args.steps,
+            "kernels_per_step": kernels_per_frame,
+            "clocks": clocks,
+            "e2e": {"value": round(e2e, 2), "unit": UNIT, "h2d_bytes_per_step": B * ROWS * COLS,
+                    "d2h_bytes_per_step": 4 * nunits},
+            "cpu_baseline": cpu,
+        }
+        print(json.dumps(line), flush=True)
+    if pg:
+        pg.barrier()
+        pg.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=30)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--streams", type=int, default=16)
+    ap.add_argument("--cpu-frames", type=int, default=40)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        bench_reference(args)
+    else:
+        bench_ours(args)
+
+
+if __name__ == "__main__":
+    main()

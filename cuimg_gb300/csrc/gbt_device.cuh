@@ -1,0 +1,144 @@
+// Device-side data layout and helpers shared by the tracker kernels.
+//
+// The tracker state of one (stream, scale) pair -- a "unit" -- lives in HBM as:
+//   level image   uint8, H x W, pitch ipitch (multiple of 64 B), no border:
+//                 the reference's clamp-filled border (cuimg/border.h:128-137)
+//                 is reproduced by clamping coordinates on read;
+//   s1, s2        uint8 BC2S blurs with a zero border of RB rows / CB columns
+//                 (the reference's never-written outer ring and clamp-filled
+//                 border are all zero, cuimg/cpu/gaussian_blur.h:9-47);
+//   occ, pmask    one 64-bit word per 8x8-pixel bin, bit (r&7)*8 + (c&7):
+//                 "a particle moved here this frame" and the detector's
+//                 particle mask (tracking_strategies.hpp:202-225);
+//   idx           64-bit per pixel: (stamp << 32) | particle index, the
+//                 reference's sparse index image (particle_container.h:172)
+//                 without per-frame clearing -- an entry is current when its
+//                 stamp belongs to the current frame;
+//   bins          per 8x8 bin: stats count / last speed, flow, multiscale count;
+//   particles     structure of arrays, double-buffered for compaction:
+//                 pos (short2 row,col), speed (short2; integral on this path),
+//                 age (uint16), feature (16 bytes).
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace gbt {
+
+constexpr int RB = 8;    // rows of zero border around s1/s2
+constexpr int CB = 16;   // columns of zero border around s1/s2
+constexpr int CHUNK = 1024;  // particle slots per compaction chunk
+
+struct Unit {
+  int H, W;
+  int stream, scale, nscales;
+  int upper;        // unit index of scale + 1 of the same stream, -1 at the top
+  int threshold, nfast, k, det_freq, filt_freq, with_merge;
+  // images
+  uint8_t* img;
+  int ipitch;
+  uint8_t* s1;
+  uint8_t* s2;
+  int fpitch;
+  // bins
+  int BH, BW;
+  unsigned long long* occ;
+  unsigned long long* pmask;
+  unsigned long long* idx;
+  int* st_n;
+  int2* st_sp;
+  float2* flow;
+  unsigned* msc;
+  // particles
+  short2* pos[2];
+  short2* spd[2];
+  unsigned short* age[2];
+  uint4* feat[2];
+  int* matches;
+  int cap;
+  int max_chunks;
+  int* chunk_cnt;     // max_chunks survivor counts, then offsets
+  // detector
+  int TH, TW;
+  uint8_t* tilecode;  // TH * TW
+  int birth_chunks;   // ceil(3 * TH * TW / CHUNK)
+  int* birth_cnt;     // birth_chunks counts, then offsets
+  // merge
+  int* act_cnt;       // max_chunks active counts, then offsets
+  uint8_t* cmask;     // cap candidate direction masks
+  int4* act_list;     // cap entries: (i, pos packed, ncand, first cand) + cand store
+  int* act_cand;      // cap * 8 candidate indices
+};
+
+// Mutable per-unit counters, kept on the device so that captured graphs replay.
+struct UState {
+  int n;         // particle slots in the current buffer
+  int cur;       // current particle buffer (0/1)
+  int nmatches;  // slots before the last compaction
+  int compact;   // did this frame compact
+  int n_old;     // slots before compaction (scratch)
+  int S;         // survivors (scratch)
+  int B;         // births (scratch)
+  int A;         // merge actives (scratch)
+};
+
+struct Frame {
+  int f;         // frames completed so far (the frame being processed)
+  int err;       // error bits
+};
+
+constexpr int ERR_CAPACITY = 1;
+constexpr int ERR_MERGE_OVERFLOW = 2;
+
+// c8_h in raster order (cuimg/neighb2d_data.h:80-85), (row, col).
+__constant__ int8_t c_c8[8][2] = {{-1, 1}, {0, 1}, {1, 1}, {-1, 0}, {1, 0}, {-1, -1}, {0, -1}, {1, -1}};
+// c8_it_h (cuimg/neighb2d_data.h:162-180).
+__constant__ int8_t c_c8it[9][2] = {{6, 3}, {0, 3}, {0, 5}, {2, 5}, {2, 7}, {4, 7}, {4, 1}, {6, 1}, {0, 0}};
+// circle_r3_h (cuimg/neighb2d_data.h:184-189).
+__constant__ int8_t c_ring[16][2] = {{-3, 0}, {-3, 1}, {-2, 2}, {-1, 3}, {0, 3},   {1, 3},   {2, 2},   {3, 1},
+                                     {3, 0},  {3, -1}, {2, -2}, {1, -3}, {0, -3}, {-1, -3}, {-2, -2}, {-3, -1}};
+
+__device__ __forceinline__ int clampi(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }
+
+// Level image read with the reference's clamp-to-edge border semantics.
+__device__ __forceinline__ int img_at(const Unit& u, int r, int c) {
+  r = clampi(r, 0, u.H - 1);
+  c = clampi(c, 0, u.W - 1);
+  return u.img[(size_t)r * u.ipitch + c];
+}
+
+__device__ __forceinline__ const uint8_t* fptr(const uint8_t* base, int pitch, int r, int c) {
+  return base + (size_t)(r + RB) * pitch + (c + CB);
+}
+
+__device__ __forceinline__ bool in_dom(const Unit& u, int r, int c) {
+  return r >= 0 && r < u.H && c >= 0 && c < u.W;
+}
+
+__device__ __forceinline__ size_t bin_word(const Unit& u, int r, int c) {
+  return (size_t)(r >> 3) * u.BW + (c >> 3);
+}
+__device__ __forceinline__ unsigned long long bin_bit(int r, int c) {
+  return 1ull << (((r & 7) << 3) | (c & 7));
+}
+
+// Index-map stamps: frame f writes 2(f+1) during matching and 2(f+1)+1 for
+// compaction, so that atomicMax resolves "last writer = highest index" within a
+// phase and a later phase always wins; zero-initialised memory is never current.
+__device__ __forceinline__ unsigned stamp_match(int f) { return 2u * (unsigned)(f + 1); }
+__device__ __forceinline__ unsigned stamp_compact(int f) { return 2u * (unsigned)(f + 1) + 1u; }
+__device__ __forceinline__ bool idx_current(unsigned long long e, int f) {
+  return (unsigned)(e >> 33) == (unsigned)(f + 1);
+}
+
+// Unit lookup in a prefix table (first entry 0, nunits + 1 entries).
+__device__ __forceinline__ int find_unit(const int* prefix, int nunits, int t) {
+  int lo = 0, hi = nunits - 1;
+  while (lo < hi) {
+    int mid = (lo + hi + 1) >> 1;
+    if (prefix[mid] <= t) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
+}  // namespace gbt

@@ -1,0 +1,731 @@
+// Host side of the GB300 tracker: context, HBM layout, per-frame launch
+// sequence (optionally replayed from CUDA graphs) and the C ABI declared in
+// include/cuimg_gb300.h.
+//
+// One gbt_run advances every stream of the context by one frame, the batched
+// equivalent of calling tracker<F>::run(frame) (cuimg/tracking2/tracker.hpp:72-91)
+// on each stream: pyramid, then for all scales at once the BC2S blurs,
+// matcher, flow statistics, detector/births/compaction on detector frames, and
+// filter/merge on filtering frames.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "cuimg_gb300.h"
+#include "tracker_kernels.cuh"
+
+using namespace gbt;
+
+namespace {
+
+inline int round_up(int v, int m) { return (v + m - 1) / m * m; }
+
+struct StreamInfo {
+  gbt_config cfg;
+  int unit0;
+  uint8_t* pinned;  // staging buffer for pageable host frames
+  size_t pinned_bytes;
+};
+
+}  // namespace
+
+struct gbt_ctx {
+  int device = 0;
+  int nsm = 0;
+  cudaStream_t stream = nullptr;
+  std::vector<StreamInfo> streams;
+  std::vector<Unit> units;
+  Unit* d_units = nullptr;
+  UState* d_state = nullptr;
+  Frame* d_frame = nullptr;
+  int host_frame = 0;
+  // static work tables (device)
+  int* d_stream_unit0 = nullptr;
+  int* d_pyr_prefix[2] = {nullptr, nullptr};
+  int pyr_tiles[2] = {0, 0};
+  int* d_blur_prefix = nullptr;
+  int blur_tiles = 0;
+  int* d_bin_prefix = nullptr;
+  int nbins = 0;
+  int* d_det_prefix = nullptr;
+  int det_blocks = 0;
+  int* d_btable = nullptr;
+  // dynamic chunk tables
+  int* d_pre = nullptr;
+  int* d_post = nullptr;
+  // bulk buffers cleared per frame
+  void* occ_all = nullptr;
+  size_t occ_bytes = 0;
+  void* pmask_all = nullptr;
+  size_t pmask_bytes = 0;
+  std::vector<void*> allocs;
+  // graphs, keyed by (any detector unit, any filtering unit)
+  bool use_graphs = false;
+  cudaGraphExec_t graph[4] = {nullptr, nullptr, nullptr, nullptr};
+  int launches_per_frame = 0;
+  std::string err;
+  // scratch for stage dumps
+  void* dump_buf = nullptr;
+  size_t dump_bytes = 0;
+  // per-kernel event timing (eager launches only)
+  bool profiling = false;
+  struct Prof {
+    std::string name;
+    double ms = 0;
+    int launches = 0;
+  };
+  std::vector<Prof> prof;
+  std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> pending;
+  std::vector<cudaEvent_t> event_pool;
+  size_t event_next = 0;
+};
+
+static int set_err(gbt_ctx* c, int code, const char* fmt, ...) {
+  if (c) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    c->err = buf;
+  }
+  return code;
+}
+
+#define CK(call)                                                                                 \
+  do {                                                                                           \
+    cudaError_t e_ = (call);                                                                     \
+    if (e_ != cudaSuccess)                                                                       \
+      return set_err(ctx, GBT_E_CUDA, "%s failed: %s (%s:%d)", #call, cudaGetErrorString(e_), \
+                     __FILE__, __LINE__);                                                        \
+  } while (0)
+
+static int dalloc(gbt_ctx* ctx, void** p, size_t bytes, bool zero) {
+  if (bytes == 0) bytes = 16;
+  cudaError_t e = cudaMalloc(p, bytes);
+  if (e != cudaSuccess) return set_err(ctx, GBT_E_OOM, "cudaMalloc(%zu) failed: %s", bytes, cudaGetErrorString(e));
+  ctx->allocs.push_back(*p);
+  if (zero) CK(cudaMemset(*p, 0, bytes));
+  return GBT_OK;
+}
+
+template <typename T>
+static int dalloc_t(gbt_ctx* ctx, T** p, size_t n, bool zero = true) {
+  return dalloc(ctx, (void**)p, n * sizeof(T), zero);
+}
+
+static int upload_table(gbt_ctx* ctx, int** d, const std::vector<int>& h) {
+  int r = dalloc_t(ctx, d, h.size(), false);
+  if (r) return r;
+  CK(cudaMemcpy(*d, h.data(), h.size() * sizeof(int), cudaMemcpyHostToDevice));
+  return GBT_OK;
+}
+
+extern "C" void gbt_config_default(gbt_config* cfg, int32_t rows, int32_t cols, int32_t nscales) {
+  cfg->rows = rows;
+  cfg->cols = cols;
+  cfg->nscales = nscales;
+  cfg->detector_threshold = 20;
+  cfg->detector_n = 9;
+  cfg->detector_frequency = 1;   // generic_strategy defaults (tracking_strategies.hpp:45-48)
+  cfg->filtering_frequency = 1;
+  cfg->k = 300;
+  cfg->with_merge = 1;
+}
+
+extern "C" int gbt_sizes_ok(int32_t rows, int32_t cols, int32_t nscales) {
+  if (nscales < 1 || nscales > 9 || rows > 32767 || cols > 32767) return 0;
+  int H = rows, W = cols;
+  for (int s = 0; s < nscales; s++) {
+    if (H < 16 || W < 16) return 0;
+    if (s + 1 < nscales) {
+      int bh = (H + 7) / 8, bw = (W + 7) / 8, ubh = (H / 2 + 7) / 8, ubw = (W / 2 + 7) / 8;
+      if ((bh - 1) / 2 >= ubh || (bw - 1) / 2 >= ubw) return 0;
+    }
+    H /= 2;
+    W /= 2;
+  }
+  return 1;
+}
+
+static void free_ctx(gbt_ctx* ctx) {
+  if (!ctx) return;
+  if (ctx->device >= 0) cudaSetDevice(ctx->device);
+  for (auto e : ctx->event_pool) cudaEventDestroy(e);
+  for (auto& g : ctx->graph)
+    if (g) cudaGraphExecDestroy(g);
+  for (void* p : ctx->allocs) cudaFree(p);
+  for (auto& s : ctx->streams)
+    if (s.pinned) cudaFreeHost(s.pinned);
+  if (ctx->stream) cudaStreamDestroy(ctx->stream);
+  delete ctx;
+}
+
+static int build(gbt_ctx* ctx, const gbt_config* cfgs, int nstreams) {
+  CK(cudaSetDevice(ctx->device));
+  CK(cudaDeviceGetAttribute(&ctx->nsm, cudaDevAttrMultiProcessorCount, ctx->device));
+  CK(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
+  // Units: streams in order, scales 0..L-1 of each stream contiguous.
+  size_t occ_words = 0;
+  for (int s = 0; s < nstreams; s++) {
+    StreamInfo si{};
+    si.cfg = cfgs[s];
+    si.unit0 = (int)ctx->units.size();
+    const gbt_config& c = cfgs[s];
+    int H = c.rows, W = c.cols;
+    for (int l = 0; l < c.nscales; l++) {
+      Unit u{};
+      u.H = H;
+      u.W = W;
+      u.stream = s;
+      u.scale = l;
+      u.nscales = c.nscales;
+      u.upper = l + 1 < c.nscales ? si.unit0 + l + 1 : -1;
+      u.threshold = c.detector_threshold;
+      u.nfast = c.detector_n;
+      u.k = c.k;
+      u.det_freq = c.detector_frequency;
+      u.filt_freq = c.filtering_frequency;
+      u.with_merge = c.with_merge;
+      u.BH = (H + 7) / 8;
+      u.BW = (W + 7) / 8;
+      u.TH = H / 3;
+      u.TW = W / 3;
+      occ_words += (size_t)u.BH * u.BW;
+      ctx->units.push_back(u);
+      H /= 2;
+      W /= 2;
+    }
+    ctx->streams.push_back(si);
+  }
+  const int nunits = (int)ctx->units.size();
+  ctx->occ_bytes = occ_words * 8;
+  ctx->pmask_bytes = occ_words * 8;
+  int r;
+  if ((r = dalloc(ctx, &ctx->occ_all, ctx->occ_bytes, true))) return r;
+  if ((r = dalloc(ctx, &ctx->pmask_all, ctx->pmask_bytes, true))) return r;
+  size_t woff = 0;
+  for (auto& u : ctx->units) {
+    size_t nb = (size_t)u.BH * u.BW;
+    u.occ = (unsigned long long*)ctx->occ_all + woff;
+    u.pmask = (unsigned long long*)ctx->pmask_all + woff;
+    woff += nb;
+    u.ipitch = round_up(u.W, 64);
+    if ((r = dalloc(ctx, (void**)&u.img, (size_t)u.ipitch * u.H, true))) return r;
+    u.fpitch = round_up(u.W + 2 * CB, 64);
+    if ((r = dalloc(ctx, (void**)&u.s1, (size_t)u.fpitch * (u.H + 2 * RB), true))) return r;
+    if ((r = dalloc(ctx, (void**)&u.s2, (size_t)u.fpitch * (u.H + 2 * RB), true))) return r;
+    if ((r = dalloc_t(ctx, &u.idx, (size_t)u.H * u.W))) return r;
+    if ((r = dalloc_t(ctx, &u.st_n, nb))) return r;
+    if ((r = dalloc_t(ctx, &u.st_sp, nb))) return r;
+    if ((r = dalloc_t(ctx, &u.flow, nb))) return r;
+    if ((r = dalloc_t(ctx, &u.msc, nb))) return r;
+    u.cap = u.H * u.W / 6 + 4096;
+    u.cap = round_up(u.cap, CHUNK);
+    u.max_chunks = u.cap / CHUNK;
+    for (int b = 0; b < 2; b++) {
+      if ((r = dalloc_t(ctx, &u.pos[b], u.cap))) return r;
+      if ((r = dalloc_t(ctx, &u.spd[b], u.cap))) return r;
+      if ((r = dalloc_t(ctx, &u.age[b], u.cap))) return r;
+      if ((r = dalloc_t(ctx, &u.feat[b], u.cap))) return r;
+    }
+    if ((r = dalloc_t(ctx, &u.matches, (size_t)u.cap + (size_t)u.TH * u.TW))) return r;
+    if ((r = dalloc_t(ctx, &u.chunk_cnt, u.max_chunks))) return r;
+    if ((r = dalloc_t(ctx, &u.tilecode, (size_t)u.TH * u.TW + 1))) return r;
+    u.birth_chunks = (3 * u.TH * u.TW + CHUNK - 1) / CHUNK;
+    if ((r = dalloc_t(ctx, &u.birth_cnt, u.birth_chunks + 1))) return r;
+    if ((r = dalloc_t(ctx, &u.act_cnt, u.max_chunks))) return r;
+    if ((r = dalloc_t(ctx, &u.cmask, u.cap))) return r;
+    if ((r = dalloc_t(ctx, &u.act_list, u.cap))) return r;
+    if ((r = dalloc_t(ctx, &u.act_cand, (size_t)u.cap * 8, false))) return r;
+  }
+  if ((r = dalloc_t(ctx, &ctx->d_units, nunits, false))) return r;
+  CK(cudaMemcpy(ctx->d_units, ctx->units.data(), nunits * sizeof(Unit), cudaMemcpyHostToDevice));
+  if ((r = dalloc_t(ctx, &ctx->d_state, nunits))) return r;
+  if ((r = dalloc_t(ctx, &ctx->d_frame, 1))) return r;
+  if ((r = dalloc_t(ctx, &ctx->d_pre, nunits + 1))) return r;
+  if ((r = dalloc_t(ctx, &ctx->d_post, nunits + 1))) return r;
+
+  // Static tables.
+  std::vector<int> su0, pyr0(1, 0), pyr1(1, 0);
+  for (auto& s : ctx->streams) {
+    su0.push_back(s.unit0);
+    const Unit& b0 = ctx->units[s.unit0];
+    pyr0.push_back(pyr0.back() + ((b0.H + PYR_TR - 1) / PYR_TR) * ((b0.W + PYR_TC - 1) / PYR_TC));
+    int t1 = 0;
+    if (s.cfg.nscales > 6) {
+      const Unit& b5 = ctx->units[s.unit0 + 5];
+      t1 = ((b5.H + PYR_TR - 1) / PYR_TR) * ((b5.W + PYR_TC - 1) / PYR_TC);
+    }
+    pyr1.push_back(pyr1.back() + t1);
+  }
+  ctx->pyr_tiles[0] = pyr0.back();
+  ctx->pyr_tiles[1] = pyr1.back();
+  std::vector<int> blur(1, 0), bins(1, 0), det(1, 0), bt(1, 0);
+  for (auto& u : ctx->units) {
+    blur.push_back(blur.back() + ((u.H + BL_TR - 1) / BL_TR) * ((u.W + BL_TC - 1) / BL_TC));
+    bins.push_back(bins.back() + u.BH * u.BW);
+    det.push_back(det.back() + ((u.TH + DT_R - 1) / DT_R) * ((u.TW + DT_C - 1) / DT_C));
+    bt.push_back(bt.back() + u.birth_chunks);
+  }
+  ctx->blur_tiles = blur.back();
+  ctx->nbins = bins.back();
+  ctx->det_blocks = det.back();
+  if ((r = upload_table(ctx, &ctx->d_stream_unit0, su0))) return r;
+  if ((r = upload_table(ctx, &ctx->d_pyr_prefix[0], pyr0))) return r;
+  if ((r = upload_table(ctx, &ctx->d_pyr_prefix[1], pyr1))) return r;
+  if ((r = upload_table(ctx, &ctx->d_blur_prefix, blur))) return r;
+  if ((r = upload_table(ctx, &ctx->d_bin_prefix, bins))) return r;
+  if ((r = upload_table(ctx, &ctx->d_det_prefix, det))) return r;
+  if ((r = upload_table(ctx, &ctx->d_btable, bt))) return r;
+  for (auto& s : ctx->streams) {
+    const Unit& u = ctx->units[s.unit0];
+    s.pinned_bytes = (size_t)u.H * u.W * 3;
+    CK(cudaMallocHost((void**)&s.pinned, s.pinned_bytes));
+  }
+  CK(cudaDeviceSynchronize());
+  return GBT_OK;
+}
+
+extern "C" int gbt_create(const gbt_config* cfgs, int32_t nstreams, int32_t device, gbt_ctx** out) {
+  if (!out) return GBT_E_INVALID;
+  *out = nullptr;
+  if (!cfgs || nstreams < 1) return GBT_E_INVALID;
+  for (int s = 0; s < nstreams; s++) {
+    const gbt_config& c = cfgs[s];
+    if (!gbt_sizes_ok(c.rows, c.cols, c.nscales) || c.detector_frequency < 1 || c.filtering_frequency < 1 ||
+        c.detector_n < 1 || c.detector_n > 16)
+      return GBT_E_INVALID;
+  }
+  gbt_ctx* ctx = new gbt_ctx;
+  ctx->device = device;
+  int r = build(ctx, cfgs, nstreams);
+  if (r) {
+    fprintf(stderr, "gbt_create: %s\n", ctx->err.c_str());
+    free_ctx(ctx);
+    return r;
+  }
+  *out = ctx;
+  return GBT_OK;
+}
+
+extern "C" int gbt_destroy(gbt_ctx* ctx) {
+  if (!ctx) return GBT_E_INVALID;
+  cudaSetDevice(ctx->device);
+  cudaStreamSynchronize(ctx->stream);
+  free_ctx(ctx);
+  return GBT_OK;
+}
+
+extern "C" int gbt_last_error(gbt_ctx* ctx, char* buf, size_t len) {
+  if (!ctx || !buf || !len) return GBT_E_INVALID;
+  snprintf(buf, len, "%s", ctx->err.c_str());
+  return GBT_OK;
+}
+
+extern "C" int gbt_stream(gbt_ctx* ctx, void** s) {
+  if (!ctx || !s) return GBT_E_INVALID;
+  *s = (void*)ctx->stream;
+  return GBT_OK;
+}
+
+extern "C" int gbt_input_slot(gbt_ctx* ctx, int32_t stream, uint8_t** dptr, int64_t* pitch) {
+  if (!ctx || stream < 0 || stream >= (int)ctx->streams.size()) return GBT_E_INVALID;
+  const Unit& u = ctx->units[ctx->streams[stream].unit0];
+  if (dptr) *dptr = u.img;
+  if (pitch) *pitch = u.ipitch;
+  return GBT_OK;
+}
+
+// Frame kind of the frame about to run.
+static void frame_kind(gbt_ctx* ctx, bool& any_det, bool& any_filt) {
+  any_det = any_filt = false;
+  for (auto& s : ctx->streams) {
+    if (ctx->host_frame % s.cfg.detector_frequency == 0) any_det = true;
+    if (ctx->host_frame % s.cfg.filtering_frequency == 0) any_filt = true;
+  }
+}
+
+static cudaEvent_t next_event(gbt_ctx* ctx) {
+  if (ctx->event_next == ctx->event_pool.size()) {
+    cudaEvent_t e;
+    cudaEventCreate(&e);
+    ctx->event_pool.push_back(e);
+  }
+  return ctx->event_pool[ctx->event_next++];
+}
+
+static int prof_slot(gbt_ctx* ctx, const char* name) {
+  for (size_t i = 0; i < ctx->prof.size(); i++)
+    if (ctx->prof[i].name == name) return (int)i;
+  gbt_ctx::Prof p;
+  p.name = name;
+  ctx->prof.push_back(p);
+  return (int)ctx->prof.size() - 1;
+}
+
+// Brackets one launch with events when profiling (never inside a capture).
+struct ProfScope {
+  gbt_ctx* ctx;
+  int slot = -1;
+  cudaEvent_t a = nullptr;
+  ProfScope(gbt_ctx* c, const char* name) : ctx(c) {
+    if (!ctx->profiling) return;
+    slot = prof_slot(ctx, name);
+    a = next_event(ctx);
+    cudaEventRecord(a, ctx->stream);
+  }
+  ~ProfScope() {
+    if (slot < 0) return;
+    cudaEvent_t b = next_event(ctx);
+    cudaEventRecord(b, ctx->stream);
+    ctx->pending.push_back({slot, {a, b}});
+  }
+};
+
+static void prof_collect(gbt_ctx* ctx) {
+  if (ctx->pending.empty()) return;
+  cudaStreamSynchronize(ctx->stream);
+  for (auto& p : ctx->pending) {
+    float ms = 0;
+    cudaEventElapsedTime(&ms, p.second.first, p.second.second);
+    ctx->prof[p.first].ms += ms;
+    ctx->prof[p.first].launches++;
+  }
+  ctx->pending.clear();
+  ctx->event_next = 0;
+}
+
+#define PROF(name) ProfScope prof_scope_##__LINE__(ctx, name)
+
+// Issues the kernels of one frame on the context stream.
+static int enqueue_frame(gbt_ctx* ctx, bool any_det, bool any_filt) {
+  const int nunits = (int)ctx->units.size();
+  const int nstreams = (int)ctx->streams.size();
+  const int pgrid = std::max(1, ctx->nsm * 2);
+  cudaStream_t st = ctx->stream;
+  int n = 0;
+  CK(cudaMemsetAsync(ctx->occ_all, 0, ctx->occ_bytes, st));
+  n++;
+  { PROF("k_pyramid"); k_pyramid<<<ctx->pyr_tiles[0], 256, 0, st>>>(ctx->d_units, ctx->d_stream_unit0, ctx->d_pyr_prefix[0], nstreams, 0); }
+  n++;
+  if (ctx->pyr_tiles[1] > 0) {
+    PROF("k_pyramid5");
+    k_pyramid<<<ctx->pyr_tiles[1], 256, 0, st>>>(ctx->d_units, ctx->d_stream_unit0, ctx->d_pyr_prefix[1], nstreams, 5);
+    n++;
+  }
+  { PROF("k_blur"); k_blur<<<ctx->blur_tiles, 256, 0, st>>>(ctx->d_units, ctx->d_blur_prefix, nunits); }
+  { PROF("k_match"); k_match<<<pgrid, CHUNK, 0, st>>>(ctx->d_units, ctx->d_state, ctx->d_frame, ctx->d_pre, nunits); }
+  { PROF("k_stats"); k_stats<<<(ctx->nbins + 255) / 256, 256, 0, st>>>(ctx->d_units, ctx->d_state, ctx->d_bin_prefix, nunits); }
+  n += 3;
+  if (any_det) {
+    CK(cudaMemsetAsync(ctx->pmask_all, 0, ctx->pmask_bytes, st));
+    { PROF("k_pmask"); k_pmask<<<pgrid, CHUNK, 0, st>>>(ctx->d_units, ctx->d_state, ctx->d_frame, ctx->d_pre, nunits); }
+    { PROF("k_detect"); k_detect<<<ctx->det_blocks, 256, 0, st>>>(ctx->d_units, ctx->d_frame, ctx->d_det_prefix, nunits); }
+    { PROF("k_det_count"); k_det_count<<<pgrid, CHUNK, 0, st>>>(ctx->d_units, ctx->d_state, ctx->d_frame, ctx->d_pre, ctx->d_btable, nunits); }
+    { PROF("k_unit_scan"); k_unit_scan<<<nunits, 1024, 0, st>>>(ctx->d_units, ctx->d_state, ctx->d_frame, 0); }
+    { PROF("k_det_scatter"); k_det_scatter<<<pgrid, CHUNK, 0, st>>>(ctx->d_units, ctx->d_state, ctx->d_frame, ctx->d_pre, ctx->d_btable,
+                                           nunits); }
+    { PROF("k_commit"); k_commit<<<1, 1024, 0, st>>>(ctx->d_units, ctx->d_state, ctx->d_frame, ctx->d_post, nunits); }
+    n += 7;
+  }
+  int* table = any_det ? ctx->d_post : ctx->d_pre;
+  if (any_filt) {
+    { PROF("k_filter"); k_filter<<<pgrid, CHUNK, 0, st>>>(ctx->d_units, ctx->d_state, ctx->d_frame, table, nunits); }
+    { PROF("k_merge_count"); k_merge_count<<<pgrid, CHUNK, 0, st>>>(ctx->d_units, ctx->d_state, ctx->d_frame, table, nunits); }
+    { PROF("k_unit_scan"); k_unit_scan<<<nunits, 1024, 0, st>>>(ctx->d_units, ctx->d_state, ctx->d_frame, 1); }
+    { PROF("k_merge_scatter"); k_merge_scatter<<<pgrid, CHUNK, 0, st>>>(ctx->d_units, ctx->d_state, ctx->d_frame, table, nunits); }
+    { PROF("k_merge_resolve"); k_merge_resolve<<<nunits, 256, 0, st>>>(ctx->d_units, ctx->d_state, ctx->d_frame); }
+    n += 5;
+  }
+  { PROF("k_tick"); k_tick<<<1, 1024, 0, st>>>(ctx->d_units, ctx->d_state, ctx->d_frame, ctx->d_pre, nunits); }
+  n++;
+  ctx->launches_per_frame = n;
+  CK(cudaGetLastError());
+  return GBT_OK;
+}
+
+static int run_frame(gbt_ctx* ctx) {
+  bool any_det, any_filt;
+  frame_kind(ctx, any_det, any_filt);
+  int key = (any_det ? 1 : 0) | (any_filt ? 2 : 0);
+  if (ctx->use_graphs) {
+    if (!ctx->graph[key]) {
+      cudaGraph_t g;
+      CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+      int r = enqueue_frame(ctx, any_det, any_filt);
+      cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
+      if (r) return r;
+      if (e != cudaSuccess) return set_err(ctx, GBT_E_CUDA, "graph capture failed: %s", cudaGetErrorString(e));
+      e = cudaGraphInstantiate(&ctx->graph[key], g, 0);
+      cudaGraphDestroy(g);
+      if (e != cudaSuccess) return set_err(ctx, GBT_E_CUDA, "graph instantiate failed: %s", cudaGetErrorString(e));
+    }
+    CK(cudaGraphLaunch(ctx->graph[key], ctx->stream));
+  } else {
+    int r = enqueue_frame(ctx, any_det, any_filt);
+    if (r) return r;
+    prof_collect(ctx);
+  }
+  ctx->host_frame++;
+  return GBT_OK;
+}
+
+extern "C" int gbt_use_graphs(gbt_ctx* ctx, int32_t enable) {
+  if (!ctx) return GBT_E_INVALID;
+  ctx->use_graphs = enable != 0;
+  return GBT_OK;
+}
+
+extern "C" int gbt_run_resident(gbt_ctx* ctx) {
+  if (!ctx) return GBT_E_INVALID;
+  CK(cudaSetDevice(ctx->device));
+  return run_frame(ctx);
+}
+
+extern "C" int gbt_run(gbt_ctx* ctx, const uint8_t* const* frames, const int64_t* pitches, int32_t location) {
+  if (!ctx || !frames) return GBT_E_INVALID;
+  CK(cudaSetDevice(ctx->device));
+  for (size_t s = 0; s < ctx->streams.size(); s++) {
+    StreamInfo& si = ctx->streams[s];
+    const Unit& u = ctx->units[si.unit0];
+    const uint8_t* src = frames[s];
+    if (!src) return set_err(ctx, GBT_E_INVALID, "frame %zu is NULL", s);
+    if (location == GBT_FRAMES_DEVICE) {
+      int64_t p = pitches ? pitches[s] : u.W;
+      if (p < u.W) return set_err(ctx, GBT_E_INVALID, "pitch %lld < cols %d", (long long)p, u.W);
+      CK(cudaMemcpy2DAsync(u.img, u.ipitch, src, p, u.W, u.H, cudaMemcpyDeviceToDevice, ctx->stream));
+    } else if (location == GBT_FRAMES_HOST) {
+      int64_t p = pitches ? pitches[s] : u.W;
+      if (p < u.W) return set_err(ctx, GBT_E_INVALID, "pitch %lld < cols %d", (long long)p, u.W);
+      cudaPointerAttributes at;
+      bool pinned = cudaPointerGetAttributes(&at, src) == cudaSuccess && at.type == cudaMemoryTypeHost;
+      cudaGetLastError();
+      if (pinned) {
+        CK(cudaMemcpy2DAsync(u.img, u.ipitch, src, p, u.W, u.H, cudaMemcpyHostToDevice, ctx->stream));
+      } else {
+        // The staging buffer may still feed the previous frame's copy.
+        CK(cudaStreamSynchronize(ctx->stream));
+        for (int r = 0; r < u.H; r++) memcpy(si.pinned + (size_t)r * u.W, src + (size_t)r * p, u.W);
+        CK(cudaMemcpy2DAsync(u.img, u.ipitch, si.pinned, u.W, u.W, u.H, cudaMemcpyHostToDevice, ctx->stream));
+      }
+    } else if (location == GBT_FRAMES_HOST_RGB) {
+      int64_t p = pitches ? pitches[s] : (int64_t)u.W * 3;
+      if (p < (int64_t)u.W * 3) return set_err(ctx, GBT_E_INVALID, "pitch too small for RGB");
+      CK(cudaStreamSynchronize(ctx->stream));
+      for (int r = 0; r < u.H; r++) {
+        const uint8_t* row = src + (size_t)r * p;
+        uint8_t* d = si.pinned + (size_t)r * u.W;
+        for (int c = 0; c < u.W; c++) d[c] = row[3 * c];  // get_x: channel 0 (dsl/get_comp.h:105)
+      }
+      CK(cudaMemcpy2DAsync(u.img, u.ipitch, si.pinned, u.W, u.W, u.H, cudaMemcpyHostToDevice, ctx->stream));
+    } else {
+      return set_err(ctx, GBT_E_INVALID, "bad frame location %d", location);
+    }
+  }
+  return run_frame(ctx);
+}
+
+extern "C" int gbt_sync(gbt_ctx* ctx) {
+  if (!ctx) return GBT_E_INVALID;
+  CK(cudaSetDevice(ctx->device));
+  CK(cudaStreamSynchronize(ctx->stream));
+  Frame f;
+  CK(cudaMemcpy(&f, ctx->d_frame, sizeof f, cudaMemcpyDeviceToHost));
+  if (f.err & ERR_CAPACITY) return set_err(ctx, GBT_E_CAPACITY, "particle capacity exceeded");
+  return GBT_OK;
+}
+
+extern "C" int gbt_kernels_per_frame(gbt_ctx* ctx, int32_t* n) {
+  if (!ctx || !n) return GBT_E_INVALID;
+  *n = ctx->launches_per_frame;
+  return GBT_OK;
+}
+
+static int unit_of(gbt_ctx* ctx, int stream, int scale) {
+  if (!ctx || stream < 0 || stream >= (int)ctx->streams.size()) return -1;
+  if (scale < 0 || scale >= ctx->streams[stream].cfg.nscales) return -1;
+  return ctx->streams[stream].unit0 + scale;
+}
+
+static int read_state(gbt_ctx* ctx, int ui, UState* s) {
+  CK(cudaStreamSynchronize(ctx->stream));
+  CK(cudaMemcpy(s, ctx->d_state + ui, sizeof(UState), cudaMemcpyDeviceToHost));
+  return GBT_OK;
+}
+
+extern "C" int gbt_nparticles(gbt_ctx* ctx, int32_t stream, int32_t scale, int32_t* n) {
+  int ui = unit_of(ctx, stream, scale);
+  if (ui < 0 || !n) return GBT_E_INVALID;
+  CK(cudaSetDevice(ctx->device));
+  UState s;
+  int r = read_state(ctx, ui, &s);
+  if (r) return r;
+  *n = s.n;
+  return GBT_OK;
+}
+
+extern "C" int gbt_read_counts(gbt_ctx* ctx, int32_t* counts, int32_t n) {
+  if (!ctx || !counts || n < (int)ctx->units.size()) return GBT_E_INVALID;
+  CK(cudaSetDevice(ctx->device));
+  std::vector<UState> st(ctx->units.size());
+  CK(cudaMemcpyAsync(st.data(), ctx->d_state, st.size() * sizeof(UState), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  for (size_t i = 0; i < st.size(); i++) counts[i] = st[i].n;
+  return GBT_OK;
+}
+
+extern "C" int gbt_frame_count(gbt_ctx* ctx, int32_t stream, int32_t scale, int32_t* n) {
+  if (unit_of(ctx, stream, scale) < 0 || !n) return GBT_E_INVALID;
+  *n = ctx->host_frame;
+  return GBT_OK;
+}
+
+extern "C" int gbt_get_particles(gbt_ctx* ctx, int32_t stream, int32_t scale, float* speed, int16_t* pos,
+                                 uint16_t* age, uint8_t* features, int32_t* matches, int32_t* nmatches,
+                                 int32_t* compact_has_run) {
+  int ui = unit_of(ctx, stream, scale);
+  if (ui < 0) return GBT_E_INVALID;
+  CK(cudaSetDevice(ctx->device));
+  UState s;
+  int r = read_state(ctx, ui, &s);
+  if (r) return r;
+  const Unit& u = ctx->units[ui];
+  const int n = s.n, b = s.cur;
+  if (speed) {
+    std::vector<short2> v(n);
+    if (n) CK(cudaMemcpy(v.data(), u.spd[b], n * sizeof(short2), cudaMemcpyDeviceToHost));
+    for (int i = 0; i < n; i++) {
+      speed[2 * i] = v[i].x;
+      speed[2 * i + 1] = v[i].y;
+    }
+  }
+  if (pos && n) CK(cudaMemcpy(pos, u.pos[b], n * sizeof(short2), cudaMemcpyDeviceToHost));
+  if (age && n) CK(cudaMemcpy(age, u.age[b], n * sizeof(uint16_t), cudaMemcpyDeviceToHost));
+  if (features && n) CK(cudaMemcpy(features, u.feat[b], n * 16, cudaMemcpyDeviceToHost));
+  if (nmatches) *nmatches = s.nmatches;
+  if (matches && s.nmatches)
+    CK(cudaMemcpy(matches, u.matches, (size_t)s.nmatches * 4, cudaMemcpyDeviceToHost));
+  if (compact_has_run) *compact_has_run = s.compact;
+  return GBT_OK;
+}
+
+extern "C" int gbt_bins(gbt_ctx* ctx, int32_t stream, int32_t scale, int32_t* rows, int32_t* cols) {
+  int ui = unit_of(ctx, stream, scale);
+  if (ui < 0) return GBT_E_INVALID;
+  if (rows) *rows = ctx->units[ui].BH;
+  if (cols) *cols = ctx->units[ui].BW;
+  return GBT_OK;
+}
+
+extern "C" int gbt_get_bins(gbt_ctx* ctx, int32_t stream, int32_t scale, float* flow, uint32_t* count,
+                            int32_t* stat_n, int32_t* stat_speed) {
+  int ui = unit_of(ctx, stream, scale);
+  if (ui < 0) return GBT_E_INVALID;
+  CK(cudaSetDevice(ctx->device));
+  CK(cudaStreamSynchronize(ctx->stream));
+  const Unit& u = ctx->units[ui];
+  size_t nb = (size_t)u.BH * u.BW;
+  if (flow) CK(cudaMemcpy(flow, u.flow, nb * 8, cudaMemcpyDeviceToHost));
+  if (count) CK(cudaMemcpy(count, u.msc, nb * 4, cudaMemcpyDeviceToHost));
+  if (stat_n) CK(cudaMemcpy(stat_n, u.st_n, nb * 4, cudaMemcpyDeviceToHost));
+  if (stat_speed) CK(cudaMemcpy(stat_speed, u.st_sp, nb * 8, cudaMemcpyDeviceToHost));
+  return GBT_OK;
+}
+
+// Stage images computed on demand from the resident state (checks only).
+namespace gbt {
+__global__ void k_dump(const Unit* __restrict__ units, const UState* __restrict__ st, const Frame* __restrict__ fr,
+                       int ui, int what, void* out) {
+  const Unit& u = units[ui];
+  const int total = u.H * u.W;
+  const int flast = fr->f - 1;
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < total; t += gridDim.x * blockDim.x) {
+    int r = t / u.W, c = t % u.W;
+    if (what == GBT_STAGE_CONTRAST) {
+      ((uint32_t*)out)[t] = (uint32_t)contrast_at(u, r, c);
+    } else if (what == GBT_STAGE_SPARSE) {
+      unsigned long long e = u.idx[t];
+      ((uint32_t*)out)[t] = idx_current(e, flast) ? (uint32_t)(e & 0xffffffffu) : 0xffffffffu;
+    } else {
+      bool masked = (u.pmask[bin_word(u, r, c)] & bin_bit(r, c)) != 0 || contrast_at(u, r, c) < 5;
+      if (what == GBT_STAGE_MASK) {
+        ((uint8_t*)out)[t] = masked ? 0 : 255;
+      } else {
+        uint8_t v = 0;
+        if (!masked) {
+          uint8_t win[7][7];
+          for (int a = 0; a < 7; a++)
+            for (int b = 0; b < 7; b++) win[a][b] = (uint8_t)img_at(u, r - 3 + a, c - 3 + b);
+          v = (uint8_t)fast_saliency(&win[3][3], 7, u.nfast, u.threshold);
+        }
+        ((uint8_t*)out)[t] = v;
+      }
+    }
+  }
+}
+}  // namespace gbt
+
+extern "C" int gbt_get_stage(gbt_ctx* ctx, int32_t stream, int32_t scale, int32_t stage, int32_t border, void* out) {
+  int ui = unit_of(ctx, stream, scale);
+  if (ui < 0 || !out || border < 0 || border > 6) return GBT_E_INVALID;
+  CK(cudaSetDevice(ctx->device));
+  CK(cudaStreamSynchronize(ctx->stream));
+  const Unit& u = ctx->units[ui];
+  const int H = u.H, W = u.W, b = border;
+  if (stage == GBT_STAGE_INPUT) {
+    std::vector<uint8_t> dom((size_t)H * W);
+    CK(cudaMemcpy2D(dom.data(), W, u.img, u.ipitch, W, H, cudaMemcpyDeviceToHost));
+    uint8_t* o = (uint8_t*)out;
+    size_t k = 0;
+    for (int r = -b; r < H + b; r++)
+      for (int c = -b; c < W + b; c++) {
+        int rr = std::min(std::max(r, 0), H - 1), cc = std::min(std::max(c, 0), W - 1);
+        o[k++] = dom[(size_t)rr * W + cc];
+      }
+    return GBT_OK;
+  }
+  if (stage == GBT_STAGE_S1 || stage == GBT_STAGE_S2) {
+    const uint8_t* base = (stage == GBT_STAGE_S1 ? u.s1 : u.s2) + (size_t)(RB - b) * u.fpitch + (CB - b);
+    CK(cudaMemcpy2D(out, W + 2 * b, base, u.fpitch, W + 2 * b, H + 2 * b, cudaMemcpyDeviceToHost));
+    return GBT_OK;
+  }
+  size_t bytes = (size_t)H * W * 4;
+  if (ctx->dump_bytes < bytes) {
+    void* p;
+    int r = dalloc(ctx, &p, bytes, false);
+    if (r) return r;
+    ctx->dump_buf = p;
+    ctx->dump_bytes = bytes;
+  }
+  if (stage != GBT_STAGE_CONTRAST && stage != GBT_STAGE_SALIENCY && stage != GBT_STAGE_MASK &&
+      stage != GBT_STAGE_SPARSE)
+    return GBT_E_INVALID;
+  k_dump<<<256, 256, 0, ctx->stream>>>(ctx->d_units, ctx->d_state, ctx->d_frame, ui, stage, ctx->dump_buf);
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(ctx->stream));
+  size_t es = (stage == GBT_STAGE_CONTRAST || stage == GBT_STAGE_SPARSE) ? 4 : 1;
+  CK(cudaMemcpy(out, ctx->dump_buf, (size_t)H * W * es, cudaMemcpyDeviceToHost));
+  return GBT_OK;
+}
+
+extern "C" int gbt_profile_enable(gbt_ctx* ctx, int32_t enable) {
+  if (!ctx) return GBT_E_INVALID;
+  ctx->profiling = enable != 0;
+  if (ctx->profiling) ctx->prof.clear();
+  return GBT_OK;
+}
+
+extern "C" int gbt_profile_read(gbt_ctx* ctx, int32_t i, char* name, size_t len, double* total_ms, int32_t* launches) {
+  if (!ctx) return -1;
+  if (i < 0 || i >= (int)ctx->prof.size()) return (int)ctx->prof.size();
+  if (name && len) snprintf(name, len, "%s", ctx->prof[i].name.c_str());
+  if (total_ms) *total_ms = ctx->prof[i].ms;
+  if (launches) *launches = ctx->prof[i].launches;
+  return (int)ctx->prof.size();
+}

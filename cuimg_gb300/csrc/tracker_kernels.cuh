@@ -1,0 +1,979 @@
+// Tracker kernels: one launch per stage processes every (stream, scale) unit.
+// Each kernel cites the reference functor whose semantics it reproduces.
+#pragma once
+#include "gbt_device.cuh"
+
+namespace gbt {
+
+// ---------------------------------------------------------------------------
+// Block-wide exclusive prefix of a 0/1 predicate (blockDim.x == 1024).
+__device__ __forceinline__ int block_prefix(bool pred, int* warp_tot, int& total) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  unsigned b = __ballot_sync(0xffffffffu, pred);
+  int local = __popc(b & ((1u << lane) - 1u));
+  if (lane == 0) warp_tot[wid] = __popc(b);
+  __syncthreads();
+  if (wid == 0) {
+    int v = warp_tot[lane];
+    int x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      int y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += y;
+    }
+    warp_tot[32 + lane] = x - v;  // exclusive
+    if (lane == 31) warp_tot[64] = x;
+  }
+  __syncthreads();
+  int r = warp_tot[32 + wid] + local;
+  total = warp_tot[64];
+  __syncthreads();
+  return r;
+}
+
+// ---------------------------------------------------------------------------
+// Pyramid: mipmap_kernel (cuimg/gpu/mipmap.h:24-49) applied level after level,
+// out(p) = (a + b + c + d) / 4 over the 2x2 block at 2p.  One CTA turns a
+// 32 x 128 tile of level `base` into up to five coarser levels held in shared
+// memory, so each frame is read from HBM once.
+constexpr int PYR_TR = 32, PYR_TC = 128;
+
+__global__ void __launch_bounds__(256) k_pyramid(const Unit* __restrict__ units,
+                                                 const int* __restrict__ stream_unit0,
+                                                 const int* __restrict__ tile_prefix, int nstreams, int base) {
+  __shared__ __align__(16) uint8_t sm[2][PYR_TR * PYR_TC];
+  const int t = blockIdx.x;
+  const int s = find_unit(tile_prefix, nstreams, t);
+  const int local = t - tile_prefix[s];
+  const int u0 = stream_unit0[s];
+  const Unit& B = units[u0 + base];
+  const int nlev = min(B.nscales - 1 - base, 5);
+  if (nlev <= 0) return;
+  const int tw = (B.W + PYR_TC - 1) / PYR_TC;
+  const int R0 = (local / tw) * PYR_TR, C0 = (local % tw) * PYR_TC;
+
+  // Load the level-`base` tile.
+  for (int v = threadIdx.x; v < PYR_TR * (PYR_TC / 16); v += blockDim.x) {
+    int r = v / (PYR_TC / 16), c16 = (v % (PYR_TC / 16)) * 16;
+    int gr = R0 + r, gc = C0 + c16;
+    uint8_t* d = &sm[0][r * PYR_TC + c16];
+    if (gr < B.H && gc + 16 <= B.W) {
+      *(uint4*)d = *(const uint4*)(B.img + (size_t)gr * B.ipitch + gc);
+    } else {
+      for (int j = 0; j < 16; j++) d[j] = (gr < B.H && gc + j < B.W) ? B.img[(size_t)gr * B.ipitch + gc + j] : 0;
+    }
+  }
+  __syncthreads();
+  int src = 0;
+  for (int l = 1; l <= nlev; l++) {
+    const Unit& O = units[u0 + base + l];
+    const int tr = PYR_TR >> l, tc = PYR_TC >> l;
+    const int r0 = R0 >> l, c0 = C0 >> l;
+    const uint8_t* S = sm[src];
+    uint8_t* D = sm[src ^ 1];
+    for (int v = threadIdx.x; v < tr * tc; v += blockDim.x) {
+      int r = v / tc, c = v % tc;
+      int a = S[(2 * r) * PYR_TC + 2 * c] + S[(2 * r) * PYR_TC + 2 * c + 1] + S[(2 * r + 1) * PYR_TC + 2 * c] +
+              S[(2 * r + 1) * PYR_TC + 2 * c + 1];
+      uint8_t o = (uint8_t)(a >> 2);
+      D[r * PYR_TC + c] = o;
+      if (r0 + r < O.H && c0 + c < O.W) O.img[(size_t)(r0 + r) * O.ipitch + c0 + c] = o;
+    }
+    __syncthreads();
+    src ^= 1;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// BC2S blurs: bc2s_feature<cpu>::update (tracking2/bc2s_feature.hpp:372-393)
+// = gaussian_blur_sigma1 twice (cuimg/cpu/gaussian_blur.h:9-47).  Row pass
+// t(r,c) = (2 x[c] + x[c-1] + x[c+1]) / 4 for c in [1, W-2]; column pass
+// s(r,c) = (2 t[r] + t[r-1] + t[r+1]) / 4 for r in [1, H-2]; every other
+// pixel (the ring and the border) is zero.  One CTA produces a 16 x 64 tile
+// of s1 and s2 from a 20 x 68 tile of the level, all in shared memory.
+constexpr int BL_TR = 16, BL_TC = 64;
+
+__global__ void __launch_bounds__(256) k_blur(const Unit* __restrict__ units, const int* __restrict__ tile_prefix,
+                                              int nunits) {
+  __shared__ uint8_t sin_[BL_TR + 4][BL_TC + 4];
+  __shared__ uint8_t st[BL_TR + 4][BL_TC + 2];
+  __shared__ uint8_t ss1[BL_TR + 2][BL_TC + 2];
+  __shared__ uint8_t st2[BL_TR + 2][BL_TC];
+  const int t = blockIdx.x;
+  const int ui = find_unit(tile_prefix, nunits, t);
+  const Unit& U = units[ui];
+  const int local = t - tile_prefix[ui];
+  const int tw = (U.W + BL_TC - 1) / BL_TC;
+  const int R0 = (local / tw) * BL_TR, C0 = (local % tw) * BL_TC;
+  const int H = U.H, W = U.W;
+
+  for (int v = threadIdx.x; v < (BL_TR + 4) * (BL_TC + 4); v += blockDim.x) {
+    int r = v / (BL_TC + 4), c = v % (BL_TC + 4);
+    int gr = R0 - 2 + r, gc = C0 - 2 + c;
+    sin_[r][c] = in_dom(U, gr, gc) ? U.img[(size_t)gr * U.ipitch + gc] : 0;
+  }
+  __syncthreads();
+  // t rows R0-2 .. R0+17, cols C0-1 .. C0+64
+  for (int v = threadIdx.x; v < (BL_TR + 4) * (BL_TC + 2); v += blockDim.x) {
+    int r = v / (BL_TC + 2), c = v % (BL_TC + 2);
+    int gr = R0 - 2 + r, gc = C0 - 1 + c;
+    int val = 0;
+    if (gr >= 0 && gr < H && gc >= 1 && gc <= W - 2) val = (2 * sin_[r][c + 1] + sin_[r][c] + sin_[r][c + 2]) >> 2;
+    st[r][c] = (uint8_t)val;
+  }
+  __syncthreads();
+  // s1 rows R0-1 .. R0+16, cols C0-1 .. C0+64
+  for (int v = threadIdx.x; v < (BL_TR + 2) * (BL_TC + 2); v += blockDim.x) {
+    int r = v / (BL_TC + 2), c = v % (BL_TC + 2);
+    int gr = R0 - 1 + r, gc = C0 - 1 + c;
+    int val = 0;
+    if (gr >= 1 && gr <= H - 2 && gc >= 0 && gc < W) val = (2 * st[r + 1][c] + st[r][c] + st[r + 2][c]) >> 2;
+    ss1[r][c] = (uint8_t)val;
+  }
+  __syncthreads();
+  // t2 rows R0-1 .. R0+16, cols C0 .. C0+63
+  for (int v = threadIdx.x; v < (BL_TR + 2) * BL_TC; v += blockDim.x) {
+    int r = v / BL_TC, c = v % BL_TC;
+    int gr = R0 - 1 + r, gc = C0 + c;
+    int val = 0;
+    if (gr >= 0 && gr < H && gc >= 1 && gc <= W - 2) val = (2 * ss1[r][c + 1] + ss1[r][c] + ss1[r][c + 2]) >> 2;
+    st2[r][c] = (uint8_t)val;
+  }
+  __syncthreads();
+  // write s1 and s2 over the tile's in-domain pixels (4 bytes per thread step)
+  for (int v = threadIdx.x; v < BL_TR * (BL_TC / 4); v += blockDim.x) {
+    int r = v / (BL_TC / 4), c4 = (v % (BL_TC / 4)) * 4;
+    int gr = R0 + r, gc = C0 + c4;
+    if (gr >= H) continue;
+    uint8_t a[4], b[4];
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+      a[j] = ss1[r + 1][c4 + j + 1];
+      int gcc = gc + j;
+      int val = 0;
+      if (gr >= 1 && gr <= H - 2 && gcc >= 0 && gcc < W) val = (2 * st2[r + 1][c4 + j] + st2[r][c4 + j] + st2[r + 2][c4 + j]) >> 2;
+      b[j] = (uint8_t)val;
+    }
+    uint8_t* p1 = (uint8_t*)fptr(U.s1, U.fpitch, gr, gc);
+    uint8_t* p2 = (uint8_t*)fptr(U.s2, U.fpitch, gr, gc);
+    if (gc + 4 <= W) {
+      *(uint32_t*)p1 = a[0] | (a[1] << 8) | (a[2] << 16) | ((uint32_t)a[3] << 24);
+      *(uint32_t*)p2 = b[0] | (b[1] << 8) | (b[2] << 16) | ((uint32_t)b[3] << 24);
+    } else {
+      for (int j = 0; j < 4 && gc + j < W; j++) {
+        p1[j] = a[j];
+        p2[j] = b[j];
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Feature access: bc2s_internals::distance / compute_feature
+// (tracking2/bc2s_feature.hpp:173-284).  Samples s1 at the even
+// circle_r3_h offsets and s2 at twice those; weights are the constant 255, so
+// the distance is the plain sum of absolute differences.
+struct Feat {
+  const uint8_t* s1;
+  const uint8_t* s2;
+  int o1[8], o2[8];
+  __device__ __forceinline__ void init(const Unit& u) {
+    s1 = fptr(u.s1, u.fpitch, 0, 0);
+    s2 = fptr(u.s2, u.fpitch, 0, 0);
+#pragma unroll
+    for (int i = 0; i < 8; i++) {
+      o1[i] = c_ring[2 * i][0] * u.fpitch + c_ring[2 * i][1];
+      o2[i] = 2 * c_ring[2 * i][0] * u.fpitch + 2 * c_ring[2 * i][1];
+    }
+  }
+  __device__ __forceinline__ uint4 at(int r, int c, int pitch) const {
+    const uint8_t* a = s1 + (ptrdiff_t)r * pitch + c;
+    const uint8_t* b = s2 + (ptrdiff_t)r * pitch + c;
+    uint4 f;
+    f.x = a[o1[0]] | (a[o1[1]] << 8) | (a[o1[2]] << 16) | ((uint32_t)a[o1[3]] << 24);
+    f.y = a[o1[4]] | (a[o1[5]] << 8) | (a[o1[6]] << 16) | ((uint32_t)a[o1[7]] << 24);
+    f.z = b[o2[0]] | (b[o2[1]] << 8) | (b[o2[2]] << 16) | ((uint32_t)b[o2[3]] << 24);
+    f.w = b[o2[4]] | (b[o2[5]] << 8) | (b[o2[6]] << 16) | ((uint32_t)b[o2[7]] << 24);
+    return f;
+  }
+  __device__ __forceinline__ int dist(const uint4& f, int r, int c, int pitch, bool with_s1) const {
+    const uint8_t* b = s2 + (ptrdiff_t)r * pitch + c;
+    uint32_t z = b[o2[0]] | (b[o2[1]] << 8) | (b[o2[2]] << 16) | ((uint32_t)b[o2[3]] << 24);
+    uint32_t w = b[o2[4]] | (b[o2[5]] << 8) | (b[o2[6]] << 16) | ((uint32_t)b[o2[7]] << 24);
+    int d = (int)(__vsadu4(z, f.z) + __vsadu4(w, f.w));
+    if (with_s1) {
+      const uint8_t* a = s1 + (ptrdiff_t)r * pitch + c;
+      uint32_t x = a[o1[0]] | (a[o1[1]] << 8) | (a[o1[2]] << 16) | ((uint32_t)a[o1[3]] << 24);
+      uint32_t y = a[o1[4]] | (a[o1[5]] << 8) | (a[o1[6]] << 16) | ((uint32_t)a[o1[7]] << 24);
+      d += (int)(__vsadu4(x, f.x) + __vsadu4(y, f.y));
+    }
+    return d;
+  }
+};
+
+// gradient_descent_match (tracking2/gradient_descent_matcher.hpp:9-76): greedy
+// 8-neighbour descent over c8_h with the c8_it_h partial sweeps; the first
+// distance is always the s1+s2 one.  (pr, pc) is inside the domain.
+__device__ __forceinline__ void gd_match(const Unit& u, const Feat& F, const uint4& f, int pr, int pc, bool with_s1,
+                                         int& dr, int& dc) {
+  int predr = pr, predc = pc, mr = pr, mc = pc;
+  int best = F.dist(f, pr, pc, u.fpitch, true);
+  int mi = 8;
+  for (int search = 0; search < 10; search++) {
+    int i = c_c8it[mi][0];
+    const int end = c_c8it[mi][1];
+    bool first = true;
+    while (first || i != end) {
+      first = false;
+      int nr = predr + c_c8[i][0], nc = predc + c_c8[i][1];
+      if (in_dom(u, nr, nc)) {
+        int d = F.dist(f, nr, nc, u.fpitch, with_s1);
+        if (d < best) {
+          mr = nr;
+          mc = nc;
+          mi = i;
+          best = d;
+        }
+      }
+      i = (i + 1) & 7;
+    }
+    if ((predr == mr && predc == mc) || !in_dom(u, mr, mc)) break;
+    predr = mr;
+    predc = mc;
+  }
+  dr = mr - pr;
+  dc = mc - pc;
+}
+
+// contrast_kernel (tracking_strategies.hpp:101-135), clamped level reads.
+__device__ __forceinline__ int contrast_at(const Unit& u, int r, int c) {
+  const int d = 2;
+  return abs(img_at(u, r, c + d) - img_at(u, r, c - d)) + abs(img_at(u, r - d, c) - img_at(u, r + d, c)) +
+         abs(img_at(u, r - d, c - d) - img_at(u, r + d, c + d)) + abs(img_at(u, r - d, c + d) - img_at(u, r + d, c - d));
+}
+
+// Chunk tables: table[u] = first global chunk of unit u, table[nunits] = total.
+struct ChunkCursor {
+  int unit, chunk;
+};
+__device__ __forceinline__ ChunkCursor chunk_of(const int* table, int nunits, int g) {
+  ChunkCursor cc;
+  cc.unit = find_unit(table, nunits, g);
+  cc.chunk = g - table[cc.unit];
+  return cc;
+}
+
+// ---------------------------------------------------------------------------
+// Matcher: match_particles_kernel (tracking_strategies.hpp:274-426) with
+// multiscale_prediction == motion_based_prediction (predictions.h:15-33),
+// two_step_gradient_descent_match (gradient_descent_matcher.hpp:118-124) and
+// kernel_particle_container::move (particle_container.hpp:422-466).  The
+// sparse-index write keeps the highest slot per pixel (atomicMax), i.e. the
+// single-threaded reference's last writer.
+__global__ void __launch_bounds__(CHUNK) k_match(const Unit* __restrict__ units, UState* __restrict__ st,
+                                                 const Frame* __restrict__ fr, const int* __restrict__ table,
+                                                 int nunits) {
+  const int f = fr->f;
+  const int total = table[nunits];
+  for (int g = blockIdx.x; g < total; g += gridDim.x) {
+    ChunkCursor cc = chunk_of(table, nunits, g);
+    const Unit& u = units[cc.unit];
+    const UState s = st[cc.unit];
+    const int i = cc.chunk * CHUNK + threadIdx.x;
+    if (i >= s.n) continue;
+    const int b = s.cur;
+    unsigned short age = u.age[b][i];
+    if (age == 0) continue;
+    short2 pos = u.pos[b][i];
+    short2 spd = u.spd[b][i];
+    int pr = (short)(pos.x + (age == 1 ? 0 : spd.x));
+    int pc = (short)(pos.y + (age == 1 ? 0 : spd.y));
+    if (!in_dom(u, pr, pc)) {
+      u.age[b][i] = 0;
+      continue;
+    }
+    Feat F;
+    F.init(u);
+    uint4 feat = u.feat[b][i];
+    int d1r, d1c, d2r, d2c;
+    gd_match(u, F, feat, pr, pc, false, d1r, d1c);
+    gd_match(u, F, feat, pr + d1r, pc + d1c, true, d2r, d2c);
+    const int dr = d1r + d2r, dc = d1c + d2c;
+    const int mr = (short)(pr + dr), mc = (short)(pc + dc);
+    bool accept = in_dom(u, mr, mc);
+    uint4 mf = make_uint4(0, 0, 0, 0);
+    if (accept) {
+      mf = F.at(mr, mc, u.fpitch);
+      // n_diff over the s2 entries (every weight is 255 > 150, so cpt = 8).
+      unsigned n_diff = 0;
+      const uint32_t a0 = feat.z, a1 = feat.w, c0 = mf.z, c1 = mf.w;
+#pragma unroll
+      for (int j = 0; j < 4; j++) {
+        int x = (a0 >> (8 * j)) & 255, y = (c0 >> (8 * j)) & 255;
+        if (abs(x - y) > u.k) n_diff++;
+        x = (a1 >> (8 * j)) & 255;
+        y = (c1 >> (8 * j)) & 255;
+        if (abs(x - y) > u.k) n_diff++;
+      }
+      accept = n_diff < 4u;
+    }
+    if (!accept || contrast_at(u, mr, mc) < 3) {
+      u.age[b][i] = 0;
+      continue;
+    }
+    const int sr = pr - pos.x + dr, sc = pc - pos.y + dc;
+    u.age[b][i] = (unsigned short)(age + 1);
+    u.spd[b][i] = make_short2((short)sr, (short)sc);
+    u.pos[b][i] = make_short2((short)mr, (short)mc);
+    if (sr != 0 || sc != 0) u.feat[b][i] = mf;
+    atomicOr(&u.occ[bin_word(u, mr, mc)], bin_bit(mr, mc));
+    atomicMax(&u.idx[(size_t)mr * u.W + mc], ((unsigned long long)stamp_match(f) << 32) | (unsigned)i);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Flow statistics and fusion for every 8x8 bin of every unit:
+// compute_flow_stats_kernel (tracking_strategies.hpp:525-574: count of
+// occupied pixels whose particle has age >= 1, and the speed of the last one
+// in raster order), then flow_fusion_kernel / flow_fusion_kernel_root
+// (:576-639).  The fused flow of a bin follows its chain of parent bins up to
+// the first scale with more than one particle (the root divides the speed by
+// the count), doubling per scale, so all scales are computed in one launch.
+__device__ __forceinline__ void bin_stats(const Unit& u, const UState& s, int br, int bc, int& n, int& sr, int& sc) {
+  unsigned long long w = u.occ[(size_t)br * u.BW + bc];
+  n = 0;
+  sr = 0;
+  sc = 0;
+  bool have_last = false;
+  while (w) {
+    int bit = 63 - __clzll((long long)w);
+    w &= ~(1ull << bit);
+    int r = br * 8 + (bit >> 3), c = bc * 8 + (bit & 7);
+    unsigned j = (unsigned)(u.idx[(size_t)r * u.W + c] & 0xffffffffu);
+    if (u.age[s.cur][j] >= 1) {
+      n++;
+      if (!have_last) {
+        short2 v = u.spd[s.cur][j];
+        sr = v.x;
+        sc = v.y;
+        have_last = true;
+      }
+    }
+  }
+}
+
+__global__ void __launch_bounds__(256) k_stats(const Unit* __restrict__ units, UState* __restrict__ st,
+                                               const int* __restrict__ bin_prefix, int nunits) {
+  if (blockIdx.x == 0)
+    for (int k = threadIdx.x; k < nunits; k += blockDim.x) st[k].compact = 0;
+  const int total = bin_prefix[nunits];
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= total) return;
+  const int ui = find_unit(bin_prefix, nunits, t);
+  const Unit& u = units[ui];
+  const int local = t - bin_prefix[ui];
+  const int br = local / u.BW, bc = local % u.BW;
+  int n, sr, sc;
+  bin_stats(u, st[ui], br, bc, n, sr, sc);
+  u.st_n[local] = n;
+  u.st_sp[local] = make_int2(sr, sc);
+  unsigned msc = (unsigned)n;
+  if (u.upper >= 0) {
+    int un, usr, usc;
+    bin_stats(units[u.upper], st[u.upper], br >> 1, bc >> 1, un, usr, usc);
+    msc += (unsigned)un;
+  }
+  u.msc[local] = msc;
+  // Fused flow.
+  float2 flow = make_float2(-500.f, -500.f);
+  int vi = ui, vbr = br, vbc = bc, vn = n, vsr = sr, vsc = sc;
+  float scale = 1.f;
+  while (true) {
+    const Unit& v = units[vi];
+    if (v.upper < 0) {
+      if (vn > 1) flow = make_float2((float)(vsr / vn) * scale, (float)(vsc / vn) * scale);
+      break;
+    }
+    if (vn > 1) {
+      flow = make_float2((float)vsr * scale, (float)vsc * scale);
+      break;
+    }
+    vi = v.upper;
+    vbr >>= 1;
+    vbc >>= 1;
+    scale *= 2.f;
+    bin_stats(units[vi], st[vi], vbr, vbc, vn, vsr, vsc);
+  }
+  u.flow[local] = flow;
+}
+
+// ---------------------------------------------------------------------------
+// Detector mask, part 1: particle_mask_kernel (tracking_strategies.hpp:201-225)
+// zeroes the mask at every particle slot's position and its 8 neighbours
+// (dead slots included).  Here those pixels get a bit in `pmask`.
+__device__ __forceinline__ bool det_frame(const Unit& u, int f) { return (f % u.det_freq) == 0; }
+__device__ __forceinline__ bool filt_frame(const Unit& u, int f) { return (f % u.filt_freq) == 0; }
+
+__global__ void __launch_bounds__(CHUNK) k_pmask(const Unit* __restrict__ units, const UState* __restrict__ st,
+                                                 const Frame* __restrict__ fr, const int* __restrict__ table,
+                                                 int nunits) {
+  const int f = fr->f;
+  const int total = table[nunits];
+  for (int g = blockIdx.x; g < total; g += gridDim.x) {
+    ChunkCursor cc = chunk_of(table, nunits, g);
+    const Unit& u = units[cc.unit];
+    if (!det_frame(u, f)) continue;
+    const UState s = st[cc.unit];
+    const int i = cc.chunk * CHUNK + threadIdx.x;
+    if (i >= s.n) continue;
+    short2 p = u.pos[s.cur][i];
+    for (int dr = -1; dr <= 1; dr++)
+      for (int dc = -1; dc <= 1; dc++) {
+        int r = p.x + dr, c = p.y + dc;
+        if (in_dom(u, r, c)) atomicOr(&u.pmask[bin_word(u, r, c)], bin_bit(r, c));
+      }
+  }
+}
+
+// fast::compute_saliency (tracking2/fast_detector.hpp:26-157) on a shared
+// memory tile: `P` points at the centre pixel, `ld` is the row stride.
+__device__ __forceinline__ int fast_saliency(const uint8_t* P, int ld, int n_, int th) {
+  unsigned max_n = 0, n = 0;
+  int status = 2;
+  const int vp = P[0];
+  unsigned sum_bright = 0, sum_dark = 0;
+#define RV(i) ((int)P[c_ring[i][0] * ld + c_ring[i][1]])
+  if (n_ >= 9) {
+    const int to_test[6] = {0, 4, 8, 12, 0, 4};
+    int equals = 0;
+#pragma unroll
+    for (int k = 0; k < 6; k++) {
+      int vn = RV(to_test[k]);
+      int sign = vn > vp;
+      int dist = abs(vn - vp);
+      if (dist > th) {
+        if (sign == status) {
+          n++;
+        } else {
+          if (n > max_n) max_n = n;
+          status = sign;
+          n = 1;
+        }
+      } else {
+        if (n > max_n) max_n = n;
+        status = 2;
+        equals++;
+        if (k < 4 && n_ >= 12 && equals >= 2) return 0;
+      }
+    }
+    if (n > max_n) max_n = n;
+    if (n_ >= 12 && max_n < 3) return 0;
+    else if (n_ >= 8 && max_n < 2) return 0;
+  }
+  n = 0;
+  status = 2;
+  max_n = 0;
+#pragma unroll
+  for (int i = 0; i < 16; i++) {
+    int vn = RV(i);
+    int sign = vn > vp;
+    int dist = abs(vn - vp);
+    if (dist > th) {
+      if (sign == status) {
+        n++;
+      } else {
+        if (n > max_n) max_n = n;
+        status = sign;
+        n = 1;
+      }
+      if (vn < vp) sum_dark += dist;
+      else sum_bright += dist;
+    } else {
+      if (n > max_n) max_n = n;
+      status = 2;
+    }
+  }
+  if (n != 16 && status != 2) {
+    for (int i = 0; i < 16; i++) {
+      int vn = RV(i);
+      int sign = vn > vp;
+      int dist = abs(vn - vp);
+      if (dist <= th || sign != status) break;
+      n++;
+    }
+  }
+#undef RV
+  if (n > max_n) max_n = n;
+  if (max_n < (unsigned)n_) return 0;
+  return (int)((sum_bright > sum_dark ? sum_bright : sum_dark) & 255u);  // stored as gl8u
+}
+
+// Detector mask value, saliency and contrast at a tile pixel.
+__device__ __forceinline__ int saliency_px(const Unit& u, const uint8_t* P, int ld, int r, int c) {
+  if (u.pmask[bin_word(u, r, c)] & bin_bit(r, c)) return 0;
+  const int d = 2;
+  int con = abs((int)P[d] - (int)P[-d]) + abs((int)P[-d * ld] - (int)P[d * ld]) +
+            abs((int)P[-d * ld - d] - (int)P[d * ld + d]) + abs((int)P[-d * ld + d] - (int)P[d * ld - d]);
+  if (con < 5) return 0;  // flow_mask_kernel (tracking_strategies.hpp:227-252)
+  return fast_saliency(P, ld, u.nfast, u.threshold);
+}
+
+// Saliency + 3x3 tile non-maximum selection: fast_detector::update and
+// new_particles(cpu) (tracking2/fast_detector.hpp:217-262,296-313) fused.  A
+// tile q owns pixels 3q + (1,1) + [0,2]^2; it is skipped when any of them holds
+// a particle, otherwise its first strict maximum (raster order) becomes a birth
+// if the saliency reaches the threshold and the point lies in the
+// domain - border(3).  Result per tile: dr * 3 + dc, or 0xFF.
+constexpr int DT_R = 8, DT_C = 32;  // tiles per CTA
+constexpr int DT_PR = DT_R * 3 + 6, DT_PC = DT_C * 3 + 6;
+
+__global__ void __launch_bounds__(256) k_detect(const Unit* __restrict__ units, const Frame* __restrict__ fr,
+                                                const int* __restrict__ blk_prefix, int nunits) {
+  __shared__ uint8_t tile[DT_PR][DT_PC];
+  const int f = fr->f;
+  const int t = blockIdx.x;
+  const int ui = find_unit(blk_prefix, nunits, t);
+  const Unit& u = units[ui];
+  if (!det_frame(u, f)) return;
+  const int local = t - blk_prefix[ui];
+  const int bw = (u.TW + DT_C - 1) / DT_C;
+  const int TR0 = (local / bw) * DT_R, TC0 = (local % bw) * DT_C;
+  const int pr0 = 3 * TR0 + 1 - 3, pc0 = 3 * TC0 + 1 - 3;
+  for (int v = threadIdx.x; v < DT_PR * DT_PC; v += blockDim.x) {
+    int r = v / DT_PC, c = v % DT_PC;
+    tile[r][c] = (uint8_t)img_at(u, pr0 + r, pc0 + c);
+  }
+  __syncthreads();
+  const int tr = TR0 + threadIdx.x / DT_C, tc = TC0 + threadIdx.x % DT_C;
+  if (tr >= u.TH || tc >= u.TW) return;
+  const int pr = 3 * tr + 1, pc = 3 * tc + 1;
+  uint8_t code = 0xFF;
+  bool occupied = false;
+  for (int r = 0; r < 3; r++)
+    for (int c = 0; c < 3; c++) {
+      int gr = pr + r, gc = pc + c;
+      if (in_dom(u, gr, gc) && (u.occ[bin_word(u, gr, gc)] & bin_bit(gr, gc))) occupied = true;
+    }
+  if (!occupied) {
+    const int lr = pr - pr0, lc = pc - pc0;
+    int vmax = saliency_px(u, &tile[lr][lc], DT_PC, pr, pc);
+    int mr = 0, mc = 0;
+    for (int r = 0; r < 3; r++)
+      for (int c = 0; c < 3; c++) {
+        if (r == 0 && c == 0) continue;
+        int gr = pr + r, gc = pc + c;
+        if (!in_dom(u, gr, gc)) continue;
+        int v = saliency_px(u, &tile[lr + r][lc + c], DT_PC, gr, gc);
+        if (vmax < v) {
+          vmax = v;
+          mr = r;
+          mc = c;
+        }
+      }
+    if (vmax >= u.threshold) {
+      int gr = pr + mr, gc = pc + mc;
+      if (gr >= 3 && gr <= u.H - 4 && gc >= 3 && gc <= u.W - 4) code = (uint8_t)(mr * 3 + mc);
+    }
+  }
+  u.tilecode[(size_t)tr * u.TW + tc] = code;
+}
+
+// Birth items are ordered (tile row, row inside the tile, tile column), which
+// is the raster order of the birth pixels (st_apply2d over
+// domain - border(3), fast_detector.hpp:256-260).
+__device__ __forceinline__ bool birth_item(const Unit& u, int v, int& r, int& c) {
+  const int per = u.TW;
+  int row3 = v / per, tc = v % per;
+  int tr = row3 / 3, dr = row3 % 3;
+  if (tr >= u.TH) return false;
+  uint8_t code = u.tilecode[(size_t)tr * u.TW + tc];
+  if (code == 0xFF || code / 3 != dr) return false;
+  r = 3 * tr + 1 + dr;
+  c = 3 * tc + 1 + code % 3;
+  return true;
+}
+
+// Counts per chunk: survivors (age != 0) over the pre-compaction slots of each
+// detector-frame unit, and births over its birth items.
+__global__ void __launch_bounds__(CHUNK) k_det_count(const Unit* __restrict__ units, const UState* __restrict__ st,
+                                                     const Frame* __restrict__ fr, const int* __restrict__ table,
+                                                     const int* __restrict__ btable, int nunits) {
+  __shared__ int wt[65];
+  const int f = fr->f;
+  const int ts = table[nunits], tb = btable[nunits];
+  for (int g = blockIdx.x; g < ts + tb; g += gridDim.x) {
+    bool births = g >= ts;
+    ChunkCursor cc = births ? chunk_of(btable, nunits, g - ts) : chunk_of(table, nunits, g);
+    const Unit& u = units[cc.unit];
+    if (!det_frame(u, f)) continue;  // uniform per block
+    const int i = cc.chunk * CHUNK + threadIdx.x;
+    bool pred;
+    if (births) {
+      int r, c;
+      pred = i < 3 * u.TH * u.TW && birth_item(u, i, r, c);
+    } else {
+      const UState s = st[cc.unit];
+      pred = i < s.n && u.age[s.cur][i] != 0;
+    }
+    int total;
+    block_prefix(pred, wt, total);
+    if (threadIdx.x == 0) (births ? u.birth_cnt : u.chunk_cnt)[cc.chunk] = total;
+  }
+}
+
+// Per-unit exclusive scans of chunk counts.  which: 0 = detector (survivors
+// and births), 1 = merge actives.
+__global__ void __launch_bounds__(1024) k_unit_scan(const Unit* __restrict__ units, UState* __restrict__ st,
+                                                    const Frame* __restrict__ fr, int which) {
+  __shared__ int wt[65];
+  const int ui = blockIdx.x;
+  const Unit& u = units[ui];
+  const int f = fr->f;
+  if (which == 0 ? !det_frame(u, f) : !filt_frame(u, f)) return;
+  UState& s = st[ui];
+  auto scan = [&](int* cnt, int nch) -> int {
+    int carry = 0;
+    for (int base = 0; base < nch; base += 1024) {
+      int k = base + threadIdx.x;
+      int v = k < nch ? cnt[k] : 0;
+      // inclusive block scan of v
+      const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+      int x = v;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        int y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+      }
+      if (lane == 31) wt[wid] = x;
+      __syncthreads();
+      if (wid == 0) {
+        int w = wt[lane];
+        int z = w;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          int y = __shfl_up_sync(0xffffffffu, z, o);
+          if (lane >= o) z += y;
+        }
+        wt[32 + lane] = z - w;
+        if (lane == 31) wt[64] = z;
+      }
+      __syncthreads();
+      int excl = carry + wt[32 + wid] + x - v;
+      if (k < nch) cnt[k] = excl;
+      carry += wt[64];
+      __syncthreads();
+    }
+    return carry;
+  };
+  if (which == 0) {
+    const int nch = (s.n + CHUNK - 1) / CHUNK;
+    int S = scan(u.chunk_cnt, nch);
+    int B = scan(u.birth_cnt, u.birth_chunks);
+    if (threadIdx.x == 0) {
+      s.n_old = s.n;
+      s.S = S;
+      s.B = B;
+    }
+  } else {
+    const int nch = (s.n + CHUNK - 1) / CHUNK;
+    int A = scan(u.act_cnt, nch);
+    if (threadIdx.x == 0) s.A = A;
+  }
+}
+
+// Stable compaction (particle_container::compact(cpu),
+// particle_container.hpp:215-252) and births (fast_detector.hpp:256-260 +
+// particle_container::add, :370-387): survivors keep their order, births follow
+// in raster order; matches[old] = new slot (-1 for dead slots).
+__global__ void __launch_bounds__(CHUNK) k_det_scatter(const Unit* __restrict__ units, const UState* __restrict__ st,
+                                                       Frame* __restrict__ fr, const int* __restrict__ table,
+                                                       const int* __restrict__ btable, int nunits) {
+  __shared__ int wt[65];
+  const int f = fr->f;
+  const int ts = table[nunits], tb = btable[nunits];
+  for (int g = blockIdx.x; g < ts + tb; g += gridDim.x) {
+    bool births = g >= ts;
+    ChunkCursor cc = births ? chunk_of(btable, nunits, g - ts) : chunk_of(table, nunits, g);
+    const Unit& u = units[cc.unit];
+    if (!det_frame(u, f)) continue;
+    const UState s = st[cc.unit];
+    const int i = cc.chunk * CHUNK + threadIdx.x;
+    const int ob = s.cur, nb = s.cur ^ 1;
+    const unsigned long long stamp = (unsigned long long)stamp_compact(f) << 32;
+    if (!births) {
+      bool alive = i < s.n_old && u.age[ob][i] != 0;
+      int total;
+      int o = u.chunk_cnt[cc.chunk] + block_prefix(alive, wt, total);
+      if (i < s.n_old) u.matches[i] = alive ? o : -1;
+      if (alive) {
+        short2 p = u.pos[ob][i];
+        u.pos[nb][o] = p;
+        u.spd[nb][o] = u.spd[ob][i];
+        u.age[nb][o] = u.age[ob][i];
+        u.feat[nb][o] = u.feat[ob][i];
+        atomicMax(&u.idx[(size_t)p.x * u.W + p.y], stamp | (unsigned)o);
+      }
+    } else {
+      int r = 0, c = 0;
+      bool born = i < 3 * u.TH * u.TW && birth_item(u, i, r, c);
+      int total;
+      int k = u.birth_cnt[cc.chunk] + block_prefix(born, wt, total);
+      if (born) {
+        int o = s.S + k;
+        if (o >= u.cap) {
+          atomicOr(&fr->err, ERR_CAPACITY);
+        } else {
+          Feat F;
+          F.init(u);
+          u.pos[nb][o] = make_short2((short)r, (short)c);
+          u.spd[nb][o] = make_short2(0, 0);
+          u.age[nb][o] = 1;
+          u.feat[nb][o] = F.at(r, c, u.fpitch);
+          u.matches[s.n_old + k] = o;
+          atomicMax(&u.idx[(size_t)r * u.W + c], stamp | (unsigned)o);
+        }
+      }
+    }
+  }
+}
+
+// Commits detector-frame counters and rebuilds a chunk table over the
+// current slot counts (one CTA).
+__device__ void build_table(const Unit* units, const UState* st, int nunits, int* table) {
+  __shared__ int wt[65];
+  int carry = 0;
+  for (int base = 0; base < nunits; base += blockDim.x) {
+    int k = base + threadIdx.x;
+    int v = k < nunits ? (st[k].n + CHUNK - 1) / CHUNK : 0;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    int x = v;
+    for (int o = 1; o < 32; o <<= 1) {
+      int y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += y;
+    }
+    if (lane == 31) wt[wid] = x;
+    __syncthreads();
+    if (wid == 0) {
+      int nw = blockDim.x / 32;
+      int w = lane < nw ? wt[lane] : 0;
+      int z = w;
+      for (int o = 1; o < 32; o <<= 1) {
+        int y = __shfl_up_sync(0xffffffffu, z, o);
+        if (lane >= o) z += y;
+      }
+      wt[32 + lane] = z - w;
+      if (lane == 31) wt[64] = z;
+    }
+    __syncthreads();
+    if (k < nunits) table[k] = carry + wt[32 + wid] + x - v;
+    carry += wt[64];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) table[nunits] = carry;
+}
+
+__global__ void __launch_bounds__(1024) k_commit(const Unit* __restrict__ units, UState* __restrict__ st,
+                                                 const Frame* __restrict__ fr, int* __restrict__ post_table,
+                                                 int nunits) {
+  const int f = fr->f;
+  for (int k = threadIdx.x; k < nunits; k += blockDim.x) {
+    const Unit& u = units[k];
+    if (!det_frame(u, f)) continue;
+    UState& s = st[k];
+    int n = s.S + s.B;
+    s.n = n < u.cap ? n : u.cap;
+    s.nmatches = s.n_old + s.B;
+    s.compact = 1;
+    s.cur ^= 1;
+  }
+  __syncthreads();
+  build_table(units, st, nunits, post_table);
+}
+
+// ---------------------------------------------------------------------------
+// filter_bad_particles_kernel (tracking_strategies.hpp:482-523).
+__global__ void __launch_bounds__(CHUNK) k_filter(const Unit* __restrict__ units, const UState* __restrict__ st,
+                                                  const Frame* __restrict__ fr, const int* __restrict__ table,
+                                                  int nunits) {
+  const int f = fr->f;
+  const int total = table[nunits];
+  for (int g = blockIdx.x; g < total; g += gridDim.x) {
+    ChunkCursor cc = chunk_of(table, nunits, g);
+    const Unit& u = units[cc.unit];
+    if (!filt_frame(u, f)) continue;
+    const UState s = st[cc.unit];
+    const int i = cc.chunk * CHUNK + threadIdx.x;
+    if (i >= s.n) continue;
+    const int b = s.cur;
+    const unsigned short age = u.age[b][i];
+    const short2 p = u.pos[b][i];
+    const int br = p.x / 8, bc = p.y / 8;
+    const size_t w = (size_t)br * u.BW + bc;
+    const unsigned m = u.msc[w];
+    if (age > 2 && m > 0) {
+      short2 v = u.spd[b][i];
+      float2 fl = u.flow[w];
+      float dx = __fsub_rn((float)v.x, fl.x), dy = __fsub_rn((float)v.y, fl.y);
+      float nrm = __fsqrt_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)));
+      if (nrm > 10.f) {
+        u.age[b][i] = 0;
+        continue;
+      }
+    }
+    bool alone = true;
+    for (int k = 0; k < 8; k++) {
+      int nr = br + c_c8[k][0], nc = bc + c_c8[k][1];
+      if (nr >= 0 && nr < u.BH && nc >= 0 && nc < u.BW && u.msc[(size_t)nr * u.BW + nc] != 0) alone = false;
+    }
+    if (alone && m == 1) u.age[b][i] = 0;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// merge_trajectories (tracking2/merge_trajectories.h:10-35) over the slots in
+// index order.  Kills only go from a particle to an older neighbour, and only
+// particles with at least one qualifying neighbour ("actives", a few hundred
+// per frame) can kill.  Step 1 (parallel): the qualifying c8 directions of each
+// live particle, using pre-merge ages.  Step 2: ordered list of actives.
+// Step 3: one warp per unit replays the sequential order; groups of 32 actives
+// whose positions are more than 2 pixels apart cannot interact and are
+// resolved in parallel, other groups lane by lane.
+__device__ __forceinline__ unsigned merge_dirs(const Unit& u, const UState& s, int f, int i, short2 p,
+                                               unsigned short age, int* cand, int& ncand) {
+  unsigned m = 0;
+  ncand = 0;
+  const short2 v = u.spd[s.cur][i];
+  for (int k = 0; k < 8; k++) {
+    int r = p.x + c_c8[k][0], c = p.y + c_c8[k][1];
+    if (!in_dom(u, r, c)) continue;
+    unsigned long long e = u.idx[(size_t)r * u.W + c];
+    if (!idx_current(e, f)) continue;
+    unsigned j = (unsigned)(e & 0xffffffffu);
+    unsigned short aj = u.age[s.cur][j];
+    if ((int)aj > (int)age + 2) {
+      short2 w = u.spd[s.cur][j];
+      int dx = v.x - w.x, dy = v.y - w.y;
+      if (dx * dx + dy * dy < 4) {  // sqrt(dx^2 + dy^2) < 2 with integral speeds
+        m |= 1u << k;
+        if (cand) cand[ncand] = (int)j;
+        ncand++;
+      }
+    }
+  }
+  return m;
+}
+
+__global__ void __launch_bounds__(CHUNK) k_merge_count(const Unit* __restrict__ units, const UState* __restrict__ st,
+                                                       const Frame* __restrict__ fr, const int* __restrict__ table,
+                                                       int nunits) {
+  __shared__ int wt[65];
+  const int f = fr->f;
+  const int total = table[nunits];
+  for (int g = blockIdx.x; g < total; g += gridDim.x) {
+    ChunkCursor cc = chunk_of(table, nunits, g);
+    const Unit& u = units[cc.unit];
+    if (!filt_frame(u, f) || !u.with_merge) continue;
+    const UState s = st[cc.unit];
+    const int i = cc.chunk * CHUNK + threadIdx.x;
+    unsigned m = 0;
+    if (i < s.n) {
+      unsigned short age = u.age[s.cur][i];
+      if (age != 0) {
+        int nc;
+        m = merge_dirs(u, s, f, i, u.pos[s.cur][i], age, nullptr, nc);
+      }
+      u.cmask[i] = (uint8_t)m;
+    }
+    int tot;
+    block_prefix(m != 0, wt, tot);
+    if (threadIdx.x == 0) u.act_cnt[cc.chunk] = tot;
+  }
+}
+
+__global__ void __launch_bounds__(CHUNK) k_merge_scatter(const Unit* __restrict__ units, const UState* __restrict__ st,
+                                                         const Frame* __restrict__ fr, const int* __restrict__ table,
+                                                         int nunits) {
+  __shared__ int wt[65];
+  const int f = fr->f;
+  const int total = table[nunits];
+  for (int g = blockIdx.x; g < total; g += gridDim.x) {
+    ChunkCursor cc = chunk_of(table, nunits, g);
+    const Unit& u = units[cc.unit];
+    if (!filt_frame(u, f) || !u.with_merge) continue;
+    const UState s = st[cc.unit];
+    const int i = cc.chunk * CHUNK + threadIdx.x;
+    bool act = i < s.n && u.cmask[i] != 0;
+    int tot;
+    int o = u.act_cnt[cc.chunk] + block_prefix(act, wt, tot);
+    if (act) {
+      short2 p = u.pos[s.cur][i];
+      int cand[8];
+      int nc;
+      merge_dirs(u, s, f, i, p, u.age[s.cur][i], cand, nc);
+      u.act_list[o] = make_int4(i, (int)(((unsigned)(unsigned short)p.x << 16) | (unsigned short)p.y), nc, 0);
+      for (int q = 0; q < nc; q++) u.act_cand[(size_t)o * 8 + q] = cand[q];
+    }
+  }
+}
+
+__global__ void __launch_bounds__(256) k_merge_resolve(const Unit* __restrict__ units, const UState* __restrict__ st,
+                                                       const Frame* __restrict__ fr) {
+  constexpr int NB = 1024;
+  __shared__ int4 ent[NB];
+  __shared__ int cnd[NB][8];
+  const int ui = blockIdx.x;
+  const Unit& u = units[ui];
+  const int f = fr->f;
+  if (!filt_frame(u, f) || !u.with_merge) return;
+  const UState s = st[ui];
+  unsigned short* age = u.age[s.cur];
+  const int lane = threadIdx.x & 31;
+  for (int base = 0; base < s.A; base += NB) {
+    const int nb = min(NB, s.A - base);
+    for (int k = threadIdx.x; k < nb; k += blockDim.x) {
+      int4 e = u.act_list[base + k];
+      ent[k] = e;
+      for (int q = 0; q < e.z; q++) cnd[k][q] = u.act_cand[(size_t)(base + k) * 8 + q];
+    }
+    __syncthreads();
+    if (threadIdx.x < 32) {
+      for (int g0 = 0; g0 < nb; g0 += 32) {
+        const int k = g0 + lane;
+        const bool valid = k < nb;
+        int4 e = valid ? ent[k] : make_int4(-1, 0, 0, 0);
+        const int pr = (short)((unsigned)e.y >> 16), pc = (short)((unsigned)e.y & 0xffffu);
+        bool conflict = false;
+        for (int o = 0; o < 32; o++) {
+          int qr = __shfl_sync(0xffffffffu, pr, o), qc = __shfl_sync(0xffffffffu, pc, o);
+          bool ov = __shfl_sync(0xffffffffu, valid, o);
+          if (o < lane && ov && valid && abs(qr - pr) <= 2 && abs(qc - pc) <= 2) conflict = true;
+        }
+        const bool serial = __any_sync(0xffffffffu, conflict);
+        for (int step = 0; step < (serial ? 32 : 1); step++) {
+          if (valid && (!serial || lane == step)) {
+            if (*(volatile unsigned short*)&age[e.x] != 0) {
+              for (int q = 0; q < e.z; q++) {
+                int j = cnd[k][q];
+                if (*(volatile unsigned short*)&age[j] != 0) {
+                  age[j] = 0;
+                  break;
+                }
+              }
+            }
+          }
+          __syncwarp();
+        }
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// End of frame: frame counter and the chunk table of the next frame.
+__global__ void __launch_bounds__(1024) k_tick(const Unit* __restrict__ units, const UState* __restrict__ st,
+                                               Frame* __restrict__ fr, int* __restrict__ pre_table, int nunits) {
+  build_table(units, st, nunits, pre_table);
+  if (threadIdx.x == 0) fr->f += 1;
+}
+
+}  // namespace gbt

@@ -1,0 +1,344 @@
+"""Host-side mirror of cuimg's tracker API, backed by the GB300 C ABI.
+
+    tr = Tracker((rows, cols), nscales)                 # tracker<F>(obox2d, nscales)
+    tr.strategy().set_detector_frequency(10)            # generic_strategy setters
+    tr.scale(s).strategy().detector().set_n(9).set_fast_threshold(20)
+    tr.run(frame)                                       # tracker<F>::run(const I&)
+    ps = tr.scale(s).pset()                             # particle_container view
+    ps.dense_particles(), ps.features(), ps.matches(), ps.sync_attributes(v, new)
+
+(cuimg/tracking2/tracker.h:10-47, tracking_strategies.h:28-107,
+particle_container.h:62-183.)  Settings are fixed when the first frame runs.
+``BatchTracker`` advances many independent streams of any resolution with one
+launch per stage.
+"""
+import ctypes
+
+import numpy as np
+
+from ._native import GbtError, check, cuda_lib, gbt_config
+
+GBT_FRAMES_HOST, GBT_FRAMES_DEVICE, GBT_FRAMES_HOST_RGB = 0, 1, 2
+STAGES = dict(input=0, s1=1, s2=2, contrast=3, saliency=4, mask=5, sparse=6)
+
+
+def sizes_ok(rows, cols, nscales):
+    return bool(cuda_lib().gbt_sizes_ok(rows, cols, nscales))
+
+
+class _Detector:
+    def __init__(self, owner):
+        self._o = owner
+
+    def set_n(self, n):
+        self._o._set("detector_n", int(n))
+        return self
+
+    def set_fast_threshold(self, th):
+        self._o._set("detector_threshold", int(th))
+        return self
+
+    def saliency(self):
+        return self._o._stage("saliency")
+
+
+class _Strategy:
+    def __init__(self, owner):
+        self._o = owner
+        self._det = _Detector(owner)
+
+    def set_detector_frequency(self, n):
+        self._o._set("detector_frequency", int(n))
+        return self
+
+    def set_filtering_frequency(self, n):
+        self._o._set("filtering_frequency", int(n))
+        return self
+
+    def set_k(self, k):
+        self._o._set("k", int(k))
+        return self
+
+    def set_with_merge(self, b):
+        self._o._set("with_merge", 1 if b else 0)
+        return self
+
+    def detector(self):
+        return self._det
+
+
+class ParticleSet:
+    """particle_container view of one (stream, scale) after the last frame."""
+
+    def __init__(self, tracker, stream, scale):
+        self._t, self._s, self._l = tracker, stream, scale
+        self._cache = None
+
+    def _fetch(self):
+        if self._cache is None:
+            self._cache = self._t._particles(self._s, self._l)
+        return self._cache
+
+    def size(self):
+        return len(self._fetch()["age"])
+
+    def dense_particles(self):
+        """Structured array with fields speed (2 float32), pos (2 int16), age."""
+        d = self._fetch()
+        out = np.zeros(len(d["age"]), dtype=[("speed", np.float32, 2), ("pos", np.int16, 2), ("age", np.uint16)])
+        out["speed"], out["pos"], out["age"] = d["speed"], d["pos"], d["age"]
+        return out
+
+    def features(self):
+        return self._fetch()["feat"]
+
+    def matches(self):
+        return self._fetch()["matches"]
+
+    def compact_has_run(self):
+        return self._fetch()["compact"]
+
+    def sync_attributes(self, v, new_value=None, die_fun=None):
+        """particle_container::sync_attributes (particle_container.hpp:511-545)."""
+        n = self.size()
+        if self.compact_has_run():
+            m = self.matches()
+            tmp = [new_value] * n
+            for i, ni in enumerate(m):
+                if ni >= 0:
+                    if i < len(v):
+                        tmp[ni] = v[i]
+                elif die_fun is not None and i < len(v):
+                    die_fun(v[i])
+            v[:] = tmp
+        else:
+            v.extend([new_value] * (n - len(v)))
+        return v
+
+
+class _Scale:
+    def __init__(self, tracker, stream, scale):
+        self._t, self._s, self._l = tracker, stream, scale
+
+    def pset(self):
+        return ParticleSet(self._t, self._s, self._l)
+
+    def strategy(self):
+        return _Strategy(_ScaleSetter(self._t, self._s, self._l))
+
+    def input(self, border=0):
+        return self._t.stage(self._s, self._l, "input", border)
+
+    def domain(self):
+        return self._t.dims(self._s, self._l)
+
+
+class _ScaleSetter:
+    def __init__(self, t, s, l):
+        self.t, self.s, self.l = t, s, l
+
+    def _set(self, key, value):
+        self.t._set_param(self.s, self.l, key, value)
+
+    def _stage(self, name):
+        return self.t.stage(self.s, self.l, name)
+
+
+class BatchTracker:
+    """Many independent streams advanced one frame per run() call."""
+
+    def __init__(self, configs, device=0, graphs=False):
+        self._lib = cuda_lib()
+        self._cfgs = []
+        for c in configs:
+            cfg = gbt_config()
+            self._lib.gbt_config_default(ctypes.byref(cfg), int(c["rows"]), int(c["cols"]), int(c["nscales"]))
+            for k, v in c.items():
+                if k not in ("rows", "cols", "nscales"):
+                    setattr(cfg, k, int(v))
+            self._cfgs.append(cfg)
+        self._device = device
+        self._graphs = graphs
+        self._ctx = None
+        self.nstreams = len(self._cfgs)
+
+    # -- settings (applied before the first frame) --
+    def _set_param(self, stream, scale, key, value):
+        if self._ctx is not None:
+            raise RuntimeError("tracker settings are fixed once the first frame has run")
+        streams = range(self.nstreams) if stream is None else [stream]
+        for s in streams:
+            setattr(self._cfgs[s], key, value)
+
+    def _ensure(self):
+        if self._ctx is None:
+            arr = (gbt_config * self.nstreams)(*self._cfgs)
+            ctx = ctypes.c_void_p()
+            code = self._lib.gbt_create(arr, self.nstreams, self._device, ctypes.byref(ctx))
+            if code:
+                raise GbtError(code, "gbt_create failed (sizes ok: %s)" % [
+                    sizes_ok(c.rows, c.cols, c.nscales) for c in self._cfgs])
+            self._ctx = ctx
+            if self._graphs:
+                check(self._lib.gbt_use_graphs(self._ctx, 1), self._ctx)
+        return self._ctx
+
+    def close(self):
+        if self._ctx is not None:
+            self._lib.gbt_destroy(self._ctx)
+            self._ctx = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def dims(self, stream, scale):
+        c = self._cfgs[stream]
+        return (c.rows >> scale, c.cols >> scale)
+
+    def run(self, frames, location=None):
+        """One frame per stream: numpy uint8 arrays (gray, or HxWx3 RGB whose
+        channel 0 is tracked), or device pointers with location=DEVICE."""
+        ctx = self._ensure()
+        n = self.nstreams
+        ptrs = (ctypes.c_void_p * n)()
+        pitches = (ctypes.c_int64 * n)()
+        keep = []
+        loc = location
+        for s, f in enumerate(frames):
+            if isinstance(f, np.ndarray):
+                f = np.ascontiguousarray(f, dtype=np.uint8)
+                keep.append(f)
+                ptrs[s] = f.ctypes.data
+                pitches[s] = f.strides[0]
+                if loc is None:
+                    loc = GBT_FRAMES_HOST_RGB if f.ndim == 3 else GBT_FRAMES_HOST
+            else:
+                ptr, pitch = f
+                ptrs[s] = ptr
+                pitches[s] = pitch
+        check(self._lib.gbt_run(ctx, ptrs, pitches, GBT_FRAMES_HOST if loc is None else loc), ctx)
+        return self
+
+    def run_resident(self):
+        check(self._lib.gbt_run_resident(self._ensure()), self._ctx)
+
+    def sync(self):
+        check(self._lib.gbt_sync(self._ensure()), self._ctx)
+
+    def input_slot(self, stream):
+        p, pitch = ctypes.c_void_p(), ctypes.c_int64()
+        check(self._lib.gbt_input_slot(self._ensure(), stream, ctypes.byref(p), ctypes.byref(pitch)), self._ctx)
+        return p.value, pitch.value
+
+    def cuda_stream(self):
+        p = ctypes.c_void_p()
+        check(self._lib.gbt_stream(self._ensure(), ctypes.byref(p)), self._ctx)
+        return p.value
+
+    def kernels_per_frame(self):
+        n = ctypes.c_int32()
+        check(self._lib.gbt_kernels_per_frame(self._ensure(), ctypes.byref(n)), self._ctx)
+        return n.value
+
+    def nparticles(self, stream=0, scale=None):
+        if scale is None:
+            return sum(self.nparticles(stream, s) for s in range(self._cfgs[stream].nscales))
+        n = ctypes.c_int32()
+        check(self._lib.gbt_nparticles(self._ensure(), stream, scale, ctypes.byref(n)), self._ctx)
+        return n.value
+
+    def _particles(self, stream, scale):
+        ctx = self._ensure()
+        n = self.nparticles(stream, scale)
+        speed = np.zeros((n, 2), np.float32)
+        pos = np.zeros((n, 2), np.int16)
+        age = np.zeros(n, np.uint16)
+        feat = np.zeros((n, 16), np.uint8)
+        nm, comp = ctypes.c_int32(), ctypes.c_int32()
+        check(self._lib.gbt_get_particles(ctx, stream, scale, None, None, None, None, None, ctypes.byref(nm),
+                                          ctypes.byref(comp)), ctx)
+        matches = np.zeros(max(nm.value, 1), np.int32)
+        check(self._lib.gbt_get_particles(ctx, stream, scale, speed.ctypes.data, pos.ctypes.data, age.ctypes.data,
+                                          feat.ctypes.data, matches.ctypes.data, ctypes.byref(nm),
+                                          ctypes.byref(comp)), ctx)
+        return dict(speed=speed, pos=pos, age=age, feat=feat, matches=matches[: nm.value], compact=bool(comp.value))
+
+    def stage(self, stream, scale, name, border=0):
+        ctx = self._ensure()
+        H, W = self.dims(stream, scale)
+        kind = STAGES[name]
+        if name in ("contrast", "sparse"):
+            out = np.zeros((H, W), np.uint32)
+            border = 0
+        elif name in ("saliency", "mask"):
+            out = np.zeros((H, W), np.uint8)
+            border = 0
+        else:
+            out = np.zeros((H + 2 * border, W + 2 * border), np.uint8)
+        check(self._lib.gbt_get_stage(ctx, stream, scale, kind, border, out.ctypes.data), ctx)
+        return out
+
+    def bins(self, stream, scale):
+        ctx = self._ensure()
+        r, c = ctypes.c_int32(), ctypes.c_int32()
+        check(self._lib.gbt_bins(ctx, stream, scale, ctypes.byref(r), ctypes.byref(c)), ctx)
+        BH, BW = r.value, c.value
+        flow = np.zeros((BH, BW, 2), np.float32)
+        count = np.zeros((BH, BW), np.uint32)
+        st_n = np.zeros((BH, BW), np.int32)
+        st_sp = np.zeros((BH, BW, 2), np.int32)
+        check(self._lib.gbt_get_bins(ctx, stream, scale, flow.ctypes.data, count.ctypes.data, st_n.ctypes.data,
+                                     st_sp.ctypes.data), ctx)
+        return dict(flow=flow, count=count, stat_n=st_n, stat_speed=st_sp)
+
+    def snapshot(self, stream=0, borders=True):
+        """Every stage of every scale, in the layout of tests/stage_api.snapshot."""
+        out = []
+        for s in range(self._cfgs[stream].nscales):
+            d = dict(
+                input=self.stage(stream, s, "input", 6 if borders else 0),
+                s1=self.stage(stream, s, "s1", 3 if borders else 0),
+                s2=self.stage(stream, s, "s2", 6 if borders else 0),
+                contrast=self.stage(stream, s, "contrast"),
+                saliency=self.stage(stream, s, "saliency"),
+                mask=self.stage(stream, s, "mask"),
+                sparse=self.stage(stream, s, "sparse"),
+            )
+            d.update(self.bins(stream, s))
+            p = self._particles(stream, s)
+            feat32 = np.concatenate([p["feat"], np.full_like(p["feat"], 255)], axis=1)
+            d.update(speed=p["speed"], pos=p["pos"], age=p["age"], feat=feat32, matches=p["matches"],
+                     compact=p["compact"])
+            out.append(d)
+        return out
+
+
+class Tracker(BatchTracker):
+    """Single-stream tracker with the reference's tracker<F> interface."""
+
+    def __init__(self, domain, nscales, device=0, graphs=False, **settings):
+        rows, cols = domain
+        cfg = dict(rows=rows, cols=cols, nscales=nscales)
+        cfg.update(settings)
+        super().__init__([cfg], device=device, graphs=graphs)
+
+    def run(self, frame, location=None):
+        return super().run([frame], location)
+
+    def strategy(self):
+        return _Strategy(_ScaleSetter(self, None, None))
+
+    def scale(self, s):
+        return _Scale(self, 0, s)
+
+    def pset(self):
+        return ParticleSet(self, 0, 0)
+
+    def domain(self):
+        return self.dims(0, 0)
+
+    def nparticles(self, stream=0, scale=None):
+        return super().nparticles(stream, scale)

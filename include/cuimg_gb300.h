@@ -1,0 +1,186 @@
+/*
+ * cuimg_gb300 -- C ABI of the GB300 (sm_103a) semi-dense tracking path.
+ *
+ * This is the drop-in boundary for cuimg's per-frame tracker
+ *   cuimg::tracker<tracking_strategies::bc2s_fast_gradient_cpu>::run(frame)
+ * (cuimg/tracking2/tracker.hpp:72-91): a C++ strategy object or any FFI calls
+ * these functions instead of running the reference's OpenMP functors.  All
+ * signatures use plain pointers and sizes.  Every function returns a status
+ * code (GBT_OK == 0); no exception crosses the ABI.  One context is driven by
+ * one host thread; all its GPU work is ordered on the context's CUDA stream.
+ *
+ * Geometry follows the reference: level s has floor(rows / 2^s) x
+ * floor(cols / 2^s) pixels (obox2d operator/, cuimg/obox2d.h:69-72); points
+ * are (row, col).
+ */
+#ifndef CUIMG_GB300_H_
+#define CUIMG_GB300_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes. */
+#define GBT_OK 0
+#define GBT_E_INVALID 1   /* bad argument or unsupported size */
+#define GBT_E_CUDA 2      /* a CUDA runtime call failed (see gbt_last_error) */
+#define GBT_E_OOM 3       /* device or pinned allocation failed */
+#define GBT_E_CAPACITY 4  /* a particle set outgrew its preallocated capacity */
+#define GBT_E_TIMEOUT 5   /* a bounded device-side wait gave up */
+
+typedef struct gbt_ctx gbt_ctx;
+
+/* One video stream's tracker settings.  Mirrors the reference's constructor
+ * tracker<F>(obox2d(rows, cols), nscales) and the setters of
+ * generic_strategy (tracking_strategies.hpp:56-91) and fast_detector
+ * (fast_detector.hpp:170-193). */
+typedef struct {
+  int32_t rows, cols;           /* level-0 frame size */
+  int32_t nscales;              /* number of pyramid levels / tracker scales (1..9) */
+  int32_t detector_threshold;   /* fast_detector::set_fast_threshold */
+  int32_t detector_n;           /* fast_detector::set_n (arc length, default 9) */
+  int32_t detector_frequency;   /* generic_strategy::set_detector_frequency */
+  int32_t filtering_frequency;  /* generic_strategy::set_filtering_frequency */
+  int32_t k;                    /* generic_strategy::set_k (default 300) */
+  int32_t with_merge;           /* generic_strategy::set_with_merge (default 1) */
+} gbt_config;
+
+/* Fills `cfg` with the reference defaults for a rows x cols stream. */
+void gbt_config_default(gbt_config* cfg, int32_t rows, int32_t cols, int32_t nscales);
+
+/* Returns 1 if the tracker accepts this geometry: every level at least
+ * 16 x 16 and every 8x8 flow bin's parent bin inside the next level (the
+ * reference reads outside its upper flow image otherwise,
+ * tracking_strategies.hpp:596-599). */
+int gbt_sizes_ok(int32_t rows, int32_t cols, int32_t nscales);
+
+/* Creates a context that advances `nstreams` independent streams (each with
+ * its own configuration and resolution) by one frame per gbt_run call.
+ * Replaces constructing one tracker<F> per stream (tracker.hpp:11-26). */
+int gbt_create(const gbt_config* cfgs, int32_t nstreams, int32_t device, gbt_ctx** out);
+int gbt_destroy(gbt_ctx* ctx);
+
+/* Message of the last error on this context (NUL-terminated). */
+int gbt_last_error(gbt_ctx* ctx, char* buf, size_t len);
+
+/* Frame input.  `frames[i]` is stream i's gray uint8 frame with row pitch
+ * `pitches[i]` bytes; `location` says where the pointers live.  With
+ * GBT_FRAMES_HOST the frames are staged through the context's pinned buffers
+ * (host copy + one H2D copy per stream, ordered on the context stream).
+ * Replaces tracker<F>::run(const I& in) (tracker.hpp:72-80). */
+#define GBT_FRAMES_HOST 0
+#define GBT_FRAMES_DEVICE 1
+#define GBT_FRAMES_HOST_RGB 2   /* interleaved RGB, channel 0 is tracked (get_x) */
+int gbt_run(gbt_ctx* ctx, const uint8_t* const* frames, const int64_t* pitches, int32_t location);
+
+/* Runs one frame for all streams from frames already placed in the
+ * context's input slots (gbt_input_slot); used for CUDA-graph replay. */
+int gbt_run_resident(gbt_ctx* ctx);
+
+/* Device pointer and pitch of stream `s`'s level-0 input slot. */
+int gbt_input_slot(gbt_ctx* ctx, int32_t stream, uint8_t** dptr, int64_t* pitch);
+
+/* Capture the per-frame launch sequence into CUDA graphs (one per frame
+ * kind) and replay them from then on (1), or launch stage by stage (0). */
+int gbt_use_graphs(gbt_ctx* ctx, int32_t enable);
+
+/* Waits for all queued work; returns GBT_E_CAPACITY/GBT_E_TIMEOUT if a
+ * device-side check failed since the last call. */
+int gbt_sync(gbt_ctx* ctx);
+
+/* The CUDA stream (cudaStream_t) the context orders its work on. */
+int gbt_stream(gbt_ctx* ctx, void** cuda_stream);
+
+/* Particle set of (stream, scale): dense slot count (tombstones included,
+ * as particle_container::size(), particle_container.h:137). */
+int gbt_nparticles(gbt_ctx* ctx, int32_t stream, int32_t scale, int32_t* n);
+
+/* Copies the particle set to host arrays sized for gbt_nparticles entries:
+ * speed (2 floats: row, col), pos (2 int16: row, col), age (uint16),
+ * features (16 bytes: s1 ring samples then s2 ring samples; the reference's
+ * 16 weights are the constant 255 on this path).  `matches` (size >= the
+ * pre-compaction slot count, returned in *nmatches) is the
+ * old-slot -> new-slot map of the last compaction, -1 for dead slots
+ * (particle_container::matches(), particle_container.hpp:215-252);
+ * *compact_has_run says whether this frame compacted.  Any pointer may be
+ * NULL.  Replaces pset().dense_particles()/features()/matches(). */
+int gbt_get_particles(gbt_ctx* ctx, int32_t stream, int32_t scale, float* speed, int16_t* pos,
+                      uint16_t* age, uint8_t* features, int32_t* matches, int32_t* nmatches,
+                      int32_t* compact_has_run);
+
+/* Stage images of (stream, scale) after the last frame, for checks and
+ * debugging.  Sizes: level rows x cols (+2*border for the bordered ones). */
+#define GBT_STAGE_INPUT 0     /* uint8, border b: pyramid level (clamped border) */
+#define GBT_STAGE_S1 1        /* uint8, border b: BC2S blur 1 */
+#define GBT_STAGE_S2 2        /* uint8, border b: BC2S blur 2 */
+#define GBT_STAGE_CONTRAST 3  /* uint32: contrast_kernel value */
+#define GBT_STAGE_SALIENCY 4  /* uint8: FAST saliency of the last detector frame */
+#define GBT_STAGE_MASK 5      /* uint8: detector mask of the last detector frame */
+#define GBT_STAGE_SPARSE 6    /* uint32: particle index per pixel, 0xFFFFFFFF = none */
+int gbt_get_stage(gbt_ctx* ctx, int32_t stream, int32_t scale, int32_t stage, int32_t border, void* out);
+
+/* Flow bins (8x8 px) of (stream, scale): bin grid size, then flow (2 floats
+ * per bin, NO_FLOW = -500), multiscale count, stats count and stats speed
+ * (2 int32 per bin).  compute_flow_stats_kernel / flow_fusion_kernel
+ * (tracking_strategies.hpp:525-639). */
+int gbt_bins(gbt_ctx* ctx, int32_t stream, int32_t scale, int32_t* rows, int32_t* cols);
+int gbt_get_bins(gbt_ctx* ctx, int32_t stream, int32_t scale, float* flow, uint32_t* count,
+                 int32_t* stat_n, int32_t* stat_speed);
+
+/* Particle slot counts of every (stream, scale) unit in one device read
+ * (units ordered stream-major, scales ascending); waits for queued work. */
+int gbt_read_counts(gbt_ctx* ctx, int32_t* counts, int32_t n);
+
+/* Frame counter of (stream, scale) (generic_strategy::frame_cpt_). */
+int gbt_frame_count(gbt_ctx* ctx, int32_t stream, int32_t scale, int32_t* n);
+
+/* Per-stage launch counters and device time of the last frame (for tests
+ * and the benchmark): number of kernel launches issued per frame. */
+int gbt_kernels_per_frame(gbt_ctx* ctx, int32_t* n);
+
+/* Per-kernel device-time accounting with CUDA events on the context stream
+ * (eager launches; graph replays are not split).  gbt_profile_read returns
+ * the number of entries and fills entry i: kernel name, accumulated
+ * milliseconds and launch count. */
+int gbt_profile_enable(gbt_ctx* ctx, int32_t enable);
+int gbt_profile_read(gbt_ctx* ctx, int32_t i, char* name, size_t len, double* total_ms, int32_t* launches);
+
+/* ------------------------------------------------------------------------
+ * Separable fp32 Gaussian (meta_convolve_row2d + meta_convolve_col2d,
+ * cuimg/gpu/meta_convolve.h:131-161,288-314; taps of
+ * tools/make_meta_gaussian for integer sigma, cuimg/gaussian_kernel.h:13-18
+ * otherwise; radius ceil(3 sigma); clamp-to-edge borders).
+ * `in`/`out` are device pointers to rows x cols fp32 images with row pitch in
+ * bytes; `stream` is a cudaStream_t (NULL = default stream).
+ */
+int gbt_gaussian_taps(float sigma, float* taps, int32_t* radius);
+int gbt_gaussian_f32(const float* in, int64_t in_pitch, float* out, int64_t out_pitch, int32_t rows,
+                     int32_t cols, float sigma, void* stream);
+
+/* Same filter over `nimg` images of one size in one launch; image i starts
+ * at byte offset i * in_img_bytes (in) and i * out_img_bytes (out). */
+int gbt_gaussian_f32_batch(const float* in, int64_t in_pitch, int64_t in_img_bytes, float* out,
+                           int64_t out_pitch, int64_t out_img_bytes, int32_t rows, int32_t cols,
+                           int32_t nimg, float sigma, void* stream);
+
+/* Gaussian pyramid option: sigma-1 blur then keep every second pixel
+ * (the disabled pyramid of cuimg/gpu/mipmap.h:94-108,229-246), levels
+ * 1..nlevels-1 written back to back (level l: floor(rows/2^l) x
+ * floor(cols/2^l), dense rows) into `out`. */
+int gbt_gaussian_pyramid_f32(const float* in, int64_t in_pitch, int32_t rows, int32_t cols,
+                             int32_t nlevels, float* out, void* stream);
+
+/* 2x2 floor-mean uint8 pyramid alone (subsample/mipmap_kernel,
+ * cuimg/gpu/mipmap.h:24-49,206-227): levels 1..nlevels-1, dense rows, back
+ * to back. */
+int gbt_pyramid_u8(const uint8_t* in, int64_t in_pitch, int32_t rows, int32_t cols, int32_t nlevels,
+                   uint8_t* out, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CUIMG_GB300_H_ */

@@ -39,7 +39,9 @@ int oracle_gauss_taps(float sigma, float* taps) {
     if (is_int) {
       double pi = (double)ORACLE_PI_F;
       double s = (double)sigma;
-      float res = (float)((1.0 / (sqrt(2.0 * pi) * s)) * exp(-(double)(x * x) / (2.0 * s * s)));
+      /* -(x*x) / (2*sigma*sigma) is an int / float division: float precision. */
+      float e = (float)(-(x * x)) / (2.f * sigma * sigma);
+      float res = (float)((1.0 / (sqrt(2.0 * pi) * s)) * exp((double)e));
       char buf[64];
       snprintf(buf, sizeof buf, "%.6g", (double)res);
       v = strtof(buf, NULL);

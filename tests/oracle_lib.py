@@ -1,0 +1,94 @@
+"""Loads the oracle libraries (test infrastructure only)."""
+import ctypes
+import os
+
+import numpy as np
+
+from stage_api import StageLib
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+ORACLE = os.path.join(ROOT, "oracle", "_build", "liboracle.so")
+REF = os.path.join(ROOT, "oracle", "_ref", "libcuimg_ref.so")
+GOLDEN = os.path.join(ROOT, "tests", "golden")
+
+_lib = None
+
+
+def oracle():
+    global _lib
+    if _lib is None:
+        _lib = ctypes.CDLL(ORACLE)
+        _lib.oracle_sizes_ok.argtypes = [ctypes.c_int] * 3
+        _lib.oracle_gauss_taps.argtypes = [ctypes.c_float, ctypes.c_void_p]
+        _lib.oracle_gauss_taps.restype = ctypes.c_int
+        _lib.oracle_gauss_sep_f32.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_int,
+                                              ctypes.c_void_p, ctypes.c_void_p]
+        _lib.oracle_gauss_pyramid_f32.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int] + [
+            ctypes.c_void_p] * 4
+        for n in ("oracle_set_k", "oracle_set_with_merge", "oracle_set_n"):
+            getattr(_lib, n).argtypes = [ctypes.c_void_p, ctypes.c_int]
+    return _lib
+
+
+def tracker_oracle(rows, cols, nscales, threshold=20, det_freq=10, filt_freq=1):
+    return StageLib(oracle(), "oracle_").create(rows, cols, nscales, threshold, det_freq, filt_freq)
+
+
+def reference_available():
+    return os.path.exists(REF)
+
+
+def tracker_reference(rows, cols, nscales, threshold=20, det_freq=10, filt_freq=1):
+    return StageLib(ctypes.CDLL(REF), "ref_").create(rows, cols, nscales, threshold, det_freq, filt_freq)
+
+
+def gauss_taps(sigma):
+    taps = np.zeros(2 * 200 + 1, np.float32)
+    R = oracle().oracle_gauss_taps(sigma, taps.ctypes.data)
+    return R, taps[: 2 * R + 1].copy()
+
+
+def gauss_sep(img, sigma):
+    img = np.ascontiguousarray(img, np.float32)
+    H, W = img.shape
+    R, taps = gauss_taps(sigma)
+    tmp = np.zeros_like(img)
+    out = np.zeros_like(img)
+    oracle().oracle_gauss_sep_f32(img.ctypes.data, H, W, taps.ctypes.data, R, tmp.ctypes.data, out.ctypes.data)
+    return out
+
+
+def gauss_pyramid(img, nlevels):
+    img = np.ascontiguousarray(img, np.float32)
+    H, W = img.shape
+    total = sum((H >> l) * (W >> l) for l in range(1, nlevels))
+    out = np.zeros(total, np.float32)
+    tmp, blur, work = (np.zeros_like(img) for _ in range(3))
+    oracle().oracle_gauss_pyramid_f32(img.ctypes.data, H, W, nlevels, tmp.ctypes.data, blur.ctypes.data,
+                                      work.ctypes.data, out.ctypes.data)
+    levels, off = [], 0
+    for l in range(1, nlevels):
+        n = (H >> l) * (W >> l)
+        levels.append(out[off:off + n].reshape(H >> l, W >> l))
+        off += n
+    return levels
+
+
+def box_pyramid_u8(img, nlevels):
+    """2x2 floor-mean pyramid (mipmap_kernel, cuimg/gpu/mipmap.h:24-49)."""
+    levels, cur = [], img.astype(np.int32)
+    for _ in range(1, nlevels):
+        h, w = cur.shape[0] // 2, cur.shape[1] // 2
+        c = cur[: 2 * h, : 2 * w]
+        nxt = (c[0::2, 0::2] + c[0::2, 1::2] + c[1::2, 0::2] + c[1::2, 1::2]) // 4
+        levels.append(nxt.astype(np.uint8))
+        cur = nxt
+    return levels
+
+
+def golden_cases():
+    return sorted(f[:-4] for f in os.listdir(GOLDEN) if f.startswith("tracker_") and f.endswith(".npz"))
+
+
+def load_golden(name):
+    return np.load(os.path.join(GOLDEN, name + ".npz"))

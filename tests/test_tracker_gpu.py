@@ -1,0 +1,136 @@
+"""GPU tracker parity: the CUDA path through the C ABI against the reference's
+golden outputs and the oracle restatement, bit-exact, stage by stage."""
+import numpy as np
+import pytest
+
+from oracle_lib import golden_cases, load_golden, tracker_oracle
+from stage_api import diff_snapshots, snapshot
+
+pytestmark = pytest.mark.gpu
+
+STAGE_KEYS = ("input", "s1", "s2", "contrast", "saliency", "mask", "sparse", "flow", "count", "stat_n", "stat_speed")
+
+
+def _gpu_tracker(rows, cols, L, th=20, detf=10, filtf=1, graphs=False):
+    from cuimg_gb300 import Tracker
+    tr = Tracker((rows, cols), L, graphs=graphs)
+    tr.strategy().set_detector_frequency(detf).set_filtering_frequency(filtf)
+    for s in range(L):
+        tr.scale(s).strategy().detector().set_n(9).set_fast_threshold(th)
+    return tr
+
+
+@pytest.mark.parametrize("case", golden_cases())
+def test_gpu_matches_reference_golden(case):
+    g = load_golden(case)
+    rows, cols, L, th, detf, filtf, n, seed = [int(x) for x in g["meta"]]
+    tr = _gpu_tracker(rows, cols, L, th, detf, filtf)
+    for t in range(n):
+        tr.run(g["frames"][t])
+        for s in range(L):
+            p = tr._particles(0, s)
+            for k in ("pos", "speed", "age"):
+                np.testing.assert_array_equal(p[k], g["f%d_s%d_%s" % (t, s, k)], err_msg="frame %d scale %d %s" % (t, s, k))
+            np.testing.assert_array_equal(p["feat"], g["f%d_s%d_feat" % (t, s)], err_msg="frame %d scale %d feat" % (t, s))
+            key = "f%d_s%d_matches" % (t, s)
+            assert p["compact"] == (key in g.files)
+            if key in g.files:
+                np.testing.assert_array_equal(p["matches"], g[key])
+    snap = tr.snapshot()
+    for s in range(L):
+        for k in STAGE_KEYS:
+            np.testing.assert_array_equal(snap[s][k], g["last_s%d_%s" % (s, k)], err_msg="scale %d %s" % (s, k))
+    tr.close()
+
+
+def _compare_run(rows, cols, L, n, seed, detf=10, filtf=1, graphs=False):
+    from cuimg_gb300 import synth
+    frames = synth.frames(seed, rows, cols, n)
+    tr = _gpu_tracker(rows, cols, L, 20, detf, filtf, graphs)
+    o = tracker_oracle(rows, cols, L, 20, detf, filtf)
+    for t in range(n):
+        tr.run(frames[t])
+        o.run(frames[t])
+        bad = diff_snapshots(snapshot(o, L), tr.snapshot(), detector_frame=(t % detf == 0))
+        assert not bad, "frame %d: %s" % (t, bad)
+    total = tr.nparticles()
+    tr.close()
+    o.destroy()
+    return total
+
+
+@pytest.mark.parametrize("rows,cols,L,n,seed,detf", [
+    (480, 640, 3, 24, 1, 10),
+    (240, 320, 3, 16, 2, 1),
+    (203, 317, 4, 12, 9, 3),
+    (101, 133, 3, 10, 12, 1),
+])
+def test_gpu_matches_oracle(rows, cols, L, n, seed, detf):
+    assert _compare_run(rows, cols, L, n, seed, detf) > 0
+
+
+def test_gpu_matches_oracle_1080p():
+    # The headline geometry: 1920x1080, 4 scales, detector every 10 frames.
+    total = _compare_run(1080, 1920, 4, 12, 5, 10)
+    assert total > 50000
+
+
+def test_graph_replay_matches_oracle():
+    _compare_run(240, 320, 3, 14, 4, detf=3, graphs=True)
+
+
+def test_batched_uneven_streams_match_per_stream_oracles():
+    from cuimg_gb300 import BatchTracker, synth
+    shapes = [(240, 320, 3), (480, 640, 3), (135, 201, 2), (360, 480, 4)]
+    cfgs = [dict(rows=r, cols=c, nscales=L, detector_threshold=20, detector_frequency=4) for r, c, L in shapes]
+    bt = BatchTracker(cfgs, graphs=True)
+    streams = [synth.Stream(100 + i, r, c) for i, (r, c, L) in enumerate(shapes)]
+    oracles = [tracker_oracle(r, c, L, 20, 4, 1) for r, c, L in shapes]
+    for t in range(9):
+        frames = [s.frame(t) for s in streams]
+        bt.run(frames)
+        for i, (r, c, L) in enumerate(shapes):
+            oracles[i].run(frames[i])
+            bad = diff_snapshots(snapshot(oracles[i], L), bt.snapshot(i), detector_frame=(t % 4 == 0))
+            assert not bad, "stream %d frame %d: %s" % (i, t, bad)
+    bt.close()
+
+
+def test_rgb_input_tracks_channel_zero():
+    from cuimg_gb300 import synth
+    s = synth.Stream(7, 120, 160)
+    a = _gpu_tracker(120, 160, 2, detf=2)
+    b = _gpu_tracker(120, 160, 2, detf=2)
+    for t in range(5):
+        a.run(s.frame(t))
+        b.run(s.frame_rgb(t))
+    assert not diff_snapshots(a.snapshot(), b.snapshot(), True)
+
+
+def test_deterministic_across_runs():
+    from cuimg_gb300 import synth
+    frames = synth.frames(8, 240, 320, 8)
+    snaps = []
+    for _ in range(2):
+        tr = _gpu_tracker(240, 320, 3, detf=2)
+        for f in frames:
+            tr.run(f)
+        snaps.append(tr.snapshot())
+        tr.close()
+    assert not diff_snapshots(snaps[0], snaps[1], True)
+
+
+def test_flat_and_empty_frames():
+    tr = _gpu_tracker(64, 96, 2, detf=1)
+    for _ in range(3):
+        tr.run(np.full((64, 96), 77, np.uint8))
+    assert tr.nparticles() == 0
+    assert tr.stage(0, 0, "contrast").max() == 0
+    tr.close()
+
+
+def test_invalid_geometry_rejected():
+    from cuimg_gb300 import GbtError, Tracker
+    tr = Tracker((97, 131), 3)
+    with pytest.raises(GbtError):
+        tr.run(np.zeros((97, 131), np.uint8))
