@@ -117,8 +117,8 @@ int gbt_get_particles(gbt_ctx* ctx, int32_t stream, int32_t scale, float* speed,
 #define GBT_STAGE_S1 1        /* uint8, border b: BC2S blur 1 */
 #define GBT_STAGE_S2 2        /* uint8, border b: BC2S blur 2 */
 #define GBT_STAGE_CONTRAST 3  /* uint32: contrast_kernel value */
-#define GBT_STAGE_SALIENCY 4  /* uint8: FAST saliency of the last detector frame */
-#define GBT_STAGE_MASK 5      /* uint8: detector mask of the last detector frame */
+#define GBT_STAGE_SALIENCY 4  /* uint8: FAST saliency (valid right after a detector frame) */
+#define GBT_STAGE_MASK 5      /* uint8: detector mask (valid right after a detector frame) */
 #define GBT_STAGE_SPARSE 6    /* uint32: particle index per pixel, 0xFFFFFFFF = none */
 int gbt_get_stage(gbt_ctx* ctx, int32_t stream, int32_t scale, int32_t stage, int32_t border, void* out);
 
@@ -178,6 +178,38 @@ int gbt_gaussian_pyramid_f32(const float* in, int64_t in_pitch, int32_t rows, in
  * to back. */
 int gbt_pyramid_u8(const uint8_t* in, int64_t in_pitch, int32_t rows, int32_t cols, int32_t nlevels,
                    uint8_t* out, void* stream);
+
+/* ------------------------------------------------------------------------
+ * Pyramidal Lucas-Kanade (iterative_lk_match_5x5::match,
+ * cuimg/tracking2/pyrlk_tracker.hpp:165-334, with get_flow_at's coarse-to-fine
+ * prediction :1027-1063 and pyrlk_match_particles_kernel's acceptance
+ * :677-769).  The reference hard-codes window 11, 25 masked pixels, 30
+ * iterations, step threshold 0.1 and error bound k = 300. */
+typedef struct {
+  int32_t window;    /* odd window size, 3..15 */
+  int32_t npix;      /* strongest-gradient pixels used in the normal equations */
+  int32_t max_iter;  /* Gauss-Newton iterations at most */
+  float eps;         /* stop when the step norm falls below eps */
+  float max_err;     /* accept when the mean residual is below max_err */
+} gbt_lk_params;
+
+void gbt_lk_params_default(gbt_lk_params* p);
+
+/* Scratch bytes gbt_lk_track_batch uses for npairs rows x cols pairs. */
+int64_t gbt_lk_scratch_bytes(int32_t rows, int32_t cols, int32_t nlevels, int32_t npairs);
+
+/* Tracks npts points per pair through npairs frame pairs in one batch.
+ * Device pointers: prev / cur hold npairs images (image p at byte offset
+ * p * img_bytes, rows of `pitch` bytes), uint8 when is_u8 (2x2 floor-mean
+ * pyramid, uint8 template: the reference's gl8u path) or fp32 otherwise
+ * (sigma-1 Gaussian pyramid); pts / out are npairs * npts (row, col) pairs in
+ * level-0 pixels, status is 1 when the track is accepted, err the matcher's
+ * mean residual.  Allocates (and caches) its scratch arena on the current
+ * device. */
+int gbt_lk_track_batch(const void* prev, const void* cur, int64_t pitch, int64_t img_bytes, int32_t rows,
+                       int32_t cols, int32_t is_u8, int32_t nlevels, const gbt_lk_params* params,
+                       int32_t npairs, const float* pts, int32_t npts, float* out, int32_t* status,
+                       float* err, void* stream);
 
 #ifdef __cplusplus
 }

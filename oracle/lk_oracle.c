@@ -1,0 +1,294 @@
+/*
+ * CPU restatement of cuimg's pyramidal Lucas-Kanade -- TEST INFRASTRUCTURE ONLY.
+ *
+ * Restates iterative_lk_match_5x5::match (cuimg/tracking2/pyrlk_tracker.hpp:165-334),
+ * the bilinear sampler li() (:130-146), the Sobel/8 gradient of the previous
+ * level (:910-938), pyrlk_match_particles_kernel's prediction and acceptance
+ * (:677-769), get_flow_at (:1027-1063) and recursive_prediction
+ * (cuimg/tracking2/predictions.h:61-74), for a pair of frames and a set of
+ * fresh points (age 1).  The reference hard-codes window 11, a mask of the 25
+ * strongest gradients and 30 iterations; they are parameters here.
+ *
+ * The reference leaves three cases undefined; this restatement defines them:
+ *   - window pixels outside the image are sampled with clamp-to-edge
+ *     (the reference leaves gs/as uninitialised there, :189-205);
+ *   - get_flow_at returns the identity when the match leaves the level
+ *     (the reference falls off the end of the function, :1048-1058);
+ *   - ties in the strongest-gradient selection (std::nth_element, :212-228)
+ *     are broken by the lower window index.
+ * Pyramids: pyr 0 = the tracker's 2x2 floor-mean pyramid of uint8 levels with
+ * the template truncated to uint8 (the reference's gl8u path); pyr 1 = the
+ * sigma-1 Gaussian fp32 pyramid with an fp32 template.
+ */
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+
+void oracle_gauss_pyramid_f32(const float* in, int H, int W, int L, float* tmp, float* blur, float* work, float* out);
+
+typedef struct {
+  int H, W;
+  float *prev, *cur, *gr, *gc;
+} lk_level;
+
+typedef struct {
+  int L, ws, npix, max_iter, u8;
+  float eps, kerr;
+  lk_level* lv;
+} lk_ctx;
+
+static float li(const float* img, int H, int W, float y, float x) {
+  int y0 = (int)y, x0 = (int)x; /* truncation, as i_int2(p) */
+  float a0 = y - (float)y0, a1 = x - (float)x0;
+  int y1 = y0 + 1, x1 = x0 + 1;
+  if (y0 < 0) y0 = 0;
+  if (y0 > H - 1) y0 = H - 1;
+  if (y1 < 0) y1 = 0;
+  if (y1 > H - 1) y1 = H - 1;
+  if (x0 < 0) x0 = 0;
+  if (x0 > W - 1) x0 = W - 1;
+  if (x1 < 0) x1 = 0;
+  if (x1 > W - 1) x1 = W - 1;
+  float v00 = img[(size_t)y0 * W + x0], v10 = img[(size_t)y1 * W + x0];
+  float v01 = img[(size_t)y0 * W + x1], v11 = img[(size_t)y1 * W + x1];
+  return (1 - a0) * (1 - a1) * v00 + a0 * (1 - a1) * v10 + (1 - a0) * a1 * v01 + a0 * a1 * v11;
+}
+
+static int box_has(int H, int W, int b, float y, float x) { /* (domain - border(b)).has(i_int2(p)) */
+  int r = (int)y, c = (int)x;
+  return r >= b && r <= H - b - 1 && c >= b && c <= W - b - 1;
+}
+
+/* iterative_lk_match_5x5::match.  Returns 0 on rejection (tr = (-1,-1),
+ * err = 1000 as in the reference). */
+static int lk_match(const lk_ctx* k, const lk_level* l, const float p[2], const float pred_tr[2], float tr[2],
+                    float* err_out) {
+  const int ws = k->ws, hws = ws / 2, n = ws * ws;
+  float* gsr = (float*)malloc(sizeof(float) * n);
+  float* gsc = (float*)malloc(sizeof(float) * n);
+  float* as = (float*)malloc(sizeof(float) * n);
+  float* nrm = (float*)malloc(sizeof(float) * n);
+  char* mask = (char*)calloc(n, 1);
+  float pred[2] = {p[0] + pred_tr[0], p[1] + pred_tr[1]};
+  float v[2] = {pred[0], pred[1]};
+  int ok = 1;
+  for (int i = 0, r = -hws; r <= hws; r++)
+    for (int c = -hws; c <= hws; c++, i++) {
+      float y = p[0] + (float)r, x = p[1] + (float)c;
+      gsr[i] = li(l->gr, l->H, l->W, y, x);
+      gsc[i] = li(l->gc, l->H, l->W, y, x);
+      float a = li(l->prev, l->H, l->W, y, x);
+      as[i] = k->u8 ? (float)(unsigned char)a : a;
+      nrm[i] = sqrtf(gsr[i] * gsr[i] + gsc[i] * gsc[i]);
+    }
+  /* The npix strongest gradients (ties: lower index first). */
+  int N = k->npix < n ? k->npix : n;
+  for (int i = 0; i < n; i++) {
+    int rank = 0;
+    for (int j = 0; j < n; j++)
+      if (nrm[j] > nrm[i] || (nrm[j] == nrm[i] && j < i)) rank++;
+    mask[i] = rank < N;
+  }
+  float G00 = 0, G01 = 0, G11 = 0;
+  for (int i = 0; i < n; i++)
+    if (mask[i]) {
+      G00 += gsr[i] * gsr[i];
+      G01 += gsr[i] * gsc[i];
+      G11 += gsc[i] * gsc[i];
+    }
+  /* eigenvalues of the symmetric 2x2 G */
+  float tr2 = (G00 + G11) * 0.5f, det = G00 * G11 - G01 * G01;
+  float disc = sqrtf(fmaxf(tr2 * tr2 - det, 0.f));
+  float e1 = fabsf(tr2 + disc), e2 = fabsf(tr2 - disc);
+  float min_ev = e1 < e2 ? e1 : e2;
+  if (min_ev < 0.0001f) ok = 0;
+  float i00 = 0, i01 = 0, i11 = 0;
+  if (ok) {
+    i00 = G11 / det;
+    i01 = -G01 / det;
+    i11 = G00 / det;
+  }
+  int cpt = 0;
+  if (ok) {
+    float nk0 = 1.f, nk1 = 1.f;
+    for (int it = 0; it < k->max_iter && sqrtf(nk0 * nk0 + nk1 * nk1) >= k->eps; it++) {
+      float b0 = 0, b1 = 0;
+      cpt = 0;
+      for (int i = 0, r = -hws; r <= hws; r++)
+        for (int c = -hws; c <= hws; c++, i++)
+          if (mask[i]) {
+            float dt = as[i] - li(l->cur, l->H, l->W, v[0] + (float)r, v[1] + (float)c);
+            b0 += gsr[i] * dt;
+            b1 += gsc[i] * dt;
+            cpt++;
+          }
+      nk0 = i00 * b0 + i01 * b1;
+      nk1 = i01 * b0 + i11 * b1;
+      v[0] += nk0;
+      v[1] += nk1;
+      float d0 = pred[0] - v[0], d1 = pred[1] - v[1];
+      if (sqrtf(d0 * d0 + d1 * d1) > (float)(ws * 4)) {
+        ok = 0;
+        break;
+      }
+      if (!box_has(l->H, l->W, 3, v[0], v[1])) {
+        ok = 0;
+        break;
+      }
+    }
+  }
+  if (ok) {
+    /* Mean absolute residual with the reference's window index
+     * (r+hws)*hws + (c+hws) and its running counter (:320-331). */
+    float e = 0;
+    for (int r = -hws; r <= hws; r++)
+      for (int c = -hws; c <= hws; c++) {
+        int i = (r + hws) * hws + (c + hws);
+        e += fabsf(as[i] - li(l->cur, l->H, l->W, v[0] + (float)r, v[1] + (float)c));
+        cpt++;
+      }
+    tr[0] = v[0] - p[0];
+    tr[1] = v[1] - p[1];
+    *err_out = e / (float)cpt;
+  } else {
+    tr[0] = -1.f;
+    tr[1] = -1.f;
+    *err_out = 1000.f;
+  }
+  free(gsr);
+  free(gsc);
+  free(as);
+  free(nrm);
+  free(mask);
+  return ok;
+}
+
+/* get_flow_at of level l at point q (level coordinates). */
+static void flow_at(const lk_ctx* k, int l, const float q[2], float out[2]) {
+  const lk_level* lv = &k->lv[l];
+  float pred_tr[2] = {0.f, 0.f};
+  if (l + 1 < k->L) {
+    float q2[2] = {q[0] / 2.f, q[1] / 2.f}, u[2];
+    flow_at(k, l + 1, q2, u);
+    pred_tr[0] = 2.f * u[0];
+    pred_tr[1] = 2.f * u[1];
+  }
+  float pred[2] = {q[0] + pred_tr[0], q[1] + pred_tr[1]};
+  out[0] = out[1] = 0.f;
+  if (!box_has(lv->H, lv->W, 3, pred[0], pred[1])) return;
+  float tr[2], err;
+  lk_match(k, lv, q, pred_tr, tr, &err);
+  if (box_has(lv->H, lv->W, 0, q[0] + tr[0], q[1] + tr[1])) {
+    out[0] = tr[0];
+    out[1] = tr[1];
+  }
+}
+
+static void sobel8(const float* img, int H, int W, float* gr, float* gc) {
+  memset(gr, 0, sizeof(float) * H * W);
+  memset(gc, 0, sizeof(float) * H * W);
+  for (int r = 1; r < H - 1; r++)
+    for (int c = 1; c < W - 1; c++) {
+#define P(dr, dc) img[(size_t)(r + (dr)) * W + (c + (dc))]
+      gr[(size_t)r * W + c] = (P(1, -1) + 2 * P(1, 0) + P(1, 1) - P(-1, -1) - 2 * P(-1, 0) - P(-1, 1)) / 8.f;
+      gc[(size_t)r * W + c] = (P(-1, 1) + 2 * P(0, 1) + P(1, 1) - P(-1, -1) - 2 * P(0, -1) - P(1, -1)) / 8.f;
+#undef P
+    }
+}
+
+static void box_down(const float* in, int H, int W, float* out) {
+  int H2 = H / 2, W2 = W / 2;
+  for (int r = 0; r < H2; r++)
+    for (int c = 0; c < W2; c++) {
+      int s = (int)in[(size_t)(2 * r) * W + 2 * c] + (int)in[(size_t)(2 * r) * W + 2 * c + 1] +
+              (int)in[(size_t)(2 * r + 1) * W + 2 * c] + (int)in[(size_t)(2 * r + 1) * W + 2 * c + 1];
+      out[(size_t)r * W2 + c] = (float)(s / 4);
+    }
+}
+
+/* Tracks `n` points (row, col; level-0 coordinates) from `prev` to `cur`
+ * (H x W floats; integral values for pyr 0).  Writes the new positions,
+ * status (1 accepted) and the match error. */
+int oracle_lk_track(const float* prev, const float* cur, int H, int W, int L, int pyr, int ws, int npix,
+                    int max_iter, float eps, float kerr, const float* pts, int n, float* out, int* status,
+                    float* err) {
+  if (L < 1 || ws < 3 || !(ws & 1)) return -1;
+  lk_ctx k = {L, ws, npix, max_iter, pyr == 0, eps, kerr, NULL};
+  k.lv = (lk_level*)calloc(L, sizeof(lk_level));
+  int h = H, w = W;
+  for (int l = 0; l < L; l++) {
+    k.lv[l].H = h;
+    k.lv[l].W = w;
+    size_t np = (size_t)h * w;
+    k.lv[l].prev = (float*)malloc(np * 4);
+    k.lv[l].cur = (float*)malloc(np * 4);
+    k.lv[l].gr = (float*)malloc(np * 4);
+    k.lv[l].gc = (float*)malloc(np * 4);
+    h /= 2;
+    w /= 2;
+  }
+  memcpy(k.lv[0].prev, prev, (size_t)H * W * 4);
+  memcpy(k.lv[0].cur, cur, (size_t)H * W * 4);
+  if (pyr == 0) {
+    for (int l = 1; l < L; l++) {
+      box_down(k.lv[l - 1].prev, k.lv[l - 1].H, k.lv[l - 1].W, k.lv[l].prev);
+      box_down(k.lv[l - 1].cur, k.lv[l - 1].H, k.lv[l - 1].W, k.lv[l].cur);
+    }
+  } else if (L > 1) {
+    size_t np = (size_t)H * W, tot = 0;
+    for (int l = 1; l < L; l++) tot += (size_t)k.lv[l].H * k.lv[l].W;
+    float *tmp = (float*)malloc(np * 4), *blur = (float*)malloc(np * 4), *work = (float*)malloc(np * 4);
+    float* o = (float*)malloc(tot * 4);
+    for (int which = 0; which < 2; which++) {
+      oracle_gauss_pyramid_f32(which ? cur : prev, H, W, L, tmp, blur, work, o);
+      size_t off = 0;
+      for (int l = 1; l < L; l++) {
+        size_t m = (size_t)k.lv[l].H * k.lv[l].W;
+        memcpy(which ? k.lv[l].cur : k.lv[l].prev, o + off, m * 4);
+        off += m;
+      }
+    }
+    free(tmp);
+    free(blur);
+    free(work);
+    free(o);
+  }
+  for (int l = 0; l < L; l++) sobel8(k.lv[l].prev, k.lv[l].H, k.lv[l].W, k.lv[l].gr, k.lv[l].gc);
+
+  for (int i = 0; i < n; i++) {
+    float p[2] = {pts[2 * i], pts[2 * i + 1]};
+    status[i] = 0;
+    err[i] = 1000.f;
+    out[2 * i] = p[0];
+    out[2 * i + 1] = p[1];
+    const lk_level* l0 = &k.lv[0];
+    if (!box_has(l0->H, l0->W, 3, p[0], p[1])) continue;
+    float pred_tr[2] = {0.f, 0.f};
+    if (L > 1) {
+      float q[2] = {p[0] / 2.f, p[1] / 2.f}, u[2];
+      flow_at(&k, 1, q, u);
+      pred_tr[0] = 2.f * u[0];
+      pred_tr[1] = 2.f * u[1];
+    }
+    float pred[2] = {p[0] + pred_tr[0], p[1] + pred_tr[1]};
+    if (!box_has(l0->H, l0->W, 3, pred[0], pred[1])) continue;
+    float tr[2], e;
+    lk_match(&k, l0, p, pred_tr, tr, &e);
+    float m0 = (float)(int)(p[0] + tr[0]), m1 = (float)(int)(p[1] + tr[1]);
+    float d0 = m0 - pred[0], d1 = m1 - pred[1];
+    if (box_has(l0->H, l0->W, 3, p[0] + tr[0], p[1] + tr[1]) && e < kerr && sqrtf(d0 * d0 + d1 * d1) < 160.f) {
+      status[i] = 1;
+      out[2 * i] = p[0] + tr[0];
+      out[2 * i + 1] = p[1] + tr[1];
+    }
+    err[i] = e;
+  }
+  for (int l = 0; l < L; l++) {
+    free(k.lv[l].prev);
+    free(k.lv[l].cur);
+    free(k.lv[l].gr);
+    free(k.lv[l].gc);
+  }
+  free(k.lv);
+  return 0;
+}

