@@ -19,6 +19,9 @@ OUT = os.path.join(HERE, "_build")
 INCLUDE = os.path.join(ROOT, "include")
 
 CUDA_SOURCES = ["tracker.cu", "gaussian.cu", "lk.cu"]
+# Per-file flags: the LK solver keeps separate multiply/add roundings, as the
+# reference's C++ evaluates them.
+EXTRA_FLAGS = {"lk.cu": ["--fmad=false"]}
 NVCC_FLAGS = [
     "-gencode", "arch=compute_103a,code=sm_103a",
     "-O3", "-lineinfo", "-std=c++17",
@@ -57,7 +60,7 @@ def build(force=False, verbose=False):
         obj = os.path.join(OUT, src + ".o")
         objs.append(obj)
         if force or not os.path.exists(obj) or os.path.getmtime(obj) < newest:
-            jobs.append(([nvcc] + NVCC_FLAGS + ["-dc" if False else "-c", path, "-o", obj]))
+            jobs.append([nvcc] + NVCC_FLAGS + EXTRA_FLAGS.get(src, []) + ["-c", path, "-o", obj])
     with cf.ThreadPoolExecutor(max_workers=max(1, len(jobs))) as ex:
         for out in ex.map(_run, jobs):
             if verbose and out:

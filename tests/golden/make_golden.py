@@ -109,6 +109,43 @@ def make_tracker_case(name, rows, cols, L, detf, n, seed):
     np.savez_compressed(os.path.join(HERE, name + ".npz"), **d)
 
 
+LK_CASES = [
+    # name, rows, cols, nscales, seed
+    ("lk_240x320_s3", 240, 320, 3, 21),
+]
+
+
+def make_lk_case(name, rows, cols, L, seed):
+    """The reference's own pyramidal LK tracker (pyrlk_cpu) on a frame pair:
+    detector births on frame 0, then one LK step; no filtering or merging."""
+    lib = ctypes.CDLL(os.path.join(ROOT, "oracle/_ref/libcuimg_ref.so"))
+    lib.reflk_create.restype = ctypes.c_void_p
+    lib.reflk_create.argtypes = [ctypes.c_int] * 4
+    lib.reflk_run.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
+    lib.reflk_nparticles.argtypes = [ctypes.c_void_p, ctypes.c_int]
+    lib.reflk_get.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]
+    lib.reflk_destroy.argtypes = [ctypes.c_void_p]
+    frames = synth_frames(rows, cols, 2, seed)
+    h = lib.reflk_create(rows, cols, L, 20)
+    d = dict(frames=frames, meta=np.array([rows, cols, L, seed], np.int32))
+
+    def grab(tag):
+        for s in range(L):
+            n = lib.reflk_nparticles(h, s)
+            pos = np.zeros((n, 2), np.float32)
+            age = np.zeros(n, np.uint16)
+            lib.reflk_get(h, s, pos.ctypes.data, age.ctypes.data)
+            d["%s_s%d_pos" % (tag, s)] = pos
+            d["%s_s%d_age" % (tag, s)] = age
+
+    lib.reflk_run(h, frames[0].ctypes.data)
+    grab("born")
+    lib.reflk_run(h, frames[1].ctypes.data)
+    grab("tracked")
+    lib.reflk_destroy(h)
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), **d)
+
+
 def main():
     ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
     taps = make_taps(ref)
@@ -116,6 +153,8 @@ def main():
         json.dump(taps, f, indent=0, sort_keys=True)
     for case in CASES:
         make_tracker_case(*case)
+    for case in LK_CASES:
+        make_lk_case(*case)
     print("golden fixtures written to", HERE)
 
 

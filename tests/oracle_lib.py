@@ -92,3 +92,23 @@ def golden_cases():
 
 def load_golden(name):
     return np.load(os.path.join(GOLDEN, name + ".npz"))
+
+
+def lk_track(prev, cur, pts, nlevels, pyr=0, window=11, npix=25, max_iter=30, eps=0.1, max_err=300.0):
+    """Oracle pyramidal LK (oracle/lk_oracle.c); pyr 0 = uint8 box path, 1 = fp32 Gaussian."""
+    lib = oracle()
+    if not getattr(lib, "_lk_typed", False):
+        lib.oracle_lk_track.argtypes = [ctypes.c_void_p, ctypes.c_void_p] + [ctypes.c_int] * 7 + [
+            ctypes.c_float, ctypes.c_float, ctypes.c_void_p, ctypes.c_int] + [ctypes.c_void_p] * 3
+        lib._lk_typed = True
+    A = np.ascontiguousarray(prev, np.float32)
+    B = np.ascontiguousarray(cur, np.float32)
+    p = np.ascontiguousarray(pts, np.float32)
+    n = len(p)
+    out = np.zeros((n, 2), np.float32)
+    st = np.zeros(n, np.int32)
+    er = np.zeros(n, np.float32)
+    H, W = A.shape
+    assert lib.oracle_lk_track(A.ctypes.data, B.ctypes.data, H, W, nlevels, pyr, window, npix, max_iter, eps, max_err,
+                               p.ctypes.data, n, out.ctypes.data, st.ctypes.data, er.ctypes.data) == 0
+    return out, st, er
