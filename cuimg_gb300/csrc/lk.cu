@@ -345,7 +345,8 @@ extern "C" int64_t gbt_lk_scratch_bytes(int32_t rows, int32_t cols, int32_t nlev
 static int lk_run(const void* prev, const void* cur, int64_t pitch, int64_t img_bytes, int rows, int cols, int is_u8,
                   int nlevels, const gbt_lk_params* prm, int npairs, const float* pts, int npts, float* out,
                   int* status, float* err, void* scratch, int64_t scratch_bytes, cudaStream_t st) {
-  if (!prev || !cur || !prm || !pts || !out || !status || !err || !scratch) return GBT_E_INVALID;
+  if (!prev || !cur || !prm || !scratch) return GBT_E_INVALID;
+  if (npts > 0 && (!pts || !out || !status || !err)) return GBT_E_INVALID;
   if (rows < 16 || cols < 16 || nlevels < 1 || npairs < 1 || npts < 0) return GBT_E_INVALID;
   if (prm->window < 3 || prm->window > MAXW || !(prm->window & 1) || prm->npix < 1 || prm->max_iter < 0)
     return GBT_E_INVALID;
@@ -460,3 +461,4 @@ extern "C" int gbt_lk_track_batch(const void* prev, const void* cur, int64_t pit
   return lk_run(prev, cur, pitch, img_bytes, rows, cols, is_u8, nlevels, params, npairs, pts, npts, out, status, err,
                 arena, need, (cudaStream_t)stream);
 }
+
