@@ -268,7 +268,7 @@ static int build(gbt_ctx* ctx, const gbt_config* cfgs, int nstreams) {
   ctx->pyr_tiles[1] = pyr1.back();
   std::vector<int> blur(1, 0), bins(1, 0), det(1, 0), bt(1, 0);
   for (auto& u : ctx->units) {
-    blur.push_back(blur.back() + ((u.H + BL_TR - 1) / BL_TR) * ((u.W + BL_TC - 1) / BL_TC));
+    blur.push_back(blur.back() + ((u.H + BL_SR - 1) / BL_SR) * ((u.W + BL_OC - 1) / BL_OC));
     bins.push_back(bins.back() + u.BH * u.BW);
     det.push_back(det.back() + ((u.TH + DT_R - 1) / DT_R) * ((u.TW + DT_C - 1) / DT_C));
     bt.push_back(bt.back() + u.birth_chunks);
@@ -419,8 +419,8 @@ static int enqueue_frame(gbt_ctx* ctx, bool any_det, bool any_filt) {
     k_pyramid<<<ctx->pyr_tiles[1], 256, 0, st>>>(ctx->d_units, ctx->d_stream_unit0, ctx->d_pyr_prefix[1], nstreams, 5);
     n++;
   }
-  { PROF("k_blur"); k_blur<<<ctx->blur_tiles, 256, 0, st>>>(ctx->d_units, ctx->d_blur_prefix, nunits); }
-  { PROF("k_match"); k_match<<<pgrid, CHUNK, 0, st>>>(ctx->d_units, ctx->d_state, ctx->d_frame, ctx->d_pre, nunits); }
+  { PROF("k_blur"); k_blur<<<(ctx->blur_tiles + BL_WARPS - 1) / BL_WARPS, 32 * BL_WARPS, 0, st>>>(ctx->d_units, ctx->d_blur_prefix, nunits); }
+  { PROF("k_match"); k_match<<<ctx->nsm * 8, MATCH_BLOCK, 0, st>>>(ctx->d_units, ctx->d_state, ctx->d_frame, ctx->d_pre, nunits); }
   { PROF("k_stats"); k_stats<<<(ctx->nbins + 255) / 256, 256, 0, st>>>(ctx->d_units, ctx->d_state, ctx->d_bin_prefix, nunits); }
   n += 3;
   if (any_det) {

@@ -89,81 +89,126 @@ __global__ void __launch_bounds__(256) k_pyramid(const Unit* __restrict__ units,
 // = gaussian_blur_sigma1 twice (cuimg/cpu/gaussian_blur.h:9-47).  Row pass
 // t(r,c) = (2 x[c] + x[c-1] + x[c+1]) / 4 for c in [1, W-2]; column pass
 // s(r,c) = (2 t[r] + t[r-1] + t[r+1]) / 4 for r in [1, H-2]; every other
-// pixel (the ring and the border) is zero.  One CTA produces a 16 x 64 tile
-// of s1 and s2 from a 20 x 68 tile of the level, all in shared memory.
-constexpr int BL_TR = 16, BL_TC = 64;
+// pixel (the ring and the border) is zero.
+//
+// One warp walks down a strip of BL_SR rows, 128 columns wide: every lane owns
+// four columns (one 32-bit word per row), takes its horizontal neighbours from
+// the adjacent lanes by shuffle, and keeps the last three rows of both row
+// passes in registers, so each level pixel is read once and s1 / s2 are each
+// written once.  Lanes 0 and 31 only supply the horizontal halo; strips overlap
+// by 8 columns.
+constexpr int BL_SR = 64;                 // rows per strip
+constexpr int BL_OC = 120;                // output columns per warp (lanes 1..30)
+constexpr int BL_WARPS = 8;
 
-__global__ void __launch_bounds__(256) k_blur(const Unit* __restrict__ units, const int* __restrict__ tile_prefix,
-                                              int nunits) {
-  __shared__ uint8_t sin_[BL_TR + 4][BL_TC + 4];
-  __shared__ uint8_t st[BL_TR + 4][BL_TC + 2];
-  __shared__ uint8_t ss1[BL_TR + 2][BL_TC + 2];
-  __shared__ uint8_t st2[BL_TR + 2][BL_TC];
-  const int t = blockIdx.x;
-  const int ui = find_unit(tile_prefix, nunits, t);
-  const Unit& U = units[ui];
-  const int local = t - tile_prefix[ui];
-  const int tw = (U.W + BL_TC - 1) / BL_TC;
-  const int R0 = (local / tw) * BL_TR, C0 = (local % tw) * BL_TC;
-  const int H = U.H, W = U.W;
+__device__ __forceinline__ void unpack4(uint32_t w, int* v) {
+  v[0] = w & 255;
+  v[1] = (w >> 8) & 255;
+  v[2] = (w >> 16) & 255;
+  v[3] = w >> 24;
+}
+__device__ __forceinline__ uint32_t pack4(const int* v) {
+  return (uint32_t)v[0] | ((uint32_t)v[1] << 8) | ((uint32_t)v[2] << 16) | ((uint32_t)v[3] << 24);
+}
 
-  for (int v = threadIdx.x; v < (BL_TR + 4) * (BL_TC + 4); v += blockDim.x) {
-    int r = v / (BL_TC + 4), c = v % (BL_TC + 4);
-    int gr = R0 - 2 + r, gc = C0 - 2 + c;
-    sin_[r][c] = in_dom(U, gr, gc) ? U.img[(size_t)gr * U.ipitch + gc] : 0;
-  }
-  __syncthreads();
-  // t rows R0-2 .. R0+17, cols C0-1 .. C0+64
-  for (int v = threadIdx.x; v < (BL_TR + 4) * (BL_TC + 2); v += blockDim.x) {
-    int r = v / (BL_TC + 2), c = v % (BL_TC + 2);
-    int gr = R0 - 2 + r, gc = C0 - 1 + c;
-    int val = 0;
-    if (gr >= 0 && gr < H && gc >= 1 && gc <= W - 2) val = (2 * sin_[r][c + 1] + sin_[r][c] + sin_[r][c + 2]) >> 2;
-    st[r][c] = (uint8_t)val;
-  }
-  __syncthreads();
-  // s1 rows R0-1 .. R0+16, cols C0-1 .. C0+64
-  for (int v = threadIdx.x; v < (BL_TR + 2) * (BL_TC + 2); v += blockDim.x) {
-    int r = v / (BL_TC + 2), c = v % (BL_TC + 2);
-    int gr = R0 - 1 + r, gc = C0 - 1 + c;
-    int val = 0;
-    if (gr >= 1 && gr <= H - 2 && gc >= 0 && gc < W) val = (2 * st[r + 1][c] + st[r][c] + st[r + 2][c]) >> 2;
-    ss1[r][c] = (uint8_t)val;
-  }
-  __syncthreads();
-  // t2 rows R0-1 .. R0+16, cols C0 .. C0+63
-  for (int v = threadIdx.x; v < (BL_TR + 2) * BL_TC; v += blockDim.x) {
-    int r = v / BL_TC, c = v % BL_TC;
-    int gr = R0 - 1 + r, gc = C0 + c;
-    int val = 0;
-    if (gr >= 0 && gr < H && gc >= 1 && gc <= W - 2) val = (2 * ss1[r][c + 1] + ss1[r][c] + ss1[r][c + 2]) >> 2;
-    st2[r][c] = (uint8_t)val;
-  }
-  __syncthreads();
-  // write s1 and s2 over the tile's in-domain pixels (4 bytes per thread step)
-  for (int v = threadIdx.x; v < BL_TR * (BL_TC / 4); v += blockDim.x) {
-    int r = v / (BL_TC / 4), c4 = (v % (BL_TC / 4)) * 4;
-    int gr = R0 + r, gc = C0 + c4;
-    if (gr >= H) continue;
-    uint8_t a[4], b[4];
+// Row pass of one packed word: neighbours from the adjacent lanes' words.
+__device__ __forceinline__ void row_pass(uint32_t w, uint32_t wl, uint32_t wr, int c0, int W, bool row_ok, int* t) {
+  int x[6];
+  x[0] = wl >> 24;
+  unpack4(w, x + 1);
+  x[5] = wr & 255;
 #pragma unroll
-    for (int j = 0; j < 4; j++) {
-      a[j] = ss1[r + 1][c4 + j + 1];
-      int gcc = gc + j;
-      int val = 0;
-      if (gr >= 1 && gr <= H - 2 && gcc >= 0 && gcc < W) val = (2 * st2[r + 1][c4 + j] + st2[r][c4 + j] + st2[r + 2][c4 + j]) >> 2;
-      b[j] = (uint8_t)val;
+  for (int j = 0; j < 4; j++) {
+    int c = c0 + j;
+    t[j] = (row_ok && c >= 1 && c <= W - 2) ? (2 * x[j + 1] + x[j] + x[j + 2]) >> 2 : 0;
+  }
+}
+
+// One row step of k_blur: row r of the level enters, s1 row r-1 and s2 row
+// r-2 leave.
+__device__ __forceinline__ void blur_row(const Unit& U, uint32_t w, int r, int r0, int r1, int c0, int H, int W,
+                                         bool out_lane, int* t1m2, int* t1m1, int* t10, int* t2m2, int* t2m1,
+                                         int* t20) {
+  const bool row_ok = r >= 0 && r < H;
+  uint32_t wl = __shfl_up_sync(0xffffffffu, w, 1), wr = __shfl_down_sync(0xffffffffu, w, 1);
+#pragma unroll
+  for (int j = 0; j < 4; j++) {
+    t1m2[j] = t1m1[j];
+    t1m1[j] = t10[j];
+  }
+  row_pass(w, wl, wr, c0, W, row_ok, t10);
+  // s1 at row r - 1
+  const int rs1 = r - 1;
+  int s1v[4];
+  const bool s1row = rs1 >= 1 && rs1 <= H - 2;
+#pragma unroll
+  for (int j = 0; j < 4; j++) {
+    int c = c0 + j;
+    s1v[j] = (s1row && c >= 0 && c < W) ? (2 * t1m1[j] + t1m2[j] + t10[j]) >> 2 : 0;
+  }
+  const uint32_t s1w = pack4(s1v);
+  const uint32_t s1l = __shfl_up_sync(0xffffffffu, s1w, 1), s1r = __shfl_down_sync(0xffffffffu, s1w, 1);
+#pragma unroll
+  for (int j = 0; j < 4; j++) {
+    t2m2[j] = t2m1[j];
+    t2m1[j] = t20[j];
+  }
+  row_pass(s1w, s1l, s1r, c0, W, rs1 >= 0 && rs1 < H, t20);
+  // s2 at row r - 2
+  const int rs2 = r - 2;
+  int s2v[4];
+  const bool s2row = rs2 >= 1 && rs2 <= H - 2;
+#pragma unroll
+  for (int j = 0; j < 4; j++) {
+    int c = c0 + j;
+    s2v[j] = (s2row && c >= 0 && c < W) ? (2 * t2m1[j] + t2m2[j] + t20[j]) >> 2 : 0;
+  }
+  if (out_lane && c0 < W) {
+    if (rs1 >= r0 && rs1 < r1) {
+      uint8_t* p1 = (uint8_t*)fptr(U.s1, U.fpitch, rs1, c0);
+      if (c0 + 4 <= W) *(uint32_t*)p1 = s1w;
+      else
+        for (int j = 0; j < 4 && c0 + j < W; j++) p1[j] = (uint8_t)s1v[j];
     }
-    uint8_t* p1 = (uint8_t*)fptr(U.s1, U.fpitch, gr, gc);
-    uint8_t* p2 = (uint8_t*)fptr(U.s2, U.fpitch, gr, gc);
-    if (gc + 4 <= W) {
-      *(uint32_t*)p1 = a[0] | (a[1] << 8) | (a[2] << 16) | ((uint32_t)a[3] << 24);
-      *(uint32_t*)p2 = b[0] | (b[1] << 8) | (b[2] << 16) | ((uint32_t)b[3] << 24);
-    } else {
-      for (int j = 0; j < 4 && gc + j < W; j++) {
-        p1[j] = a[j];
-        p2[j] = b[j];
-      }
+    if (rs2 >= r0 && rs2 < r1) {
+      uint8_t* p2 = (uint8_t*)fptr(U.s2, U.fpitch, rs2, c0);
+      if (c0 + 4 <= W) *(uint32_t*)p2 = pack4(s2v);
+      else
+        for (int j = 0; j < 4 && c0 + j < W; j++) p2[j] = (uint8_t)s2v[j];
+    }
+  }
+}
+
+__global__ void __launch_bounds__(32 * BL_WARPS) k_blur(const Unit* __restrict__ units,
+                                                        const int* __restrict__ item_prefix, int nunits) {
+  const int lane = threadIdx.x & 31;
+  const int item = blockIdx.x * BL_WARPS + (threadIdx.x >> 5);
+  if (item >= item_prefix[nunits]) return;
+  const int ui = find_unit(item_prefix, nunits, item);
+  const Unit& U = units[ui];
+  const int local = item - item_prefix[ui];
+  const int ncs = (U.W + BL_OC - 1) / BL_OC;
+  const int rs = local / ncs, cs = local % ncs;
+  const int H = U.H, W = U.W;
+  const int c0 = cs * BL_OC - 4 + 4 * lane;  // first column of this lane's word
+  const int r0 = rs * BL_SR, r1 = min(r0 + BL_SR, H);
+  const bool out_lane = lane >= 1 && lane <= 30;
+  int t1m2[4] = {0, 0, 0, 0}, t1m1[4] = {0, 0, 0, 0}, t10[4] = {0, 0, 0, 0};
+  int t2m2[4] = {0, 0, 0, 0}, t2m1[4] = {0, 0, 0, 0}, t20[4] = {0, 0, 0, 0};
+  const bool word_ok = c0 >= 0 && c0 < U.ipitch;
+  for (int rb = r0 - 2; rb <= r1 + 1; rb += 4) {
+    // Four independent row loads in flight per lane before any arithmetic.
+    uint32_t w4[4];
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      const int r = rb + k;
+      w4[k] = (r >= 0 && r < H && r <= r1 + 1 && word_ok) ? *(const uint32_t*)(U.img + (size_t)r * U.ipitch + c0) : 0u;
+    }
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      const int r = rb + k;
+      if (r > r1 + 1) break;
+      blur_row(U, w4[k], r, r0, r1, c0, H, W, out_lane, t1m2, t1m1, t10, t2m2, t2m1, t20);
     }
   }
 }
@@ -270,16 +315,19 @@ __device__ __forceinline__ ChunkCursor chunk_of(const int* table, int nunits, in
 // kernel_particle_container::move (particle_container.hpp:422-466).  The
 // sparse-index write keeps the highest slot per pixel (atomicMax), i.e. the
 // single-threaded reference's last writer.
-__global__ void __launch_bounds__(CHUNK) k_match(const Unit* __restrict__ units, UState* __restrict__ st,
-                                                 const Frame* __restrict__ fr, const int* __restrict__ table,
-                                                 int nunits) {
+constexpr int MATCH_BLOCK = 256;
+constexpr int MATCH_SUB = CHUNK / MATCH_BLOCK;
+
+__global__ void __launch_bounds__(MATCH_BLOCK) k_match(const Unit* __restrict__ units, UState* __restrict__ st,
+                                                       const Frame* __restrict__ fr, const int* __restrict__ table,
+                                                       int nunits) {
   const int f = fr->f;
-  const int total = table[nunits];
+  const int total = table[nunits] * MATCH_SUB;
   for (int g = blockIdx.x; g < total; g += gridDim.x) {
-    ChunkCursor cc = chunk_of(table, nunits, g);
+    ChunkCursor cc = chunk_of(table, nunits, g / MATCH_SUB);
     const Unit& u = units[cc.unit];
     const UState s = st[cc.unit];
-    const int i = cc.chunk * CHUNK + threadIdx.x;
+    const int i = cc.chunk * CHUNK + (g % MATCH_SUB) * MATCH_BLOCK + threadIdx.x;
     if (i >= s.n) continue;
     const int b = s.cur;
     unsigned short age = u.age[b][i];
