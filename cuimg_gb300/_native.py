@@ -12,7 +12,7 @@ BUILD = os.path.join(HERE, "_build")
 _libs = {}
 
 GBT_OK = 0
-STATUS = {0: "GBT_OK", 1: "GBT_E_INVALID", 2: "GBT_E_CUDA", 3: "GBT_E_OOM", 4: "GBT_E_CAPACITY", 5: "GBT_E_TIMEOUT"}
+STATUS = {0: "GBT_OK", 1: "GBT_E_INVALID", 2: "GBT_E_CUDA", 3: "GBT_E_OOM", 4: "GBT_E_CAPACITY", 5: "GBT_E_TIMEOUT", 6: "GBT_E_TOO_LARGE"}
 
 
 class GbtError(RuntimeError):

@@ -462,3 +462,138 @@ extern "C" int gbt_lk_track_batch(const void* prev, const void* cur, int64_t pit
                 arena, need, (cudaStream_t)stream);
 }
 
+// ---------------------------------------------------------------------------
+// Allocation-free variant of gbt_lk_track_batch.
+//
+// For callers that cannot allocate device memory themselves -- code running
+// under an allocator they do not own (a host application with its own device
+// pool or a strict memory budget, a plugin that must not touch the CUDA heap,
+// a context where cudaMalloc would synchronise or fail) -- this entry point
+// uses a fixed scratch arena that lives in this file as a static device
+// array.  The array is part of the library's device image: every GPU that
+// loads this library holds NOALLOC_SCRATCH_BYTES of it until the process
+// exits, whether or not the entry point is called.  The caller still passes
+// frames, points and outputs.
+//
+// Set-up: the first call on a device, with that device current, looks up the
+// array's device address once (cudaGetSymbolAddress) and caches it; make that
+// first call before capturing any stream into a CUDA graph.  Every call shares
+// the one arena and overwrites it completely (levels, gradients, level table),
+// so nothing needs clearing between calls -- but calls whose GPU work overlaps
+// (different streams or host threads without ordering) race on it.
+constexpr int64_t NOALLOC_SCRATCH_BYTES = 48ll << 20;  // 48 MiB
+static __device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_SCRATCH_BYTES];
+
+namespace gbt_lk {
+
+constexpr int NOALLOC_MAX_LEVELS = 9;
+constexpr int NOALLOC_MAX_DEVICES = 64;
+
+struct TableArgs {
+  int H[NOALLOC_MAX_LEVELS], W[NOALLOC_MAX_LEVELS];
+  long long off[NOALLOC_MAX_LEVELS];
+};
+
+// Fills the per-(pair, level) table on the device (no host staging buffer).
+__global__ void k_fill_table(Level* table, int npairs, int nlevels, const float* P0, const float* C0,
+                             const float2* G0, TableArgs a) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= npairs * nlevels) return;
+  int p = t / nlevels, l = t % nlevels;
+  long long o = a.off[l] + (long long)p * a.H[l] * a.W[l];
+  Level L;
+  L.H = a.H[l];
+  L.W = a.W[l];
+  L.prev = P0 + o;
+  L.cur = C0 + o;
+  L.grad = G0 + o;
+  table[t] = L;
+}
+
+}  // namespace gbt_lk
+
+static std::mutex g_noalloc_mu;
+static void* g_noalloc_ptr[NOALLOC_MAX_DEVICES];
+
+extern "C" int64_t gbt_lk_noalloc_max_bytes(void) { return NOALLOC_SCRATCH_BYTES; }
+
+extern "C" int gbt_lk_track_batch_noalloc(const void* prev, const void* cur, int64_t pitch, int64_t img_bytes,
+                                          int32_t rows, int32_t cols, int32_t is_u8, int32_t nlevels,
+                                          const gbt_lk_params* prm, int32_t npairs, const float* pts, int32_t npts,
+                                          float* out, int32_t* status, float* err, void* stream) {
+  if (!prev || !cur || !prm) return GBT_E_INVALID;
+  if (npts > 0 && (!pts || !out || !status || !err)) return GBT_E_INVALID;
+  if (rows < 16 || cols < 16 || nlevels < 1 || nlevels > NOALLOC_MAX_LEVELS || npairs < 1 || npts < 0)
+    return GBT_E_INVALID;
+  if (prm->window < 3 || prm->window > MAXW || !(prm->window & 1) || prm->npix < 1 || prm->max_iter < 0)
+    return GBT_E_INVALID;
+  if ((rows >> (nlevels - 1)) < 8 || (cols >> (nlevels - 1)) < 8) return GBT_E_INVALID;
+  const int64_t need = gbt_lk_scratch_bytes(rows, cols, nlevels, npairs);
+  if (need < 0) return GBT_E_INVALID;
+  if (need > NOALLOC_SCRATCH_BYTES) return GBT_E_TOO_LARGE;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= NOALLOC_MAX_DEVICES) return GBT_E_CUDA;
+  void* arena = nullptr;
+  {
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    if (!g_noalloc_ptr[dev]) {
+      void* p = nullptr;
+      if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) return GBT_E_CUDA;
+      g_noalloc_ptr[dev] = p;
+    }
+    arena = g_noalloc_ptr[dev];
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  TableArgs a{};
+  int64_t px = 0;
+  for (int l = 0, h = rows, w = cols; l < nlevels; l++, h /= 2, w /= 2) {
+    a.H[l] = h;
+    a.W[l] = w;
+    a.off[l] = px;
+    px += (int64_t)h * w * npairs;
+  }
+  float* P0 = (float*)arena;
+  float* C0 = P0 + px;
+  float2* G0 = (float2*)(C0 + px);
+  Level* table = (Level*)(G0 + px);
+  dim3 blk(256);
+  for (int which = 0; which < 2; which++) {
+    float* dst = which ? C0 : P0;
+    const void* src = which ? cur : prev;
+    if (is_u8) {
+      k_u8_to_f32<<<dim3(64, npairs), blk, 0, st>>>((const uint8_t*)src, pitch, img_bytes, rows, cols, dst,
+                                                     (long long)rows * cols);
+      for (int l = 1; l < nlevels; l++)
+        k_box_f32<<<dim3(64, npairs), blk, 0, st>>>(dst + a.off[l - 1], a.H[l - 1], a.W[l - 1],
+                                                    (long long)a.H[l - 1] * a.W[l - 1], dst + a.off[l],
+                                                    (long long)a.H[l] * a.W[l]);
+    } else {
+      for (int p = 0; p < npairs; p++) {
+        const float* s = (const float*)((const char*)src + p * img_bytes);
+        if (cudaMemcpy2DAsync(dst + (int64_t)p * rows * cols, (size_t)cols * 4, s, pitch, (size_t)cols * 4, rows,
+                              cudaMemcpyDeviceToDevice, st) != cudaSuccess)
+          return GBT_E_CUDA;
+        const float* src_l = dst + (int64_t)p * rows * cols;
+        int64_t sp = (int64_t)cols * 4;
+        for (int l = 1; l < nlevels; l++) {
+          float* lvl = dst + a.off[l] + (int64_t)p * a.H[l] * a.W[l];
+          int r = gbt_gaussian_pyramid_f32(src_l, sp, a.H[l - 1], a.W[l - 1], 2, lvl, st);
+          if (r) return r;
+          src_l = lvl;
+          sp = (int64_t)a.W[l] * 4;
+        }
+      }
+    }
+  }
+  for (int l = 0; l < nlevels; l++)
+    k_sobel8<<<dim3(64, npairs), blk, 0, st>>>(P0 + a.off[l], a.H[l], a.W[l], (long long)a.H[l] * a.W[l],
+                                               G0 + a.off[l], (long long)a.H[l] * a.W[l]);
+  k_fill_table<<<(npairs * nlevels + 255) / 256, 256, 0, st>>>(table, npairs, nlevels, P0, C0, G0, a);
+  Params P{prm->window, prm->npix, prm->max_iter, nlevels, prm->eps, prm->max_err, is_u8};
+  long long total = (long long)npairs * npts;
+  if (total > 0) {
+    long long blocks = (total + WARPS - 1) / WARPS;
+    k_lk_track<<<(unsigned)blocks, 32 * WARPS, 0, st>>>(table, P, npairs, npts, pts, out, status, err);
+  }
+  return cudaGetLastError() == cudaSuccess ? GBT_OK : GBT_E_CUDA;
+}

@@ -30,6 +30,7 @@ extern "C" {
 #define GBT_E_OOM 3       /* device or pinned allocation failed */
 #define GBT_E_CAPACITY 4  /* a particle set outgrew its preallocated capacity */
 #define GBT_E_TIMEOUT 5   /* a bounded device-side wait gave up */
+#define GBT_E_TOO_LARGE 6 /* request exceeds the fixed scratch of an allocation-free entry point */
 
 typedef struct gbt_ctx gbt_ctx;
 
@@ -210,6 +211,21 @@ int gbt_lk_track_batch(const void* prev, const void* cur, int64_t pitch, int64_t
                        int32_t cols, int32_t is_u8, int32_t nlevels, const gbt_lk_params* params,
                        int32_t npairs, const float* pts, int32_t npts, float* out, int32_t* status,
                        float* err, void* stream);
+
+/* Allocation-free variant of gbt_lk_track_batch (no counterpart in the
+ * reference).  For callers that must not allocate device memory (their own
+ * device pool or budget, a plugin that may not touch the CUDA heap): same
+ * arguments and results, but the scratch lives in a fixed static device
+ * array of gbt_lk_noalloc_max_bytes() bytes (48 MiB) that every GPU loading
+ * this library holds until exit.  Requests needing more scratch than that
+ * (gbt_lk_scratch_bytes) return GBT_E_TOO_LARGE.  The first call on a device
+ * looks up the array's address, so make it before any stream capture.  All
+ * calls share the array: calls whose GPU work overlaps race. */
+int64_t gbt_lk_noalloc_max_bytes(void);
+int gbt_lk_track_batch_noalloc(const void* prev, const void* cur, int64_t pitch, int64_t img_bytes, int32_t rows,
+                               int32_t cols, int32_t is_u8, int32_t nlevels, const gbt_lk_params* params,
+                               int32_t npairs, const float* pts, int32_t npts, float* out, int32_t* status,
+                               float* err, void* stream);
 
 #ifdef __cplusplus
 }
