@@ -180,9 +180,11 @@ def bench_ours(args):
     cfg = [dict(rows=ROWS, cols=COLS, nscales=NSCALES, detector_threshold=THRESHOLD, detector_frequency=DET_FREQ,
                 filtering_frequency=FILT_FREQ) for _ in range(B)]
 
-    def make(nstreams):
-        bt = BatchTracker(cfg[:nstreams], device=local, graphs=True)
+    def make(nstreams, graphs=True):
+        bt = BatchTracker(cfg[:nstreams], device=local, graphs=graphs)
         bt._ensure()
+        if args.matcher >= 0:
+            bt.set_tuning(0, args.matcher)
         return bt
 
     dev_frames = [torch.from_numpy(f).to(dev) for f in frames]  # resident in HBM
@@ -239,8 +241,7 @@ def bench_ours(args):
     bt1.close()
 
     # Per-kernel device time (eager, CUDA events on the context stream).
-    btp = BatchTracker(cfg, device=local, graphs=False)
-    btp._ensure()
+    btp = make(B, graphs=False)
     nprof = max(args.steps, DET_FREQ)
     for t in range(args.warmup):
         btp.run([frames[s][t % nfr] for s in range(B)])
@@ -356,6 +357,7 @@ def main():
     ap.add_argument("--streams", type=int, default=16)
     ap.add_argument("--cpu-frames", type=int, default=40)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--matcher", type=int, default=-1, help="matcher variant (default: library default)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -86,6 +86,8 @@ def _declare(lib):
     lib.gbt_frame_count.argtypes = [P, I32, I32, I32P]
     lib.gbt_kernels_per_frame.argtypes = [P, I32P]
     lib.gbt_read_counts.argtypes = [P, P, I32]
+    lib.gbt_set_tuning.argtypes = [P, I32, I32]
+    lib.gbt_get_tuning.argtypes = [P, I32, I32P]
     lib.gbt_profile_enable.argtypes = [P, I32]
     lib.gbt_profile_read.argtypes = [P, I32, ctypes.c_char_p, ctypes.c_size_t, ctypes.POINTER(ctypes.c_double), I32P]
     for name in ("gbt_set_param",):

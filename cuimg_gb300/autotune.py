@@ -1,0 +1,98 @@
+"""Autotuner for the tracker's launch shapes.
+
+The tracker's results do not depend on its tuning knobs (GBT_TUNE_* in
+include/cuimg_gb300.h); only speed does, and the best setting depends on the
+GPU and on the streams' resolutions.  ``tune`` times every setting of each
+knob on the caller's own workload -- a throwaway context per setting, a few
+warm-up frames, then per-kernel CUDA-event time of the knob's kernel over the
+timed frames -- keeps the fastest, and caches the choice in a JSON file keyed
+by GPU name and stream geometry.  ``apply`` puts the cached choice on a
+tracker.
+"""
+import ctypes
+import json
+import os
+
+from ._native import check, cuda_lib
+
+KNOBS = {
+    # knob id: (name, settings, kernel names whose time decides)
+    0: ("matcher", (0, 1), ("k_match", "k_match_warp")),
+    1: ("blur_rows", (16, 32, 64), ("k_blur",)),
+}
+DEFAULT_CACHE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "_build", "autotune.json")
+
+
+def _gpu_name(device):
+    try:
+        import torch
+        return torch.cuda.get_device_name(device)
+    except Exception:
+        return "cuda:%d" % device
+
+
+def signature(configs, device=0):
+    geo = sorted("%dx%dx%d" % (c["rows"], c["cols"], c["nscales"]) for c in configs)
+    return "%s|%s" % (_gpu_name(device), ",".join(geo))
+
+
+def _kernel_ms(bt, names):
+    lib = cuda_lib()
+    buf = ctypes.create_string_buffer(64)
+    tot, cnt = ctypes.c_double(), ctypes.c_int32()
+    ms, k = 0.0, 0
+    while True:
+        n = lib.gbt_profile_read(bt._ctx, k, buf, 64, ctypes.byref(tot), ctypes.byref(cnt))
+        if k >= n:
+            break
+        if buf.value.decode() in names:
+            ms += tot.value
+        k += 1
+    return ms
+
+
+def tune(configs, frames, warmup=3, timed=8, device=0, cache_path=DEFAULT_CACHE, force=False):
+    """frames[t][s]: frame t of stream s (numpy uint8).  Returns {knob: value}."""
+    from .tracker import BatchTracker
+    key = signature(configs, device)
+    cache = {}
+    if os.path.exists(cache_path):
+        try:
+            with open(cache_path) as f:
+                cache = json.load(f)
+        except (OSError, ValueError):
+            cache = {}
+    if key in cache and not force:
+        return {int(k): v for k, v in cache[key].items()}
+    lib = cuda_lib()
+    choice = {}
+    for knob, (name, settings, kernels) in KNOBS.items():
+        best = None
+        for value in settings:
+            bt = BatchTracker(configs, device=device, graphs=False)
+            bt._ensure()
+            for k2, v2 in choice.items():
+                bt.set_tuning(k2, v2)
+            bt.set_tuning(knob, value)
+            for t in range(warmup):
+                bt.run(frames[t % len(frames)])
+            check(lib.gbt_profile_enable(bt._ctx, 1), bt._ctx)
+            for t in range(timed):
+                bt.run(frames[(warmup + t) % len(frames)])
+            bt.sync()
+            ms = _kernel_ms(bt, kernels)
+            bt.close()
+            if best is None or ms < best[0]:
+                best = (ms, value)
+        choice[knob] = best[1]
+    cache[key] = {str(k): v for k, v in choice.items()}
+    os.makedirs(os.path.dirname(cache_path), exist_ok=True)
+    with open(cache_path, "w") as f:
+        json.dump(cache, f, indent=1, sort_keys=True)
+    return choice
+
+
+def apply(bt, choice):
+    for knob, value in choice.items():
+        bt.set_tuning(int(knob), int(value))
+    return bt

@@ -18,7 +18,7 @@ CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 INCLUDE = os.path.join(ROOT, "include")
 
-CUDA_SOURCES = ["tracker.cu", "gaussian.cu", "lk.cu"]
+CUDA_SOURCES = ["tracker.cu", "gaussian.cu", "lk.cu", "lkd.cu"]
 # Per-file flags: the LK solver keeps separate multiply/add roundings, as the
 # reference's C++ evaluates them.
 EXTRA_FLAGS = {"lk.cu": ["--fmad=false"]}

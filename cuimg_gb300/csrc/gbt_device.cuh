@@ -82,8 +82,8 @@ struct UState {
 };
 
 struct Frame {
-  int f;         // frames completed so far (the frame being processed)
-  int err;       // error bits
+  int f;    // frames completed so far (the frame being processed)
+  int err;  // error bits
 };
 
 constexpr int ERR_CAPACITY = 1;

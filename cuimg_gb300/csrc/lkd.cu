@@ -1,0 +1,589 @@
+// Differentiable pyramidal LK residual and its hand-written adjoint (sm_103a).
+//
+// Forward (per point): the translational LK of iterative_lk_match_5x5
+// (cuimg/tracking2/pyrlk_tracker.hpp:165-334) with its discrete parts removed so
+// that it is differentiable: sigma-1 Gaussian pyramids of both frames
+// (cuimg/gpu/mipmap.h:94-108 form), Sobel/8 gradients of the previous level
+// (pyrlk_tracker.hpp:910-938), every window pixel used, exactly `iters`
+// Gauss-Newton steps per level, coarse-to-fine start from twice the coarser
+// displacement (predictions.h:61-74) and from u0 / 2^(L-1) at the top,
+// floor-based bilinear sampling with clamped taps.  Loss per point = sum over
+// the level-0 window of (A0(p + o) - B0(v + o))^2 at the final position v.
+//
+// Adjoint: gradients of sum_i dloss_i * loss_i with respect to both frames and
+// u0.  The backward pass recomputes the pyramid levels (nothing from the
+// forward call is kept), replays each point's forward in a warp, then sweeps
+// back through the iterations: step v += M b with M = G^-1 gives
+// dM += dv b^T, db = M dv; b = sum g r gives dg += r db and dr = g . db; r =
+// T - B(v + o) scatters into dA, dB and dv; finally dG = -M dM M and
+// dg += (dG + dG^T) g.  Level images are then pulled back through the Sobel
+// transpose and the transpose of blur-and-decimate, top level first.
+#include <cuda_runtime.h>
+
+#include <mutex>
+#include <vector>
+
+#include "cuimg_gb300.h"
+
+extern "C" int gbt_gaussian_pyramid_f32(const float* in, int64_t in_pitch, int32_t rows, int32_t cols, int32_t nlevels,
+                                        float* out, void* stream);
+
+namespace gbt_lkd {
+
+constexpr int MAXW = 15;
+constexpr int MAXPIX = MAXW * MAXW;
+constexpr int PPL = (MAXPIX + 31) / 32;
+constexpr int MAXL = 9;
+constexpr int MAXK = 32;
+constexpr int WARPS = 4;
+
+struct Lvl {
+  int H, W;
+  const float* A;
+  const float* B;
+  const float2* S;  // Sobel/8 of A: (d/drow, d/dcol)
+  float* dA;
+  float* dB;
+  float2* dS;
+};
+
+struct Bil {
+  int i00, i10, i01, i11;
+  float w00, w10, w01, w11;
+  float a, b;  // fractional parts (row, col)
+};
+
+__device__ __forceinline__ Bil bil_at(int H, int W, float y, float x) {
+  Bil o;
+  float fy = floorf(y), fx = floorf(x);
+  int y0 = (int)fy, x0 = (int)fx;
+  o.a = y - fy;
+  o.b = x - fx;
+  int y1 = min(max(y0 + 1, 0), H - 1), x1 = min(max(x0 + 1, 0), W - 1);
+  y0 = min(max(y0, 0), H - 1);
+  x0 = min(max(x0, 0), W - 1);
+  o.i00 = y0 * W + x0;
+  o.i10 = y1 * W + x0;
+  o.i01 = y0 * W + x1;
+  o.i11 = y1 * W + x1;
+  o.w00 = (1.f - o.a) * (1.f - o.b);
+  o.w10 = o.a * (1.f - o.b);
+  o.w01 = (1.f - o.a) * o.b;
+  o.w11 = o.a * o.b;
+  return o;
+}
+
+__device__ __forceinline__ float bil_val(const float* img, const Bil& s) {
+  return s.w00 * img[s.i00] + s.w10 * img[s.i10] + s.w01 * img[s.i01] + s.w11 * img[s.i11];
+}
+__device__ __forceinline__ float2 bil_val2(const float2* img, const Bil& s) {
+  float2 a = img[s.i00], b = img[s.i10], c = img[s.i01], d = img[s.i11];
+  return make_float2(s.w00 * a.x + s.w10 * b.x + s.w01 * c.x + s.w11 * d.x,
+                     s.w00 * a.y + s.w10 * b.y + s.w01 * c.y + s.w11 * d.y);
+}
+// d/d(position) of the bilinear interpolant.
+__device__ __forceinline__ float2 bil_grad(const float* img, const Bil& s) {
+  float v00 = img[s.i00], v10 = img[s.i10], v01 = img[s.i01], v11 = img[s.i11];
+  return make_float2((1.f - s.b) * (v10 - v00) + s.b * (v11 - v01), (1.f - s.a) * (v01 - v00) + s.a * (v11 - v10));
+}
+__device__ __forceinline__ void bil_scatter(float* img, const Bil& s, float v) {
+  atomicAdd(img + s.i00, s.w00 * v);
+  atomicAdd(img + s.i10, s.w10 * v);
+  atomicAdd(img + s.i01, s.w01 * v);
+  atomicAdd(img + s.i11, s.w11 * v);
+}
+__device__ __forceinline__ void bil_scatter2(float2* img, const Bil& s, float2 v) {
+  float* f = (float*)img;
+  atomicAdd(f + 2 * s.i00, s.w00 * v.x);
+  atomicAdd(f + 2 * s.i00 + 1, s.w00 * v.y);
+  atomicAdd(f + 2 * s.i10, s.w10 * v.x);
+  atomicAdd(f + 2 * s.i10 + 1, s.w10 * v.y);
+  atomicAdd(f + 2 * s.i01, s.w01 * v.x);
+  atomicAdd(f + 2 * s.i01 + 1, s.w01 * v.y);
+  atomicAdd(f + 2 * s.i11, s.w11 * v.x);
+  atomicAdd(f + 2 * s.i11 + 1, s.w11 * v.y);
+}
+
+__device__ __forceinline__ float wsum(float v) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  return __shfl_sync(0xffffffffu, v, 0);
+}
+
+struct Setup {  // per level of one point
+  float q0, q1, M00, M01, M11;
+};
+
+// Normal matrix inverse at one level (all lanes get identical values).
+__device__ __forceinline__ void level_setup(const Lvl& e, int ws, float q0, float q1, float& M00, float& M01,
+                                            float& M11) {
+  const int lane = threadIdx.x & 31, hws = ws / 2, n = ws * ws;
+  float g00 = 0.f, g01 = 0.f, g11 = 0.f;
+  for (int i = lane; i < n; i += 32) {
+    Bil s = bil_at(e.H, e.W, q0 + (float)(i / ws - hws), q1 + (float)(i % ws - hws));
+    float2 g = bil_val2(e.S, s);
+    g00 += g.x * g.x;
+    g01 += g.x * g.y;
+    g11 += g.y * g.y;
+  }
+  g00 = wsum(g00);
+  g01 = wsum(g01);
+  g11 = wsum(g11);
+  const float det = g00 * g11 - g01 * g01;
+  M00 = g11 / det;
+  M01 = -g01 / det;
+  M11 = g00 / det;
+}
+
+// One Gauss-Newton right-hand side b = sum g (T - B(v + o)).
+__device__ __forceinline__ void rhs(const Lvl& e, int ws, float q0, float q1, float v0, float v1, float& b0,
+                                    float& b1) {
+  const int lane = threadIdx.x & 31, hws = ws / 2, n = ws * ws;
+  b0 = 0.f;
+  b1 = 0.f;
+  for (int i = lane; i < n; i += 32) {
+    const float r = (float)(i / ws - hws), c = (float)(i % ws - hws);
+    Bil st = bil_at(e.H, e.W, q0 + r, q1 + c);
+    float2 g = bil_val2(e.S, st);
+    float res = bil_val(e.A, st) - bil_val(e.B, bil_at(e.H, e.W, v0 + r, v1 + c));
+    b0 += g.x * res;
+    b1 += g.y * res;
+  }
+  b0 = wsum(b0);
+  b1 = wsum(b1);
+}
+
+__device__ __forceinline__ float level_scale(int l) {
+  float s = 1.f;
+  for (int k = 0; k < l; k++) s *= 2.f;
+  return s;
+}
+
+// Forward of one point; fills the per-level setup and the iterate history.
+__device__ float point_forward(const Lvl* lv, int L, int ws, int K, float p0, float p1, float u0, float u1,
+                               Setup* su, float2* hist, float& vf0, float& vf1) {
+  const float top = level_scale(L - 1);
+  float d0 = u0 / top, d1 = u1 / top, v0 = 0.f, v1 = 0.f;
+  for (int l = L - 1; l >= 0; l--) {
+    const Lvl& e = lv[l];
+    const float s = level_scale(l);
+    const float q0 = p0 / s, q1 = p1 / s;
+    float M00, M01, M11;
+    level_setup(e, ws, q0, q1, M00, M01, M11);
+    if (su) su[l] = Setup{q0, q1, M00, M01, M11};
+    v0 = q0 + d0;
+    v1 = q1 + d1;
+    for (int k = 0; k < K; k++) {
+      if (hist) hist[l * (MAXK + 1) + k] = make_float2(v0, v1);
+      float b0, b1;
+      rhs(e, ws, q0, q1, v0, v1, b0, b1);
+      v0 += M00 * b0 + M01 * b1;
+      v1 += M01 * b0 + M11 * b1;
+    }
+    if (hist) hist[l * (MAXK + 1) + K] = make_float2(v0, v1);
+    d0 = 2.f * (v0 - q0);
+    d1 = 2.f * (v1 - q1);
+  }
+  vf0 = v0;
+  vf1 = v1;
+  const Lvl& e = lv[0];
+  const int lane = threadIdx.x & 31, hws = ws / 2, n = ws * ws;
+  float loss = 0.f;
+  for (int i = lane; i < n; i += 32) {
+    const float r = (float)(i / ws - hws), c = (float)(i % ws - hws);
+    float res = bil_val(e.A, bil_at(e.H, e.W, p0 + r, p1 + c)) - bil_val(e.B, bil_at(e.H, e.W, v0 + r, v1 + c));
+    loss += res * res;
+  }
+  return wsum(loss);
+}
+
+__global__ void __launch_bounds__(32 * WARPS) k_lkd_forward(const Lvl* __restrict__ levels, int L, int ws, int K,
+                                                            int npairs, int npts, const float* __restrict__ pts,
+                                                            const float* __restrict__ u0, float* __restrict__ loss,
+                                                            float* __restrict__ vfinal) {
+  const long long g = (long long)blockIdx.x * WARPS + (threadIdx.x >> 5);
+  if (g >= (long long)npairs * npts) return;
+  const int pair = (int)(g / npts);
+  float vf0, vf1;
+  float l = point_forward(levels + (size_t)pair * L, L, ws, K, pts[2 * g], pts[2 * g + 1], u0[2 * g], u0[2 * g + 1],
+                          nullptr, nullptr, vf0, vf1);
+  if ((threadIdx.x & 31) == 0) {
+    loss[g] = l;
+    vfinal[2 * g] = vf0;
+    vfinal[2 * g + 1] = vf1;
+  }
+}
+
+__global__ void __launch_bounds__(32 * WARPS) k_lkd_backward(const Lvl* __restrict__ levels, int L, int ws, int K,
+                                                             int npairs, int npts, const float* __restrict__ pts,
+                                                             const float* __restrict__ u0,
+                                                             const float* __restrict__ dloss, float* __restrict__ du0) {
+  __shared__ Setup su_all[WARPS][MAXL];
+  __shared__ float2 hist_all[WARPS][MAXL * (MAXK + 1)];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const long long gidx = (long long)blockIdx.x * WARPS + warp;
+  if (gidx >= (long long)npairs * npts) return;
+  const int pair = (int)(gidx / npts);
+  const Lvl* lv = levels + (size_t)pair * L;
+  Setup* su = su_all[warp];
+  float2* hist = hist_all[warp];
+  const float p0 = pts[2 * gidx], p1 = pts[2 * gidx + 1];
+  float vf0, vf1;
+  point_forward(lv, L, ws, K, p0, p1, u0[2 * gidx], u0[2 * gidx + 1], su, hist, vf0, vf1);
+  __syncwarp();
+  const float w = dloss[gidx];
+  const int hws = ws / 2, n = ws * ws;
+  // Loss at level 0: r = A0(p + o) - B0(v + o), dL/dr = 2 r w.
+  float dv0 = 0.f, dv1 = 0.f;
+  {
+    const Lvl& e = lv[0];
+    for (int i = lane; i < n; i += 32) {
+      const float r = (float)(i / ws - hws), c = (float)(i % ws - hws);
+      Bil sa = bil_at(e.H, e.W, p0 + r, p1 + c), sb = bil_at(e.H, e.W, vf0 + r, vf1 + c);
+      const float res = bil_val(e.A, sa) - bil_val(e.B, sb);
+      const float dr = 2.f * res * w;
+      bil_scatter(e.dA, sa, dr);
+      bil_scatter(e.dB, sb, -dr);
+      float2 gb = bil_grad(e.B, sb);
+      dv0 -= dr * gb.x;
+      dv1 -= dr * gb.y;
+    }
+    dv0 = wsum(dv0);
+    dv1 = wsum(dv1);
+  }
+  for (int l = 0; l < L; l++) {
+    const Lvl& e = lv[l];
+    const Setup S = su[l];
+    float dM00 = 0.f, dM01 = 0.f, dM10 = 0.f, dM11 = 0.f;
+    float dg0[PPL], dg1[PPL], dT[PPL];
+#pragma unroll
+    for (int k = 0; k < PPL; k++) dg0[k] = dg1[k] = dT[k] = 0.f;
+    for (int k = K - 1; k >= 0; k--) {
+      const float2 vk = hist[l * (MAXK + 1) + k];
+      const float d0 = dv0, d1 = dv1;                       // adjoint of v_{k+1}
+      const float db0 = S.M00 * d0 + S.M01 * d1, db1 = S.M01 * d0 + S.M11 * d1;
+      float b0 = 0.f, b1 = 0.f, pv0 = 0.f, pv1 = 0.f;
+#pragma unroll
+      for (int kk = 0; kk < PPL; kk++) {
+        const int i = lane + 32 * kk;
+        if (i >= n) break;
+        const float r = (float)(i / ws - hws), c = (float)(i % ws - hws);
+        Bil st = bil_at(e.H, e.W, S.q0 + r, S.q1 + c), sb = bil_at(e.H, e.W, vk.x + r, vk.y + c);
+        const float2 g = bil_val2(e.S, st);
+        const float res = bil_val(e.A, st) - bil_val(e.B, sb);
+        b0 += g.x * res;
+        b1 += g.y * res;
+        const float dres = g.x * db0 + g.y * db1;
+        dg0[kk] += res * db0;
+        dg1[kk] += res * db1;
+        dT[kk] += dres;
+        bil_scatter(e.dB, sb, -dres);
+        const float2 gb = bil_grad(e.B, sb);
+        pv0 -= dres * gb.x;
+        pv1 -= dres * gb.y;
+      }
+      b0 = wsum(b0);
+      b1 = wsum(b1);
+      dv0 = d0 + wsum(pv0);
+      dv1 = d1 + wsum(pv1);
+      dM00 += d0 * b0;
+      dM01 += d0 * b1;
+      dM10 += d1 * b0;
+      dM11 += d1 * b1;
+    }
+    // dG = -M dM M (M symmetric); then dg += (dG + dG^T) g.
+    const float t00 = dM00 * S.M00 + dM01 * S.M01, t01 = dM00 * S.M01 + dM01 * S.M11;
+    const float t10 = dM10 * S.M00 + dM11 * S.M01, t11 = dM10 * S.M01 + dM11 * S.M11;
+    const float G00 = -(S.M00 * t00 + S.M01 * t10), G01 = -(S.M00 * t01 + S.M01 * t11);
+    const float G10 = -(S.M01 * t00 + S.M11 * t10), G11 = -(S.M01 * t01 + S.M11 * t11);
+    const float H00 = 2.f * G00, H01 = G01 + G10, H11 = 2.f * G11;
+#pragma unroll
+    for (int kk = 0; kk < PPL; kk++) {
+      const int i = lane + 32 * kk;
+      if (i >= n) break;
+      const float r = (float)(i / ws - hws), c = (float)(i % ws - hws);
+      Bil st = bil_at(e.H, e.W, S.q0 + r, S.q1 + c);
+      const float2 g = bil_val2(e.S, st);
+      const float2 dgv = make_float2(dg0[kk] + H00 * g.x + H01 * g.y, dg1[kk] + H01 * g.x + H11 * g.y);
+      bil_scatter2(e.dS, st, dgv);
+      bil_scatter(e.dA, st, dT[kk]);
+    }
+    // v_0 = q + d_init: the adjoint of d_init is dv.
+    if (l + 1 < L) {
+      dv0 *= 2.f;  // d_init(l) = 2 (v_K(l+1) - q(l+1))
+      dv1 *= 2.f;
+    }
+  }
+  const float top = level_scale(L - 1);
+  if (lane == 0) {
+    du0[2 * gidx] = dv0 / top;
+    du0[2 * gidx + 1] = dv1 / top;
+  }
+}
+
+__global__ void k_to_dense(const float* __restrict__ in, long long pitch, long long img_bytes, int H, int W,
+                           float* __restrict__ out) {
+  const int pair = blockIdx.y;
+  const float* s = (const float*)((const char*)in + pair * img_bytes);
+  float* d = out + (size_t)pair * H * W;
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < H * W; t += gridDim.x * blockDim.x)
+    d[t] = ((const float*)((const char*)s + (size_t)(t / W) * pitch))[t % W];
+}
+
+__global__ void k_sobel(const float* __restrict__ a, int H, int W, long long stride, float2* __restrict__ g) {
+  const int pair = blockIdx.y;
+  const float* A = a + pair * stride;
+  float2* G = g + pair * stride;
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < H * W; t += gridDim.x * blockDim.x) {
+    int r = t / W, c = t % W;
+    float2 v = make_float2(0.f, 0.f);
+    if (r >= 1 && r < H - 1 && c >= 1 && c < W - 1) {
+#define P(dr, dc) A[(size_t)(r + (dr)) * W + (c + (dc))]
+      v.x = (P(1, -1) + 2 * P(1, 0) + P(1, 1) - P(-1, -1) - 2 * P(-1, 0) - P(-1, 1)) / 8.f;
+      v.y = (P(-1, 1) + 2 * P(0, 1) + P(1, 1) - P(-1, -1) - 2 * P(0, -1) - P(1, -1)) / 8.f;
+#undef P
+    }
+    G[t] = v;
+  }
+}
+
+// dA += Sobel^T(dS): each interior source pixel's weights, gathered.
+__global__ void k_sobel_t(const float2* __restrict__ dS, int H, int W, long long stride, float* __restrict__ dA) {
+  const int pair = blockIdx.y;
+  const float2* G = dS + pair * stride;
+  float* A = dA + pair * stride;
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < H * W; t += gridDim.x * blockDim.x) {
+    const int y = t / W, x = t % W;
+    float acc = 0.f;
+    for (int dr = -1; dr <= 1; dr++)
+      for (int dc = -1; dc <= 1; dc++) {
+        const int r = y - dr, c = x - dc;  // source pixel that reads A(y, x) at offset (dr, dc)
+        if (r < 1 || r >= H - 1 || c < 1 || c >= W - 1) continue;
+        const float wr = (dr == 0) ? 0.f : (float)dr * (dc == 0 ? 2.f : 1.f) / 8.f;
+        const float wc = (dc == 0) ? 0.f : (float)dc * (dr == 0 ? 2.f : 1.f) / 8.f;
+        const float2 gv = G[(size_t)r * W + c];
+        acc += wr * gv.x + wc * gv.y;
+      }
+    A[t] += acc;
+  }
+}
+
+struct Taps7 {
+  float w[7];
+};
+
+// Transpose of "blur columns at even positions, keep row 2r": fills tmp
+// (H x W) from the level above (H2 x W2).
+__global__ void k_decimate_t_rows(const float* __restrict__ up, int H2, int W2, long long ustride,
+                                  float* __restrict__ tmp, int H, int W, long long tstride, Taps7 t) {
+  const int pair = blockIdx.y;
+  const float* U = up + pair * ustride;
+  float* T = tmp + pair * tstride;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < H * W; i += gridDim.x * blockDim.x) {
+    const int y = i / W, x = i % W;
+    float acc = 0.f;
+    if ((x & 1) == 0 && x / 2 < W2) {
+      const int c = x / 2;
+      const int rlo = max(0, (y - 4) / 2 - 1), rhi = min(H2 - 1, (y + 4) / 2 + 1);
+      for (int r = rlo; r <= rhi; r++)
+        for (int k = -3; k <= 3; k++) {
+          const int yy = min(max(2 * r + k, 0), H - 1);
+          if (yy == y) acc += t.w[k + 3] * U[(size_t)r * W2 + c];
+        }
+      // Rows beyond the small window can only reach y through clamping.
+      if (y == 0 || y == H - 1)
+        for (int r = 0; r < H2; r++) {
+          if (r >= rlo && r <= rhi) continue;
+          for (int k = -3; k <= 3; k++) {
+            const int yy = min(max(2 * r + k, 0), H - 1);
+            if (yy == y) acc += t.w[k + 3] * U[(size_t)r * W2 + c];
+          }
+        }
+    }
+    T[i] = acc;
+  }
+}
+
+// Transpose of the row blur (clamped): dA(y, x) += sum_{c, k: clamp(c + k) == x} w_k tmp(y, c).
+__global__ void k_blur_t_cols(const float* __restrict__ tmp, int H, int W, long long stride, float* __restrict__ dA,
+                              Taps7 t) {
+  const int pair = blockIdx.y;
+  const float* T = tmp + pair * stride;
+  float* A = dA + pair * stride;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < H * W; i += gridDim.x * blockDim.x) {
+    const int y = i / W, x = i % W;
+    float acc = 0.f;
+    const int clo = (x == 0) ? 0 : max(0, x - 3), chi = (x == W - 1) ? W - 1 : min(W - 1, x + 3);
+    for (int c = clo; c <= chi; c++)
+      for (int k = -3; k <= 3; k++) {
+        const int xx = min(max(c + k, 0), W - 1);
+        if (xx == x) acc += t.w[k + 3] * T[(size_t)y * W + c];
+      }
+    A[i] += acc;
+  }
+}
+
+}  // namespace gbt_lkd
+
+using namespace gbt_lkd;
+
+extern "C" int64_t gbt_lkd_scratch_bytes(int32_t rows, int32_t cols, int32_t nlevels, int32_t npairs) {
+  if (rows < 16 || cols < 16 || nlevels < 1 || nlevels > MAXL || npairs < 1) return -1;
+  int64_t px = 0;
+  for (int l = 0, h = rows, w = cols; l < nlevels; l++, h /= 2, w /= 2) px += (int64_t)h * w;
+  // A, B, S (2), dA, dB, dS (2), tmp: 9 floats per pixel; plus the level table.
+  return px * npairs * 36 + (int64_t)npairs * nlevels * sizeof(Lvl) + 4096;
+}
+
+namespace {
+
+std::mutex g_mu;
+std::vector<std::pair<void*, int64_t>> g_arena;
+
+void* arena_for(int64_t need, cudaStream_t st) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return nullptr;
+  std::lock_guard<std::mutex> lk(g_mu);
+  if ((int)g_arena.size() <= dev) g_arena.resize(dev + 1, {nullptr, 0});
+  if (g_arena[dev].second < need) {
+    if (g_arena[dev].first) {
+      cudaStreamSynchronize(st);
+      cudaFree(g_arena[dev].first);
+    }
+    g_arena[dev] = {nullptr, 0};
+    if (cudaMalloc(&g_arena[dev].first, need) != cudaSuccess) return nullptr;
+    g_arena[dev].second = need;
+  }
+  return g_arena[dev].first;
+}
+
+struct Plan {
+  int L, H[MAXL], W[MAXL];
+  int64_t off[MAXL], px;
+  float *A, *B, *dA, *dB, *tmp;
+  float2 *S, *dS;
+  Lvl* table;
+};
+
+// Lays out the arena and builds both pyramids and the Sobel images.
+int prepare(const float* I0, const float* I1, int64_t pitch, int64_t img_bytes, int rows, int cols, int L, int npairs,
+            bool adjoint, Plan& P, cudaStream_t st) {
+  const int64_t need = gbt_lkd_scratch_bytes(rows, cols, L, npairs);
+  if (need < 0) return GBT_E_INVALID;
+  char* base = (char*)arena_for(need, st);
+  if (!base) return GBT_E_OOM;
+  P.L = L;
+  P.px = 0;
+  for (int l = 0, h = rows, w = cols; l < L; l++, h /= 2, w /= 2) {
+    P.H[l] = h;
+    P.W[l] = w;
+    P.off[l] = P.px;
+    P.px += (int64_t)h * w * npairs;
+  }
+  float* f = (float*)base;
+  P.A = f;
+  P.B = f + P.px;
+  P.dA = f + 2 * P.px;
+  P.dB = f + 3 * P.px;
+  P.tmp = f + 4 * P.px;
+  P.S = (float2*)(f + 5 * P.px);
+  P.dS = (float2*)(f + 7 * P.px);
+  P.table = (Lvl*)(f + 9 * P.px);
+  dim3 blk(256);
+  for (int which = 0; which < 2; which++) {
+    float* dst = which ? P.B : P.A;
+    k_to_dense<<<dim3(128, npairs), blk, 0, st>>>(which ? I1 : I0, pitch, img_bytes, rows, cols, dst);
+    for (int p = 0; p < npairs; p++) {
+      const float* src = dst + (int64_t)p * rows * cols;
+      int64_t sp = (int64_t)cols * 4;
+      for (int l = 1; l < L; l++) {
+        float* lvl = dst + P.off[l] + (int64_t)p * P.H[l] * P.W[l];
+        int r = gbt_gaussian_pyramid_f32(src, sp, P.H[l - 1], P.W[l - 1], 2, lvl, st);
+        if (r) return r;
+        src = lvl;
+        sp = (int64_t)P.W[l] * 4;
+      }
+    }
+  }
+  for (int l = 0; l < L; l++)
+    k_sobel<<<dim3(64, npairs), blk, 0, st>>>(P.A + P.off[l], P.H[l], P.W[l], (long long)P.H[l] * P.W[l],
+                                              P.S + P.off[l]);
+  if (adjoint) {
+    cudaMemsetAsync(P.dA, 0, P.px * 8, st);           // dA and dB
+    cudaMemsetAsync(P.dS, 0, P.px * 8, st);
+  }
+  std::vector<Lvl> h((size_t)npairs * L);
+  for (int p = 0; p < npairs; p++)
+    for (int l = 0; l < L; l++) {
+      int64_t o = P.off[l] + (int64_t)p * P.H[l] * P.W[l];
+      h[(size_t)p * L + l] = Lvl{P.H[l], P.W[l], P.A + o, P.B + o, P.S + o, P.dA + o, P.dB + o, P.dS + o};
+    }
+  cudaMemcpyAsync(P.table, h.data(), h.size() * sizeof(Lvl), cudaMemcpyHostToDevice, st);
+  cudaStreamSynchronize(st);  // the host table must outlive the copy
+  return cudaGetLastError() == cudaSuccess ? GBT_OK : GBT_E_CUDA;
+}
+
+int check_args(const float* I0, const float* I1, int rows, int cols, int L, int ws, int K, int npairs, int npts) {
+  if (!I0 || !I1 || rows < 16 || cols < 16 || L < 1 || L > MAXL || npairs < 1 || npts < 0) return GBT_E_INVALID;
+  if (ws < 3 || ws > MAXW || !(ws & 1) || K < 0 || K > MAXK) return GBT_E_INVALID;
+  if ((rows >> (L - 1)) < 4 || (cols >> (L - 1)) < 4) return GBT_E_INVALID;
+  return GBT_OK;
+}
+
+}  // namespace
+
+extern "C" int gbt_lkd_forward(const float* I0, const float* I1, int64_t pitch, int64_t img_bytes, int32_t rows,
+                               int32_t cols, int32_t nlevels, int32_t window, int32_t iters, int32_t npairs,
+                               const float* pts, const float* u0, int32_t npts, float* loss, float* vfinal,
+                               void* stream) {
+  int r = check_args(I0, I1, rows, cols, nlevels, window, iters, npairs, npts);
+  if (r) return r;
+  if (npts > 0 && (!pts || !u0 || !loss || !vfinal)) return GBT_E_INVALID;
+  cudaStream_t st = (cudaStream_t)stream;
+  Plan P;
+  if ((r = prepare(I0, I1, pitch, img_bytes, rows, cols, nlevels, npairs, false, P, st))) return r;
+  long long total = (long long)npairs * npts;
+  if (total > 0)
+    k_lkd_forward<<<(unsigned)((total + WARPS - 1) / WARPS), 32 * WARPS, 0, st>>>(P.table, nlevels, window, iters,
+                                                                                  npairs, npts, pts, u0, loss, vfinal);
+  return cudaGetLastError() == cudaSuccess ? GBT_OK : GBT_E_CUDA;
+}
+
+extern "C" int gbt_lkd_backward(const float* I0, const float* I1, int64_t pitch, int64_t img_bytes, int32_t rows,
+                                int32_t cols, int32_t nlevels, int32_t window, int32_t iters, int32_t npairs,
+                                const float* pts, const float* u0, int32_t npts, const float* dloss, float* dI0,
+                                float* dI1, float* du0, void* stream) {
+  int r = check_args(I0, I1, rows, cols, nlevels, window, iters, npairs, npts);
+  if (r) return r;
+  if (!dI0 || !dI1) return GBT_E_INVALID;
+  if (npts > 0 && (!pts || !u0 || !dloss || !du0)) return GBT_E_INVALID;
+  cudaStream_t st = (cudaStream_t)stream;
+  Plan P;
+  if ((r = prepare(I0, I1, pitch, img_bytes, rows, cols, nlevels, npairs, true, P, st))) return r;
+  long long total = (long long)npairs * npts;
+  if (total > 0)
+    k_lkd_backward<<<(unsigned)((total + WARPS - 1) / WARPS), 32 * WARPS, 0, st>>>(
+        P.table, nlevels, window, iters, npairs, npts, pts, u0, dloss, du0);
+  float taps_f[16];
+  int32_t R;
+  gbt_gaussian_taps(1.f, taps_f, &R);
+  Taps7 t;
+  for (int k = 0; k < 7; k++) t.w[k] = taps_f[k];
+  dim3 blk(256);
+  // Sobel transpose on every level, then pull each level down the pyramid.
+  for (int l = 0; l < nlevels; l++)
+    k_sobel_t<<<dim3(64, npairs), blk, 0, st>>>(P.dS + P.off[l], P.H[l], P.W[l], (long long)P.H[l] * P.W[l],
+                                                P.dA + P.off[l]);
+  for (int which = 0; which < 2; which++) {
+    float* d = which ? P.dB : P.dA;
+    for (int l = nlevels - 1; l >= 1; l--) {
+      k_decimate_t_rows<<<dim3(64, npairs), blk, 0, st>>>(d + P.off[l], P.H[l], P.W[l], (long long)P.H[l] * P.W[l],
+                                                          P.tmp, P.H[l - 1], P.W[l - 1],
+                                                          (long long)P.H[l - 1] * P.W[l - 1], t);
+      k_blur_t_cols<<<dim3(64, npairs), blk, 0, st>>>(P.tmp, P.H[l - 1], P.W[l - 1],
+                                                      (long long)P.H[l - 1] * P.W[l - 1], d + P.off[l - 1], t);
+    }
+  }
+  cudaMemcpyAsync(dI0, P.dA, (size_t)npairs * rows * cols * 4, cudaMemcpyDeviceToDevice, st);
+  cudaMemcpyAsync(dI1, P.dB, (size_t)npairs * rows * cols * 4, cudaMemcpyDeviceToDevice, st);
+  return cudaGetLastError() == cudaSuccess ? GBT_OK : GBT_E_CUDA;
+}

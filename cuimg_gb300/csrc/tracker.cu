@@ -48,8 +48,11 @@ struct gbt_ctx {
   int* d_stream_unit0 = nullptr;
   int* d_pyr_prefix[2] = {nullptr, nullptr};
   int pyr_tiles[2] = {0, 0};
-  int* d_blur_prefix = nullptr;
+  int* d_blur_prefix = nullptr;  // for blur_rows
   int blur_tiles = 0;
+  int* d_blur_prefix_v[3] = {nullptr, nullptr, nullptr};  // strips of 16, 32, 64 rows
+  int blur_tiles_v[3] = {0, 0, 0};
+  int blur_rows = BL_SR;
   int* d_bin_prefix = nullptr;
   int nbins = 0;
   int* d_det_prefix = nullptr;
@@ -68,6 +71,7 @@ struct gbt_ctx {
   bool use_graphs = false;
   cudaGraphExec_t graph[4] = {nullptr, nullptr, nullptr, nullptr};
   int launches_per_frame = 0;
+  int match_variant = 0;  // 0: thread per particle, 1: warp per particle
   std::string err;
   // scratch for stage dumps
   void* dump_buf = nullptr;
@@ -266,20 +270,26 @@ static int build(gbt_ctx* ctx, const gbt_config* cfgs, int nstreams) {
   }
   ctx->pyr_tiles[0] = pyr0.back();
   ctx->pyr_tiles[1] = pyr1.back();
-  std::vector<int> blur(1, 0), bins(1, 0), det(1, 0), bt(1, 0);
+  std::vector<int> bins(1, 0), det(1, 0), bt(1, 0);
+  for (int v = 0; v < 3; v++) {
+    const int sr = 16 << v;
+    std::vector<int> blur(1, 0);
+    for (auto& u : ctx->units) blur.push_back(blur.back() + ((u.H + sr - 1) / sr) * ((u.W + BL_OC - 1) / BL_OC));
+    ctx->blur_tiles_v[v] = blur.back();
+    if ((r = upload_table(ctx, &ctx->d_blur_prefix_v[v], blur))) return r;
+  }
+  ctx->d_blur_prefix = ctx->d_blur_prefix_v[2];
+  ctx->blur_tiles = ctx->blur_tiles_v[2];
   for (auto& u : ctx->units) {
-    blur.push_back(blur.back() + ((u.H + BL_SR - 1) / BL_SR) * ((u.W + BL_OC - 1) / BL_OC));
     bins.push_back(bins.back() + u.BH * u.BW);
     det.push_back(det.back() + ((u.TH + DT_R - 1) / DT_R) * ((u.TW + DT_C - 1) / DT_C));
     bt.push_back(bt.back() + u.birth_chunks);
   }
-  ctx->blur_tiles = blur.back();
   ctx->nbins = bins.back();
   ctx->det_blocks = det.back();
   if ((r = upload_table(ctx, &ctx->d_stream_unit0, su0))) return r;
   if ((r = upload_table(ctx, &ctx->d_pyr_prefix[0], pyr0))) return r;
   if ((r = upload_table(ctx, &ctx->d_pyr_prefix[1], pyr1))) return r;
-  if ((r = upload_table(ctx, &ctx->d_blur_prefix, blur))) return r;
   if ((r = upload_table(ctx, &ctx->d_bin_prefix, bins))) return r;
   if ((r = upload_table(ctx, &ctx->d_det_prefix, det))) return r;
   if ((r = upload_table(ctx, &ctx->d_btable, bt))) return r;
@@ -419,8 +429,23 @@ static int enqueue_frame(gbt_ctx* ctx, bool any_det, bool any_filt) {
     k_pyramid<<<ctx->pyr_tiles[1], 256, 0, st>>>(ctx->d_units, ctx->d_stream_unit0, ctx->d_pyr_prefix[1], nstreams, 5);
     n++;
   }
-  { PROF("k_blur"); k_blur<<<(ctx->blur_tiles + BL_WARPS - 1) / BL_WARPS, 32 * BL_WARPS, 0, st>>>(ctx->d_units, ctx->d_blur_prefix, nunits); }
-  { PROF("k_match"); k_match<<<ctx->nsm * 8, MATCH_BLOCK, 0, st>>>(ctx->d_units, ctx->d_state, ctx->d_frame, ctx->d_pre, nunits); }
+  {
+    PROF("k_blur");
+    const int nb = (ctx->blur_tiles + BL_WARPS - 1) / BL_WARPS;
+    if (ctx->blur_rows == 16)
+      k_blur<16><<<nb, 32 * BL_WARPS, 0, st>>>(ctx->d_units, ctx->d_blur_prefix, nunits);
+    else if (ctx->blur_rows == 32)
+      k_blur<32><<<nb, 32 * BL_WARPS, 0, st>>>(ctx->d_units, ctx->d_blur_prefix, nunits);
+    else
+      k_blur<64><<<nb, 32 * BL_WARPS, 0, st>>>(ctx->d_units, ctx->d_blur_prefix, nunits);
+  }
+  if (ctx->match_variant == 1) {
+    PROF("k_match_warp");
+    k_match_warp<<<ctx->nsm * 4, 32 * MW_WARPS, 0, st>>>(ctx->d_units, ctx->d_state, ctx->d_frame, ctx->d_pre, nunits);
+  } else {
+    PROF("k_match");
+    k_match<<<ctx->nsm * 8, MATCH_BLOCK, 0, st>>>(ctx->d_units, ctx->d_state, ctx->d_frame, ctx->d_pre, nunits);
+  }
   { PROF("k_stats"); k_stats<<<(ctx->nbins + 255) / 256, 256, 0, st>>>(ctx->d_units, ctx->d_state, ctx->d_bin_prefix, nunits); }
   n += 3;
   if (any_det) {
@@ -474,6 +499,44 @@ static int run_frame(gbt_ctx* ctx) {
   }
   ctx->host_frame++;
   return GBT_OK;
+}
+
+extern "C" int gbt_set_tuning(gbt_ctx* ctx, int32_t knob, int32_t value) {
+  if (!ctx) return GBT_E_INVALID;
+  auto drop_graphs = [&]() {
+    for (auto& g : ctx->graph)
+      if (g) {
+        cudaGraphExecDestroy(g);
+        g = nullptr;
+      }
+  };
+  if (knob == GBT_TUNE_MATCHER && (value == 0 || value == 1)) {
+    if (ctx->match_variant != value) drop_graphs();
+    ctx->match_variant = value;
+    return GBT_OK;
+  }
+  if (knob == GBT_TUNE_BLUR_ROWS && (value == 16 || value == 32 || value == 64)) {
+    const int v = value == 16 ? 0 : (value == 32 ? 1 : 2);
+    if (ctx->blur_rows != value) drop_graphs();
+    ctx->blur_rows = value;
+    ctx->d_blur_prefix = ctx->d_blur_prefix_v[v];
+    ctx->blur_tiles = ctx->blur_tiles_v[v];
+    return GBT_OK;
+  }
+  return GBT_E_INVALID;
+}
+
+extern "C" int gbt_get_tuning(gbt_ctx* ctx, int32_t knob, int32_t* value) {
+  if (!ctx || !value) return GBT_E_INVALID;
+  if (knob == GBT_TUNE_MATCHER) {
+    *value = ctx->match_variant;
+    return GBT_OK;
+  }
+  if (knob == GBT_TUNE_BLUR_ROWS) {
+    *value = ctx->blur_rows;
+    return GBT_OK;
+  }
+  return GBT_E_INVALID;
 }
 
 extern "C" int gbt_use_graphs(gbt_ctx* ctx, int32_t enable) {

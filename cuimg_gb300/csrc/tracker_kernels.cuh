@@ -97,7 +97,7 @@ __global__ void __launch_bounds__(256) k_pyramid(const Unit* __restrict__ units,
 // passes in registers, so each level pixel is read once and s1 / s2 are each
 // written once.  Lanes 0 and 31 only supply the horizontal halo; strips overlap
 // by 8 columns.
-constexpr int BL_SR = 64;                 // rows per strip
+constexpr int BL_SR = 64;                 // default rows per strip (tunable: 16, 32, 64)
 constexpr int BL_OC = 120;                // output columns per warp (lanes 1..30)
 constexpr int BL_WARPS = 8;
 
@@ -179,6 +179,7 @@ __device__ __forceinline__ void blur_row(const Unit& U, uint32_t w, int r, int r
   }
 }
 
+template <int SR>
 __global__ void __launch_bounds__(32 * BL_WARPS) k_blur(const Unit* __restrict__ units,
                                                         const int* __restrict__ item_prefix, int nunits) {
   const int lane = threadIdx.x & 31;
@@ -191,7 +192,7 @@ __global__ void __launch_bounds__(32 * BL_WARPS) k_blur(const Unit* __restrict__
   const int rs = local / ncs, cs = local % ncs;
   const int H = U.H, W = U.W;
   const int c0 = cs * BL_OC - 4 + 4 * lane;  // first column of this lane's word
-  const int r0 = rs * BL_SR, r1 = min(r0 + BL_SR, H);
+  const int r0 = rs * SR, r1 = min(r0 + SR, H);
   const bool out_lane = lane >= 1 && lane <= 30;
   int t1m2[4] = {0, 0, 0, 0}, t1m1[4] = {0, 0, 0, 0}, t10[4] = {0, 0, 0, 0};
   int t2m2[4] = {0, 0, 0, 0}, t2m1[4] = {0, 0, 0, 0}, t20[4] = {0, 0, 0, 0};
@@ -376,6 +377,149 @@ __global__ void __launch_bounds__(MATCH_BLOCK) k_match(const Unit* __restrict__ 
     if (sr != 0 || sc != 0) u.feat[b][i] = mf;
     atomicOr(&u.occ[bin_word(u, mr, mc)], bin_bit(mr, mc));
     atomicMax(&u.idx[(size_t)mr * u.W + mc], ((unsigned long long)stamp_match(f) << 32) | (unsigned)i);
+  }
+}
+
+// Warp-per-particle matcher variant (same results as k_match).  Four lanes
+// evaluate one sweep candidate (each gathers two s1 and two s2 ring samples),
+// so a whole sweep -- up to 8 candidates -- is one round of gathers whose lanes
+// share rows and therefore L1 sectors, and the warp never waits on another
+// particle's longer descent.  The order of the sweep and the strict "<" keep
+// gradient_descent_match's first-best-in-sweep-order semantics.
+constexpr int MW_WARPS = 8;
+
+struct LaneRing {  // the lane's two s1 and two s2 ring offsets (ring index q and q + 4)
+  int s1a, s1b, s2a, s2b;
+};
+
+__device__ __forceinline__ int warp_eval(const Unit& u, const uint8_t* s1, const uint8_t* s2, const LaneRing& o,
+                                         const uint4& f, int q, int r, int c, bool with_s1, bool active) {
+  int d = 0;
+  if (active) {
+    const ptrdiff_t off = (ptrdiff_t)r * u.fpitch + c;
+    const int fa2 = (q < 4 ? (f.z >> (8 * q)) : (f.w >> (8 * (q - 4)))) & 255;  // s2 ring q
+    const int fb2 = (f.w >> (8 * q)) & 255;                                      // s2 ring q + 4
+    d = abs((int)__ldg(s2 + off + o.s2a) - fa2) + abs((int)__ldg(s2 + off + o.s2b) - fb2);
+    if (with_s1) {
+      const int fa1 = (f.x >> (8 * q)) & 255, fb1 = (f.y >> (8 * q)) & 255;
+      d += abs((int)__ldg(s1 + off + o.s1a) - fa1) + abs((int)__ldg(s1 + off + o.s1b) - fb1);
+    }
+  }
+  d += __shfl_xor_sync(0xffffffffu, d, 1);
+  d += __shfl_xor_sync(0xffffffffu, d, 2);
+  return d;  // every lane of the 4-lane group holds its candidate's distance
+}
+
+__global__ void __launch_bounds__(32 * MW_WARPS) k_match_warp(const Unit* __restrict__ units, UState* __restrict__ st,
+                                                              const Frame* __restrict__ fr,
+                                                              const int* __restrict__ table, int nunits) {
+  const int f = fr->f;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int cand = lane >> 2, q = lane & 3;
+  const int total = table[nunits];
+  for (int g = blockIdx.x; g < total; g += gridDim.x) {
+    ChunkCursor cc = chunk_of(table, nunits, g);
+    const Unit& u = units[cc.unit];
+    const UState s = st[cc.unit];
+    const int b = s.cur;
+    const uint8_t* s1 = fptr(u.s1, u.fpitch, 0, 0);
+    const uint8_t* s2 = fptr(u.s2, u.fpitch, 0, 0);
+    LaneRing o;
+    o.s1a = c_ring[2 * q][0] * u.fpitch + c_ring[2 * q][1];
+    o.s1b = c_ring[2 * (q + 4)][0] * u.fpitch + c_ring[2 * (q + 4)][1];
+    o.s2a = 2 * o.s1a;
+    o.s2b = 2 * o.s1b;
+    for (int k = warp; k < CHUNK; k += MW_WARPS) {
+      const int i = cc.chunk * CHUNK + k;
+      if (i >= s.n) break;
+      const unsigned short age = u.age[b][i];
+      if (age == 0) continue;
+      const short2 pos = u.pos[b][i];
+      const short2 spd = u.spd[b][i];
+      const int pr = (short)(pos.x + (age == 1 ? 0 : spd.x)), pc = (short)(pos.y + (age == 1 ? 0 : spd.y));
+      if (!in_dom(u, pr, pc)) {
+        if (lane == 0) u.age[b][i] = 0;
+        continue;
+      }
+      const uint4 feat = u.feat[b][i];
+      int mr = pr, mc = pc;
+      for (int desc = 0; desc < 2; desc++) {
+        const bool with_s1 = desc == 1;
+        int predr = mr, predc = mc;
+        // First distance: always s1 + s2 (lanes 0..3).
+        int best = __shfl_sync(0xffffffffu, warp_eval(u, s1, s2, o, feat, q, predr, predc, true, cand == 0), 0);
+        int mi = 8;
+        for (int search = 0; search < 10; search++) {
+          const int start = c_c8it[mi][0], end = c_c8it[mi][1];
+          const int m = ((end - start + 7) & 7) + 1;  // sweep length: 8 when start == end
+          const int pos_in_sweep = (cand - start + 8) & 7;
+          const bool in_sweep = pos_in_sweep < m;
+          const int nr = predr + c_c8[cand][0], nc = predc + c_c8[cand][1];
+          const bool ok = in_sweep && in_dom(u, nr, nc);
+          const int d = warp_eval(u, s1, s2, o, feat, q, nr, nc, with_s1, ok);
+          // Sequential compare in sweep order (identical on every lane).
+          int nmr = mr, nmc = mc, nmi = mi, nbest = best;
+          for (int t = 0; t < m; t++) {
+            const int cidx = (start + t) & 7;
+            const int dc = __shfl_sync(0xffffffffu, d, 4 * cidx);
+            const bool okc = __shfl_sync(0xffffffffu, ok, 4 * cidx);
+            if (okc && dc < nbest) {
+              nbest = dc;
+              nmr = predr + c_c8[cidx][0];
+              nmc = predc + c_c8[cidx][1];
+              nmi = cidx;
+            }
+          }
+          mr = nmr;
+          mc = nmc;
+          mi = nmi;
+          best = nbest;
+          if ((predr == mr && predc == mc) || !in_dom(u, mr, mc)) break;
+          predr = mr;
+          predc = mc;
+        }
+      }
+      // Feature at the match (lanes 0..3 hold it), acceptance and move.
+      uint32_t x = 0, y = 0, z = 0, w = 0;
+      if (cand == 0) {
+        const ptrdiff_t off = (ptrdiff_t)mr * u.fpitch + mc;
+        x = (uint32_t)__ldg(s1 + off + o.s1a) << (8 * q);
+        y = (uint32_t)__ldg(s1 + off + o.s1b) << (8 * q);
+        z = (uint32_t)__ldg(s2 + off + o.s2a) << (8 * q);
+        w = (uint32_t)__ldg(s2 + off + o.s2b) << (8 * q);
+      }
+      x |= __shfl_xor_sync(0xffffffffu, x, 1);
+      y |= __shfl_xor_sync(0xffffffffu, y, 1);
+      z |= __shfl_xor_sync(0xffffffffu, z, 1);
+      w |= __shfl_xor_sync(0xffffffffu, w, 1);
+      x |= __shfl_xor_sync(0xffffffffu, x, 2);
+      y |= __shfl_xor_sync(0xffffffffu, y, 2);
+      z |= __shfl_xor_sync(0xffffffffu, z, 2);
+      w |= __shfl_xor_sync(0xffffffffu, w, 2);
+      if (lane == 0) {
+        const uint4 mf = make_uint4(x, y, z, w);
+        unsigned n_diff = 0;
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+          int a = (feat.z >> (8 * j)) & 255, c = (mf.z >> (8 * j)) & 255;
+          if (abs(a - c) > u.k) n_diff++;
+          a = (feat.w >> (8 * j)) & 255;
+          c = (mf.w >> (8 * j)) & 255;
+          if (abs(a - c) > u.k) n_diff++;
+        }
+        if (n_diff >= 4u || contrast_at(u, mr, mc) < 3) {
+          u.age[b][i] = 0;
+        } else {
+          const int sr = mr - pos.x, sc = mc - pos.y;  // = pred - pos + delta
+          u.age[b][i] = (unsigned short)(age + 1);
+          u.spd[b][i] = make_short2((short)sr, (short)sc);
+          u.pos[b][i] = make_short2((short)mr, (short)mc);
+          if (sr != 0 || sc != 0) u.feat[b][i] = mf;
+          atomicOr(&u.occ[bin_word(u, mr, mc)], bin_bit(mr, mc));
+          atomicMax(&u.idx[(size_t)mr * u.W + mc], ((unsigned long long)stamp_match(f) << 32) | (unsigned)i);
+        }
+      }
+    }
   }
 }
 
@@ -964,11 +1108,28 @@ __global__ void __launch_bounds__(CHUNK) k_merge_scatter(const Unit* __restrict_
   }
 }
 
+// Liveness of the particles a batch of actives touches, in a shared-memory
+// open-addressing table (key = slot + 1, top bit = killed).  Falls back to the
+// global age array when the table would overflow.
+constexpr int MR_NB = 512;      // actives per batch
+constexpr int MR_HASH = 4096;   // table slots (power of two)
+
+__device__ __forceinline__ int mr_find(unsigned* tab, unsigned key) {
+  unsigned h = (key * 2654435761u) & (MR_HASH - 1);
+  for (int probe = 0; probe < MR_HASH; probe++) {
+    unsigned k = tab[h] & 0x7fffffffu;
+    if (k == key || k == 0) return (int)h;
+    h = (h + 1) & (MR_HASH - 1);
+  }
+  return -1;
+}
+
 __global__ void __launch_bounds__(256) k_merge_resolve(const Unit* __restrict__ units, const UState* __restrict__ st,
                                                        const Frame* __restrict__ fr) {
-  constexpr int NB = 1024;
-  __shared__ int4 ent[NB];
-  __shared__ int cnd[NB][8];
+  __shared__ int4 ent[MR_NB];
+  __shared__ int cnd[MR_NB][8];
+  __shared__ unsigned tab[MR_HASH];
+  __shared__ int tab_fill, tab_over;
   const int ui = blockIdx.x;
   const Unit& u = units[ui];
   const int f = fr->f;
@@ -976,33 +1137,81 @@ __global__ void __launch_bounds__(256) k_merge_resolve(const Unit* __restrict__ 
   const UState s = st[ui];
   unsigned short* age = u.age[s.cur];
   const int lane = threadIdx.x & 31;
-  for (int base = 0; base < s.A; base += NB) {
-    const int nb = min(NB, s.A - base);
+  for (int base = 0; base < s.A; base += MR_NB) {
+    const int nb = min(MR_NB, s.A - base);
+    for (int k = threadIdx.x; k < MR_HASH; k += blockDim.x) tab[k] = 0;
+    if (threadIdx.x == 0) {
+      tab_fill = 0;
+      tab_over = 0;
+    }
+    __syncthreads();
     for (int k = threadIdx.x; k < nb; k += blockDim.x) {
       int4 e = u.act_list[base + k];
       ent[k] = e;
       for (int q = 0; q < e.z; q++) cnd[k][q] = u.act_cand[(size_t)(base + k) * 8 + q];
     }
     __syncthreads();
+    // Register every touched slot with its current liveness (killed bit set
+    // when an earlier batch already killed it).
+    for (int k = threadIdx.x; k < nb; k += blockDim.x) {
+      const int4 e = ent[k];
+      for (int q = -1; q < e.z; q++) {
+        const unsigned slot = (unsigned)(q < 0 ? e.x : cnd[k][q]);
+        const unsigned key = slot + 1u;
+        if (atomicAdd(&tab_fill, 1) >= MR_HASH / 2) {
+          tab_over = 1;
+          continue;
+        }
+        unsigned h = (key * 2654435761u) & (MR_HASH - 1);
+        for (int probe = 0; probe < MR_HASH; probe++) {
+          unsigned prev = atomicCAS(&tab[h], 0u, key | (age[slot] == 0 ? 0x80000000u : 0u));
+          if (prev == 0 || (prev & 0x7fffffffu) == key) break;
+          h = (h + 1) & (MR_HASH - 1);
+        }
+      }
+    }
+    __syncthreads();
+    const bool smem = !tab_over;
     if (threadIdx.x < 32) {
       for (int g0 = 0; g0 < nb; g0 += 32) {
         const int k = g0 + lane;
         const bool valid = k < nb;
-        int4 e = valid ? ent[k] : make_int4(-1, 0, 0, 0);
+        const int4 e = valid ? ent[k] : make_int4(-1, 0, 0, 0);
         const int pr = (short)((unsigned)e.y >> 16), pc = (short)((unsigned)e.y & 0xffffu);
-        bool conflict = false;
+        // Earlier lanes whose candidate sets may meet this lane's (within 2 px).
+        unsigned before = 0;
         for (int o = 0; o < 32; o++) {
           int qr = __shfl_sync(0xffffffffu, pr, o), qc = __shfl_sync(0xffffffffu, pc, o);
           bool ov = __shfl_sync(0xffffffffu, valid, o);
-          if (o < lane && ov && valid && abs(qr - pr) <= 2 && abs(qc - pc) <= 2) conflict = true;
+          if (o < lane && ov && valid && abs(qr - pr) <= 2 && abs(qc - pc) <= 2) before |= 1u << o;
         }
-        const bool serial = __any_sync(0xffffffffu, conflict);
-        for (int step = 0; step < (serial ? 32 : 1); step++) {
-          if (valid && (!serial || lane == step)) {
-            if (*(volatile unsigned short*)&age[e.x] != 0) {
+        // Wavefronts: a lane decides once no earlier unresolved lane conflicts.
+        unsigned pending = __ballot_sync(0xffffffffu, valid);
+        while (pending) {
+          const bool mine = (pending >> lane) & 1u;
+          const bool ready = mine && !(before & pending);
+          if (ready) {
+            bool alive;
+            int hs = -1;
+            if (smem) {
+              hs = mr_find(tab, (unsigned)e.x + 1u);
+              alive = !(tab[hs] & 0x80000000u);
+            } else {
+              alive = *(volatile unsigned short*)&age[e.x] != 0;
+            }
+            if (alive) {
               for (int q = 0; q < e.z; q++) {
-                int j = cnd[k][q];
-                if (*(volatile unsigned short*)&age[j] != 0) {
+                const int j = cnd[k][q];
+                bool jalive;
+                int hj = -1;
+                if (smem) {
+                  hj = mr_find(tab, (unsigned)j + 1u);
+                  jalive = !(tab[hj] & 0x80000000u);
+                } else {
+                  jalive = *(volatile unsigned short*)&age[j] != 0;
+                }
+                if (jalive) {
+                  if (smem) tab[hj] |= 0x80000000u;
                   age[j] = 0;
                   break;
                 }
@@ -1010,6 +1219,7 @@ __global__ void __launch_bounds__(256) k_merge_resolve(const Unit* __restrict__ 
             }
           }
           __syncwarp();
+          pending &= ~__ballot_sync(0xffffffffu, ready);
         }
       }
     }

@@ -238,6 +238,14 @@ class BatchTracker:
         check(self._lib.gbt_stream(self._ensure(), ctypes.byref(p)), self._ctx)
         return p.value
 
+    def set_tuning(self, knob, value):
+        check(self._lib.gbt_set_tuning(self._ensure(), knob, value), self._ctx)
+
+    def get_tuning(self, knob):
+        v = ctypes.c_int32()
+        check(self._lib.gbt_get_tuning(self._ensure(), knob, ctypes.byref(v)), self._ctx)
+        return v.value
+
     def kernels_per_frame(self):
         n = ctypes.c_int32()
         check(self._lib.gbt_kernels_per_frame(self._ensure(), ctypes.byref(n)), self._ctx)

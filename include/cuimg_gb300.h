@@ -138,6 +138,17 @@ int gbt_read_counts(gbt_ctx* ctx, int32_t* counts, int32_t n);
 /* Frame counter of (stream, scale) (generic_strategy::frame_cpt_). */
 int gbt_frame_count(gbt_ctx* ctx, int32_t stream, int32_t scale, int32_t* n);
 
+/* Tuning knobs (results are identical for every setting; only speed
+ * changes).  GBT_TUNE_MATCHER: 0 = one thread per particle, 1 = one warp per
+ * particle with the sweep candidates spread over its lanes.
+ * GBT_TUNE_BLUR_ROWS: height of the strip one warp walks in the BC2S blur.  The package's
+ * autotuner (cuimg_gb300/autotune.py) times the settings on the caller's
+ * workload and caches the winner. */
+#define GBT_TUNE_MATCHER 0
+#define GBT_TUNE_BLUR_ROWS 1   /* rows per warp strip of the BC2S blur: 16, 32 or 64 */
+int gbt_set_tuning(gbt_ctx* ctx, int32_t knob, int32_t value);
+int gbt_get_tuning(gbt_ctx* ctx, int32_t knob, int32_t* value);
+
 /* Per-stage launch counters and device time of the last frame (for tests
  * and the benchmark): number of kernel launches issued per frame. */
 int gbt_kernels_per_frame(gbt_ctx* ctx, int32_t* n);
@@ -211,6 +222,27 @@ int gbt_lk_track_batch(const void* prev, const void* cur, int64_t pitch, int64_t
                        int32_t cols, int32_t is_u8, int32_t nlevels, const gbt_lk_params* params,
                        int32_t npairs, const float* pts, int32_t npts, float* out, int32_t* status,
                        float* err, void* stream);
+
+/* ------------------------------------------------------------------------
+ * Differentiable LK residual and its adjoint (new: the reference has no
+ * gradients).  Forward per point: the translational LK of
+ * iterative_lk_match_5x5 (cuimg/tracking2/pyrlk_tracker.hpp:165-334) made
+ * differentiable -- sigma-1 Gaussian pyramids of both fp32 frames, Sobel/8
+ * gradients, the full window, exactly `iters` Gauss-Newton steps per level,
+ * coarse-to-fine from the initial flow u0 (level-0 pixels) -- and
+ * loss = sum over the level-0 window of (I0-level(p + o) - I1-level(v + o))^2
+ * at the final position v.  The backward pass recomputes the pyramids
+ * (nothing is kept between the two calls) and returns the gradients of
+ * sum_i dloss_i * loss_i with respect to I0, I1 (dense npairs x rows x cols)
+ * and u0.  Image and point layouts as gbt_lk_track_batch (fp32 only). */
+int64_t gbt_lkd_scratch_bytes(int32_t rows, int32_t cols, int32_t nlevels, int32_t npairs);
+int gbt_lkd_forward(const float* I0, const float* I1, int64_t pitch, int64_t img_bytes, int32_t rows, int32_t cols,
+                    int32_t nlevels, int32_t window, int32_t iters, int32_t npairs, const float* pts,
+                    const float* u0, int32_t npts, float* loss, float* vfinal, void* stream);
+int gbt_lkd_backward(const float* I0, const float* I1, int64_t pitch, int64_t img_bytes, int32_t rows,
+                     int32_t cols, int32_t nlevels, int32_t window, int32_t iters, int32_t npairs,
+                     const float* pts, const float* u0, int32_t npts, const float* dloss, float* dI0,
+                     float* dI1, float* du0, void* stream);
 
 /* Allocation-free variant of gbt_lk_track_batch (no counterpart in the
  * reference).  For callers that must not allocate device memory (their own

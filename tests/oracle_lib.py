@@ -112,3 +112,39 @@ def lk_track(prev, cur, pts, nlevels, pyr=0, window=11, npix=25, max_iter=30, ep
     assert lib.oracle_lk_track(A.ctypes.data, B.ctypes.data, H, W, nlevels, pyr, window, npix, max_iter, eps, max_err,
                                p.ctypes.data, n, out.ctypes.data, st.ctypes.data, er.ctypes.data) == 0
     return out, st, er
+
+
+def lkd_forward64(I0, I1, pts, u0, L, window, iters):
+    lib = oracle()
+    if not getattr(lib, "_lkd_typed", False):
+        lib.oracle_lkd_forward.argtypes = [ctypes.c_void_p, ctypes.c_void_p] + [ctypes.c_int] * 5 + [
+            ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]
+        lib.oracle_lkd_grad_fd.argtypes = [ctypes.c_void_p, ctypes.c_void_p] + [ctypes.c_int] * 5 + [
+            ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_double] + [ctypes.c_void_p] * 3
+        lib._lkd_typed = True
+    a = np.ascontiguousarray(I0, np.float64)
+    b = np.ascontiguousarray(I1, np.float64)
+    p = np.ascontiguousarray(pts, np.float64)
+    u = np.ascontiguousarray(u0, np.float64)
+    n = len(p)
+    loss = np.zeros(n)
+    vf = np.zeros((n, 2))
+    H, W = a.shape
+    lib.oracle_lkd_forward(a.ctypes.data, b.ctypes.data, H, W, L, window, iters, p.ctypes.data, u.ctypes.data, n,
+                           loss.ctypes.data, vf.ctypes.data)
+    return loss, vf
+
+
+def lkd_grad_fd64(I0, I1, pts, u0, L, window, iters, wts, h=1e-3):
+    lkd_forward64(I0[:16, :16] * 0 + 1, I1[:16, :16] * 0 + 1, pts[:0], u0[:0], 1, 3, 0)  # declares types
+    lib = oracle()
+    a = np.ascontiguousarray(I0, np.float64)
+    b = np.ascontiguousarray(I1, np.float64)
+    p = np.ascontiguousarray(pts, np.float64)
+    u = np.ascontiguousarray(u0, np.float64)
+    w = np.ascontiguousarray(wts, np.float64)
+    H, W = a.shape
+    g0, g1, gu = np.zeros((H, W)), np.zeros((H, W)), np.zeros_like(u)
+    lib.oracle_lkd_grad_fd(a.ctypes.data, b.ctypes.data, H, W, L, window, iters, p.ctypes.data, u.ctypes.data,
+                           len(p), w.ctypes.data, h, g0.ctypes.data, g1.ctypes.data, gu.ctypes.data)
+    return g0, g1, gu

@@ -46,10 +46,12 @@ def test_gpu_matches_reference_golden(case):
     tr.close()
 
 
-def _compare_run(rows, cols, L, n, seed, detf=10, filtf=1, graphs=False):
+def _compare_run(rows, cols, L, n, seed, detf=10, filtf=1, graphs=False, matcher=None):
     from cuimg_gb300 import synth
     frames = synth.frames(seed, rows, cols, n)
     tr = _gpu_tracker(rows, cols, L, 20, detf, filtf, graphs)
+    if matcher is not None:
+        tr.set_tuning(0, matcher)
     o = tracker_oracle(rows, cols, L, 20, detf, filtf)
     for t in range(n):
         tr.run(frames[t])
@@ -76,6 +78,11 @@ def test_gpu_matches_oracle_1080p():
     # The headline geometry: 1920x1080, 4 scales, detector every 10 frames.
     total = _compare_run(1080, 1920, 4, 12, 5, 10)
     assert total > 50000
+
+
+@pytest.mark.parametrize("matcher", [0, 1])
+def test_matcher_variants_match_oracle(matcher):
+    _compare_run(480, 640, 3, 14, 6, detf=5, matcher=matcher)
 
 
 def test_graph_replay_matches_oracle():
