@@ -17,7 +17,7 @@ from ._native import check, cuda_lib
 
 KNOBS = {
     # knob id: (name, settings, kernel names whose time decides)
-    0: ("matcher", (0, 1), ("k_match", "k_match_warp")),
+    0: ("matcher", (0, 1, 2), ("k_match", "k_match_warp")),
     1: ("blur_rows", (16, 32, 64), ("k_blur",)),
 }
 DEFAULT_CACHE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "_build", "autotune.json")

@@ -11,9 +11,16 @@
 //
 // Filter: row pass then column pass (meta_convolve_row2d / col2d,
 // cuimg/gpu/meta_convolve.h:131-161,288-314) with clamp-to-edge sampling,
-// fused in one kernel: a CTA stages a (32 + 2R) x (64 + 2R) input tile in shared
-// memory, runs the row pass into a second shared tile and the column pass into
-// registers, so each image is read from and written to HBM once (8 B/pixel).
+// fused in one kernel so each image is read from and written to HBM once
+// (8 B/pixel).  k_gauss_strip (radius 2, 3, 6, 9, 12): a CTA walks down a
+// 128-column strip, 16 input rows at a time; cp.async stages the next rows in
+// shared memory while the row pass computes four adjacent outputs per thread
+// from 16-byte shared loads, and each thread runs the column pass of its own
+// column from a register window of the last 2R + 1 row-pass values, so the
+// column pass reads no shared memory at all.  k_gauss (any other radius) is
+// the plain tile version: (32 + 2R) x (64 + 2R) input tile, row pass into a
+// second shared tile, column pass from it.  Both accumulate the taps in the
+// same order (x, then y, ascending from -R) and give the same bits.
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -82,6 +89,129 @@ __global__ void __launch_bounds__(256) k_gauss(const float* __restrict__ in, lon
       for (int y = 0; y <= 2 * RR; y++) acc = fmaf(p[y * (TC + 1)], taps.w[y], acc);
     }
     ((float*)((char*)dst + gr * out_pitch))[gc] = acc;
+  }
+}
+
+__device__ __forceinline__ void cp_async4(void* sdst, const void* gsrc) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(sdst);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(s), "l"(gsrc) : "memory");
+}
+__device__ __forceinline__ void cp_async16(void* sdst, const void* gsrc) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(sdst);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gsrc) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}
+
+constexpr int SC = 128;  // strip width = threads per CTA
+constexpr int RB = 16;   // input rows per batch
+
+// Grid (strips, row segments, images); a segment is `SR` output rows, which
+// need SR + 2R input rows (clamped at the image edges).  The staged row holds
+// image columns C0 - RA .. C0 + SC + RA - 1 with RA = R rounded up to a
+// multiple of 4, so interior strips of a 16-byte aligned image are staged with
+// 16-byte copies; edge strips (and unaligned images) copy clamped floats.
+template <int R>
+__global__ void __launch_bounds__(SC) k_gauss_strip(const float* __restrict__ in, long long in_pitch, long long in_img,
+                                                    float* __restrict__ out, long long out_pitch, long long out_img,
+                                                    int H, int W, int SR, Taps taps) {
+  constexpr int NW = 2 * R + 1;              // taps
+  constexpr int RA = (R + 3) / 4 * 4;        // staged halo
+  constexpr int OFF = RA - R;                // staged index of column C0 - R
+  constexpr int LW = SC + 2 * RA;            // staged row length (16-byte multiple)
+  constexpr int CH = LW / 4;                 // 16-byte chunks per staged row
+  constexpr int NV = (OFF + 3 + 2 * R) / 4 + 1;  // float4 reads per quad of row-pass outputs
+  static_assert(4 * (SC / 4 - 1) + 4 * NV <= LW, "row pass reads stay inside the staged row");
+  __shared__ __align__(16) float tin[2][RB][LW];
+  __shared__ __align__(16) float th[RB][SC];
+  const float* src = (const float*)((const char*)in + blockIdx.z * in_img);
+  float* dst = (float*)((char*)out + blockIdx.z * out_img);
+  const int t = threadIdx.x;
+  const int C0 = blockIdx.x * SC, R0 = blockIdx.y * SR;
+  const int nout = min(SR, H - R0);
+  const int nin = nout + 2 * R;  // segment input row k is image row R0 - R + k
+  const int nb = (nin + RB - 1) / RB;
+  const bool vec = ((((unsigned long long)src) | (unsigned long long)in_pitch) & 15) == 0 && C0 - RA >= 0 &&
+                   C0 + SC + RA <= W;
+
+  auto issue = [&](int b) {
+    float(*buf)[LW] = tin[b & 1];
+    if (vec) {
+      for (int v = t; v < RB * CH; v += SC) {
+        const int i = v / CH, ch = v % CH;
+        const int gr = min(max(R0 - R + b * RB + i, 0), H - 1);
+        cp_async16(&buf[i][4 * ch], (const float*)((const char*)src + gr * in_pitch) + C0 - RA + 4 * ch);
+      }
+    } else {
+#pragma unroll 4
+      for (int i = 0; i < RB; i++) {
+        const int gr = min(max(R0 - R + b * RB + i, 0), H - 1);
+        const float* row = (const float*)((const char*)src + gr * in_pitch);
+        for (int c = t; c < LW; c += SC) cp_async4(&buf[i][c], row + min(max(C0 - RA + c, 0), W - 1));
+      }
+    }
+    cp_async_commit();
+  };
+
+  float win[NW];  // win[NW - 1] is the newest row-pass value of this thread's column
+#pragma unroll
+  for (int y = 0; y < NW; y++) win[y] = 0.f;
+  issue(0);
+  for (int b = 0; b < nb; b++) {
+    if (b + 1 < nb) {
+      issue(b + 1);  // into the buffer whose row pass finished before the last barrier
+      cp_async_wait<1>();
+    } else {
+      cp_async_wait<0>();
+    }
+    __syncthreads();
+    // Row pass: RB rows x 32 quads, four outputs per quad.
+#pragma unroll
+    for (int it = 0; it < RB * (SC / 4) / SC; it++) {
+      const int item = t + it * SC, i = item / (SC / 4), q = item % (SC / 4);
+      const float4* p4 = reinterpret_cast<const float4*>(&tin[b & 1][i][4 * q]);
+      float v[4 * NV];
+#pragma unroll
+      for (int k = 0; k < NV; k++) {
+        const float4 f = p4[k];
+        v[4 * k] = f.x;
+        v[4 * k + 1] = f.y;
+        v[4 * k + 2] = f.z;
+        v[4 * k + 3] = f.w;
+      }
+      float a0 = 0.f, a1 = 0.f, a2 = 0.f, a3 = 0.f;
+#pragma unroll
+      for (int x = 0; x < NW; x++) {
+        a0 = fmaf(v[OFF + x], taps.w[x], a0);
+        a1 = fmaf(v[OFF + x + 1], taps.w[x], a1);
+        a2 = fmaf(v[OFF + x + 2], taps.w[x], a2);
+        a3 = fmaf(v[OFF + x + 3], taps.w[x], a3);
+      }
+      *reinterpret_cast<float4*>(&th[i][4 * q]) = make_float4(a0, a1, a2, a3);
+    }
+    __syncthreads();
+    // Column pass from the register window.  The shift is unconditional (rows
+    // past the segment are clamped copies and only skip their store), so the
+    // unrolled batch renames registers instead of moving them.
+    // Rows i in [lo, hi) of this batch complete an output row.
+    const int lo = max(0, 2 * R - b * RB), hi = C0 + t < W ? min(RB, nin - b * RB) : 0;
+    char* orow = (char*)(dst + C0 + t) + (long long)(R0 - 2 * R + b * RB) * out_pitch;
+#pragma unroll
+    for (int i = 0; i < RB; i++) {
+#pragma unroll
+      for (int y = 0; y < NW - 1; y++) win[y] = win[y + 1];
+      win[NW - 1] = th[i][t];
+      if (i >= lo) {
+        float acc = 0.f;
+#pragma unroll
+        for (int y = 0; y < NW; y++) acc = fmaf(win[y], taps.w[y], acc);
+        if (i < hi) *(float*)orow = acc;
+      }
+      orow += out_pitch;
+    }
   }
 }
 
@@ -165,6 +295,39 @@ static int launch_gauss(const float* in, long long in_pitch, long long in_img, f
   int R;
   int r = gbt_gaussian_taps(sigma, t.w, &R);
   if (r) return r;
+  auto strip = [&](auto kern) {
+    // Segments per strip: minimise (waves of CTAs) x (rows a CTA stages), so
+    // that the last wave is not a sliver and the halo rows stay a small share.
+    static int sms = 0, per_sm[32] = {};
+    if (!sms) {
+      int dev = 0;
+      cudaGetDevice(&dev);
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    }
+    if (!per_sm[R]) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm[R], kern, SC, 0);
+    const long long slots = (long long)(sms > 0 ? sms : 152) * (per_sm[R] > 0 ? per_sm[R] : 1);
+    const long long M = (long long)((cols + SC - 1) / SC) * nimg;
+    int best_s = 1;
+    long long best = -1;
+    for (int sg = 1; sg <= (rows + 15) / 16; sg++) {
+      const int SR = (rows + sg - 1) / sg;
+      if (sg > 1 && (rows + SR - 1) / SR != sg) continue;
+      const long long cost = ((M * sg + slots - 1) / slots) * (long long)(SR + 2 * R);
+      if (best < 0 || cost < best) best = cost, best_s = sg;
+    }
+    const int SR = (rows + best_s - 1) / best_s;
+    dim3 g((cols + SC - 1) / SC, (rows + SR - 1) / SR, nimg);
+    kern<<<g, SC, 0, st>>>(in, in_pitch, in_img, out, out_pitch, out_img, rows, cols, SR, t);
+    return cudaGetLastError() == cudaSuccess ? GBT_OK : GBT_E_CUDA;
+  };
+  switch (R) {
+    case 2: return strip(k_gauss_strip<2>);
+    case 3: return strip(k_gauss_strip<3>);
+    case 6: return strip(k_gauss_strip<6>);
+    case 9: return strip(k_gauss_strip<9>);
+    case 12: return strip(k_gauss_strip<12>);
+    default: break;
+  }
   const int tiles = ((rows + TR - 1) / TR) * ((cols + TC - 1) / TC);
   dim3 grid(tiles, nimg);
   size_t sm = (size_t)((TR + 2 * R) * (TC + 2 * R + 1) + (TR + 2 * R) * (TC + 1)) * sizeof(float);
@@ -172,13 +335,7 @@ static int launch_gauss(const float* in, long long in_pitch, long long in_img, f
     if (sm > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     kern<<<grid, 256, sm, st>>>(in, in_pitch, in_img, out, out_pitch, out_img, rows, cols, tiles, t, R);
   };
-  switch (R) {
-    case 2: go(k_gauss<2>); break;
-    case 3: go(k_gauss<3>); break;
-    case 6: go(k_gauss<6>); break;
-    case 12: go(k_gauss<12>); break;
-    default: go(k_gauss<0>); break;
-  }
+  go(k_gauss<0>);
   return cudaGetLastError() == cudaSuccess ? GBT_OK : GBT_E_CUDA;
 }
 

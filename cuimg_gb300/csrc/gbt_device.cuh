@@ -27,6 +27,9 @@ namespace gbt {
 constexpr int RB = 8;    // rows of zero border around s1/s2
 constexpr int CB = 16;   // columns of zero border around s1/s2
 constexpr int CHUNK = 1024;  // particle slots per compaction chunk
+// s1/s2 row pitch of every unit whose bordered width fits: a compile-time
+// pitch turns the matcher's ring offsets into load immediates.
+constexpr int FIXED_FPITCH = 4096;
 
 struct Unit {
   int H, W;

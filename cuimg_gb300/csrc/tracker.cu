@@ -71,7 +71,8 @@ struct gbt_ctx {
   bool use_graphs = false;
   cudaGraphExec_t graph[4] = {nullptr, nullptr, nullptr, nullptr};
   int launches_per_frame = 0;
-  int match_variant = 0;  // 0: thread per particle, 1: warp per particle
+  int match_variant = 0;  // GBT_TUNE_MATCHER
+  bool fixed_fpitch = true;  // every unit's s1/s2 pitch is FIXED_FPITCH
   std::string err;
   // scratch for stage dumps
   void* dump_buf = nullptr;
@@ -221,7 +222,8 @@ static int build(gbt_ctx* ctx, const gbt_config* cfgs, int nstreams) {
     woff += nb;
     u.ipitch = round_up(u.W, 64);
     if ((r = dalloc(ctx, (void**)&u.img, (size_t)u.ipitch * u.H, true))) return r;
-    u.fpitch = round_up(u.W + 2 * CB, 64);
+    u.fpitch = u.W + 2 * CB <= FIXED_FPITCH ? FIXED_FPITCH : round_up(u.W + 2 * CB, 64);
+    if (u.fpitch != FIXED_FPITCH) ctx->fixed_fpitch = false;
     if ((r = dalloc(ctx, (void**)&u.s1, (size_t)u.fpitch * (u.H + 2 * RB), true))) return r;
     if ((r = dalloc(ctx, (void**)&u.s2, (size_t)u.fpitch * (u.H + 2 * RB), true))) return r;
     if ((r = dalloc_t(ctx, &u.idx, (size_t)u.H * u.W))) return r;
@@ -444,7 +446,12 @@ static int enqueue_frame(gbt_ctx* ctx, bool any_det, bool any_filt) {
     k_match_warp<<<ctx->nsm * 4, 32 * MW_WARPS, 0, st>>>(ctx->d_units, ctx->d_state, ctx->d_frame, ctx->d_pre, nunits);
   } else {
     PROF("k_match");
-    k_match<<<ctx->nsm * 8, MATCH_BLOCK, 0, st>>>(ctx->d_units, ctx->d_state, ctx->d_frame, ctx->d_pre, nunits);
+    const dim3 g(ctx->nsm * 8);
+    if (ctx->match_variant == 0 && ctx->fixed_fpitch)
+      k_match<FeatFP<FIXED_FPITCH>>
+          <<<g, MATCH_BLOCK, 0, st>>>(ctx->d_units, ctx->d_state, ctx->d_frame, ctx->d_pre, nunits);
+    else
+      k_match<Feat><<<g, MATCH_BLOCK, 0, st>>>(ctx->d_units, ctx->d_state, ctx->d_frame, ctx->d_pre, nunits);
   }
   { PROF("k_stats"); k_stats<<<(ctx->nbins + 255) / 256, 256, 0, st>>>(ctx->d_units, ctx->d_state, ctx->d_bin_prefix, nunits); }
   n += 3;
@@ -510,7 +517,7 @@ extern "C" int gbt_set_tuning(gbt_ctx* ctx, int32_t knob, int32_t value) {
         g = nullptr;
       }
   };
-  if (knob == GBT_TUNE_MATCHER && (value == 0 || value == 1)) {
+  if (knob == GBT_TUNE_MATCHER && value >= 0 && value <= 2) {
     if (ctx->match_variant != value) drop_graphs();
     ctx->match_variant = value;
     return GBT_OK;

@@ -257,32 +257,105 @@ struct Feat {
   }
 };
 
+// The even entries of circle_r3_h (the BC2S feature ring) as constant
+// expressions, so that with a compile-time pitch every ring offset folds into
+// the load instruction's immediate.
+__host__ __device__ constexpr int ring_r(int k) {
+  return k == 0 ? -3 : k == 1 ? -2 : k == 2 ? 0 : k == 3 ? 2 : k == 4 ? 3 : k == 5 ? 2 : k == 6 ? 0 : -2;
+}
+__host__ __device__ constexpr int ring_c(int k) {
+  return k == 0 ? 0 : k == 1 ? 2 : k == 2 ? 3 : k == 3 ? 2 : k == 4 ? 0 : k == 5 ? -2 : k == 6 ? -3 : -2;
+}
+
+// Feat with the s1/s2 pitch fixed at compile time (every unit's fpitch == P).
+template <int P>
+struct FeatFP {
+  const uint8_t* s1;
+  const uint8_t* s2;
+  __device__ __forceinline__ void init(const Unit& u) {
+    s1 = fptr(u.s1, P, 0, 0);
+    s2 = fptr(u.s2, P, 0, 0);
+  }
+  template <int S, int K>
+  __device__ __forceinline__ static uint32_t word(const uint8_t* a) {
+    // Four ring samples K..K+3 at S times the ring radius.
+    constexpr int o0 = S * (ring_r(K) * P + ring_c(K)), o1 = S * (ring_r(K + 1) * P + ring_c(K + 1));
+    constexpr int o2 = S * (ring_r(K + 2) * P + ring_c(K + 2)), o3 = S * (ring_r(K + 3) * P + ring_c(K + 3));
+    return (uint32_t)a[o0] | ((uint32_t)a[o1] << 8) | ((uint32_t)a[o2] << 16) | ((uint32_t)a[o3] << 24);
+  }
+  __device__ __forceinline__ uint4 at(int r, int c, int) const {
+    const uint8_t* a = s1 + (r * P + c);
+    const uint8_t* b = s2 + (r * P + c);
+    return make_uint4(word<1, 0>(a), word<1, 4>(a), word<2, 0>(b), word<2, 4>(b));
+  }
+  __device__ __forceinline__ int dist(const uint4& f, int r, int c, int, bool with_s1) const {
+    const uint8_t* b = s2 + (r * P + c);
+    int d = (int)(__vsadu4(word<2, 0>(b), f.z) + __vsadu4(word<2, 4>(b), f.w));
+    if (with_s1) {
+      const uint8_t* a = s1 + (r * P + c);
+      d += (int)(__vsadu4(word<1, 0>(a), f.x) + __vsadu4(word<1, 4>(a), f.y));
+    }
+    return d;
+  }
+};
+
 // gradient_descent_match (tracking2/gradient_descent_matcher.hpp:9-76): greedy
 // 8-neighbour descent over c8_h with the c8_it_h partial sweeps; the first
 // distance is always the s1+s2 one.  (pr, pc) is inside the domain.
-__device__ __forceinline__ void gd_match(const Unit& u, const Feat& F, const uint4& f, int pr, int pc, bool with_s1,
+// c8_h and c8_it_h (cuimg/neighb2d_data.h:80-85,162-180) in registers: the
+// tables are indexed by per-lane values, which constant memory serialises.
+// c8_h entry i = (c8r(i), c8c(i)); the sweep after a move to neighbour mi
+// starts at c8_it_h[mi][0] and runs up to (not including) c8_it_h[mi][1],
+// wrapping mod 8; mi = 8 (no move yet) sweeps all eight.
+__host__ __device__ constexpr int c8r(int i) {
+  return i == 0 ? -1 : i == 1 ? 0 : i == 2 ? 1 : i == 3 ? -1 : i == 4 ? 1 : i == 5 ? -1 : i == 6 ? 0 : 1;
+}
+__host__ __device__ constexpr int c8c(int i) { return i < 3 ? 1 : i < 5 ? 0 : -1; }
+__host__ __device__ constexpr unsigned c8_pack(bool col) {
+  unsigned v = 0;
+  for (int i = 0; i < 8; i++) v |= (unsigned)((col ? c8c(i) : c8r(i)) + 1) << (2 * i);
+  return v;
+}
+__host__ __device__ constexpr int sweep_first(int mi) { return mi == 8 ? 0 : (mi & 1) ? mi - 1 : (mi + 6) & 7; }
+__host__ __device__ constexpr int sweep_len(int mi) { return mi == 8 ? 8 : (mi & 1) ? 3 : 5; }
+constexpr int k_c8_tab[8][2] = {{-1, 1}, {0, 1}, {1, 1}, {-1, 0}, {1, 0}, {-1, -1}, {0, -1}, {1, -1}};
+constexpr int k_c8it_tab[9][2] = {{6, 3}, {0, 3}, {0, 5}, {2, 5}, {2, 7}, {4, 7}, {4, 1}, {6, 1}, {0, 0}};
+constexpr bool c8_tables_agree() {
+  for (int i = 0; i < 8; i++)
+    if (c8r(i) != k_c8_tab[i][0] || c8c(i) != k_c8_tab[i][1]) return false;
+  for (int m = 0; m < 9; m++)
+    if (sweep_first(m) != k_c8it_tab[m][0] || ((k_c8it_tab[m][1] - k_c8it_tab[m][0] - 1) & 7) + 1 != sweep_len(m))
+      return false;
+  return true;
+}
+static_assert(c8_tables_agree(), "register forms of c8_h / c8_it_h");
+__device__ __forceinline__ int c8_dr(int i) { return (int)((c8_pack(false) >> (2 * i)) & 3u) - 1; }
+__device__ __forceinline__ int c8_dc(int i) { return (int)((c8_pack(true) >> (2 * i)) & 3u) - 1; }
+
+// gradient_descent_match (tracking2/gradient_descent_matcher.hpp:9-76): greedy
+// 8-neighbour descent over c8_h with the c8_it_h partial sweeps; the first
+// distance is always the s1+s2 one.  (pr, pc) is inside the domain.
+template <class FeatT>
+__device__ __forceinline__ void gd_match(const Unit& u, const FeatT& F, const uint4& f, int pr, int pc, bool with_s1,
                                          int& dr, int& dc) {
   int predr = pr, predc = pc, mr = pr, mc = pc;
   int best = F.dist(f, pr, pc, u.fpitch, true);
   int mi = 8;
   for (int search = 0; search < 10; search++) {
-    int i = c_c8it[mi][0];
-    const int end = c_c8it[mi][1];
-    bool first = true;
-    while (first || i != end) {
-      first = false;
-      int nr = predr + c_c8[i][0], nc = predc + c_c8[i][1];
-      if (in_dom(u, nr, nc)) {
-        int d = F.dist(f, nr, nc, u.fpitch, with_s1);
-        if (d < best) {
-          mr = nr;
-          mc = nc;
-          mi = i;
-          best = d;
+    const int i0 = sweep_first(mi), n = sweep_len(mi);
+      for (int j = 0; j < n; j++) {
+        const int i = (i0 + j) & 7;
+        const int nr = predr + c8_dr(i), nc = predc + c8_dc(i);
+        if (in_dom(u, nr, nc)) {
+          const int d = F.dist(f, nr, nc, u.fpitch, with_s1);
+          if (d < best) {
+            mr = nr;
+            mc = nc;
+            mi = i;
+            best = d;
+          }
         }
       }
-      i = (i + 1) & 7;
-    }
     if ((predr == mr && predc == mc) || !in_dom(u, mr, mc)) break;
     predr = mr;
     predc = mc;
@@ -319,6 +392,7 @@ __device__ __forceinline__ ChunkCursor chunk_of(const int* table, int nunits, in
 constexpr int MATCH_BLOCK = 256;
 constexpr int MATCH_SUB = CHUNK / MATCH_BLOCK;
 
+template <class FeatT>
 __global__ void __launch_bounds__(MATCH_BLOCK) k_match(const Unit* __restrict__ units, UState* __restrict__ st,
                                                        const Frame* __restrict__ fr, const int* __restrict__ table,
                                                        int nunits) {
@@ -341,7 +415,7 @@ __global__ void __launch_bounds__(MATCH_BLOCK) k_match(const Unit* __restrict__ 
       u.age[b][i] = 0;
       continue;
     }
-    Feat F;
+    FeatT F;
     F.init(u);
     uint4 feat = u.feat[b][i];
     int d1r, d1c, d2r, d2c;

@@ -30,8 +30,8 @@ def _gauss_gpu(img, sigma):
     return y.cpu().numpy()
 
 
-@pytest.mark.parametrize("sigma", [0.5, 1.0, 2.0, 4.0])
-@pytest.mark.parametrize("shape", [(1080, 1920), (37, 53), (5, 300), (130, 7)])
+@pytest.mark.parametrize("sigma", [0.5, 1.0, 2.0, 3.0, 4.0, 1.5])
+@pytest.mark.parametrize("shape", [(1080, 1920), (37, 53), (5, 300), (130, 7), (300, 129)])
 def test_gaussian_matches_oracle(sigma, shape):
     from cuimg_gb300 import synth
     H, W = shape
