@@ -35,6 +35,10 @@ DET_FREQ, FILT_FREQ, THRESHOLD = 10, 1, 20
 METRIC = "tracked_frames_per_s_1080p"
 UNIT = "frames/s"
 PER_PARTICLE_BYTES = 84  # state read/write, template read/write, sparse index
+# DRAM bytes (read + write) of one k_match launch per 1080p stream, from the
+# ncu capture summarised in profiles/k_match_1080p_x4.md (4 streams, 76.8 MB
+# per launch); the launch's traffic grows with the streams it covers.
+K_MATCH_DRAM_BYTES_PER_STREAM = 19.2e6
 
 
 def level_pixels():
@@ -53,7 +57,7 @@ def kernel_bytes_model(name, live_particles, nstreams):
     Pt = sum(P)
     per = {
         "k_blur": 3 * Pt,
-        "k_match": PER_PARTICLE_BYTES * live_particles,
+        "k_match": 2 * Pt + PER_PARTICLE_BYTES * live_particles,  # s1 + s2 read once, per-particle state
         "k_pyramid": P[0] + sum(P[1:]),
         "k_detect": Pt + Pt / 4 + Pt / 9,
     }.get(name)
@@ -196,6 +200,8 @@ def bench_ours(args):
     dev_frames = [torch.from_numpy(f).to(dev) for f in frames]  # resident in HBM
     torch.cuda.synchronize()
 
+    launches = [0]  # kernels launched inside the last timed region
+
     def timed_resident(bt, nstreams, steps, warmup, offset=0, sustain_s=0.0):
         stream = torch.cuda.ExternalStream(bt.cuda_stream(), device=dev)
         ptrs = (ctypes.c_void_p * nstreams)()
@@ -213,10 +219,12 @@ def bench_ours(args):
             pg.barrier()
         torch.cuda.synchronize()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        k0 = bt.kernel_launches()
         e0.record(stream)
         for t in range(steps):
             step(offset + warmup + t)
         e1.record(stream)
+        launches[0] = bt.kernel_launches() - k0
         e1.synchronize()
         torch.cuda.synchronize()
         ms = e0.elapsed_time(e1)
@@ -238,15 +246,10 @@ def bench_ours(args):
     bt = make(B)
     with ClockSampler(local) as clk:
         ms = timed_resident(bt, B, args.steps, args.warmup, sustain_s=1.5)
+    timed_launches = launches[0]
     clocks = clk.summary()
     clocks["window"] = "timed region + 1.5 s more of the same step"
     value = B * world * args.steps / (ms / 1000.0)
-    live = []
-    for s in range(B):
-        p = [bt._particles(s, l) for l in range(NSCALES)]
-        live.append(sum(int((q["age"] > 0).sum()) for q in p))
-    live_mean = float(np.mean(live))
-    kernels_per_frame = bt.kernels_per_frame()
     bt.close()
 
     # Plain single stream, resident.
@@ -279,6 +282,12 @@ def bench_ours(args):
             break
         prof[nameb.value.decode()] = (tot.value, cnt.value)
         k += 1
+    # Live particles after the same frames the timed region ran.
+    live = []
+    for s in range(B):
+        p = [btp._particles(s, l) for l in range(NSCALES)]
+        live.append(sum(int((q["age"] > 0).sum()) for q in p))
+    live_mean = float(np.mean(live))
     btp.close()
     total_ms = sum(v[0] for v in prof.values())
     shares = {n: round(v[0] / total_ms, 4) for n, v in sorted(prof.items(), key=lambda kv: -kv[1][0])}
@@ -289,6 +298,7 @@ def bench_ours(args):
     peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
         os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}
     peak = peaks.get("hbm_gbs", 6800.0)
+    peak_source = "measured (MEASURED_PEAKS.json)" if "hbm_gbs" in peaks else "fallback 6.8 TB/s"
     achieved = dom_bytes / dom_avg_s / 1e9
     frame_bytes = frame_bytes_model(live_mean) * B
     frame_gbs = frame_bytes * args.steps / (ms / 1000.0) / 1e9
@@ -349,11 +359,12 @@ def bench_ours(args):
                                "frac": round(frame_gbs / peak, 4),
                                "bytes_per_frame_model": round(frame_bytes / B)},
             "roofline": {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-                         "frac": round(achieved / peak, 4), "traffic": None,
-                         "avg_launch_ms": round(dom_avg_s * 1000, 5), "peak_source": "measured (MEASURED_PEAKS.json)"},
+                         "frac": round(achieved / peak, 4),
+                         "traffic": round(K_MATCH_DRAM_BYTES_PER_STREAM * B) if dom == "k_match" else None,
+                         "traffic_source": "ncu dram__bytes_read+write of a 4-stream 1080p launch, scaled by streams",
+                         "avg_launch_ms": round(dom_avg_s * 1000, 5), "peak_source": peak_source},
             "kernel_time_shares": shares,
-            "gpu_launches": kernels_per_frame * args.steps,
-            "kernels_per_step": kernels_per_frame,
+            "gpu_launches": timed_launches,
             "clocks": clocks,
             "e2e": {"value": round(e2e, 2), "unit": UNIT, "h2d_bytes_per_step": B * ROWS * COLS,
                     "d2h_bytes_per_step": 4 * nunits},

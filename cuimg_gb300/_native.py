@@ -85,6 +85,7 @@ def _declare(lib):
     lib.gbt_get_bins.argtypes = [P, I32, I32, P, P, P, P]
     lib.gbt_frame_count.argtypes = [P, I32, I32, I32P]
     lib.gbt_kernels_per_frame.argtypes = [P, I32P]
+    lib.gbt_kernel_launches.argtypes = [P, ctypes.POINTER(ctypes.c_int64)]
     lib.gbt_read_counts.argtypes = [P, P, I32]
     lib.gbt_set_tuning.argtypes = [P, I32, I32]
     lib.gbt_get_tuning.argtypes = [P, I32, I32P]

@@ -70,7 +70,9 @@ struct gbt_ctx {
   // graphs, keyed by (any detector unit, any filtering unit)
   bool use_graphs = false;
   cudaGraphExec_t graph[4] = {nullptr, nullptr, nullptr, nullptr};
-  int launches_per_frame = 0;
+  int launches_per_frame = 0;   // kernels of the last frame enqueued (memsets not counted)
+  int graph_launches[4] = {};   // kernels in each captured frame graph
+  long long kernels_total = 0;  // kernels launched by this context, graph nodes included
   int match_variant = 0;  // GBT_TUNE_MATCHER
   bool fixed_fpitch = true;  // every unit's s1/s2 pitch is FIXED_FPITCH
   std::string err;
@@ -423,7 +425,6 @@ static int enqueue_frame(gbt_ctx* ctx, bool any_det, bool any_filt) {
   cudaStream_t st = ctx->stream;
   int n = 0;
   CK(cudaMemsetAsync(ctx->occ_all, 0, ctx->occ_bytes, st));
-  n++;
   { PROF("k_pyramid"); k_pyramid<<<ctx->pyr_tiles[0], 256, 0, st>>>(ctx->d_units, ctx->d_stream_unit0, ctx->d_pyr_prefix[0], nstreams, 0); }
   n++;
   if (ctx->pyr_tiles[1] > 0) {
@@ -464,7 +465,7 @@ static int enqueue_frame(gbt_ctx* ctx, bool any_det, bool any_filt) {
     { PROF("k_det_scatter"); k_det_scatter<<<pgrid, CHUNK, 0, st>>>(ctx->d_units, ctx->d_state, ctx->d_frame, ctx->d_pre, ctx->d_btable,
                                            nunits); }
     { PROF("k_commit"); k_commit<<<1, 1024, 0, st>>>(ctx->d_units, ctx->d_state, ctx->d_frame, ctx->d_post, nunits); }
-    n += 7;
+    n += 6;
   }
   int* table = any_det ? ctx->d_post : ctx->d_pre;
   if (any_filt) {
@@ -497,13 +498,16 @@ static int run_frame(gbt_ctx* ctx) {
       e = cudaGraphInstantiate(&ctx->graph[key], g, 0);
       cudaGraphDestroy(g);
       if (e != cudaSuccess) return set_err(ctx, GBT_E_CUDA, "graph instantiate failed: %s", cudaGetErrorString(e));
+      ctx->graph_launches[key] = ctx->launches_per_frame;
     }
     CK(cudaGraphLaunch(ctx->graph[key], ctx->stream));
+    ctx->launches_per_frame = ctx->graph_launches[key];
   } else {
     int r = enqueue_frame(ctx, any_det, any_filt);
     if (r) return r;
     prof_collect(ctx);
   }
+  ctx->kernels_total += ctx->launches_per_frame;
   ctx->host_frame++;
   return GBT_OK;
 }
@@ -608,6 +612,12 @@ extern "C" int gbt_sync(gbt_ctx* ctx) {
   Frame f;
   CK(cudaMemcpy(&f, ctx->d_frame, sizeof f, cudaMemcpyDeviceToHost));
   if (f.err & ERR_CAPACITY) return set_err(ctx, GBT_E_CAPACITY, "particle capacity exceeded");
+  return GBT_OK;
+}
+
+extern "C" int gbt_kernel_launches(gbt_ctx* ctx, int64_t* total) {
+  if (!ctx || !total) return GBT_E_INVALID;
+  *total = ctx->kernels_total;
   return GBT_OK;
 }
 

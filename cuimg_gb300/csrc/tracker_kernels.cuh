@@ -96,85 +96,71 @@ __global__ void __launch_bounds__(256) k_pyramid(const Unit* __restrict__ units,
 // the adjacent lanes by shuffle, and keeps the last three rows of both row
 // passes in registers, so each level pixel is read once and s1 / s2 are each
 // written once.  Lanes 0 and 31 only supply the horizontal halo; strips overlap
-// by 8 columns.
+// by 8 columns.  The arithmetic is SIMD within a register: a word's even and
+// odd bytes sit in the two 16-bit halves of two words, where the sums (at
+// most 4 x 255) cannot carry into the neighbouring half, so every operation
+// filters two pixels.
 constexpr int BL_SR = 64;                 // default rows per strip (tunable: 16, 32, 64)
 constexpr int BL_OC = 120;                // output columns per warp (lanes 1..30)
 constexpr int BL_WARPS = 8;
+constexpr uint32_t BL_LO = 0x00FF00FFu;   // the two 16-bit halves' low bytes
 
-__device__ __forceinline__ void unpack4(uint32_t w, int* v) {
-  v[0] = w & 255;
-  v[1] = (w >> 8) & 255;
-  v[2] = (w >> 16) & 255;
-  v[3] = w >> 24;
-}
-__device__ __forceinline__ uint32_t pack4(const int* v) {
-  return (uint32_t)v[0] | ((uint32_t)v[1] << 8) | ((uint32_t)v[2] << 16) | ((uint32_t)v[3] << 24);
-}
+// Two 16-bit lanes per word: e holds pixels 0 and 2 of a lane's four, o pixels 1 and 3.
+struct Pair {
+  uint32_t e, o;
+};
 
-// Row pass of one packed word: neighbours from the adjacent lanes' words.
-__device__ __forceinline__ void row_pass(uint32_t w, uint32_t wl, uint32_t wr, int c0, int W, bool row_ok, int* t) {
-  int x[6];
-  x[0] = wl >> 24;
-  unpack4(w, x + 1);
-  x[5] = wr & 255;
-#pragma unroll
-  for (int j = 0; j < 4; j++) {
-    int c = c0 + j;
-    t[j] = (row_ok && c >= 1 && c <= W - 2) ? (2 * x[j + 1] + x[j] + x[j + 2]) >> 2 : 0;
-  }
+// Row pass (2 x[c] + x[c-1] + x[c+1]) / 4 of a lane's word w; the left
+// neighbour of pixel 0 is the top byte of wl, the right neighbour of pixel 3
+// the low byte of wr.  me / mo zero the pixels outside [1, W-2] (or the row).
+__device__ __forceinline__ Pair row_pass2(uint32_t E, uint32_t O, uint32_t wl, uint32_t wr, uint32_t me,
+                                          uint32_t mo) {
+  const uint32_t L = (O << 16) | (wl >> 24);           // left neighbours of pixels 0, 2
+  const uint32_t R = (E >> 16) | ((wr & 0xFFu) << 16); // right neighbours of pixels 1, 3
+  Pair t;
+  t.e = (((E << 1) + O + L) >> 2) & me;
+  t.o = (((O << 1) + E + R) >> 2) & mo;
+  return t;
 }
 
-// One row step of k_blur: row r of the level enters, s1 row r-1 and s2 row
-// r-2 leave.
-__device__ __forceinline__ void blur_row(const Unit& U, uint32_t w, int r, int r0, int r1, int c0, int H, int W,
-                                         bool out_lane, int* t1m2, int* t1m1, int* t10, int* t2m2, int* t2m1,
-                                         int* t20) {
+// Column pass (2 t[r] + t[r-1] + t[r+1]) / 4; m zeroes a row outside [1, H-2].
+__device__ __forceinline__ Pair col_pass2(const Pair& up, const Pair& mid, const Pair& dn, uint32_t m) {
+  Pair s;
+  s.e = (((mid.e << 1) + up.e + dn.e) >> 2) & m;
+  s.o = (((mid.o << 1) + up.o + dn.o) >> 2) & m;
+  return s;
+}
+
+// One row step: level row r enters (word w); s1 row r-1 and s2 row r-2 leave.
+// a1/b1/c1 are the row-pass values of rows r-2, r-1 and (written here) r;
+// a2/b2/c2 those of s1 rows r-3, r-2 and (written here) r-1.
+__device__ __forceinline__ void blur_step(const Unit& U, uint32_t w, int r, int r0, int r1, int c0, int H,
+                                          bool out_lane, bool full_word, uint32_t me, uint32_t mo, const Pair& a1,
+                                          const Pair& b1, Pair& c1, const Pair& a2, const Pair& b2, Pair& c2) {
+  const uint32_t wl = __shfl_up_sync(0xffffffffu, w, 1), wr = __shfl_down_sync(0xffffffffu, w, 1);
   const bool row_ok = r >= 0 && r < H;
-  uint32_t wl = __shfl_up_sync(0xffffffffu, w, 1), wr = __shfl_down_sync(0xffffffffu, w, 1);
-#pragma unroll
-  for (int j = 0; j < 4; j++) {
-    t1m2[j] = t1m1[j];
-    t1m1[j] = t10[j];
-  }
-  row_pass(w, wl, wr, c0, W, row_ok, t10);
-  // s1 at row r - 1
+  c1 = row_pass2(w & BL_LO, (w >> 8) & BL_LO, wl, wr, row_ok ? me : 0u, row_ok ? mo : 0u);
   const int rs1 = r - 1;
-  int s1v[4];
-  const bool s1row = rs1 >= 1 && rs1 <= H - 2;
-#pragma unroll
-  for (int j = 0; j < 4; j++) {
-    int c = c0 + j;
-    s1v[j] = (s1row && c >= 0 && c < W) ? (2 * t1m1[j] + t1m2[j] + t10[j]) >> 2 : 0;
-  }
-  const uint32_t s1w = pack4(s1v);
+  const Pair s1 = col_pass2(a1, b1, c1, (rs1 >= 1 && rs1 <= H - 2) ? BL_LO : 0u);
+  const uint32_t s1w = s1.e | (s1.o << 8);
   const uint32_t s1l = __shfl_up_sync(0xffffffffu, s1w, 1), s1r = __shfl_down_sync(0xffffffffu, s1w, 1);
-#pragma unroll
-  for (int j = 0; j < 4; j++) {
-    t2m2[j] = t2m1[j];
-    t2m1[j] = t20[j];
-  }
-  row_pass(s1w, s1l, s1r, c0, W, rs1 >= 0 && rs1 < H, t20);
-  // s2 at row r - 2
+  const bool row1_ok = rs1 >= 0 && rs1 < H;
+  c2 = row_pass2(s1.e, s1.o, s1l, s1r, row1_ok ? me : 0u, row1_ok ? mo : 0u);
   const int rs2 = r - 2;
-  int s2v[4];
-  const bool s2row = rs2 >= 1 && rs2 <= H - 2;
-#pragma unroll
-  for (int j = 0; j < 4; j++) {
-    int c = c0 + j;
-    s2v[j] = (s2row && c >= 0 && c < W) ? (2 * t2m1[j] + t2m2[j] + t20[j]) >> 2 : 0;
-  }
-  if (out_lane && c0 < W) {
+  const Pair s2 = col_pass2(a2, b2, c2, (rs2 >= 1 && rs2 <= H - 2) ? BL_LO : 0u);
+  if (out_lane) {
     if (rs1 >= r0 && rs1 < r1) {
       uint8_t* p1 = (uint8_t*)fptr(U.s1, U.fpitch, rs1, c0);
-      if (c0 + 4 <= W) *(uint32_t*)p1 = s1w;
+      if (full_word) *(uint32_t*)p1 = s1w;
       else
-        for (int j = 0; j < 4 && c0 + j < W; j++) p1[j] = (uint8_t)s1v[j];
+        for (int j = 0; j < 4 && c0 + j < U.W; j++) p1[j] = (uint8_t)(s1w >> (8 * j));
     }
     if (rs2 >= r0 && rs2 < r1) {
+      const uint32_t s2w = s2.e | (s2.o << 8);
       uint8_t* p2 = (uint8_t*)fptr(U.s2, U.fpitch, rs2, c0);
-      if (c0 + 4 <= W) *(uint32_t*)p2 = pack4(s2v);
+      if (full_word) *(uint32_t*)p2 = s2w;
       else
-        for (int j = 0; j < 4 && c0 + j < W; j++) p2[j] = (uint8_t)s2v[j];
+        for (int j = 0; j < 4 && c0 + j < U.W; j++) p2[j] = (uint8_t)(s2w >> (8 * j));
     }
   }
 }
@@ -193,23 +179,35 @@ __global__ void __launch_bounds__(32 * BL_WARPS) k_blur(const Unit* __restrict__
   const int H = U.H, W = U.W;
   const int c0 = cs * BL_OC - 4 + 4 * lane;  // first column of this lane's word
   const int r0 = rs * SR, r1 = min(r0 + SR, H);
-  const bool out_lane = lane >= 1 && lane <= 30;
-  int t1m2[4] = {0, 0, 0, 0}, t1m1[4] = {0, 0, 0, 0}, t10[4] = {0, 0, 0, 0};
-  int t2m2[4] = {0, 0, 0, 0}, t2m1[4] = {0, 0, 0, 0}, t20[4] = {0, 0, 0, 0};
-  const bool word_ok = c0 >= 0 && c0 < U.ipitch;
-  for (int rb = r0 - 2; rb <= r1 + 1; rb += 4) {
-    // Four independent row loads in flight per lane before any arithmetic.
-    uint32_t w4[4];
+  const bool out_lane = lane >= 1 && lane <= 30 && c0 < W;
+  const bool full_word = c0 + 4 <= W;
+  // Row-pass column masks: pixel c0 + j is filtered iff 1 <= c0 + j <= W - 2.
+  uint32_t me = 0, mo = 0;
 #pragma unroll
-    for (int k = 0; k < 4; k++) {
+  for (int j = 0; j < 4; j++) {
+    const int c = c0 + j;
+    if (c >= 1 && c <= W - 2) {
+      if (j & 1) mo |= 0xFFu << (16 * (j >> 1));
+      else me |= 0xFFu << (16 * (j >> 1));
+    }
+  }
+  const bool word_ok = c0 >= 0 && c0 < U.ipitch;
+  Pair p1a{0, 0}, p1b{0, 0}, p1c{0, 0}, p2a{0, 0}, p2b{0, 0}, p2c{0, 0};
+  // Rows r0 - 2 .. r1 + 1 enter, six per batch: two rounds of three steps in
+  // which the register windows rotate by renaming.
+  for (int rb = r0 - 2; rb <= r1 + 1; rb += 6) {
+    uint32_t w6[6];
+#pragma unroll
+    for (int k = 0; k < 6; k++) {
       const int r = rb + k;
-      w4[k] = (r >= 0 && r < H && r <= r1 + 1 && word_ok) ? *(const uint32_t*)(U.img + (size_t)r * U.ipitch + c0) : 0u;
+      w6[k] = (r >= 0 && r < H && word_ok) ? *(const uint32_t*)(U.img + (size_t)r * U.ipitch + c0) : 0u;
     }
 #pragma unroll
-    for (int k = 0; k < 4; k++) {
-      const int r = rb + k;
-      if (r > r1 + 1) break;
-      blur_row(U, w4[k], r, r0, r1, c0, H, W, out_lane, t1m2, t1m1, t10, t2m2, t2m1, t20);
+    for (int h = 0; h < 2; h++) {
+      const int r = rb + 3 * h;
+      blur_step(U, w6[3 * h], r, r0, r1, c0, H, out_lane, full_word, me, mo, p1b, p1c, p1a, p2b, p2c, p2a);
+      blur_step(U, w6[3 * h + 1], r + 1, r0, r1, c0, H, out_lane, full_word, me, mo, p1c, p1a, p1b, p2c, p2a, p2b);
+      blur_step(U, w6[3 * h + 2], r + 2, r0, r1, c0, H, out_lane, full_word, me, mo, p1a, p1b, p1c, p2a, p2b, p2c);
     }
   }
 }

@@ -251,6 +251,12 @@ class BatchTracker:
         check(self._lib.gbt_kernels_per_frame(self._ensure(), ctypes.byref(n)), self._ctx)
         return n.value
 
+    def kernel_launches(self):
+        """Kernels launched by this tracker so far (graph replays included)."""
+        n = ctypes.c_int64()
+        check(self._lib.gbt_kernel_launches(self._ensure(), ctypes.byref(n)), self._ctx)
+        return n.value
+
     def nparticles(self, stream=0, scale=None):
         if scale is None:
             return sum(self.nparticles(stream, s) for s in range(self._cfgs[stream].nscales))

@@ -154,6 +154,9 @@ int gbt_get_tuning(gbt_ctx* ctx, int32_t knob, int32_t* value);
 /* Per-stage launch counters and device time of the last frame (for tests
  * and the benchmark): number of kernel launches issued per frame. */
 int gbt_kernels_per_frame(gbt_ctx* ctx, int32_t* n);
+/* Kernels this context has launched since gbt_create (frame-graph replays
+ * count every kernel node they run). */
+int gbt_kernel_launches(gbt_ctx* ctx, int64_t* total);
 
 /* Per-kernel device-time accounting with CUDA events on the context stream
  * (eager launches; graph replays are not split).  gbt_profile_read returns
