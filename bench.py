@@ -58,6 +58,7 @@ def kernel_bytes_model(name, live_particles, nstreams):
     per = {
         "k_blur": 3 * Pt,
         "k_match": 2 * Pt + PER_PARTICLE_BYTES * live_particles,  # s1 + s2 read once, per-particle state
+        "k_match_tiled": 2 * Pt + PER_PARTICLE_BYTES * live_particles,
         "k_pyramid": P[0] + sum(P[1:]),
         "k_detect": Pt + Pt / 4 + Pt / 9,
     }.get(name)

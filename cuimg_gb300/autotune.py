@@ -17,7 +17,8 @@ from ._native import check, cuda_lib
 
 KNOBS = {
     # knob id: (name, settings, kernel names whose time decides)
-    0: ("matcher", (0, 1, 2), ("k_match", "k_match_warp")),
+    0: ("matcher", (0, 1, 2, 3), ("k_match", "k_match_warp", "k_match_tiled", "k_mt_count", "k_mt_scan",
+                                  "k_mt_scatter")),
     1: ("blur_rows", (16, 32, 64), ("k_blur",)),
 }
 DEFAULT_CACHE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "_build", "autotune.json")

@@ -70,6 +70,9 @@ struct Unit {
   uint8_t* cmask;     // cap candidate direction masks
   int4* act_list;     // cap entries: (i, pos packed, ncand, first cand) + cand store
   int* act_cand;      // cap * 8 candidate indices
+  // matcher tiles (k_match_tiled)
+  int MTR, MTC;       // tiles per column / row
+  int mt_base;        // first tile of this unit in the context-wide tile arrays
 };
 
 // Mutable per-unit counters, kept on the device so that captured graphs replay.
@@ -99,6 +102,13 @@ __constant__ int8_t c_c8it[9][2] = {{6, 3}, {0, 3}, {0, 5}, {2, 5}, {2, 7}, {4, 
 // circle_r3_h (cuimg/neighb2d_data.h:184-189).
 __constant__ int8_t c_ring[16][2] = {{-3, 0}, {-3, 1}, {-2, 2}, {-1, 3}, {0, 3},   {1, 3},   {2, 2},   {3, 1},
                                      {3, 0},  {3, -1}, {2, -2}, {1, -3}, {0, -3}, {-1, -3}, {-2, -2}, {-3, -1}};
+// The same ring as constant expressions (offsets fold into load immediates
+// when the index and the pitch are compile-time constants).
+__host__ __device__ constexpr int circle16_r(int i) {
+  return i == 0 ? -3 : i == 1 ? -3 : i == 2 ? -2 : i == 3 ? -1 : i == 4 ? 0 : i == 5 ? 1 : i == 6 ? 2 : i == 7 ? 3
+       : i == 8 ? 3 : i == 9 ? 3 : i == 10 ? 2 : i == 11 ? 1 : i == 12 ? 0 : i == 13 ? -1 : i == 14 ? -2 : -3;
+}
+__host__ __device__ constexpr int circle16_c(int i) { return circle16_r((i + 4) & 15); }
 
 __device__ __forceinline__ int clampi(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }
 

@@ -60,6 +60,13 @@ struct gbt_ctx {
   int* d_btable = nullptr;
   // dynamic chunk tables
   int* d_pre = nullptr;
+  // tiled matcher: tiles over all units, per-tile counts / offsets, binned slots
+  int mt_tiles = 0;
+  long long mt_list_cap = 0;
+  int* d_mt_prefix = nullptr;
+  int* d_mt_cnt = nullptr;
+  int* d_mt_off = nullptr;
+  int* d_mt_list = nullptr;
   int* d_post = nullptr;
   // bulk buffers cleared per frame
   void* occ_all = nullptr;
@@ -236,6 +243,11 @@ static int build(gbt_ctx* ctx, const gbt_config* cfgs, int nstreams) {
     u.cap = u.H * u.W / 6 + 4096;
     u.cap = round_up(u.cap, CHUNK);
     u.max_chunks = u.cap / CHUNK;
+    u.MTR = (u.H + MT_R - 1) / MT_R;
+    u.MTC = (u.W + MT_C - 1) / MT_C;
+    u.mt_base = ctx->mt_tiles;
+    ctx->mt_tiles += u.MTR * u.MTC;
+    ctx->mt_list_cap += u.cap;
     for (int b = 0; b < 2; b++) {
       if ((r = dalloc_t(ctx, &u.pos[b], u.cap))) return r;
       if ((r = dalloc_t(ctx, &u.spd[b], u.cap))) return r;
@@ -257,6 +269,9 @@ static int build(gbt_ctx* ctx, const gbt_config* cfgs, int nstreams) {
   if ((r = dalloc_t(ctx, &ctx->d_state, nunits))) return r;
   if ((r = dalloc_t(ctx, &ctx->d_frame, 1))) return r;
   if ((r = dalloc_t(ctx, &ctx->d_pre, nunits + 1))) return r;
+  if ((r = dalloc_t(ctx, &ctx->d_mt_cnt, ctx->mt_tiles + 1))) return r;
+  if ((r = dalloc_t(ctx, &ctx->d_mt_off, ctx->mt_tiles + 1))) return r;
+  if ((r = dalloc_t(ctx, &ctx->d_mt_list, ctx->mt_list_cap))) return r;
   if ((r = dalloc_t(ctx, &ctx->d_post, nunits + 1))) return r;
 
   // Static tables.
@@ -297,6 +312,12 @@ static int build(gbt_ctx* ctx, const gbt_config* cfgs, int nstreams) {
   if ((r = upload_table(ctx, &ctx->d_bin_prefix, bins))) return r;
   if ((r = upload_table(ctx, &ctx->d_det_prefix, det))) return r;
   if ((r = upload_table(ctx, &ctx->d_btable, bt))) return r;
+  {
+    std::vector<int> mt;
+    for (auto& u : ctx->units) mt.push_back(u.mt_base);
+    mt.push_back(ctx->mt_tiles);
+    if ((r = upload_table(ctx, &ctx->d_mt_prefix, mt))) return r;
+  }
   for (auto& s : ctx->streams) {
     const Unit& u = ctx->units[s.unit0];
     s.pinned_bytes = (size_t)u.H * u.W * 3;
@@ -442,13 +463,20 @@ static int enqueue_frame(gbt_ctx* ctx, bool any_det, bool any_filt) {
     else
       k_blur<64><<<nb, 32 * BL_WARPS, 0, st>>>(ctx->d_units, ctx->d_blur_prefix, nunits);
   }
-  if (ctx->match_variant == 1) {
+  if (ctx->match_variant == 0 && ctx->fixed_fpitch) {
+    CK(cudaMemsetAsync(ctx->d_mt_cnt, 0, (size_t)ctx->mt_tiles * sizeof(int), st));
+    { PROF("k_mt_count"); k_mt_bin<0><<<pgrid, CHUNK, 0, st>>>(ctx->d_units, ctx->d_state, ctx->d_pre, nunits, ctx->d_mt_cnt, nullptr); }
+    { PROF("k_mt_scan"); k_mt_scan<<<1, 1024, 0, st>>>(ctx->d_mt_cnt, ctx->mt_tiles, ctx->d_mt_off, ctx->d_mt_cnt); }
+    { PROF("k_mt_scatter"); k_mt_bin<1><<<pgrid, CHUNK, 0, st>>>(ctx->d_units, ctx->d_state, ctx->d_pre, nunits, ctx->d_mt_cnt, ctx->d_mt_list); }
+    { PROF("k_match_tiled"); k_match_tiled<<<ctx->mt_tiles, MT_THREADS, 0, st>>>(ctx->d_units, ctx->d_state, ctx->d_frame, ctx->d_mt_prefix, nunits, ctx->d_mt_off, ctx->d_mt_list); }
+    n += 3;
+  } else if (ctx->match_variant == 1) {
     PROF("k_match_warp");
     k_match_warp<<<ctx->nsm * 4, 32 * MW_WARPS, 0, st>>>(ctx->d_units, ctx->d_state, ctx->d_frame, ctx->d_pre, nunits);
   } else {
     PROF("k_match");
     const dim3 g(ctx->nsm * 8);
-    if (ctx->match_variant == 0 && ctx->fixed_fpitch)
+    if (ctx->match_variant == 3 && ctx->fixed_fpitch)
       k_match<FeatFP<FIXED_FPITCH>>
           <<<g, MATCH_BLOCK, 0, st>>>(ctx->d_units, ctx->d_state, ctx->d_frame, ctx->d_pre, nunits);
     else
@@ -521,7 +549,7 @@ extern "C" int gbt_set_tuning(gbt_ctx* ctx, int32_t knob, int32_t value) {
         g = nullptr;
       }
   };
-  if (knob == GBT_TUNE_MATCHER && value >= 0 && value <= 2) {
+  if (knob == GBT_TUNE_MATCHER && value >= 0 && value <= 3) {
     if (ctx->match_variant != value) drop_graphs();
     ctx->match_variant = value;
     return GBT_OK;

@@ -258,12 +258,11 @@ struct Feat {
 // The even entries of circle_r3_h (the BC2S feature ring) as constant
 // expressions, so that with a compile-time pitch every ring offset folds into
 // the load instruction's immediate.
-__host__ __device__ constexpr int ring_r(int k) {
-  return k == 0 ? -3 : k == 1 ? -2 : k == 2 ? 0 : k == 3 ? 2 : k == 4 ? 3 : k == 5 ? 2 : k == 6 ? 0 : -2;
-}
-__host__ __device__ constexpr int ring_c(int k) {
-  return k == 0 ? 0 : k == 1 ? 2 : k == 2 ? 3 : k == 3 ? 2 : k == 4 ? 0 : k == 5 ? -2 : k == 6 ? -3 : -2;
-}
+__host__ __device__ constexpr int ring_r(int k) { return circle16_r(2 * k); }
+__host__ __device__ constexpr int ring_c(int k) { return circle16_c(2 * k); }
+static_assert(ring_r(0) == -3 && ring_c(0) == 0 && ring_r(1) == -2 && ring_c(1) == 2 && ring_r(2) == 0 &&
+                  ring_c(2) == 3 && ring_r(5) == 2 && ring_c(5) == -2 && ring_r(7) == -2 && ring_c(7) == -2,
+              "even entries of circle_r3_h");
 
 // Feat with the s1/s2 pitch fixed at compile time (every unit's fpitch == P).
 template <int P>
@@ -390,6 +389,53 @@ __device__ __forceinline__ ChunkCursor chunk_of(const int* table, int nunits, in
 constexpr int MATCH_BLOCK = 256;
 constexpr int MATCH_SUB = CHUNK / MATCH_BLOCK;
 
+// Prediction of a live particle (motion_based_prediction, predictions.h:15-33).
+__device__ __forceinline__ void predict(unsigned short age, short2 pos, short2 spd, int& pr, int& pc) {
+  pr = (short)(pos.x + (age == 1 ? 0 : spd.x));
+  pc = (short)(pos.y + (age == 1 ? 0 : spd.y));
+}
+
+// Match one live particle whose prediction (pr, pc) is inside the domain, and
+// apply the result (kernel_particle_container::move or remove).
+template <class FeatT>
+__device__ __forceinline__ void match_one(const Unit& u, const FeatT& F, int f, int b, int i, unsigned short age,
+                                          short2 pos, int pr, int pc) {
+  const uint4 feat = u.feat[b][i];
+  int d1r, d1c, d2r, d2c;
+  gd_match(u, F, feat, pr, pc, false, d1r, d1c);
+  gd_match(u, F, feat, pr + d1r, pc + d1c, true, d2r, d2c);
+  const int dr = d1r + d2r, dc = d1c + d2c;
+  const int mr = (short)(pr + dr), mc = (short)(pc + dc);
+  bool accept = in_dom(u, mr, mc);
+  uint4 mf = make_uint4(0, 0, 0, 0);
+  if (accept) {
+    mf = F.at(mr, mc, u.fpitch);
+    // n_diff over the s2 entries (every weight is 255 > 150, so cpt = 8).
+    unsigned n_diff = 0;
+    const uint32_t a0 = feat.z, a1 = feat.w, c0 = mf.z, c1 = mf.w;
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+      int x = (a0 >> (8 * j)) & 255, y = (c0 >> (8 * j)) & 255;
+      if (abs(x - y) > u.k) n_diff++;
+      x = (a1 >> (8 * j)) & 255;
+      y = (c1 >> (8 * j)) & 255;
+      if (abs(x - y) > u.k) n_diff++;
+    }
+    accept = n_diff < 4u;
+  }
+  if (!accept || contrast_at(u, mr, mc) < 3) {
+    u.age[b][i] = 0;
+    return;
+  }
+  const int sr = pr - pos.x + dr, sc = pc - pos.y + dc;
+  u.age[b][i] = (unsigned short)(age + 1);
+  u.spd[b][i] = make_short2((short)sr, (short)sc);
+  u.pos[b][i] = make_short2((short)mr, (short)mc);
+  if (sr != 0 || sc != 0) u.feat[b][i] = mf;
+  atomicOr(&u.occ[bin_word(u, mr, mc)], bin_bit(mr, mc));
+  atomicMax(&u.idx[(size_t)mr * u.W + mc], ((unsigned long long)stamp_match(f) << 32) | (unsigned)i);
+}
+
 template <class FeatT>
 __global__ void __launch_bounds__(MATCH_BLOCK) k_match(const Unit* __restrict__ units, UState* __restrict__ st,
                                                        const Frame* __restrict__ fr, const int* __restrict__ table,
@@ -403,52 +449,160 @@ __global__ void __launch_bounds__(MATCH_BLOCK) k_match(const Unit* __restrict__ 
     const int i = cc.chunk * CHUNK + (g % MATCH_SUB) * MATCH_BLOCK + threadIdx.x;
     if (i >= s.n) continue;
     const int b = s.cur;
-    unsigned short age = u.age[b][i];
+    const unsigned short age = u.age[b][i];
     if (age == 0) continue;
-    short2 pos = u.pos[b][i];
-    short2 spd = u.spd[b][i];
-    int pr = (short)(pos.x + (age == 1 ? 0 : spd.x));
-    int pc = (short)(pos.y + (age == 1 ? 0 : spd.y));
+    const short2 pos = u.pos[b][i];
+    int pr, pc;
+    predict(age, pos, u.spd[b][i], pr, pc);
     if (!in_dom(u, pr, pc)) {
       u.age[b][i] = 0;
       continue;
     }
     FeatT F;
     F.init(u);
-    uint4 feat = u.feat[b][i];
-    int d1r, d1c, d2r, d2c;
-    gd_match(u, F, feat, pr, pc, false, d1r, d1c);
-    gd_match(u, F, feat, pr + d1r, pc + d1c, true, d2r, d2c);
-    const int dr = d1r + d2r, dc = d1c + d2c;
-    const int mr = (short)(pr + dr), mc = (short)(pc + dc);
-    bool accept = in_dom(u, mr, mc);
-    uint4 mf = make_uint4(0, 0, 0, 0);
-    if (accept) {
-      mf = F.at(mr, mc, u.fpitch);
-      // n_diff over the s2 entries (every weight is 255 > 150, so cpt = 8).
-      unsigned n_diff = 0;
-      const uint32_t a0 = feat.z, a1 = feat.w, c0 = mf.z, c1 = mf.w;
-#pragma unroll
-      for (int j = 0; j < 4; j++) {
-        int x = (a0 >> (8 * j)) & 255, y = (c0 >> (8 * j)) & 255;
-        if (abs(x - y) > u.k) n_diff++;
-        x = (a1 >> (8 * j)) & 255;
-        y = (c1 >> (8 * j)) & 255;
-        if (abs(x - y) > u.k) n_diff++;
-      }
-      accept = n_diff < 4u;
-    }
-    if (!accept || contrast_at(u, mr, mc) < 3) {
-      u.age[b][i] = 0;
+    match_one(u, F, f, b, i, age, pos, pr, pc);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Tiled matcher.  Live particles are binned by their prediction into tiles of
+// MT_R x MT_C pixels (count, scan, scatter); one CTA per non-empty tile stages
+// the tile's s1 / s2 neighbourhood in shared memory with 16-byte cp.async
+// copies and matches its particles from there.  A descent moves at most 10
+// pixels per step in each axis (two steps) and the BC2S taps reach 6 pixels
+// further, so with margins of 26 rows and 32 columns every sample a particle
+// of the tile can touch is staged.  Particles are independent (each writes
+// only its own slot; the sparse index keeps the highest slot with atomicMax),
+// so the order inside a tile does not change any result.
+constexpr int MT_R = 32, MT_C = 128;                // tile
+constexpr int MT_MR = 26, MT_MC = 32;              // staged margins
+constexpr int MT_SR = MT_R + 2 * MT_MR;            // staged rows (84)
+constexpr int MT_SC = MT_C + 2 * MT_MC;            // staged columns (192), 16-byte chunks
+constexpr int MT_THREADS = 128;
+static_assert(MT_MR >= 2 * 10 + 6 && MT_MC >= 2 * 10 + 6, "staged margins cover a full descent");
+static_assert(MT_SC % 16 == 0 && MT_MC % 16 == 0, "16-byte staging");
+
+__device__ __forceinline__ int mt_tile(const Unit& u, int pr, int pc) {
+  return u.mt_base + (pr / MT_R) * u.MTC + pc / MT_C;
+}
+
+// Pass 0 counts live particles per tile (and removes those predicted outside
+// the domain, as the matcher does); pass 1 scatters slot indices.
+template <int PASS>
+__global__ void __launch_bounds__(CHUNK) k_mt_bin(const Unit* __restrict__ units, const UState* __restrict__ st,
+                                                  const int* __restrict__ table, int nunits, int* __restrict__ cnt,
+                                                  int* __restrict__ list) {
+  const int total = table[nunits];
+  for (int g = blockIdx.x; g < total; g += gridDim.x) {
+    ChunkCursor cc = chunk_of(table, nunits, g);
+    const Unit& u = units[cc.unit];
+    const UState s = st[cc.unit];
+    const int i = cc.chunk * CHUNK + threadIdx.x;
+    if (i >= s.n) continue;
+    const int b = s.cur;
+    const unsigned short age = u.age[b][i];
+    if (age == 0) continue;
+    int pr, pc;
+    predict(age, u.pos[b][i], u.spd[b][i], pr, pc);
+    if (!in_dom(u, pr, pc)) {
+      if (PASS == 0) u.age[b][i] = 0;
       continue;
     }
-    const int sr = pr - pos.x + dr, sc = pc - pos.y + dc;
-    u.age[b][i] = (unsigned short)(age + 1);
-    u.spd[b][i] = make_short2((short)sr, (short)sc);
-    u.pos[b][i] = make_short2((short)mr, (short)mc);
-    if (sr != 0 || sc != 0) u.feat[b][i] = mf;
-    atomicOr(&u.occ[bin_word(u, mr, mc)], bin_bit(mr, mc));
-    atomicMax(&u.idx[(size_t)mr * u.W + mc], ((unsigned long long)stamp_match(f) << 32) | (unsigned)i);
+    const int t = mt_tile(u, pr, pc);
+    if (PASS == 0) atomicAdd(&cnt[t], 1);
+    else list[atomicAdd(&cnt[t], 1)] = i;
+  }
+}
+
+// Exclusive scan of the tile counts into offsets (off[ntiles] = total); the
+// cursor array starts at the offsets for the scatter pass.
+__global__ void __launch_bounds__(1024) k_mt_scan(const int* __restrict__ cnt, int ntiles, int* __restrict__ off,
+                                                  int* __restrict__ cursor) {
+  __shared__ int wt[65];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  int carry = 0;
+  for (int base = 0; base < ntiles; base += 1024) {
+    const int k = base + threadIdx.x;
+    const int v = k < ntiles ? cnt[k] : 0;
+    int x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += y;
+    }
+    if (lane == 31) wt[wid] = x;
+    __syncthreads();
+    if (wid == 0) {
+      const int w = wt[lane];
+      int z = w;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, z, o);
+        if (lane >= o) z += y;
+      }
+      wt[32 + lane] = z - w;
+      if (lane == 31) wt[64] = z;
+    }
+    __syncthreads();
+    if (k < ntiles) {
+      const int e = carry + wt[32 + wid] + x - v;
+      off[k] = e;
+      cursor[k] = e;
+    }
+    carry += wt[64];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) off[ntiles] = carry;
+}
+
+__device__ __forceinline__ void cp_async16(void* sdst, const void* gsrc) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(sdst);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(gsrc) : "memory");
+}
+
+__global__ void __launch_bounds__(MT_THREADS) k_match_tiled(const Unit* __restrict__ units,
+                                                            const UState* __restrict__ st,
+                                                            const Frame* __restrict__ fr,
+                                                            const int* __restrict__ tile_prefix, int nunits,
+                                                            const int* __restrict__ off,
+                                                            const int* __restrict__ list) {
+  __shared__ __align__(16) uint8_t ts1[MT_SR * MT_SC];
+  __shared__ __align__(16) uint8_t ts2[MT_SR * MT_SC];
+  const int t = blockIdx.x;
+  const int n0 = off[t], n1 = off[t + 1];
+  if (n0 == n1) return;
+  const int ui = find_unit(tile_prefix, nunits, t);
+  const Unit& u = units[ui];
+  const int local = t - tile_prefix[ui];
+  const int R0s = (local / u.MTC) * MT_R - MT_MR, C0s = (local % u.MTC) * MT_C - MT_MC;
+  // Stage rows R0s .. R0s + MT_SR - 1 and columns C0s .. C0s + MT_SC - 1 of s1
+  // and s2, skipping chunks outside the bordered images (never sampled: the
+  // taps stay within 6 pixels of the domain, inside the zero border).
+  constexpr int CPR = MT_SC / 16;
+  for (int v = threadIdx.x; v < MT_SR * CPR; v += MT_THREADS) {
+    const int row = v / CPR, ck = v % CPR;
+    const int gr = R0s + row;                    // image row
+    const int gb = C0s + CB + 16 * ck;           // byte offset inside the bordered row
+    if (gr < -RB || gr >= u.H + RB || gb < 0 || gb + 16 > FIXED_FPITCH) continue;
+    const size_t go = (size_t)(gr + RB) * FIXED_FPITCH + gb;
+    cp_async16(&ts1[row * MT_SC + 16 * ck], u.s1 + go);
+    cp_async16(&ts2[row * MT_SC + 16 * ck], u.s2 + go);
+  }
+  asm volatile("cp.async.commit_group;\n" ::: "memory");
+  asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+  __syncthreads();
+  const int f = fr->f;
+  const int b = st[ui].cur;
+  FeatFP<MT_SC> F;
+  F.s1 = ts1 - (R0s * MT_SC + C0s);  // F.s1 + (r * MT_SC + c) is staged pixel (r, c)
+  F.s2 = ts2 - (R0s * MT_SC + C0s);
+  for (int k = n0 + threadIdx.x; k < n1; k += MT_THREADS) {
+    const int i = list[k];
+    const unsigned short age = u.age[b][i];
+    const short2 pos = u.pos[b][i];
+    int pr, pc;
+    predict(age, pos, u.spd[b][i], pr, pc);
+    match_one(u, F, f, b, i, age, pos, pr, pc);
   }
 }
 
@@ -706,7 +860,7 @@ __device__ __forceinline__ int fast_saliency(const uint8_t* P, int ld, int n_, i
   int status = 2;
   const int vp = P[0];
   unsigned sum_bright = 0, sum_dark = 0;
-#define RV(i) ((int)P[c_ring[i][0] * ld + c_ring[i][1]])
+#define RV(i) ((int)P[circle16_r(i) * ld + circle16_c(i)])
   if (n_ >= 9) {
     const int to_test[6] = {0, 4, 8, 12, 0, 4};
     int equals = 0;
@@ -758,6 +912,7 @@ __device__ __forceinline__ int fast_saliency(const uint8_t* P, int ld, int n_, i
     }
   }
   if (n != 16 && status != 2) {
+#pragma unroll
     for (int i = 0; i < 16; i++) {
       int vn = RV(i);
       int sign = vn > vp;

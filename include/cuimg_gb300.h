@@ -139,10 +139,13 @@ int gbt_read_counts(gbt_ctx* ctx, int32_t* counts, int32_t n);
 int gbt_frame_count(gbt_ctx* ctx, int32_t stream, int32_t scale, int32_t* n);
 
 /* Tuning knobs (results are identical for every setting; only speed
- * changes).  GBT_TUNE_MATCHER: 0 = one thread per particle (ring offsets
- * compiled in when every stream is at most 4064 pixels wide), 1 = one warp
+ * changes).  GBT_TUNE_MATCHER: 0 = particles binned by prediction into
+ * 32 x 128 tiles, one CTA per tile matching from shared memory, 1 = one warp
  * per particle with the sweep candidates spread over its lanes, 2 = one thread
- * per particle with ring offsets computed from each level's pitch.
+ * per particle with ring offsets computed from each level's pitch, 3 = one
+ * thread per particle with compile-time ring offsets.  0 and 3 need every
+ * stream to be at most 4064 pixels wide (fixed s1/s2 pitch) and fall back to 2
+ * otherwise.
  * GBT_TUNE_BLUR_ROWS: height of the strip one warp walks in the BC2S blur.  The package's
  * autotuner (cuimg_gb300/autotune.py) times the settings on the caller's
  * workload and caches the winner. */

@@ -80,7 +80,7 @@ def test_gpu_matches_oracle_1080p():
     assert total > 50000
 
 
-@pytest.mark.parametrize("matcher", [0, 1, 2])
+@pytest.mark.parametrize("matcher", [0, 1, 2, 3])
 def test_matcher_variants_match_oracle(matcher):
     _compare_run(480, 640, 3, 14, 6, detf=5, matcher=matcher)
 
