@@ -334,7 +334,7 @@ extern "C" int gbt_create(const gbt_config* cfgs, int32_t nstreams, int32_t devi
   for (int s = 0; s < nstreams; s++) {
     const gbt_config& c = cfgs[s];
     if (!gbt_sizes_ok(c.rows, c.cols, c.nscales) || c.detector_frequency < 1 || c.filtering_frequency < 1 ||
-        c.detector_n < 1 || c.detector_n > 16)
+        c.detector_n < 1 || c.detector_n > 16 || c.detector_threshold < 0)
       return GBT_E_INVALID;
   }
   gbt_ctx* ctx = new gbt_ctx;
@@ -770,7 +770,7 @@ __global__ void k_dump(const Unit* __restrict__ units, const UState* __restrict_
           uint8_t win[7][7];
           for (int a = 0; a < 7; a++)
             for (int b = 0; b < 7; b++) win[a][b] = (uint8_t)img_at(u, r - 3 + a, c - 3 + b);
-          v = (uint8_t)fast_saliency(&win[3][3], 7, u.nfast, u.threshold);
+          v = (uint8_t)fast_saliency_bf<7>(&win[3][3], u.nfast, u.threshold);
         }
         ((uint8_t*)out)[t] = v;
       }

@@ -6,7 +6,7 @@
 namespace gbt {
 
 // ---------------------------------------------------------------------------
-// Block-wide exclusive prefix of a 0/1 predicate (blockDim.x == 1024).
+// Block-wide exclusive prefix of a 0/1 predicate (blockDim.x a multiple of 32).
 __device__ __forceinline__ int block_prefix(bool pred, int* warp_tot, int& total) {
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   unsigned b = __ballot_sync(0xffffffffu, pred);
@@ -14,7 +14,7 @@ __device__ __forceinline__ int block_prefix(bool pred, int* warp_tot, int& total
   if (lane == 0) warp_tot[wid] = __popc(b);
   __syncthreads();
   if (wid == 0) {
-    int v = warp_tot[lane];
+    int v = lane < (int)(blockDim.x >> 5) ? warp_tot[lane] : 0;
     int x = v;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
@@ -853,88 +853,52 @@ __global__ void __launch_bounds__(CHUNK) k_pmask(const Unit* __restrict__ units,
   }
 }
 
-// fast::compute_saliency (tracking2/fast_detector.hpp:26-157) on a shared
-// memory tile: `P` points at the centre pixel, `ld` is the row stride.
-__device__ __forceinline__ int fast_saliency(const uint8_t* P, int ld, int n_, int th) {
-  unsigned max_n = 0, n = 0;
-  int status = 2;
+// fast::compute_saliency without branches, for a pixel P of a shared tile
+// with compile-time row length LD.  A ring pixel is "strong" when it differs
+// from the centre by more than th (bright: above, dark: below); the reference
+// scans the ring for the longest run of strong pixels of one sign, wrapping
+// around (fast_detector.hpp:95-146), and scores max(sum bright, sum dark) over
+// all strong pixels (stored as gl8u).  Here the runs are tested on 16-bit
+// masks doubled to 32 bits (so a run may wrap): a run of n_ exists iff the AND
+// of the mask shifted by 0..n_-1 is non-zero.  The reference's pre-test on
+// ring pixels 0, 4, 8, 12 only rejects pixels the full test rejects too (a run
+// of n_ >= 9 covers two cyclically adjacent ones of them, n_ >= 12 three), so
+// it is left out.  th >= 0 (the context rejects negative thresholds).
+template <int LD>
+__device__ __forceinline__ int fast_saliency_bf(const uint8_t* P, int n_, int th) {
   const int vp = P[0];
-  unsigned sum_bright = 0, sum_dark = 0;
-#define RV(i) ((int)P[circle16_r(i) * ld + circle16_c(i)])
-  if (n_ >= 9) {
-    const int to_test[6] = {0, 4, 8, 12, 0, 4};
-    int equals = 0;
-#pragma unroll
-    for (int k = 0; k < 6; k++) {
-      int vn = RV(to_test[k]);
-      int sign = vn > vp;
-      int dist = abs(vn - vp);
-      if (dist > th) {
-        if (sign == status) {
-          n++;
-        } else {
-          if (n > max_n) max_n = n;
-          status = sign;
-          n = 1;
-        }
-      } else {
-        if (n > max_n) max_n = n;
-        status = 2;
-        equals++;
-        if (k < 4 && n_ >= 12 && equals >= 2) return 0;
-      }
-    }
-    if (n > max_n) max_n = n;
-    if (n_ >= 12 && max_n < 3) return 0;
-    else if (n_ >= 8 && max_n < 2) return 0;
-  }
-  n = 0;
-  status = 2;
-  max_n = 0;
+  unsigned B = 0, D = 0;
+  int sb = 0, sd = 0;
 #pragma unroll
   for (int i = 0; i < 16; i++) {
-    int vn = RV(i);
-    int sign = vn > vp;
-    int dist = abs(vn - vp);
-    if (dist > th) {
-      if (sign == status) {
-        n++;
-      } else {
-        if (n > max_n) max_n = n;
-        status = sign;
-        n = 1;
-      }
-      if (vn < vp) sum_dark += dist;
-      else sum_bright += dist;
-    } else {
-      if (n > max_n) max_n = n;
-      status = 2;
+    const int d = (int)P[circle16_r(i) * LD + circle16_c(i)] - vp;
+    const bool br = d > th, dk = -d > th;
+    B |= (unsigned)br << i;
+    D |= (unsigned)dk << i;
+    sb += br ? d : 0;
+    sd += dk ? -d : 0;
+  }
+  if (n_ > 16) return 0;
+  const unsigned MB = B | (B << 16), MD = D | (D << 16);
+  unsigned xb, xd;
+  if (n_ == 9) {  // runs of 2, 4, 8, then 9
+    xb = MB & (MB >> 1);
+    xd = MD & (MD >> 1);
+    xb &= xb >> 2;
+    xd &= xd >> 2;
+    xb &= xb >> 4;
+    xd &= xd >> 4;
+    xb &= MB >> 8;
+    xd &= MD >> 8;
+  } else {
+    xb = MB;
+    xd = MD;
+    for (int k = 1; k < n_; k++) {
+      xb &= MB >> k;
+      xd &= MD >> k;
     }
   }
-  if (n != 16 && status != 2) {
-#pragma unroll
-    for (int i = 0; i < 16; i++) {
-      int vn = RV(i);
-      int sign = vn > vp;
-      int dist = abs(vn - vp);
-      if (dist <= th || sign != status) break;
-      n++;
-    }
-  }
-#undef RV
-  if (n > max_n) max_n = n;
-  if (max_n < (unsigned)n_) return 0;
-  return (int)((sum_bright > sum_dark ? sum_bright : sum_dark) & 255u);  // stored as gl8u
-}
-
-// Detector mask value, saliency and contrast at a tile pixel.
-__device__ __forceinline__ int saliency_px(const Unit& u, const uint8_t* P, int ld, int r, int c) {
-  if (u.pmask[bin_word(u, r, c)] & bin_bit(r, c)) return 0;
-  const int d = 2;
-  int con = abs((int)P[d] - (int)P[-d]) + abs((int)P[-d * ld] - (int)P[d * ld]) +
-            abs((int)P[-d * ld - d] - (int)P[d * ld + d]) + abs((int)P[-d * ld + d] - (int)P[d * ld - d]);
-  if (con < 5) return 0;  // flow_mask_kernel (tracking_strategies.hpp:227-252)
-  return fast_saliency(P, ld, u.nfast, u.threshold);
+  return (xb | xd) ? ((sb > sd ? sb : sd) & 255) : 0;
 }
 
 // Saliency + 3x3 tile non-maximum selection: fast_detector::update and
@@ -942,13 +906,26 @@ __device__ __forceinline__ int saliency_px(const Unit& u, const uint8_t* P, int 
 // tile q owns pixels 3q + (1,1) + [0,2]^2; it is skipped when any of them holds
 // a particle, otherwise its first strict maximum (raster order) becomes a birth
 // if the saliency reaches the threshold and the point lies in the
-// domain - border(3).  Result per tile: dr * 3 + dc, or 0xFF.
+// domain - border(3).  Result per tile: dr * 3 + dc, or 0xFF.  A pixel's
+// saliency is 0 where the detector mask is cleared (next to a particle,
+// particle_mask_kernel) or the contrast is below 5 (flow_mask_kernel,
+// tracking_strategies.hpp:202-252).
+//
+// A CTA covers 8 x 32 tiles: it stages their pixels (with the ring's 3-pixel
+// halo) and the occupancy / mask words of the bins they touch in shared
+// memory, lists the unoccupied tiles, and gives each listed tile to one
+// thread, which computes the saliency of its nine pixels with the branch-free
+// form above (no divergence) and selects the maximum.
 constexpr int DT_R = 8, DT_C = 32;  // tiles per CTA
 constexpr int DT_PR = DT_R * 3 + 6, DT_PC = DT_C * 3 + 6;
+constexpr int DT_BR = (DT_R * 3 + 7) / 8 + 1, DT_BC = (DT_C * 3 + 7) / 8 + 1;  // bins touched
 
 __global__ void __launch_bounds__(256) k_detect(const Unit* __restrict__ units, const Frame* __restrict__ fr,
                                                 const int* __restrict__ blk_prefix, int nunits) {
   __shared__ uint8_t tile[DT_PR][DT_PC];
+  __shared__ unsigned long long s_occ[DT_BR][DT_BC], s_pm[DT_BR][DT_BC];
+  __shared__ short list[DT_R * DT_C];
+  __shared__ int wt[65];
   const int f = fr->f;
   const int t = blockIdx.x;
   const int ui = find_unit(blk_prefix, nunits, t);
@@ -957,44 +934,75 @@ __global__ void __launch_bounds__(256) k_detect(const Unit* __restrict__ units, 
   const int local = t - blk_prefix[ui];
   const int bw = (u.TW + DT_C - 1) / DT_C;
   const int TR0 = (local / bw) * DT_R, TC0 = (local % bw) * DT_C;
-  const int pr0 = 3 * TR0 + 1 - 3, pc0 = 3 * TC0 + 1 - 3;
+  const int pr0 = 3 * TR0 + 1 - 3, pc0 = 3 * TC0 + 1 - 3;  // staged origin
+  const int br0 = (3 * TR0 + 1) >> 3, bc0 = (3 * TC0 + 1) >> 3;
   for (int v = threadIdx.x; v < DT_PR * DT_PC; v += blockDim.x) {
-    int r = v / DT_PC, c = v % DT_PC;
+    const int r = v / DT_PC, c = v % DT_PC;
     tile[r][c] = (uint8_t)img_at(u, pr0 + r, pc0 + c);
   }
+  for (int v = threadIdx.x; v < DT_BR * DT_BC; v += blockDim.x) {
+    const int r = v / DT_BC, c = v % DT_BC;
+    const int br = br0 + r, bc = bc0 + c;
+    const bool ok = br < u.BH && bc < u.BW;
+    s_occ[r][c] = ok ? u.occ[(size_t)br * u.BW + bc] : 0ull;
+    s_pm[r][c] = ok ? u.pmask[(size_t)br * u.BW + bc] : 0ull;
+  }
   __syncthreads();
+  auto bit = [&](const unsigned long long (*w)[DT_BC], int r, int c) -> bool {
+    return (w[(r >> 3) - br0][(c >> 3) - bc0] >> (((r & 7) << 3) | (c & 7))) & 1ull;
+  };
+  // Tiles of this CTA: occupied ones are decided now, the others are listed.
   const int tr = TR0 + threadIdx.x / DT_C, tc = TC0 + threadIdx.x % DT_C;
-  if (tr >= u.TH || tc >= u.TW) return;
-  const int pr = 3 * tr + 1, pc = 3 * tc + 1;
-  uint8_t code = 0xFF;
-  bool occupied = false;
-  for (int r = 0; r < 3; r++)
-    for (int c = 0; c < 3; c++) {
-      int gr = pr + r, gc = pc + c;
-      if (in_dom(u, gr, gc) && (u.occ[bin_word(u, gr, gc)] & bin_bit(gr, gc))) occupied = true;
-    }
-  if (!occupied) {
-    const int lr = pr - pr0, lc = pc - pc0;
-    int vmax = saliency_px(u, &tile[lr][lc], DT_PC, pr, pc);
-    int mr = 0, mc = 0;
+  const bool valid = tr < u.TH && tc < u.TW;
+  bool open = false;
+  if (valid) {
+    const int pr = 3 * tr + 1, pc = 3 * tc + 1;
+    bool occupied = false;
+#pragma unroll
     for (int r = 0; r < 3; r++)
-      for (int c = 0; c < 3; c++) {
-        if (r == 0 && c == 0) continue;
-        int gr = pr + r, gc = pc + c;
-        if (!in_dom(u, gr, gc)) continue;
-        int v = saliency_px(u, &tile[lr + r][lc + c], DT_PC, gr, gc);
-        if (vmax < v) {
-          vmax = v;
-          mr = r;
-          mc = c;
-        }
+#pragma unroll
+      for (int c = 0; c < 3; c++)
+        if (in_dom(u, pr + r, pc + c) && bit(s_occ, pr + r, pc + c)) occupied = true;
+    open = !occupied;
+    if (occupied) u.tilecode[(size_t)tr * u.TW + tc] = 0xFF;
+  }
+  int nopen;
+  const int slot = block_prefix(open, wt, nopen);
+  if (open) list[slot] = (short)threadIdx.x;
+  __syncthreads();
+  // One open tile per thread (packed by the list, so warps stay full): the
+  // saliency of its nine pixels, then the first strict maximum.
+  if (threadIdx.x < nopen) {
+    const int lt = list[threadIdx.x];
+    const int ttr = TR0 + lt / DT_C, ttc = TC0 + lt % DT_C;
+    const int pr = 3 * ttr + 1, pc = 3 * ttc + 1;
+    const bool inner = pr + 2 < u.H && pc + 2 < u.W;  // all nine pixels in the domain
+    const uint8_t* P0 = &tile[pr - pr0][pc - pc0];
+    int vmax = -1, mr = 0, mc = 0;
+#pragma unroll
+    for (int q = 0; q < 9; q++) {
+      const int r = q / 3, c = q % 3;
+      if (!inner && !in_dom(u, pr + r, pc + c)) continue;
+      const uint8_t* P = P0 + r * DT_PC + c;
+      const int d = 2;
+      const int con = abs((int)P[d] - (int)P[-d]) + abs((int)P[-d * DT_PC] - (int)P[d * DT_PC]) +
+                      abs((int)P[-d * DT_PC - d] - (int)P[d * DT_PC + d]) +
+                      abs((int)P[-d * DT_PC + d] - (int)P[d * DT_PC - d]);
+      const int fs = fast_saliency_bf<DT_PC>(P, u.nfast, u.threshold);
+      const int v = (bit(s_pm, pr + r, pc + c) || con < 5) ? 0 : fs;
+      if (vmax < v) {  // pixel 0 always enters (v >= 0)
+        vmax = v;
+        mr = r;
+        mc = c;
       }
+    }
+    uint8_t code = 0xFF;
     if (vmax >= u.threshold) {
-      int gr = pr + mr, gc = pc + mc;
+      const int gr = pr + mr, gc = pc + mc;
       if (gr >= 3 && gr <= u.H - 4 && gc >= 3 && gc <= u.W - 4) code = (uint8_t)(mr * 3 + mc);
     }
+    u.tilecode[(size_t)ttr * u.TW + ttc] = code;
   }
-  u.tilecode[(size_t)tr * u.TW + tc] = code;
 }
 
 // Birth items are ordered (tile row, row inside the tile, tile column), which

@@ -4,6 +4,7 @@
     python -m cuimg_gb300.profile_cases lk         # 4 fp32 640x480 pairs, 5 levels, 20k points each
     python -m cuimg_gb300.profile_cases adjoint    # LK residual forward + backward, same batch
     python -m cuimg_gb300.profile_cases tracker    # 4 streams of 1920x1080, 6 frames
+    python -m cuimg_gb300.profile_cases tracker_det  # the same with the detector every third frame
 
 Each case runs its kernels a few times on inputs larger than L2 but a few GB
 at most on the device, so a capture of one or two launches ends quickly.
@@ -80,7 +81,19 @@ def tracker(frames=6):
     bt.close()
 
 
-CASES = {"gaussian": gaussian, "lk": lk_case, "adjoint": adjoint, "tracker": tracker}
+def tracker_det(frames=8):
+    """4 streams of 1920x1080 with the detector every third frame (frames 0, 3, 6)."""
+    from . import BatchTracker, synth
+    cfg = [dict(rows=1080, cols=1920, nscales=4, detector_threshold=20, detector_frequency=3)] * 4
+    vids = [synth.frames(1000 + i, 1080, 1920, frames) for i in range(4)]
+    bt = BatchTracker(cfg, graphs=False)
+    for t in range(frames):
+        bt.run([v[t] for v in vids])
+    bt.sync()
+    bt.close()
+
+
+CASES = {"gaussian": gaussian, "lk": lk_case, "adjoint": adjoint, "tracker": tracker, "tracker_det": tracker_det}
 
 if __name__ == "__main__":
     for name in sys.argv[1:] or list(CASES):

@@ -41,7 +41,7 @@ typedef struct gbt_ctx gbt_ctx;
 typedef struct {
   int32_t rows, cols;           /* level-0 frame size */
   int32_t nscales;              /* number of pyramid levels / tracker scales (1..9) */
-  int32_t detector_threshold;   /* fast_detector::set_fast_threshold */
+  int32_t detector_threshold;   /* fast_detector::set_fast_threshold (>= 0) */
   int32_t detector_n;           /* fast_detector::set_n (arc length, default 9) */
   int32_t detector_frequency;   /* generic_strategy::set_detector_frequency */
   int32_t filtering_frequency;  /* generic_strategy::set_filtering_frequency */

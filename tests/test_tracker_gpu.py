@@ -74,6 +74,29 @@ def test_gpu_matches_oracle(rows, cols, L, n, seed, detf):
     assert _compare_run(rows, cols, L, n, seed, detf) > 0
 
 
+@pytest.mark.parametrize("n_fast,th", [(7, 10), (12, 35), (16, 5)])
+def test_detector_arc_lengths_and_thresholds(n_fast, th):
+    # FAST arc lengths other than 9 take the generic run test; the oracle keeps
+    # the reference's branchy scan with its pre-test.
+    from cuimg_gb300 import Tracker, synth
+    rows, cols, L, n = 240, 320, 3, 8
+    frames = synth.frames(21, rows, cols, n)
+    tr = Tracker((rows, cols), L)
+    tr.strategy().set_detector_frequency(2).set_filtering_frequency(1)
+    for s in range(L):
+        tr.scale(s).strategy().detector().set_n(n_fast).set_fast_threshold(th)
+    o = tracker_oracle(rows, cols, L, th, 2, 1)
+    o.lib.oracle_set_n(o.h, n_fast)
+    for t in range(n):
+        tr.run(frames[t])
+        o.run(frames[t])
+        bad = diff_snapshots(snapshot(o, L), tr.snapshot(), detector_frame=(t % 2 == 0))
+        assert not bad, "frame %d: %s" % (t, bad)
+    assert tr.nparticles() > 0 or n_fast == 16
+    tr.close()
+    o.destroy()
+
+
 def test_gpu_matches_oracle_1080p():
     # The headline geometry: 1920x1080, 4 scales, detector every 10 frames.
     total = _compare_run(1080, 1920, 4, 12, 5, 10)
