@@ -253,6 +253,13 @@ def bench_ours(args):
     value = B * world * args.steps / (ms / 1000.0)
     bt.close()
 
+    # The same with device-side trajectories (20 positions per particle).
+    btt = make(B)
+    btt.enable_trajectories(20)
+    ms_t = timed_resident(btt, B, args.steps, args.warmup)
+    traj_fps = B * world * args.steps / (ms_t / 1000.0)
+    btt.close()
+
     # Plain single stream, resident.
     bt1 = make(1)
     ms1 = timed_resident(bt1, 1, args.steps, args.warmup)
@@ -366,6 +373,8 @@ def bench_ours(args):
                          "avg_launch_ms": round(dom_avg_s * 1000, 5), "peak_source": peak_source},
             "kernel_time_shares": shares,
             "gpu_launches": timed_launches,
+            "trajectories": {"history": 20, "frames_per_s": round(traj_fps, 2),
+                             "relative_to_value": round(traj_fps / value, 3)},
             "clocks": clocks,
             "e2e": {"value": round(e2e, 2), "unit": UNIT, "h2d_bytes_per_step": B * ROWS * COLS,
                     "d2h_bytes_per_step": 4 * nunits},

@@ -73,6 +73,11 @@ struct Unit {
   // matcher tiles (k_match_tiled)
   int MTR, MTC;       // tiles per column / row
   int mt_base;        // first tile of this unit in the context-wide tile arrays
+  // trajectories (k_traj; null until enabled): position k of slot j's history
+  // ring at tpos[b][k * cap + j], next write at thead, length tlen
+  short2* tpos[2];
+  uint8_t* thead[2];
+  uint8_t* tlen[2];
 };
 
 // Mutable per-unit counters, kept on the device so that captured graphs replay.

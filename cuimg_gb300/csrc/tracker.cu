@@ -54,6 +54,8 @@ struct gbt_ctx {
   int blur_tiles_v[3] = {0, 0, 0};
   int blur_rows = BL_SR;
   int* d_bin_prefix = nullptr;
+  int* d_cap_table = nullptr;  // particle-capacity chunks per unit (trajectories)
+  int traj_T = 0;              // trajectory history length, 0 = off
   int nbins = 0;
   int* d_det_prefix = nullptr;
   int det_blocks = 0;
@@ -313,6 +315,11 @@ static int build(gbt_ctx* ctx, const gbt_config* cfgs, int nstreams) {
   if ((r = upload_table(ctx, &ctx->d_det_prefix, det))) return r;
   if ((r = upload_table(ctx, &ctx->d_btable, bt))) return r;
   {
+    std::vector<int> capt(1, 0);
+    for (auto& u : ctx->units) capt.push_back(capt.back() + u.max_chunks);
+    if ((r = upload_table(ctx, &ctx->d_cap_table, capt))) return r;
+  }
+  {
     std::vector<int> mt;
     for (auto& u : ctx->units) mt.push_back(u.mt_base);
     mt.push_back(ctx->mt_tiles);
@@ -504,6 +511,11 @@ static int enqueue_frame(gbt_ctx* ctx, bool any_det, bool any_filt) {
     { PROF("k_merge_resolve"); k_merge_resolve<<<nunits, 256, 0, st>>>(ctx->d_units, ctx->d_state, ctx->d_frame); }
     n += 5;
   }
+  if (ctx->traj_T) {
+    PROF("k_traj");
+    k_traj<<<ctx->nsm * 4, CHUNK, 0, st>>>(ctx->d_units, ctx->d_state, ctx->d_cap_table, nunits, ctx->traj_T);
+    n++;
+  }
   { PROF("k_tick"); k_tick<<<1, 1024, 0, st>>>(ctx->d_units, ctx->d_state, ctx->d_frame, ctx->d_pre, nunits); }
   n++;
   ctx->launches_per_frame = n;
@@ -576,6 +588,28 @@ extern "C" int gbt_get_tuning(gbt_ctx* ctx, int32_t knob, int32_t* value) {
     return GBT_OK;
   }
   return GBT_E_INVALID;
+}
+
+extern "C" int gbt_trajectories_enable(gbt_ctx* ctx, int32_t history) {
+  if (!ctx || history < 1 || history > 255) return GBT_E_INVALID;
+  if (ctx->traj_T) return ctx->traj_T == history ? GBT_OK : GBT_E_INVALID;
+  CK(cudaSetDevice(ctx->device));
+  CK(cudaStreamSynchronize(ctx->stream));
+  int r;
+  for (auto& u : ctx->units)
+    for (int b = 0; b < 2; b++) {
+      if ((r = dalloc_t(ctx, &u.tpos[b], (size_t)history * u.cap))) return r;
+      if ((r = dalloc_t(ctx, &u.thead[b], u.cap))) return r;
+      if ((r = dalloc_t(ctx, &u.tlen[b], u.cap))) return r;
+    }
+  CK(cudaMemcpy(ctx->d_units, ctx->units.data(), ctx->units.size() * sizeof(Unit), cudaMemcpyHostToDevice));
+  for (auto& g : ctx->graph)
+    if (g) {
+      cudaGraphExecDestroy(g);
+      g = nullptr;
+    }
+  ctx->traj_T = history;
+  return GBT_OK;
 }
 
 extern "C" int gbt_use_graphs(gbt_ctx* ctx, int32_t enable) {
@@ -720,6 +754,43 @@ extern "C" int gbt_get_particles(gbt_ctx* ctx, int32_t stream, int32_t scale, fl
   if (matches && s.nmatches)
     CK(cudaMemcpy(matches, u.matches, (size_t)s.nmatches * 4, cudaMemcpyDeviceToHost));
   if (compact_has_run) *compact_has_run = s.compact;
+  return GBT_OK;
+}
+
+extern "C" int gbt_get_trajectories(gbt_ctx* ctx, int32_t stream, int32_t scale, int16_t* xy, uint8_t* len,
+                                    int32_t* n, int32_t* history) {
+  int ui = unit_of(ctx, stream, scale);
+  if (ui < 0 || !n || !ctx->traj_T) return GBT_E_INVALID;
+  CK(cudaSetDevice(ctx->device));
+  UState s;
+  int r = read_state(ctx, ui, &s);
+  if (r) return r;
+  const Unit& u = ctx->units[ui];
+  const int T = ctx->traj_T, np = s.n, b = s.cur;
+  *n = np;
+  if (history) *history = T;
+  if ((!xy && !len) || np == 0) return GBT_OK;
+  std::vector<uint8_t> hl(np), hh(np);
+  std::vector<short2> hp((size_t)T * np);
+  CK(cudaMemcpy(hl.data(), u.tlen[b], np, cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(hh.data(), u.thead[b], np, cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy2D(hp.data(), (size_t)np * sizeof(short2), u.tpos[b], (size_t)u.cap * sizeof(short2),
+                  (size_t)np * sizeof(short2), T, cudaMemcpyDeviceToHost));
+  for (int j = 0; j < np; j++) {
+    const int L = hl[j], h = hh[j];
+    if (len) len[j] = (uint8_t)L;
+    if (!xy) continue;
+    int16_t* o = xy + (size_t)j * T * 2;
+    for (int m = 0; m < T; m++) {
+      if (m < L) {
+        const short2 p = hp[(size_t)((h - L + m + T) % T) * np + j];
+        o[2 * m] = p.x;
+        o[2 * m + 1] = p.y;
+      } else {
+        o[2 * m] = o[2 * m + 1] = 0;
+      }
+    }
+  }
   return GBT_OK;
 }
 

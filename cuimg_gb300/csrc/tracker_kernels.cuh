@@ -1463,6 +1463,52 @@ __global__ void __launch_bounds__(256) k_merge_resolve(const Unit* __restrict__ 
 }
 
 // End of frame: frame counter and the chunk table of the next frame.
+// ---------------------------------------------------------------------------
+// Device-side trajectories: the sample's per-particle position history
+// (samples/tracking/main.cc:39-57,125-127, at most T positions) kept in step
+// with the particle slots the way particle_container::sync_attributes does
+// (particle_container.hpp:514-553): after a compaction the history of old slot
+// i moves to slot matches[i] (and is dropped when matches[i] < 0) and births
+// start empty; then every live particle appends its position, dropping the
+// oldest beyond T, and every dead slot's history is cleared
+// (update_trajectories).  Runs after the frame's last kill.
+__device__ __forceinline__ void traj_append(const Unit& u, int b, int j, int T, uint8_t head, uint8_t len) {
+  if (u.age[b][j] > 0) {
+    u.tpos[b][(size_t)head * u.cap + j] = u.pos[b][j];
+    u.thead[b][j] = (uint8_t)(head + 1 == T ? 0 : head + 1);
+    u.tlen[b][j] = (uint8_t)(len < T ? len + 1 : T);
+  } else {
+    u.thead[b][j] = 0;
+    u.tlen[b][j] = 0;
+  }
+}
+
+__global__ void __launch_bounds__(CHUNK) k_traj(const Unit* __restrict__ units, const UState* __restrict__ st,
+                                                const int* __restrict__ cap_table, int nunits, int T) {
+  const int total = cap_table[nunits];
+  for (int g = blockIdx.x; g < total; g += gridDim.x) {
+    ChunkCursor cc = chunk_of(cap_table, nunits, g);
+    const Unit& u = units[cc.unit];
+    const UState s = st[cc.unit];
+    const int i = cc.chunk * CHUNK + threadIdx.x;
+    const int b = s.cur;
+    if (s.compact) {
+      const int ob = b ^ 1;
+      if (i < s.n_old) {
+        const int ni = u.matches[i];
+        if (ni >= 0) {
+          const uint8_t len = u.tlen[ob][i], head = u.thead[ob][i];
+          for (int k = 0; k < T; k++) u.tpos[b][(size_t)k * u.cap + ni] = u.tpos[ob][(size_t)k * u.cap + i];
+          traj_append(u, b, ni, T, head, len);
+        }
+      }
+      if (i >= s.S && i < s.n) traj_append(u, b, i, T, 0, 0);  // birth
+    } else if (i < s.n) {
+      traj_append(u, b, i, T, u.thead[b][i], u.tlen[b][i]);
+    }
+  }
+}
+
 __global__ void __launch_bounds__(1024) k_tick(const Unit* __restrict__ units, const UState* __restrict__ st,
                                                Frame* __restrict__ fr, int* __restrict__ pre_table, int nunits) {
   build_table(units, st, nunits, pre_table);

@@ -280,6 +280,24 @@ class BatchTracker:
                                           ctypes.byref(comp)), ctx)
         return dict(speed=speed, pos=pos, age=age, feat=feat, matches=matches[: nm.value], compact=bool(comp.value))
 
+    def enable_trajectories(self, history=20):
+        """Keep every particle's last `history` positions on the GPU, in step
+        with the slots (gbt_trajectories_enable)."""
+        check(self._lib.gbt_trajectories_enable(self._ensure(), int(history)), self._ctx)
+        return self
+
+    def trajectories(self, stream=0, scale=0):
+        """(xy[n, history, 2] oldest first and zero padded, length[n]) for the
+        current particle slots."""
+        ctx = self._ensure()
+        n, T = ctypes.c_int32(), ctypes.c_int32()
+        check(self._lib.gbt_get_trajectories(ctx, stream, scale, None, None, ctypes.byref(n), ctypes.byref(T)), ctx)
+        xy = np.zeros((n.value, T.value, 2), np.int16)
+        ln = np.zeros(n.value, np.uint8)
+        check(self._lib.gbt_get_trajectories(ctx, stream, scale, xy.ctypes.data, ln.ctypes.data, ctypes.byref(n),
+                                             ctypes.byref(T)), ctx)
+        return xy, ln
+
     def stage(self, stream, scale, name, border=0):
         ctx = self._ensure()
         H, W = self.dims(stream, scale)

@@ -138,6 +138,20 @@ int gbt_read_counts(gbt_ctx* ctx, int32_t* counts, int32_t n);
 /* Frame counter of (stream, scale) (generic_strategy::frame_cpt_). */
 int gbt_frame_count(gbt_ctx* ctx, int32_t stream, int32_t scale, int32_t* n);
 
+/* Device-side trajectories (the sample's per-particle position history,
+ * samples/tracking/main.cc:39-57,125-127, kept in step with the particle slots
+ * as particle_container::sync_attributes does, particle_container.hpp:514-553).
+ * Once enabled, every frame appends each live particle's position (keeping the
+ * last `history` <= 255), clears dead slots' histories, and moves histories to
+ * their new slots when a compaction renumbers them; births start empty.  The
+ * history buffers stay on the GPU: no per-frame copy of the particle vectors.
+ * gbt_get_trajectories fills xy[n][history][2] (row, col; oldest first, zero
+ * padded) and len[n] for the current slots; with xy and len NULL it only
+ * returns n and history. */
+int gbt_trajectories_enable(gbt_ctx* ctx, int32_t history);
+int gbt_get_trajectories(gbt_ctx* ctx, int32_t stream, int32_t scale, int16_t* xy, uint8_t* len, int32_t* n,
+                         int32_t* history);
+
 /* Tuning knobs (results are identical for every setting; only speed
  * changes).  GBT_TUNE_MATCHER: 0 = particles binned by prediction into
  * 32 x 128 tiles, one CTA per tile matching from shared memory, 1 = one warp
