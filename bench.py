@@ -35,10 +35,11 @@ DET_FREQ, FILT_FREQ, THRESHOLD = 10, 1, 20
 METRIC = "tracked_frames_per_s_1080p"
 UNIT = "frames/s"
 PER_PARTICLE_BYTES = 84  # state read/write, template read/write, sparse index
-# DRAM bytes (read + write) of one k_match launch per 1080p stream, from the
-# ncu capture summarised in profiles/k_match_1080p_x4.md (4 streams, 76.8 MB
-# per launch); the launch's traffic grows with the streams it covers.
-K_MATCH_DRAM_BYTES_PER_STREAM = 19.2e6
+# DRAM bytes (read + write) of one matcher launch per 1080p stream, from the
+# ncu captures summarised in profiles/k_match_tiled_1080p_x4.md (4 streams,
+# 75.0 MB per launch) and profiles/k_match_1080p_x4.md (76.8 MB); a launch's
+# traffic grows with the streams it covers.
+DRAM_BYTES_PER_STREAM = {"k_match_tiled": 18.75e6, "k_match": 19.2e6}
 
 
 def level_pixels():
@@ -339,6 +340,37 @@ def bench_ours(args):
         e2e_s = float(tt.item())
     e2e = B * world * args.steps / e2e_s
     bte.close()
+    del host
+
+    # End to end with RGB frames: 3 bytes per pixel go to the device and the
+    # pyramid kernel makes them gray (channel 0, as the reference's sample).
+    nrgb = min(nfr, 8)
+    host_rgb = [torch.from_numpy(np.ascontiguousarray(np.repeat(frames[s][:nrgb, :, :, None], 3, axis=3))).pin_memory()
+                for s in range(B)]
+    btr = make(B)
+
+    def rstep(t):
+        for s in range(B):
+            hptrs[s] = host_rgb[s][t % nrgb].data_ptr()
+        check(lib.gbt_run(btr._ctx, hptrs, rpitch, 2), btr._ctx)
+        check(lib.gbt_read_counts(btr._ctx, counts.ctypes.data, nunits), btr._ctx)
+
+    rpitch = (ctypes.c_int64 * B)(*([COLS * 3] * B))
+    for t in range(args.warmup):
+        rstep(t)
+    if pg:
+        pg.barrier()
+    t0 = time.perf_counter()
+    for t in range(args.steps):
+        rstep(args.warmup + t)
+    rgb_s = time.perf_counter() - t0
+    if pg:
+        tt = torch.tensor([rgb_s], device=dev)
+        pg.all_reduce(tt, op=pg.ReduceOp.MAX)
+        rgb_s = float(tt.item())
+    e2e_rgb = B * world * args.steps / rgb_s
+    btr.close()
+    del host_rgb
 
     extras = {} if args.no_extras else measure_extras(args, dev, local, peak)
 
@@ -368,7 +400,7 @@ def bench_ours(args):
                                "bytes_per_frame_model": round(frame_bytes / B)},
             "roofline": {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                          "frac": round(achieved / peak, 4),
-                         "traffic": round(K_MATCH_DRAM_BYTES_PER_STREAM * B) if dom == "k_match" else None,
+                         "traffic": round(DRAM_BYTES_PER_STREAM[dom] * B) if dom in DRAM_BYTES_PER_STREAM else None,
                          "traffic_source": "ncu dram__bytes_read+write of a 4-stream 1080p launch, scaled by streams",
                          "avg_launch_ms": round(dom_avg_s * 1000, 5), "peak_source": peak_source},
             "kernel_time_shares": shares,
@@ -376,6 +408,8 @@ def bench_ours(args):
             "trajectories": {"history": 20, "frames_per_s": round(traj_fps, 2),
                              "relative_to_value": round(traj_fps / value, 3)},
             "clocks": clocks,
+            "e2e_rgb": {"value": round(e2e_rgb, 2), "unit": UNIT, "h2d_bytes_per_step": B * ROWS * COLS * 3,
+                        "d2h_bytes_per_step": nunits * 4, "note": "pinned RGB host frames, gray made on the GPU"},
             "e2e": {"value": round(e2e, 2), "unit": UNIT, "h2d_bytes_per_step": B * ROWS * COLS,
                     "d2h_bytes_per_step": 4 * nunits},
             "cpu_baseline": cpu,

@@ -87,6 +87,7 @@ def _declare(lib):
     lib.gbt_kernels_per_frame.argtypes = [P, I32P]
     lib.gbt_kernel_launches.argtypes = [P, ctypes.POINTER(ctypes.c_int64)]
     lib.gbt_trajectories_enable.argtypes = [P, I32]
+    lib.gbt_set_rgb_to_gray.argtypes = [P, I32]
     lib.gbt_get_trajectories.argtypes = [P, I32, I32, P, P, I32P, I32P]
     lib.gbt_read_counts.argtypes = [P, P, I32]
     lib.gbt_set_tuning.argtypes = [P, I32, I32]

@@ -80,6 +80,16 @@ struct Unit {
   uint8_t* tlen[2];
 };
 
+// Frame ingest of one stream for the next frame: mode 0 = the gray frame is
+// already in level 0; 1 = interleaved RGB at `rgb`, track channel 0 (get_x,
+// dsl/get_comp.h:105); 2 = the same, BT.601 luma (77 R + 150 G + 29 B + 128) / 256.
+struct Ingest {
+  const uint8_t* rgb;
+  long long pitch;
+  int mode;
+  int pad;
+};
+
 // Mutable per-unit counters, kept on the device so that captured graphs replay.
 struct UState {
   int n;         // particle slots in the current buffer

@@ -30,6 +30,8 @@ struct StreamInfo {
   int unit0;
   uint8_t* pinned;  // staging buffer for pageable host frames
   size_t pinned_bytes;
+  uint8_t* d_rgb = nullptr;  // device RGB frame, allocated on the first RGB input
+  int64_t rgb_pitch = 0;
 };
 
 }  // namespace
@@ -55,6 +57,10 @@ struct gbt_ctx {
   int blur_rows = BL_SR;
   int* d_bin_prefix = nullptr;
   int* d_cap_table = nullptr;  // particle-capacity chunks per unit (trajectories)
+  Ingest* d_ingest = nullptr;   // per stream: how k_pyramid gets level 0
+  Ingest* h_ingest = nullptr;   // pinned host copy of what d_ingest holds
+  bool ingest_dirty = true;
+  int rgb_mode = GBT_RGB_CHANNEL0;
   int traj_T = 0;              // trajectory history length, 0 = off
   int nbins = 0;
   int* d_det_prefix = nullptr;
@@ -178,6 +184,7 @@ static void free_ctx(gbt_ctx* ctx) {
   for (void* p : ctx->allocs) cudaFree(p);
   for (auto& s : ctx->streams)
     if (s.pinned) cudaFreeHost(s.pinned);
+  if (ctx->h_ingest) cudaFreeHost(ctx->h_ingest);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
   delete ctx;
 }
@@ -330,6 +337,9 @@ static int build(gbt_ctx* ctx, const gbt_config* cfgs, int nstreams) {
     s.pinned_bytes = (size_t)u.H * u.W * 3;
     CK(cudaMallocHost((void**)&s.pinned, s.pinned_bytes));
   }
+  if ((r = dalloc_t(ctx, &ctx->d_ingest, nstreams))) return r;
+  CK(cudaMallocHost((void**)&ctx->h_ingest, sizeof(Ingest) * nstreams));
+  memset(ctx->h_ingest, 0, sizeof(Ingest) * nstreams);
   CK(cudaDeviceSynchronize());
   return GBT_OK;
 }
@@ -453,11 +463,11 @@ static int enqueue_frame(gbt_ctx* ctx, bool any_det, bool any_filt) {
   cudaStream_t st = ctx->stream;
   int n = 0;
   CK(cudaMemsetAsync(ctx->occ_all, 0, ctx->occ_bytes, st));
-  { PROF("k_pyramid"); k_pyramid<<<ctx->pyr_tiles[0], 256, 0, st>>>(ctx->d_units, ctx->d_stream_unit0, ctx->d_pyr_prefix[0], nstreams, 0); }
+  { PROF("k_pyramid"); k_pyramid<<<ctx->pyr_tiles[0], 256, 0, st>>>(ctx->d_units, ctx->d_stream_unit0, ctx->d_pyr_prefix[0], nstreams, 0, ctx->d_ingest); }
   n++;
   if (ctx->pyr_tiles[1] > 0) {
     PROF("k_pyramid5");
-    k_pyramid<<<ctx->pyr_tiles[1], 256, 0, st>>>(ctx->d_units, ctx->d_stream_unit0, ctx->d_pyr_prefix[1], nstreams, 5);
+    k_pyramid<<<ctx->pyr_tiles[1], 256, 0, st>>>(ctx->d_units, ctx->d_stream_unit0, ctx->d_pyr_prefix[1], nstreams, 5, ctx->d_ingest);
     n++;
   }
   {
@@ -590,6 +600,29 @@ extern "C" int gbt_get_tuning(gbt_ctx* ctx, int32_t knob, int32_t* value) {
   return GBT_E_INVALID;
 }
 
+// Uploads the per-stream ingest modes when they changed (ordered on the
+// context stream before the frame's kernels).
+static int set_ingest(gbt_ctx* ctx, size_t s, int mode) {
+  StreamInfo& si = ctx->streams[s];
+  Ingest want{mode ? si.d_rgb : nullptr, mode ? si.rgb_pitch : 0, mode, 0};
+  Ingest& have = ctx->h_ingest[s];
+  if (have.rgb != want.rgb || have.pitch != want.pitch || have.mode != want.mode) {
+    if (!ctx->ingest_dirty) CK(cudaStreamSynchronize(ctx->stream));  // h_ingest may feed a copy in flight
+    have = want;
+    ctx->ingest_dirty = true;
+  }
+  return GBT_OK;
+}
+
+static int flush_ingest(gbt_ctx* ctx) {
+  if (ctx->ingest_dirty) {
+    CK(cudaMemcpyAsync(ctx->d_ingest, ctx->h_ingest, sizeof(Ingest) * ctx->streams.size(), cudaMemcpyHostToDevice,
+                       ctx->stream));
+    ctx->ingest_dirty = false;
+  }
+  return GBT_OK;
+}
+
 extern "C" int gbt_trajectories_enable(gbt_ctx* ctx, int32_t history) {
   if (!ctx || history < 1 || history > 255) return GBT_E_INVALID;
   if (ctx->traj_T) return ctx->traj_T == history ? GBT_OK : GBT_E_INVALID;
@@ -621,6 +654,12 @@ extern "C" int gbt_use_graphs(gbt_ctx* ctx, int32_t enable) {
 extern "C" int gbt_run_resident(gbt_ctx* ctx) {
   if (!ctx) return GBT_E_INVALID;
   CK(cudaSetDevice(ctx->device));
+  for (size_t s = 0; s < ctx->streams.size(); s++) {
+    int r = set_ingest(ctx, s, 0);
+    if (r) return r;
+  }
+  int r = flush_ingest(ctx);
+  if (r) return r;
   return run_frame(ctx);
 }
 
@@ -631,6 +670,7 @@ extern "C" int gbt_run(gbt_ctx* ctx, const uint8_t* const* frames, const int64_t
     StreamInfo& si = ctx->streams[s];
     const Unit& u = ctx->units[si.unit0];
     const uint8_t* src = frames[s];
+    int mode = 0;
     if (!src) return set_err(ctx, GBT_E_INVALID, "frame %zu is NULL", s);
     if (location == GBT_FRAMES_DEVICE) {
       int64_t p = pitches ? pitches[s] : u.W;
@@ -650,21 +690,46 @@ extern "C" int gbt_run(gbt_ctx* ctx, const uint8_t* const* frames, const int64_t
         for (int r = 0; r < u.H; r++) memcpy(si.pinned + (size_t)r * u.W, src + (size_t)r * p, u.W);
         CK(cudaMemcpy2DAsync(u.img, u.ipitch, si.pinned, u.W, u.W, u.H, cudaMemcpyHostToDevice, ctx->stream));
       }
-    } else if (location == GBT_FRAMES_HOST_RGB) {
-      int64_t p = pitches ? pitches[s] : (int64_t)u.W * 3;
-      if (p < (int64_t)u.W * 3) return set_err(ctx, GBT_E_INVALID, "pitch too small for RGB");
-      CK(cudaStreamSynchronize(ctx->stream));
-      for (int r = 0; r < u.H; r++) {
-        const uint8_t* row = src + (size_t)r * p;
-        uint8_t* d = si.pinned + (size_t)r * u.W;
-        for (int c = 0; c < u.W; c++) d[c] = row[3 * c];  // get_x: channel 0 (dsl/get_comp.h:105)
+    } else if (location == GBT_FRAMES_HOST_RGB || location == GBT_FRAMES_DEVICE_RGB) {
+      const int64_t row = (int64_t)u.W * 3;
+      int64_t p = pitches ? pitches[s] : row;
+      if (p < row) return set_err(ctx, GBT_E_INVALID, "pitch %lld too small for RGB", (long long)p);
+      if (!si.d_rgb) {
+        si.rgb_pitch = (row + 15) / 16 * 16;
+        int r = dalloc(ctx, (void**)&si.d_rgb, (size_t)si.rgb_pitch * u.H, false);
+        if (r) return r;
       }
-      CK(cudaMemcpy2DAsync(u.img, u.ipitch, si.pinned, u.W, u.W, u.H, cudaMemcpyHostToDevice, ctx->stream));
+      if (location == GBT_FRAMES_DEVICE_RGB) {
+        CK(cudaMemcpy2DAsync(si.d_rgb, si.rgb_pitch, src, p, row, u.H, cudaMemcpyDeviceToDevice, ctx->stream));
+      } else {
+        cudaPointerAttributes at;
+        bool pinned = cudaPointerGetAttributes(&at, src) == cudaSuccess && at.type == cudaMemoryTypeHost;
+        cudaGetLastError();
+        if (!pinned) {
+          // The staging buffer may still feed the previous frame's copy.
+          CK(cudaStreamSynchronize(ctx->stream));
+          for (int rr = 0; rr < u.H; rr++) memcpy(si.pinned + (size_t)rr * row, src + (size_t)rr * p, row);
+          src = si.pinned;
+          p = row;
+        }
+        CK(cudaMemcpy2DAsync(si.d_rgb, si.rgb_pitch, src, p, row, u.H, cudaMemcpyHostToDevice, ctx->stream));
+      }
+      mode = ctx->rgb_mode == GBT_RGB_BT601 ? 2 : 1;
     } else {
       return set_err(ctx, GBT_E_INVALID, "bad frame location %d", location);
     }
+    int r = set_ingest(ctx, s, mode);
+    if (r) return r;
   }
+  int r = flush_ingest(ctx);
+  if (r) return r;
   return run_frame(ctx);
+}
+
+extern "C" int gbt_set_rgb_to_gray(gbt_ctx* ctx, int32_t mode) {
+  if (!ctx || (mode != GBT_RGB_CHANNEL0 && mode != GBT_RGB_BT601)) return GBT_E_INVALID;
+  ctx->rgb_mode = mode;
+  return GBT_OK;
 }
 
 extern "C" int gbt_sync(gbt_ctx* ctx) {

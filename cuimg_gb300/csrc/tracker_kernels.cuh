@@ -40,7 +40,8 @@ constexpr int PYR_TR = 32, PYR_TC = 128;
 
 __global__ void __launch_bounds__(256) k_pyramid(const Unit* __restrict__ units,
                                                  const int* __restrict__ stream_unit0,
-                                                 const int* __restrict__ tile_prefix, int nstreams, int base) {
+                                                 const int* __restrict__ tile_prefix, int nstreams, int base,
+                                                 const Ingest* __restrict__ ingest) {
   __shared__ __align__(16) uint8_t sm[2][PYR_TR * PYR_TC];
   const int t = blockIdx.x;
   const int s = find_unit(tile_prefix, nstreams, t);
@@ -48,19 +49,35 @@ __global__ void __launch_bounds__(256) k_pyramid(const Unit* __restrict__ units,
   const int u0 = stream_unit0[s];
   const Unit& B = units[u0 + base];
   const int nlev = min(B.nscales - 1 - base, 5);
-  if (nlev <= 0) return;
+  const Ingest in = base == 0 ? ingest[s] : Ingest{nullptr, 0, 0, 0};
+  if (nlev <= 0 && in.mode == 0) return;
   const int tw = (B.W + PYR_TC - 1) / PYR_TC;
   const int R0 = (local / tw) * PYR_TR, C0 = (local % tw) * PYR_TC;
 
-  // Load the level-`base` tile.
-  for (int v = threadIdx.x; v < PYR_TR * (PYR_TC / 16); v += blockDim.x) {
-    int r = v / (PYR_TC / 16), c16 = (v % (PYR_TC / 16)) * 16;
-    int gr = R0 + r, gc = C0 + c16;
-    uint8_t* d = &sm[0][r * PYR_TC + c16];
-    if (gr < B.H && gc + 16 <= B.W) {
-      *(uint4*)d = *(const uint4*)(B.img + (size_t)gr * B.ipitch + gc);
-    } else {
-      for (int j = 0; j < 16; j++) d[j] = (gr < B.H && gc + j < B.W) ? B.img[(size_t)gr * B.ipitch + gc + j] : 0;
+  if (in.mode != 0) {
+    // Fused ingest: RGB -> gray into level 0 and the shared tile.
+    for (int v = threadIdx.x; v < PYR_TR * PYR_TC; v += blockDim.x) {
+      const int r = v / PYR_TC, c = v % PYR_TC, gr = R0 + r, gc = C0 + c;
+      uint8_t g = 0;
+      if (gr < B.H && gc < B.W) {
+        const uint8_t* px = in.rgb + (size_t)gr * in.pitch + 3 * gc;
+        g = in.mode == 1 ? px[0] : (uint8_t)((77 * px[0] + 150 * px[1] + 29 * px[2] + 128) >> 8);
+        B.img[(size_t)gr * B.ipitch + gc] = g;
+      }
+      sm[0][r * PYR_TC + c] = g;
+    }
+    if (nlev <= 0) return;
+  } else {
+    // Load the level-`base` tile.
+    for (int v = threadIdx.x; v < PYR_TR * (PYR_TC / 16); v += blockDim.x) {
+      int r = v / (PYR_TC / 16), c16 = (v % (PYR_TC / 16)) * 16;
+      int gr = R0 + r, gc = C0 + c16;
+      uint8_t* d = &sm[0][r * PYR_TC + c16];
+      if (gr < B.H && gc + 16 <= B.W) {
+        *(uint4*)d = *(const uint4*)(B.img + (size_t)gr * B.ipitch + gc);
+      } else {
+        for (int j = 0; j < 16; j++) d[j] = (gr < B.H && gc + j < B.W) ? B.img[(size_t)gr * B.ipitch + gc + j] : 0;
+      }
     }
   }
   __syncthreads();

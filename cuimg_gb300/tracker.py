@@ -18,7 +18,8 @@ import numpy as np
 
 from ._native import GbtError, check, cuda_lib, gbt_config
 
-GBT_FRAMES_HOST, GBT_FRAMES_DEVICE, GBT_FRAMES_HOST_RGB = 0, 1, 2
+GBT_FRAMES_HOST, GBT_FRAMES_DEVICE, GBT_FRAMES_HOST_RGB, GBT_FRAMES_DEVICE_RGB = 0, 1, 2, 3
+GBT_RGB_CHANNEL0, GBT_RGB_BT601 = 0, 1
 STAGES = dict(input=0, s1=1, s2=2, contrast=3, saliency=4, mask=5, sparse=6)
 
 
@@ -279,6 +280,11 @@ class BatchTracker:
                                           feat.ctypes.data, matches.ctypes.data, ctypes.byref(nm),
                                           ctypes.byref(comp)), ctx)
         return dict(speed=speed, pos=pos, age=age, feat=feat, matches=matches[: nm.value], compact=bool(comp.value))
+
+    def set_rgb_to_gray(self, mode):
+        """GBT_RGB_CHANNEL0 (the reference's get_x) or GBT_RGB_BT601 for RGB frames."""
+        check(self._lib.gbt_set_rgb_to_gray(self._ensure(), int(mode)), self._ctx)
+        return self
 
     def enable_trajectories(self, history=20):
         """Keep every particle's last `history` positions on the GPU, in step

@@ -74,8 +74,19 @@ int gbt_last_error(gbt_ctx* ctx, char* buf, size_t len);
  * Replaces tracker<F>::run(const I& in) (tracker.hpp:72-80). */
 #define GBT_FRAMES_HOST 0
 #define GBT_FRAMES_DEVICE 1
-#define GBT_FRAMES_HOST_RGB 2   /* interleaved RGB, channel 0 is tracked (get_x) */
+#define GBT_FRAMES_HOST_RGB 2   /* interleaved RGB on the host */
+#define GBT_FRAMES_DEVICE_RGB 3 /* interleaved RGB on the device */
 int gbt_run(gbt_ctx* ctx, const uint8_t* const* frames, const int64_t* pitches, int32_t location);
+
+/* RGB frames are copied to the device as they are (3 bytes per pixel; one
+ * H2D copy straight from pinned host memory) and turned into gray inside the
+ * pyramid kernel, which writes level 0 and the coarser levels in one pass.
+ * GBT_RGB_CHANNEL0 (default) tracks channel 0, as the reference's sample does
+ * (get_x, dsl/get_comp.h:105; samples/tracking/main.cc:117); GBT_RGB_BT601
+ * tracks the luma (77 R + 150 G + 29 B + 128) >> 8 (not a reference path). */
+#define GBT_RGB_CHANNEL0 0
+#define GBT_RGB_BT601 1
+int gbt_set_rgb_to_gray(gbt_ctx* ctx, int32_t mode);
 
 /* Runs one frame for all streams from frames already placed in the
  * context's input slots (gbt_input_slot); used for CUDA-graph replay. */

@@ -140,6 +140,41 @@ def test_rgb_input_tracks_channel_zero():
     assert not diff_snapshots(a.snapshot(), b.snapshot(), True)
 
 
+@pytest.mark.parametrize("where", ["host", "host_pinned", "device"])
+@pytest.mark.parametrize("mode", [0, 1])
+@pytest.mark.parametrize("rows,cols,L", [(120, 160, 2), (121, 163, 1), (133, 301, 3)])
+def test_rgb_ingest_fused_in_pyramid(where, mode, rows, cols, L):
+    # RGB frames go to the device as they are and become gray inside the
+    # pyramid kernel; the result must equal tracking the gray image directly.
+    torch = pytest.importorskip("torch")
+    from cuimg_gb300 import synth
+    from cuimg_gb300.tracker import GBT_FRAMES_DEVICE_RGB, GBT_FRAMES_HOST_RGB
+    s = synth.Stream(17, rows, cols)
+    rng = np.random.default_rng(3)
+    a = _gpu_tracker(rows, cols, L, detf=2)
+    b = _gpu_tracker(rows, cols, L, detf=2)
+    b.set_rgb_to_gray(mode)
+    for t in range(5):
+        rgb = s.frame_rgb(t).copy()
+        rgb[..., 1] = rng.integers(0, 256, rgb.shape[:2])  # make the channels differ
+        r, g, bl = (rgb[..., k].astype(np.int32) for k in range(3))
+        gray = rgb[..., 0] if mode == 0 else ((77 * r + 150 * g + 29 * bl + 128) >> 8).astype(np.uint8)
+        a.run(np.ascontiguousarray(gray))
+        if where == "host":
+            b.run(rgb)
+        elif where == "host_pinned":
+            h = torch.from_numpy(rgb).pin_memory()
+            b.run((h.data_ptr(), cols * 3), location=GBT_FRAMES_HOST_RGB)
+            b.sync()
+        else:
+            d = torch.from_numpy(rgb).cuda()
+            b.run((d.data_ptr(), cols * 3), location=GBT_FRAMES_DEVICE_RGB)
+            b.sync()
+        assert not diff_snapshots(a.snapshot(), b.snapshot(), t % 2 == 0), t
+    a.close()
+    b.close()
+
+
 def test_deterministic_across_runs():
     from cuimg_gb300 import synth
     frames = synth.frames(8, 240, 320, 8)
