@@ -88,6 +88,9 @@ def _declare(lib):
     lib.gbt_kernel_launches.argtypes = [P, ctypes.POINTER(ctypes.c_int64)]
     lib.gbt_trajectories_enable.argtypes = [P, I32]
     lib.gbt_set_rgb_to_gray.argtypes = [P, I32]
+    lib.gbt_checkpoint_size.argtypes = [P, ctypes.POINTER(ctypes.c_size_t)]
+    lib.gbt_checkpoint_save.argtypes = [P, P, ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)]
+    lib.gbt_checkpoint_load.argtypes = [P, ctypes.c_char_p, ctypes.c_size_t]
     lib.gbt_get_trajectories.argtypes = [P, I32, I32, P, P, I32P, I32P]
     lib.gbt_read_counts.argtypes = [P, P, I32]
     lib.gbt_set_tuning.argtypes = [P, I32, I32]

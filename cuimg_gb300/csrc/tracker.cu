@@ -859,6 +859,182 @@ extern "C" int gbt_get_trajectories(gbt_ctx* ctx, int32_t stream, int32_t scale,
   return GBT_OK;
 }
 
+// ---------------------------------------------------------------------------
+// Checkpoint / resume: the tracker's whole carried state (particle_container:
+// particles, features, matches, counters, particle_container.h:171-182; the
+// strategy's frame counter, tracking_strategies.h:84-106; the device-side
+// trajectories) as one byte blob.
+namespace {
+struct CkHeader {
+  char magic[8];
+  uint32_t version;
+  int32_t nstreams, nunits, traj_T, host_frame, dev_f, dev_err, reserved;
+};
+constexpr char CK_MAGIC[8] = {'G', 'B', 'T', 'C', 'K', 'P', 'T', '1'};
+
+size_t unit_blob_bytes(const UState& s, int T) {
+  size_t n = (size_t)s.n;
+  return sizeof(UState) + n * (sizeof(short2) * 2 + sizeof(uint16_t) + sizeof(uint4)) + (size_t)s.nmatches * 4 +
+         (T ? n * (2 + (size_t)T * sizeof(short2)) : 0);
+}
+}  // namespace
+
+static int read_all_states(gbt_ctx* ctx, std::vector<UState>& st) {
+  st.resize(ctx->units.size());
+  CK(cudaStreamSynchronize(ctx->stream));
+  CK(cudaMemcpy(st.data(), ctx->d_state, st.size() * sizeof(UState), cudaMemcpyDeviceToHost));
+  return GBT_OK;
+}
+
+extern "C" int gbt_checkpoint_size(gbt_ctx* ctx, size_t* bytes) {
+  if (!ctx || !bytes) return GBT_E_INVALID;
+  CK(cudaSetDevice(ctx->device));
+  std::vector<UState> st;
+  int r = read_all_states(ctx, st);
+  if (r) return r;
+  size_t b = sizeof(CkHeader) + ctx->streams.size() * sizeof(gbt_config);
+  for (auto& s : st) b += unit_blob_bytes(s, ctx->traj_T);
+  *bytes = b;
+  return GBT_OK;
+}
+
+extern "C" int gbt_checkpoint_save(gbt_ctx* ctx, void* buf, size_t cap, size_t* written) {
+  if (!ctx || !buf) return GBT_E_INVALID;
+  CK(cudaSetDevice(ctx->device));
+  size_t need;
+  int r = gbt_checkpoint_size(ctx, &need);
+  if (r) return r;
+  if (cap < need) return set_err(ctx, GBT_E_INVALID, "checkpoint needs %zu bytes", need);
+  std::vector<UState> st;
+  if ((r = read_all_states(ctx, st))) return r;
+  Frame fr;
+  CK(cudaMemcpy(&fr, ctx->d_frame, sizeof(Frame), cudaMemcpyDeviceToHost));
+  uint8_t* o = (uint8_t*)buf;
+  CkHeader h{};
+  memcpy(h.magic, CK_MAGIC, 8);
+  h.version = 1;
+  h.nstreams = (int32_t)ctx->streams.size();
+  h.nunits = (int32_t)ctx->units.size();
+  h.traj_T = ctx->traj_T;
+  h.host_frame = ctx->host_frame;
+  h.dev_f = fr.f;
+  h.dev_err = fr.err;
+  memcpy(o, &h, sizeof h);
+  o += sizeof h;
+  for (auto& si : ctx->streams) {
+    memcpy(o, &si.cfg, sizeof(gbt_config));
+    o += sizeof(gbt_config);
+  }
+  const int T = ctx->traj_T;
+  for (size_t k = 0; k < ctx->units.size(); k++) {
+    const Unit& u = ctx->units[k];
+    UState s = st[k];
+    const int b = s.cur, n = s.n;
+    s.cur = 0;  // stored as buffer 0
+    memcpy(o, &s, sizeof s);
+    o += sizeof s;
+    auto get = [&](const void* src, size_t bytes) -> int {
+      if (bytes) CK(cudaMemcpy(o, src, bytes, cudaMemcpyDeviceToHost));
+      o += bytes;
+      return GBT_OK;
+    };
+    if ((r = get(u.pos[b], n * sizeof(short2))) || (r = get(u.spd[b], n * sizeof(short2))) ||
+        (r = get(u.age[b], n * sizeof(uint16_t))) || (r = get(u.feat[b], n * sizeof(uint4))) ||
+        (r = get(u.matches, (size_t)s.nmatches * 4)))
+      return r;
+    if (T) {
+      if ((r = get(u.tlen[b], n)) || (r = get(u.thead[b], n))) return r;
+      if (n) CK(cudaMemcpy2D(o, n * sizeof(short2), u.tpos[b], (size_t)u.cap * sizeof(short2), n * sizeof(short2), T,
+                             cudaMemcpyDeviceToHost));
+      o += (size_t)T * n * sizeof(short2);
+    }
+  }
+  if (written) *written = (size_t)(o - (uint8_t*)buf);
+  return GBT_OK;
+}
+
+extern "C" int gbt_checkpoint_load(gbt_ctx* ctx, const void* buf, size_t len) {
+  if (!ctx || !buf || len < sizeof(CkHeader)) return GBT_E_INVALID;
+  CK(cudaSetDevice(ctx->device));
+  const uint8_t* p = (const uint8_t*)buf;
+  const uint8_t* end = p + len;
+  CkHeader h;
+  memcpy(&h, p, sizeof h);
+  p += sizeof h;
+  if (memcmp(h.magic, CK_MAGIC, 8) != 0 || h.version != 1 || h.nstreams != (int32_t)ctx->streams.size() ||
+      h.nunits != (int32_t)ctx->units.size())
+    return set_err(ctx, GBT_E_INVALID, "checkpoint does not belong to a context of this shape");
+  if ((size_t)(end - p) < ctx->streams.size() * sizeof(gbt_config)) return GBT_E_INVALID;
+  for (auto& si : ctx->streams) {
+    if (memcmp(p, &si.cfg, sizeof(gbt_config)) != 0)
+      return set_err(ctx, GBT_E_INVALID, "checkpoint stream configuration differs");
+    p += sizeof(gbt_config);
+  }
+  const int T = h.traj_T;
+  if (T < 0 || T > 255 || (ctx->traj_T && T && ctx->traj_T != T))
+    return set_err(ctx, GBT_E_INVALID, "checkpoint trajectory length differs");
+  // Validate every unit before changing anything.
+  {
+    const uint8_t* q = p;
+    for (size_t k = 0; k < ctx->units.size(); k++) {
+      const Unit& u = ctx->units[k];
+      UState s;
+      if ((size_t)(end - q) < sizeof(UState)) return set_err(ctx, GBT_E_INVALID, "checkpoint is truncated");
+      memcpy(&s, q, sizeof s);
+      if (s.n < 0 || s.n > u.cap || s.nmatches < 0 || s.nmatches > u.cap + u.TH * u.TW || s.cur != 0)
+        return set_err(ctx, GBT_E_INVALID, "checkpoint unit %zu is inconsistent", k);
+      if ((size_t)(end - q) < unit_blob_bytes(s, T)) return set_err(ctx, GBT_E_INVALID, "checkpoint is truncated");
+      q += unit_blob_bytes(s, T);
+    }
+  }
+  if (T && ctx->traj_T != T) {
+    int r = gbt_trajectories_enable(ctx, T);
+    if (r) return r;
+  }
+  CK(cudaStreamSynchronize(ctx->stream));
+  std::vector<UState> st(ctx->units.size());
+  for (size_t k = 0; k < ctx->units.size(); k++) {
+    const Unit& u = ctx->units[k];
+    UState s;
+    memcpy(&s, p, sizeof s);
+    p += sizeof s;
+    const int n = s.n;
+    auto put = [&](void* dst, size_t bytes) -> int {
+      if (bytes) CK(cudaMemcpy(dst, p, bytes, cudaMemcpyHostToDevice));
+      p += bytes;
+      return GBT_OK;
+    };
+    int r;
+    if ((r = put(u.pos[0], n * sizeof(short2))) || (r = put(u.spd[0], n * sizeof(short2))) ||
+        (r = put(u.age[0], n * sizeof(uint16_t))) || (r = put(u.feat[0], n * sizeof(uint4))) ||
+        (r = put(u.matches, (size_t)s.nmatches * 4)))
+      return r;
+    if (T) {
+      if ((r = put(u.tlen[0], n)) || (r = put(u.thead[0], n))) return r;
+      if (n) CK(cudaMemcpy2D(u.tpos[0], (size_t)u.cap * sizeof(short2), p, n * sizeof(short2), n * sizeof(short2), T,
+                             cudaMemcpyHostToDevice));
+      p += (size_t)T * n * sizeof(short2);
+    }
+    if (ctx->traj_T && !T) {  // a blob without trajectories: histories start empty
+      CK(cudaMemset(u.tlen[0], 0, u.cap));
+      CK(cudaMemset(u.thead[0], 0, u.cap));
+    }
+    // Sparse-index entries of this context's own earlier frames could carry
+    // the stamps of the frames to come: start from "nothing current".
+    CK(cudaMemset(u.idx, 0, (size_t)u.H * u.W * sizeof(unsigned long long)));
+    st[k] = s;
+  }
+  CK(cudaMemcpy(ctx->d_state, st.data(), st.size() * sizeof(UState), cudaMemcpyHostToDevice));
+  Frame fr{h.dev_f, h.dev_err};
+  CK(cudaMemcpy(ctx->d_frame, &fr, sizeof fr, cudaMemcpyHostToDevice));
+  // The chunk table of the first frame after the load follows the new counts.
+  k_tick_table<<<1, 1024, 0, ctx->stream>>>(ctx->d_units, ctx->d_state, (int)ctx->units.size(), ctx->d_pre);
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(ctx->stream));
+  ctx->host_frame = h.host_frame;
+  return GBT_OK;
+}
+
 extern "C" int gbt_bins(gbt_ctx* ctx, int32_t stream, int32_t scale, int32_t* rows, int32_t* cols) {
   int ui = unit_of(ctx, stream, scale);
   if (ui < 0) return GBT_E_INVALID;

@@ -1526,6 +1526,13 @@ __global__ void __launch_bounds__(CHUNK) k_traj(const Unit* __restrict__ units, 
   }
 }
 
+// Rebuilds the per-frame chunk table from the current counters (after a
+// checkpoint load).
+__global__ void __launch_bounds__(1024) k_tick_table(const Unit* __restrict__ units, const UState* __restrict__ st,
+                                                     int nunits, int* __restrict__ pre_table) {
+  build_table(units, st, nunits, pre_table);
+}
+
 __global__ void __launch_bounds__(1024) k_tick(const Unit* __restrict__ units, const UState* __restrict__ st,
                                                Frame* __restrict__ fr, int* __restrict__ pre_table, int nunits) {
   build_table(units, st, nunits, pre_table);

@@ -281,6 +281,22 @@ class BatchTracker:
                                           ctypes.byref(comp)), ctx)
         return dict(speed=speed, pos=pos, age=age, feat=feat, matches=matches[: nm.value], compact=bool(comp.value))
 
+    def checkpoint(self):
+        """The carried state of every stream as bytes (gbt_checkpoint_save)."""
+        ctx = self._ensure()
+        n = ctypes.c_size_t()
+        check(self._lib.gbt_checkpoint_size(ctx, ctypes.byref(n)), ctx)
+        buf = ctypes.create_string_buffer(n.value)
+        w = ctypes.c_size_t()
+        check(self._lib.gbt_checkpoint_save(ctx, buf, n.value, ctypes.byref(w)), ctx)
+        return buf.raw[: w.value]
+
+    def restore(self, blob):
+        """Continue from a checkpoint of a tracker with the same configuration."""
+        ctx = self._ensure()
+        check(self._lib.gbt_checkpoint_load(ctx, blob, len(blob)), ctx)
+        return self
+
     def set_rgb_to_gray(self, mode):
         """GBT_RGB_CHANNEL0 (the reference's get_x) or GBT_RGB_BT601 for RGB frames."""
         check(self._lib.gbt_set_rgb_to_gray(self._ensure(), int(mode)), self._ctx)

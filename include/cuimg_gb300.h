@@ -163,6 +163,16 @@ int gbt_trajectories_enable(gbt_ctx* ctx, int32_t history);
 int gbt_get_trajectories(gbt_ctx* ctx, int32_t stream, int32_t scale, int16_t* xy, uint8_t* len, int32_t* n,
                          int32_t* history);
 
+/* Checkpoint / resume.  The carried state of every stream and scale (the
+ * particle_container's particles, features, matches and counters,
+ * particle_container.h:171-182; the frame counter, tracking_strategies.h:84-106;
+ * the device-side trajectories) as one byte blob.  gbt_checkpoint_load accepts
+ * only a blob saved from a context with the same stream configurations and
+ * continues bit for bit where the saved context stood. */
+int gbt_checkpoint_size(gbt_ctx* ctx, size_t* bytes);
+int gbt_checkpoint_save(gbt_ctx* ctx, void* buf, size_t cap, size_t* written);
+int gbt_checkpoint_load(gbt_ctx* ctx, const void* buf, size_t len);
+
 /* Tuning knobs (results are identical for every setting; only speed
  * changes).  GBT_TUNE_MATCHER: 0 = particles binned by prediction into
  * 32 x 128 tiles, one CTA per tile matching from shared memory, 1 = one warp
