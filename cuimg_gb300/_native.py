@@ -59,7 +59,7 @@ def synth_lib():
 class gbt_config(ctypes.Structure):
     _fields_ = [(n, ctypes.c_int32) for n in (
         "rows", "cols", "nscales", "detector_threshold", "detector_n", "detector_frequency",
-        "filtering_frequency", "k", "with_merge")]
+        "filtering_frequency", "k", "with_merge", "detector", "detector_step", "detector_grad_th")]
 
 
 def _declare(lib):

@@ -36,6 +36,9 @@ struct Unit {
   int stream, scale, nscales;
   int upper;        // unit index of scale + 1 of the same stream, -1 at the top
   int threshold, nfast, k, det_freq, filt_freq, with_merge;
+  int det_kind, det_step, det_grad_th;  // GBT_DETECTOR_*, regular_detector step / grad_th
+  int max_births;                       // births one detector frame can add
+  int birth_items;                      // ordered birth candidates (3 x tiles for FAST, pixels otherwise)
   // images
   uint8_t* img;
   int ipitch;

@@ -90,6 +90,7 @@ struct gbt_ctx {
   long long kernels_total = 0;  // kernels launched by this context, graph nodes included
   int match_variant = 0;  // GBT_TUNE_MATCHER
   bool fixed_fpitch = true;  // every unit's s1/s2 pitch is FIXED_FPITCH
+  bool any_alt_detector = false;  // a stream uses the regular or the dense detector
   std::string err;
   // scratch for stage dumps
   void* dump_buf = nullptr;
@@ -158,6 +159,9 @@ extern "C" void gbt_config_default(gbt_config* cfg, int32_t rows, int32_t cols, 
   cfg->filtering_frequency = 1;
   cfg->k = 300;
   cfg->with_merge = 1;
+  cfg->detector = GBT_DETECTOR_FAST;
+  cfg->detector_step = 1;   // regular_detector defaults (regular_detector.hpp:12-17)
+  cfg->detector_grad_th = 1;
 }
 
 extern "C" int gbt_sizes_ok(int32_t rows, int32_t cols, int32_t nscales) {
@@ -215,6 +219,9 @@ static int build(gbt_ctx* ctx, const gbt_config* cfgs, int nstreams) {
       u.det_freq = c.detector_frequency;
       u.filt_freq = c.filtering_frequency;
       u.with_merge = c.with_merge;
+      u.det_kind = c.detector;
+      u.det_step = c.detector_step;
+      u.det_grad_th = c.detector_grad_th;
       u.BH = (H + 7) / 8;
       u.BW = (W + 7) / 8;
       u.TH = H / 3;
@@ -249,7 +256,18 @@ static int build(gbt_ctx* ctx, const gbt_config* cfgs, int nstreams) {
     if ((r = dalloc_t(ctx, &u.st_sp, nb))) return r;
     if ((r = dalloc_t(ctx, &u.flow, nb))) return r;
     if ((r = dalloc_t(ctx, &u.msc, nb))) return r;
-    u.cap = u.H * u.W / 6 + 4096;
+    if (u.det_kind == GBT_DETECTOR_FAST) {
+      u.max_births = u.TH * u.TW;
+      u.birth_items = 3 * u.TH * u.TW;
+      u.cap = u.H * u.W / 6 + 4096;
+    } else {
+      u.max_births = u.det_kind == GBT_DETECTOR_DENSE
+                         ? u.H * u.W
+                         : ((u.H + u.det_step - 1) / u.det_step) * ((u.W + u.det_step - 1) / u.det_step);
+      u.birth_items = u.H * u.W;
+      u.cap = 4 * u.max_births + 4096;  // both detectors add particles where some already are
+    }
+    if (u.det_kind != GBT_DETECTOR_FAST) ctx->any_alt_detector = true;
     u.cap = round_up(u.cap, CHUNK);
     u.max_chunks = u.cap / CHUNK;
     u.MTR = (u.H + MT_R - 1) / MT_R;
@@ -263,10 +281,10 @@ static int build(gbt_ctx* ctx, const gbt_config* cfgs, int nstreams) {
       if ((r = dalloc_t(ctx, &u.age[b], u.cap))) return r;
       if ((r = dalloc_t(ctx, &u.feat[b], u.cap))) return r;
     }
-    if ((r = dalloc_t(ctx, &u.matches, (size_t)u.cap + (size_t)u.TH * u.TW))) return r;
+    if ((r = dalloc_t(ctx, &u.matches, (size_t)u.cap + (size_t)u.max_births))) return r;
     if ((r = dalloc_t(ctx, &u.chunk_cnt, u.max_chunks))) return r;
     if ((r = dalloc_t(ctx, &u.tilecode, (size_t)u.TH * u.TW + 1))) return r;
-    u.birth_chunks = (3 * u.TH * u.TW + CHUNK - 1) / CHUNK;
+    u.birth_chunks = (u.birth_items + CHUNK - 1) / CHUNK;
     if ((r = dalloc_t(ctx, &u.birth_cnt, u.birth_chunks + 1))) return r;
     if ((r = dalloc_t(ctx, &u.act_cnt, u.max_chunks))) return r;
     if ((r = dalloc_t(ctx, &u.cmask, u.cap))) return r;
@@ -351,7 +369,8 @@ extern "C" int gbt_create(const gbt_config* cfgs, int32_t nstreams, int32_t devi
   for (int s = 0; s < nstreams; s++) {
     const gbt_config& c = cfgs[s];
     if (!gbt_sizes_ok(c.rows, c.cols, c.nscales) || c.detector_frequency < 1 || c.filtering_frequency < 1 ||
-        c.detector_n < 1 || c.detector_n > 16 || c.detector_threshold < 0)
+        c.detector_n < 1 || c.detector_n > 16 || c.detector_threshold < 0 || c.detector < GBT_DETECTOR_FAST ||
+        c.detector > GBT_DETECTOR_DENSE || c.detector_step < 1)
       return GBT_E_INVALID;
   }
   gbt_ctx* ctx = new gbt_ctx;
@@ -505,6 +524,11 @@ static int enqueue_frame(gbt_ctx* ctx, bool any_det, bool any_filt) {
     CK(cudaMemsetAsync(ctx->pmask_all, 0, ctx->pmask_bytes, st));
     { PROF("k_pmask"); k_pmask<<<pgrid, CHUNK, 0, st>>>(ctx->d_units, ctx->d_state, ctx->d_frame, ctx->d_pre, nunits); }
     { PROF("k_detect"); k_detect<<<ctx->det_blocks, 256, 0, st>>>(ctx->d_units, ctx->d_frame, ctx->d_det_prefix, nunits); }
+    if (ctx->any_alt_detector) {
+      PROF("k_detect_alt");
+      k_detect_alt<<<(ctx->nbins + 255) / 256, 256, 0, st>>>(ctx->d_units, ctx->d_frame, ctx->d_bin_prefix, nunits);
+      n++;
+    }
     { PROF("k_det_count"); k_det_count<<<pgrid, CHUNK, 0, st>>>(ctx->d_units, ctx->d_state, ctx->d_frame, ctx->d_pre, ctx->d_btable, nunits); }
     { PROF("k_unit_scan"); k_unit_scan<<<nunits, 1024, 0, st>>>(ctx->d_units, ctx->d_state, ctx->d_frame, 0); }
     { PROF("k_det_scatter"); k_det_scatter<<<pgrid, CHUNK, 0, st>>>(ctx->d_units, ctx->d_state, ctx->d_frame, ctx->d_pre, ctx->d_btable,
@@ -981,7 +1005,7 @@ extern "C" int gbt_checkpoint_load(gbt_ctx* ctx, const void* buf, size_t len) {
       UState s;
       if ((size_t)(end - q) < sizeof(UState)) return set_err(ctx, GBT_E_INVALID, "checkpoint is truncated");
       memcpy(&s, q, sizeof s);
-      if (s.n < 0 || s.n > u.cap || s.nmatches < 0 || s.nmatches > u.cap + u.TH * u.TW || s.cur != 0)
+      if (s.n < 0 || s.n > u.cap || s.nmatches < 0 || s.nmatches > u.cap + u.max_births || s.cur != 0)
         return set_err(ctx, GBT_E_INVALID, "checkpoint unit %zu is inconsistent", k);
       if ((size_t)(end - q) < unit_blob_bytes(s, T)) return set_err(ctx, GBT_E_INVALID, "checkpoint is truncated");
       q += unit_blob_bytes(s, T);

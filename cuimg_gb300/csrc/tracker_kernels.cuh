@@ -857,7 +857,7 @@ __global__ void __launch_bounds__(CHUNK) k_pmask(const Unit* __restrict__ units,
   for (int g = blockIdx.x; g < total; g += gridDim.x) {
     ChunkCursor cc = chunk_of(table, nunits, g);
     const Unit& u = units[cc.unit];
-    if (!det_frame(u, f)) continue;
+    if (!det_frame(u, f) || u.det_kind != GBT_DETECTOR_FAST) continue;
     const UState s = st[cc.unit];
     const int i = cc.chunk * CHUNK + threadIdx.x;
     if (i >= s.n) continue;
@@ -947,7 +947,7 @@ __global__ void __launch_bounds__(256) k_detect(const Unit* __restrict__ units, 
   const int t = blockIdx.x;
   const int ui = find_unit(blk_prefix, nunits, t);
   const Unit& u = units[ui];
-  if (!det_frame(u, f)) return;
+  if (!det_frame(u, f) || u.det_kind != GBT_DETECTOR_FAST) return;
   const int local = t - blk_prefix[ui];
   const int bw = (u.TW + DT_C - 1) / DT_C;
   const int TR0 = (local / bw) * DT_R, TC0 = (local % bw) * DT_C;
@@ -1022,10 +1022,59 @@ __global__ void __launch_bounds__(256) k_detect(const Unit* __restrict__ units, 
   }
 }
 
-// Birth items are ordered (tile row, row inside the tile, tile column), which
-// is the raster order of the birth pixels (st_apply2d over
-// domain - border(3), fast_detector.hpp:256-260).
+// The regular and dense detectors (regular_detector.hpp:62-103,
+// dense_detector.hpp:19-31): one thread per 8x8 bin writes the bin's birth
+// bits into `pmask` (which the FAST mask does not use for these units).
+// Regular: pixels whose row and column are multiples of `step` and whose
+// contrast -- the mean of |I(p + 2 c8_h[i]) - I(p)| over the 8 neighbours, on
+// domain - border(1), 0 on the outer ring -- reaches grad_th (existing
+// particles are not checked).  Dense: every pixel no particle matched to.
+__global__ void __launch_bounds__(256) k_detect_alt(const Unit* __restrict__ units, const Frame* __restrict__ fr,
+                                                    const int* __restrict__ bin_prefix, int nunits) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= bin_prefix[nunits]) return;
+  const int ui = find_unit(bin_prefix, nunits, t);
+  const Unit& u = units[ui];
+  if (u.det_kind == GBT_DETECTOR_FAST || !det_frame(u, fr->f)) return;
+  const int local = t - bin_prefix[ui];
+  const int br = local / u.BW, bc = local % u.BW;
+  unsigned long long w = 0;
+  if (u.det_kind == GBT_DETECTOR_DENSE) {
+    w = ~u.occ[local];
+  } else {
+    for (int k = 0; k < 64; k++) {
+      const int r = br * 8 + (k >> 3), c = bc * 8 + (k & 7);
+      if (r % u.det_step || c % u.det_step) continue;
+      int rc = 0;
+      if (r >= 1 && r <= u.H - 2 && c >= 1 && c <= u.W - 2) {
+        const int vp = img_at(u, r, c);
+        int res = 0;
+#pragma unroll
+        for (int i = 0; i < 8; i++) res += abs(img_at(u, r + 2 * c8r(i), c + 2 * c8c(i)) - vp);
+        rc = res / 8;
+      }
+      if (rc >= u.det_grad_th) w |= 1ull << k;
+    }
+  }
+  // Pixels outside the domain (last bin row / column) never give birth.
+  const int vr = min(8, u.H - br * 8), vc = min(8, u.W - bc * 8);
+  unsigned long long valid = 0;
+  for (int k = 0; k < 64; k++)
+    if ((k >> 3) < vr && (k & 7) < vc) valid |= 1ull << k;
+  u.pmask[local] = w & valid;
+}
+
+// Birth items.  FAST: ordered (tile row, row inside the tile, tile column),
+// which is the raster order of the birth pixels (st_apply2d over
+// domain - border(3), fast_detector.hpp:256-260).  Regular / dense: the
+// pixels of the domain in raster order (domain - border(0)), births where
+// k_detect_alt set a bit.
 __device__ __forceinline__ bool birth_item(const Unit& u, int v, int& r, int& c) {
+  if (u.det_kind != GBT_DETECTOR_FAST) {
+    r = v / u.W;
+    c = v % u.W;
+    return (u.pmask[bin_word(u, r, c)] & bin_bit(r, c)) != 0;
+  }
   const int per = u.TW;
   int row3 = v / per, tc = v % per;
   int tr = row3 / 3, dr = row3 % 3;
@@ -1054,7 +1103,7 @@ __global__ void __launch_bounds__(CHUNK) k_det_count(const Unit* __restrict__ un
     bool pred;
     if (births) {
       int r, c;
-      pred = i < 3 * u.TH * u.TW && birth_item(u, i, r, c);
+      pred = i < u.birth_items && birth_item(u, i, r, c);
     } else {
       const UState s = st[cc.unit];
       pred = i < s.n && u.age[s.cur][i] != 0;
@@ -1159,7 +1208,7 @@ __global__ void __launch_bounds__(CHUNK) k_det_scatter(const Unit* __restrict__ 
       }
     } else {
       int r = 0, c = 0;
-      bool born = i < 3 * u.TH * u.TW && birth_item(u, i, r, c);
+      bool born = i < u.birth_items && birth_item(u, i, r, c);
       int total;
       int k = u.birth_cnt[cc.chunk] + block_prefix(born, wt, total);
       if (born) {

@@ -47,7 +47,26 @@ typedef struct {
   int32_t filtering_frequency;  /* generic_strategy::set_filtering_frequency */
   int32_t k;                    /* generic_strategy::set_k (default 300) */
   int32_t with_merge;           /* generic_strategy::set_with_merge (default 1) */
+  int32_t detector;             /* GBT_DETECTOR_*: the strategy's detector (default FAST) */
+  int32_t detector_step;        /* regular_detector::set_step (default 1) */
+  int32_t detector_grad_th;     /* regular_detector::set_grad_th (default 1) */
 } gbt_config;
+
+/* Detectors of the reference's generic strategy (tracking_strategies.h):
+ * bc2s_fast_gradient_cpu (fast_detector), bc2s_regular_gradient_cpu
+ * (regular_detector: a particle at every `step`-th pixel of every row and
+ * column whose 8-neighbour contrast at distance 2, averaged, reaches
+ * `grad_th`, regular_detector.hpp:62-103) and bc2s_dense_gradient_cpu
+ * (dense_detector: a particle at every pixel without one,
+ * dense_detector.hpp:19-31).  Births are added in raster order before the
+ * compaction, like the FAST births.  The particle capacity of a level is
+ * H*W/6 + 4096 for FAST, 4 * ceil(H/step) * ceil(W/step) + 4096 for regular
+ * and 4*H*W + 4096 for dense (neither checks for particles already at a
+ * pixel the way FAST does, so the reference's counts grow without bound);
+ * gbt_run reports GBT_E_CAPACITY when births overflow it. */
+#define GBT_DETECTOR_FAST 0
+#define GBT_DETECTOR_REGULAR 1
+#define GBT_DETECTOR_DENSE 2
 
 /* Fills `cfg` with the reference defaults for a rows x cols stream. */
 void gbt_config_default(gbt_config* cfg, int32_t rows, int32_t cols, int32_t nscales);

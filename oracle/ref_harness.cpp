@@ -298,3 +298,92 @@ void reflk_get(void* h, int scale, float* pos, uint16_t* age) {
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// The generic strategy with the reference's other detectors:
+// tracker<bc2s_regular_gradient_cpu> (regular_detector) and
+// tracker<bc2s_dense_gradient_cpu> (dense_detector),
+// cuimg/tracking2/tracking_strategies.h:169-181,216-227.  Particles, features
+// and matches only.
+struct refx_base {
+  virtual ~refx_base() {}
+  virtual void run(const host_image2d<gl8u>& in) = 0;
+  virtual int nparticles(int s) = 0;
+  virtual int compact_has_run(int s) = 0;
+  virtual void get(int s, float* speed, int16_t* pos, uint16_t* age, uint8_t* feat, int32_t* matches,
+                   int* nmatches) = 0;
+  obox2d dom;
+};
+
+template <typename ST>
+struct refx_impl : refx_base {
+  tracker<ST>* tr;
+  ~refx_impl() { delete tr; }
+  void run(const host_image2d<gl8u>& in) { tr->run(in); }
+  int nparticles(int s) { return tr->scale(s).pset().size(); }
+  int compact_has_run(int s) { return tr->scale(s).pset().compact_has_run(); }
+  void get(int s, float* speed, int16_t* pos, uint16_t* age, uint8_t* feat, int32_t* matches, int* nmatches) {
+    auto& ps = tr->scale(s).pset();
+    const auto& P = ps.dense_particles();
+    const auto& F = ps.features();
+    for (size_t i = 0; i < P.size(); i++) {
+      speed[2 * i] = P[i].speed.x;
+      speed[2 * i + 1] = P[i].speed.y;
+      pos[2 * i] = P[i].pos.x;
+      pos[2 * i + 1] = P[i].pos.y;
+      age[i] = P[i].age;
+      for (int j = 0; j < 16; j++) {
+        feat[32 * i + j] = F[i].distances[j];
+        feat[32 * i + 16 + j] = F[i].weights[j];
+      }
+    }
+    const auto& M = ps.matches();
+    *nmatches = (int)M.size();
+    if (matches)
+      for (size_t i = 0; i < M.size(); i++) matches[i] = (int32_t)M[i];
+  }
+};
+
+extern "C" {
+
+// kind 1: regular (step, grad_th), kind 2: dense.
+void* refx_create(int kind, int rows, int cols, int nscales, int detector_frequency, int filtering_frequency,
+                  int step, int grad_th) {
+  refx_base* b = nullptr;
+  obox2d dom(rows, cols);
+  if (kind == 1) {
+    auto* x = new refx_impl<tracking_strategies::bc2s_regular_gradient_cpu>;
+    x->tr = new tracker<tracking_strategies::bc2s_regular_gradient_cpu>(dom, nscales);
+    x->tr->strategy().set_detector_frequency(detector_frequency);
+    x->tr->strategy().set_filtering_frequency(filtering_frequency);
+    for (int s = 0; s < nscales; s++) x->tr->scale(s).strategy().detector().set_step(step).set_grad_th(grad_th);
+    b = x;
+  } else if (kind == 2) {
+    auto* x = new refx_impl<tracking_strategies::bc2s_dense_gradient_cpu>;
+    x->tr = new tracker<tracking_strategies::bc2s_dense_gradient_cpu>(dom, nscales);
+    x->tr->strategy().set_detector_frequency(detector_frequency);
+    x->tr->strategy().set_filtering_frequency(filtering_frequency);
+    b = x;
+  }
+  if (b) b->dom = dom;
+  return b;
+}
+
+void refx_destroy(void* h) { delete (refx_base*)h; }
+
+void refx_run(void* h, const uint8_t* frame) {
+  refx_base* b = (refx_base*)h;
+  host_image2d<gl8u> in(b->dom);
+  for (int r = 0; r < b->dom.nrows(); r++)
+    std::memcpy(&in(r, 0), frame + (size_t)r * b->dom.ncols(), b->dom.ncols());
+  b->run(in);
+}
+
+int refx_nparticles(void* h, int s) { return ((refx_base*)h)->nparticles(s); }
+int refx_compact_has_run(void* h, int s) { return ((refx_base*)h)->compact_has_run(s); }
+void refx_get_particles(void* h, int s, float* speed, int16_t* pos, uint16_t* age, uint8_t* feat,
+                        int32_t* matches, int* nmatches) {
+  ((refx_base*)h)->get(s, speed, pos, age, feat, matches, nmatches);
+}
+
+}  // extern "C"

@@ -72,6 +72,7 @@ typedef struct {
   int L;
   olevel* lv;
   int threshold, det_freq, filt_freq, k, with_merge, n_fast;
+  int detector, step, grad_th; /* 0 FAST, 1 regular, 2 dense */
 } otracker;
 
 #define AT(img, pitch, b, r, c) ((img)[(size_t)((r) + (b)) * (pitch) + ((c) + (b))])
@@ -479,9 +480,53 @@ static uint8_t fast_saliency(const olevel* l, int r, int c, int n_, int th) {
  * (fast_detector.hpp:296-313), new_particles(cpu) (:217-262),
  * particle_container::add (particle_container.hpp:370-387) and compact(cpu)
  * (:215-252). */
+static int add_particle(olevel* l, int r, int c) {
+  if (particles_reserve(l, l->n + 1)) return -1;
+  int i = l->n++;
+  l->age[i] = 1;
+  l->speed[2 * i] = 0.f;
+  l->speed[2 * i + 1] = 0.f;
+  l->pos[2 * i] = (int16_t)r;
+  l->pos[2 * i + 1] = (int16_t)c;
+  compute_feature(l, r, c, l->feat + 16 * (size_t)i);
+  AT(l->sparse, l->psp, 7, r, c) = (uint32_t)i;
+  return 0;
+}
+
+/* regular_detector::update + new_particles (regular_detector.hpp:62-103):
+ * contrast = mean over the 8 neighbours at distance 2 of |I(q) - I(p)| on
+ * domain - border(1) (the outer ring is never written: 0); a particle at every
+ * pixel whose row and column are multiples of step and whose contrast reaches
+ * grad_th, in raster order over the whole domain.  dense_detector
+ * (dense_detector.hpp:19-31): a particle at every pixel without one. */
+static int alt_births(otracker* t, olevel* l) {
+  int H = l->H, W = l->W;
+  for (int r = 0; r < H; r++)
+    for (int c = 0; c < W; c++) {
+      if (t->detector == 2) {
+        if (AT(l->sparse, l->psp, 7, r, c) != SPARSE_NONE) continue;
+      } else {
+        if (r % t->step || c % t->step) continue;
+        int rc = 0;
+        if (r >= 1 && r <= H - 2 && c >= 1 && c <= W - 2) {
+          int vp = AT(l->in, l->pin, 6, r, c), res = 0;
+          for (int i = 0; i < 8; i++) res += abs((int)AT(l->in, l->pin, 6, r + 2 * C8[i][0], c + 2 * C8[i][1]) - vp);
+          rc = res / 8;
+        }
+        if (rc < t->grad_th) continue;
+      }
+      if (add_particle(l, r, c)) return -1;
+    }
+  return 0;
+}
+
 static int detect_and_compact(otracker* t, int s) {
   olevel* l = &t->lv[s];
   int H = l->H, W = l->W;
+  if (t->detector != 0) {
+    if (alt_births(t, l)) return -1;
+    goto compact;
+  }
   memset(l->mask, 255, (size_t)(H + 8) * l->pmask);
   for (int i = 0; i < l->n; i++) { /* every slot, dead ones included */
     int pr = l->pos[2 * i], pc = l->pos[2 * i + 1];
@@ -531,17 +576,9 @@ static int detect_and_compact(otracker* t, int s) {
   /* Births in raster order over domain - border(3). */
   for (int r = 3; r <= H - 4; r++)
     for (int c = 3; c <= W - 4; c++)
-      if (l->newpts[(size_t)r * W + c]) {
-        if (particles_reserve(l, l->n + 1)) return -1;
-        int i = l->n++;
-        l->age[i] = 1;
-        l->speed[2 * i] = 0.f;
-        l->speed[2 * i + 1] = 0.f;
-        l->pos[2 * i] = (int16_t)r;
-        l->pos[2 * i + 1] = (int16_t)c;
-        compute_feature(l, r, c, l->feat + 16 * (size_t)i);
-        AT(l->sparse, l->psp, 7, r, c) = (uint32_t)i;
-      }
+      if (l->newpts[(size_t)r * W + c])
+        if (add_particle(l, r, c)) return -1;
+compact:
   /* Stable compaction. */
   l->compact_has_run = 1;
   l->nmatches = l->n;
@@ -674,6 +711,12 @@ void oracle_destroy(void* h) {
 void oracle_set_k(void* h, int k) { ((otracker*)h)->k = k; }
 void oracle_set_with_merge(void* h, int m) { ((otracker*)h)->with_merge = m; }
 void oracle_set_n(void* h, int n) { ((otracker*)h)->n_fast = n; }
+void oracle_set_detector(void* h, int kind, int step, int grad_th) {
+  otracker* t = (otracker*)h;
+  t->detector = kind;
+  t->step = step;
+  t->grad_th = grad_th;
+}
 
 int oracle_run(void* h, const uint8_t* frame) {
   otracker* t = (otracker*)h;

@@ -12,7 +12,10 @@ Outputs (small, committed):
   tracker_*.npz -- input frames and the reference CPU tracker's state after
       every frame (particles, features, matches) plus every stage image after
       the last frame, from oracle/_ref/libcuimg_ref.so (built by
-      `make -C oracle ref`).
+      `make -C oracle ref`);
+  altdet_*.npz -- the same particle state for the generic strategy with the
+      reference's regular_detector and dense_detector;
+  lk_*.npz -- the reference's pyramidal LK tracker on a frame pair.
 """
 import ctypes
 import json
@@ -28,6 +31,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, os.path.dirname(HERE))
 from stage_api import StageLib, snapshot  # noqa: E402
+from oracle_lib import alt_reference, alt_reference_particles  # noqa: E402
 
 CASES = [
     # name, rows, cols, nscales, detector_frequency, frames, seed
@@ -109,6 +113,33 @@ def make_tracker_case(name, rows, cols, L, detf, n, seed):
     np.savez_compressed(os.path.join(HERE, name + ".npz"), **d)
 
 
+ALT_CASES = [
+    # name, detector (1 regular, 2 dense), rows, cols, nscales, detector_frequency, frames, seed, step, grad_th
+    ("altdet_regular_120x160_s2", 1, 120, 160, 2, 3, 8, 7, 3, 8),
+    ("altdet_dense_64x80_s2", 2, 64, 80, 2, 2, 5, 8, 1, 1),
+]
+
+
+def make_alt_case(name, kind, rows, cols, L, detf, n, seed, step, grad_th):
+    """The reference's generic strategy with regular_detector or dense_detector."""
+    os.environ["OMP_NUM_THREADS"] = "1"
+    lib, h = alt_reference(kind, rows, cols, L, detf, 1, step, grad_th)
+    frames = synth_frames(rows, cols, n, seed)
+    d = dict(frames=frames, meta=np.array([kind, rows, cols, L, detf, 1, n, seed, step, grad_th], np.int32))
+    for t in range(n):
+        lib.refx_run(h, frames[t].ctypes.data)
+        for s in range(L):
+            p = alt_reference_particles(lib, h, s)
+            d["f%d_s%d_pos" % (t, s)] = p["pos"]
+            d["f%d_s%d_speed" % (t, s)] = p["speed"]
+            d["f%d_s%d_age" % (t, s)] = p["age"]
+            d["f%d_s%d_feat" % (t, s)] = p["feat"][:, :16]
+            if p["compact"]:
+                d["f%d_s%d_matches" % (t, s)] = p["matches"]
+    lib.refx_destroy(h)
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), **d)
+
+
 LK_CASES = [
     # name, rows, cols, nscales, seed
     ("lk_240x320_s3", 240, 320, 3, 21),
@@ -153,6 +184,8 @@ def main():
         json.dump(taps, f, indent=0, sort_keys=True)
     for case in CASES:
         make_tracker_case(*case)
+    for case in ALT_CASES:
+        make_alt_case(*case)
     for case in LK_CASES:
         make_lk_case(*case)
     print("golden fixtures written to", HERE)

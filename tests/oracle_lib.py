@@ -27,6 +27,7 @@ def oracle():
             ctypes.c_void_p] * 4
         for n in ("oracle_set_k", "oracle_set_with_merge", "oracle_set_n"):
             getattr(_lib, n).argtypes = [ctypes.c_void_p, ctypes.c_int]
+        _lib.oracle_set_detector.argtypes = [ctypes.c_void_p] + [ctypes.c_int] * 3
     return _lib
 
 
@@ -84,6 +85,48 @@ def box_pyramid_u8(img, nlevels):
         levels.append(nxt.astype(np.uint8))
         cur = nxt
     return levels
+
+
+def alt_tracker_oracle(kind, rows, cols, nscales, det_freq, filt_freq, step=1, grad_th=1):
+    """Oracle with the regular (kind 1) or dense (kind 2) detector."""
+    o = tracker_oracle(rows, cols, nscales, 20, det_freq, filt_freq)
+    oracle().oracle_set_detector(o.h, kind, step, grad_th)
+    return o
+
+
+def alt_golden_cases():
+    return sorted(f[:-4] for f in os.listdir(GOLDEN) if f.startswith("altdet_") and f.endswith(".npz"))
+
+
+def alt_reference(kind, rows, cols, nscales, det_freq, filt_freq, step=1, grad_th=1):
+    """The reference's generic strategy with regular_detector / dense_detector
+    (oracle/_ref, built here only): returns (lib, handle)."""
+    lib = ctypes.CDLL(REF)
+    lib.refx_create.restype = ctypes.c_void_p
+    lib.refx_create.argtypes = [ctypes.c_int] * 8
+    lib.refx_run.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
+    lib.refx_nparticles.argtypes = [ctypes.c_void_p, ctypes.c_int]
+    lib.refx_compact_has_run.argtypes = [ctypes.c_void_p, ctypes.c_int]
+    lib.refx_get_particles.argtypes = [ctypes.c_void_p, ctypes.c_int] + [ctypes.c_void_p] * 6
+    lib.refx_destroy.argtypes = [ctypes.c_void_p]
+    return lib, lib.refx_create(kind, rows, cols, nscales, det_freq, filt_freq, step, grad_th)
+
+
+def alt_reference_particles(lib, h, s):
+    """Particle state of scale s of an alt_reference tracker."""
+    n = lib.refx_nparticles(h, s)
+    speed = np.zeros((n, 2), np.float32)
+    pos = np.zeros((n, 2), np.int16)
+    age = np.zeros(n, np.uint16)
+    feat = np.zeros((n, 32), np.uint8)
+    nm = ctypes.c_int()
+    lib.refx_get_particles(h, s, speed.ctypes.data, pos.ctypes.data, age.ctypes.data, feat.ctypes.data, None,
+                           ctypes.byref(nm))
+    matches = np.zeros(max(nm.value, 1), np.int32)
+    lib.refx_get_particles(h, s, speed.ctypes.data, pos.ctypes.data, age.ctypes.data, feat.ctypes.data,
+                           matches.ctypes.data, ctypes.byref(nm))
+    return dict(speed=speed, pos=pos, age=age, feat=feat, matches=matches[: nm.value],
+                compact=bool(lib.refx_compact_has_run(h, s)))
 
 
 def golden_cases():

@@ -10,8 +10,9 @@ import os
 import numpy as np
 import pytest
 
-from oracle_lib import (GOLDEN, box_pyramid_u8, gauss_pyramid, gauss_sep, gauss_taps, golden_cases, load_golden,
-                        oracle, reference_available, tracker_oracle, tracker_reference)
+from oracle_lib import (GOLDEN, alt_golden_cases, alt_reference, alt_reference_particles, alt_tracker_oracle, box_pyramid_u8, gauss_pyramid,
+                        gauss_sep, gauss_taps, golden_cases, load_golden, oracle, reference_available, tracker_oracle,
+                        tracker_reference)
 from stage_api import diff_snapshots, snapshot
 
 STAGE_KEYS = ("input", "s1", "s2", "contrast", "saliency", "mask", "sparse", "flow", "count", "stat_n", "stat_speed")
@@ -74,6 +75,55 @@ def test_oracle_matches_reference_live(rows, cols, L, detf, n, seed):
         bad = diff_snapshots(snapshot(ref, L), snapshot(o, L), detector_frame=(t % detf == 0))
         assert not bad, "frame %d: %s" % (t, bad)
     ref.destroy()
+    o.destroy()
+
+
+def _alt_check(get, g, L, n, tag):
+    for t in range(n):
+        for s in range(L):
+            p = get(t, s)
+            for k in ("pos", "speed", "age"):
+                np.testing.assert_array_equal(p[k], g["f%d_s%d_%s" % (t, s, k)], err_msg="%s f%d s%d %s" % (tag, t, s, k))
+            np.testing.assert_array_equal(p["feat"][:, :16], g["f%d_s%d_feat" % (t, s)], err_msg="%s f%d s%d feat" % (tag, t, s))
+            key = "f%d_s%d_matches" % (t, s)
+            if key in g.files:
+                np.testing.assert_array_equal(p["matches"], g[key], err_msg="%s f%d s%d matches" % (tag, t, s))
+
+
+@pytest.mark.parametrize("case", alt_golden_cases())
+def test_alt_detector_oracle_matches_reference_golden(case):
+    # The regular and dense detectors of the reference's generic strategy.
+    g = load_golden(case)
+    kind, rows, cols, L, detf, filtf, n, seed, step, grad_th = [int(x) for x in g["meta"]]
+    o = alt_tracker_oracle(kind, rows, cols, L, detf, filtf, step, grad_th)
+    snaps = []
+    for t in range(n):
+        o.run(g["frames"][t])
+        snaps.append([o.particles(s) for s in range(L)])
+    _alt_check(lambda t, s: snaps[t][s], g, L, n, case)
+    o.destroy()
+
+
+@pytest.mark.skipif(not reference_available(), reason="reference not built here (oracle/_ref)")
+@pytest.mark.parametrize("kind,rows,cols,L,detf,n,step,grad_th", [
+    (1, 101, 133, 3, 2, 7, 2, 5),
+    (2, 60, 90, 2, 3, 6, 1, 1),
+])
+def test_alt_detector_oracle_matches_reference_live(kind, rows, cols, L, detf, n, step, grad_th):
+    from cuimg_gb300 import synth
+    frames = synth.frames(13, rows, cols, n)
+    lib, h = alt_reference(kind, rows, cols, L, detf, 1, step, grad_th)
+    o = alt_tracker_oracle(kind, rows, cols, L, detf, 1, step, grad_th)
+    for t in range(n):
+        lib.refx_run(h, frames[t].ctypes.data)
+        o.run(frames[t])
+        for s in range(L):
+            r, p = alt_reference_particles(lib, h, s), o.particles(s)
+            for k in ("pos", "speed", "age", "feat"):
+                np.testing.assert_array_equal(p[k], r[k], err_msg="f%d s%d %s" % (t, s, k))
+            if r["compact"]:
+                np.testing.assert_array_equal(p["matches"], r["matches"])
+    lib.refx_destroy(h)
     o.destroy()
 
 
