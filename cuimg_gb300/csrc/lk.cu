@@ -92,20 +92,25 @@ struct WarpSmem {
   short mr[MAXPIX], mc[MAXPIX];
 };
 
-// iterative_lk_match_5x5::match for one point (all lanes of the warp).
+// iterative_lk_match_5x5::match for one point (all lanes of the warp); PPL
+// window pixels per lane (ceil(window^2 / 32)).
 // Returns true when accepted by the matcher itself; tr / err as the reference.
+template <int PPL>
 __device__ bool lk_match(const Level& lv, const Params& P, WarpSmem& S, float py, float px, float ptr_y, float ptr_x,
                          float& tr_y, float& tr_x, float& err) {
   const int lane = threadIdx.x & 31;
   const int ws = P.ws, hws = ws / 2, n = ws * ws;
   const int N = P.npix < n ? P.npix : n;
-  float gr[PPL], gc[PPL], nrm[PPL];
+  float gr[PPL], gc[PPL];
+  unsigned nb[PPL];  // gradient norm bits (norms are >= 0, so they order like the floats)
+  bool valid[PPL];
 #pragma unroll
   for (int k = 0; k < PPL; k++) {
     int i = lane + 32 * k;
     gr[k] = gc[k] = 0.f;
-    nrm[k] = -1.f;
-    if (i < n) {
+    nb[k] = 0;
+    valid[k] = i < n;
+    if (valid[k]) {
       int r = i / ws - hws, c = i % ws - hws;
       float y = py + (float)r, x = px + (float)c;
       float2 g = li2(lv.grad, lv.H, lv.W, y, x);
@@ -113,36 +118,55 @@ __device__ bool lk_match(const Level& lv, const Params& P, WarpSmem& S, float py
       gc[k] = g.y;
       float a = li(lv.prev, lv.H, lv.W, y, x);
       S.as[i] = P.u8 ? (float)(unsigned char)a : a;
-      nrm[k] = __fsqrt_rn(__fadd_rn(__fmul_rn(g.x, g.x), __fmul_rn(g.y, g.y)));
+      nb[k] = __float_as_uint(__fsqrt_rn(__fadd_rn(__fmul_rn(g.x, g.x), __fmul_rn(g.y, g.y))));
     }
   }
-  __syncwarp();
-  // Rank of every window pixel by decreasing gradient norm (ties: lower index).
-  int rank[PPL];
+  // The N strongest gradients (ties: lower window index), the reference's
+  // nth_element selection (pyrlk_tracker.hpp:212-228): a bitwise search for
+  // the N-th largest norm t, then every norm above t and the first
+  // N - #(above t) norms equal to t in window order.
+  bool sel[PPL];
+  if (N >= n) {
 #pragma unroll
-  for (int k = 0; k < PPL; k++) rank[k] = 0;
+    for (int k = 0; k < PPL; k++) sel[k] = valid[k];
+  } else {
+    unsigned t = 0;
+    for (int bit = 30; bit >= 0; bit--) {
+      const unsigned cand = t | (1u << bit);
+      int cnt = 0;
 #pragma unroll
-  for (int kk = 0; kk < PPL; kk++) {
-    if (32 * kk >= n) break;
-    for (int src = 0; src < 32; src++) {
-      float v = __shfl_sync(0xffffffffu, nrm[kk], src);
-      int j = src + 32 * kk;
+      for (int k = 0; k < PPL; k++) cnt += __popc(__ballot_sync(0xffffffffu, valid[k] && nb[k] >= cand));
+      if (cnt >= N) t = cand;
+    }
+    int above = 0;
 #pragma unroll
-      for (int k = 0; k < PPL; k++) {
-        int i = lane + 32 * k;
-        if (j < n && i < n && (v > nrm[k] || (v == nrm[k] && j < i))) rank[k]++;
+    for (int k = 0; k < PPL; k++) above += __popc(__ballot_sync(0xffffffffu, valid[k] && nb[k] > t));
+    const unsigned lt = (1u << lane) - 1u;
+    int eq_before = 0;
+#pragma unroll
+    for (int k = 0; k < PPL; k++) {
+      const bool eq = valid[k] && nb[k] == t;
+      const unsigned be = __ballot_sync(0xffffffffu, eq);
+      sel[k] = (valid[k] && nb[k] > t) || (eq && eq_before + __popc(be & lt) < N - above);
+      eq_before += __popc(be);
+    }
+  }
+  // Selected pixels, compacted in window order.
+  {
+    const unsigned lt = (1u << lane) - 1u;
+    int base = 0;
+#pragma unroll
+    for (int k = 0; k < PPL; k++) {
+      const unsigned bs = __ballot_sync(0xffffffffu, sel[k]);
+      if (sel[k]) {
+        const int m = base + __popc(bs & lt), i = lane + 32 * k;
+        S.mgr[m] = gr[k];
+        S.mgc[m] = gc[k];
+        S.mas[m] = S.as[i];
+        S.mr[m] = (short)(i / ws - hws);
+        S.mc[m] = (short)(i % ws - hws);
       }
-    }
-  }
-#pragma unroll
-  for (int k = 0; k < PPL; k++) {
-    int i = lane + 32 * k;
-    if (i < n && rank[k] < N) {
-      S.mgr[rank[k]] = gr[k];
-      S.mgc[rank[k]] = gc[k];
-      S.mas[rank[k]] = S.as[i];
-      S.mr[rank[k]] = (short)(i / ws - hws);
-      S.mc[rank[k]] = (short)(i % ws - hws);
+      base += __popc(bs);
     }
   }
   __syncwarp();
@@ -207,6 +231,7 @@ __device__ bool lk_match(const Level& lv, const Params& P, WarpSmem& S, float py
   return ok;
 }
 
+template <int PPL>
 __global__ void __launch_bounds__(32 * WARPS) k_lk_track(const Level* __restrict__ levels, Params P, int npairs,
                                                          int npts, const float* __restrict__ pts,
                                                          float* __restrict__ out, int* __restrict__ status,
@@ -232,7 +257,7 @@ __global__ void __launch_bounds__(32 * WARPS) k_lk_track(const Level* __restrict
     float ny = 0.f, nx = 0.f;
     if (box_has(L.H, L.W, 3, qy + ptr_y, qx + ptr_x)) {
       float ty, tx, e;
-      lk_match(L, P, S, qy, qx, ptr_y, ptr_x, ty, tx, e);
+      lk_match<PPL>(L, P, S, qy, qx, ptr_y, ptr_x, ty, tx, e);
       if (box_has(L.H, L.W, 0, qy + ty, qx + tx)) {
         ny = ty;
         nx = tx;
@@ -250,7 +275,7 @@ __global__ void __launch_bounds__(32 * WARPS) k_lk_track(const Level* __restrict
     float pred_y = p_y + ptr_y, pred_x = p_x + ptr_x;
     if (box_has(L0.H, L0.W, 3, pred_y, pred_x)) {
       float ty, tx, e;
-      lk_match(L0, P, S, p_y, p_x, ptr_y, ptr_x, ty, tx, e);
+      lk_match<PPL>(L0, P, S, p_y, p_x, ptr_y, ptr_x, ty, tx, e);
       float m0 = (float)(int)(p_y + ty), m1 = (float)(int)(p_x + tx);
       float d0 = m0 - pred_y, d1 = m1 - pred_x;
       oe = e;
@@ -423,7 +448,15 @@ static int lk_run(const void* prev, const void* cur, int64_t pitch, int64_t img_
   long long total = (long long)npairs * npts;
   if (total > 0) {
     long long blocks = (total + WARPS - 1) / WARPS;
-    k_lk_track<<<(unsigned)blocks, 32 * WARPS, 0, st>>>(table, P, npairs, npts, pts, out, status, err);
+    auto go = [&](auto kern) { kern<<<(unsigned)blocks, 32 * WARPS, 0, st>>>(table, P, npairs, npts, pts, out, status, err); };
+    switch ((prm->window * prm->window + 31) / 32) {
+      case 1: go(k_lk_track<1>); break;
+      case 2: go(k_lk_track<2>); break;
+      case 3: go(k_lk_track<3>); break;
+      case 4: go(k_lk_track<4>); break;
+      case 5: case 6: go(k_lk_track<6>); break;
+      default: go(k_lk_track<8>); break;
+    }
   }
   // The host table must outlive the asynchronous copy.
   cudaStreamSynchronize(st);
@@ -593,7 +626,15 @@ extern "C" int gbt_lk_track_batch_noalloc(const void* prev, const void* cur, int
   long long total = (long long)npairs * npts;
   if (total > 0) {
     long long blocks = (total + WARPS - 1) / WARPS;
-    k_lk_track<<<(unsigned)blocks, 32 * WARPS, 0, st>>>(table, P, npairs, npts, pts, out, status, err);
+    auto go = [&](auto kern) { kern<<<(unsigned)blocks, 32 * WARPS, 0, st>>>(table, P, npairs, npts, pts, out, status, err); };
+    switch ((prm->window * prm->window + 31) / 32) {
+      case 1: go(k_lk_track<1>); break;
+      case 2: go(k_lk_track<2>); break;
+      case 3: go(k_lk_track<3>); break;
+      case 4: go(k_lk_track<4>); break;
+      case 5: case 6: go(k_lk_track<6>); break;
+      default: go(k_lk_track<8>); break;
+    }
   }
   return cudaGetLastError() == cudaSuccess ? GBT_OK : GBT_E_CUDA;
 }
