@@ -32,7 +32,6 @@ namespace gbt_lkd {
 
 constexpr int MAXW = 15;
 constexpr int MAXPIX = MAXW * MAXW;
-constexpr int PPL = (MAXPIX + 31) / 32;
 constexpr int MAXL = 9;
 constexpr int MAXK = 32;
 constexpr int WARPS = 4;
@@ -50,7 +49,9 @@ struct Lvl {
 struct Bil {
   int i00, i10, i01, i11;
   float w00, w10, w01, w11;
-  float a, b;  // fractional parts (row, col)
+  float a, b;       // fractional parts (row, col)
+  int y0, x0;       // clamped top-left tap (the others are y0 or y0 + 1, x0 or x0 + 1 clamped)
+  int dy, dx;       // 1 where the second tap row / column differs from the first, 0 at the clamp
 };
 
 __device__ __forceinline__ Bil bil_at(int H, int W, float y, float x) {
@@ -66,6 +67,10 @@ __device__ __forceinline__ Bil bil_at(int H, int W, float y, float x) {
   o.i10 = y1 * W + x0;
   o.i01 = y0 * W + x1;
   o.i11 = y1 * W + x1;
+  o.y0 = y0;
+  o.x0 = x0;
+  o.dy = y1 - y0;
+  o.dx = x1 - x0;
   o.w00 = (1.f - o.a) * (1.f - o.b);
   o.w10 = o.a * (1.f - o.b);
   o.w01 = (1.f - o.a) * o.b;
@@ -92,17 +97,6 @@ __device__ __forceinline__ void bil_scatter(float* img, const Bil& s, float v) {
   atomicAdd(img + s.i01, s.w01 * v);
   atomicAdd(img + s.i11, s.w11 * v);
 }
-__device__ __forceinline__ void bil_scatter2(float2* img, const Bil& s, float2 v) {
-  float* f = (float*)img;
-  atomicAdd(f + 2 * s.i00, s.w00 * v.x);
-  atomicAdd(f + 2 * s.i00 + 1, s.w00 * v.y);
-  atomicAdd(f + 2 * s.i10, s.w10 * v.x);
-  atomicAdd(f + 2 * s.i10 + 1, s.w10 * v.y);
-  atomicAdd(f + 2 * s.i01, s.w01 * v.x);
-  atomicAdd(f + 2 * s.i01 + 1, s.w01 * v.y);
-  atomicAdd(f + 2 * s.i11, s.w11 * v.x);
-  atomicAdd(f + 2 * s.i11 + 1, s.w11 * v.y);
-}
 
 __device__ __forceinline__ float wsum(float v) {
   for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
@@ -113,18 +107,49 @@ struct Setup {  // per level of one point
   float q0, q1, M00, M01, M11;
 };
 
-// Normal matrix inverse at one level (all lanes get identical values).
-__device__ __forceinline__ void level_setup(const Lvl& e, int ws, float q0, float q1, float& M00, float& M01,
-                                            float& M11) {
+__device__ __forceinline__ float level_scale(int l) {
+  float s = 1.f;
+  for (int k = 0; k < l; k++) s *= 2.f;
+  return s;
+}
+
+// The level's template at q + o for the lane's window pixels: Sobel gradient
+// and A value, fixed through the level's Gauss-Newton steps.
+template <int PPL>
+struct Tmpl {
+  float2 g[PPL];
+  float a[PPL];
+};
+
+template <int PPL>
+__device__ __forceinline__ void load_template(const Lvl& e, int ws, float q0, float q1, Tmpl<PPL>& T) {
   const int lane = threadIdx.x & 31, hws = ws / 2, n = ws * ws;
-  float g00 = 0.f, g01 = 0.f, g11 = 0.f;
-  for (int i = lane; i < n; i += 32) {
-    Bil s = bil_at(e.H, e.W, q0 + (float)(i / ws - hws), q1 + (float)(i % ws - hws));
-    float2 g = bil_val2(e.S, s);
-    g00 += g.x * g.x;
-    g01 += g.x * g.y;
-    g11 += g.y * g.y;
+#pragma unroll
+  for (int k = 0; k < PPL; k++) {
+    const int i = lane + 32 * k;
+    T.g[k] = make_float2(0.f, 0.f);
+    T.a[k] = 0.f;
+    if (i < n) {
+      Bil st = bil_at(e.H, e.W, q0 + (float)(i / ws - hws), q1 + (float)(i % ws - hws));
+      T.g[k] = bil_val2(e.S, st);
+      T.a[k] = bil_val(e.A, st);
+    }
   }
+}
+
+// Normal matrix inverse at one level (all lanes get identical values).
+template <int PPL>
+__device__ __forceinline__ void level_setup(const Tmpl<PPL>& T, int n, float& M00, float& M01, float& M11) {
+  const int lane = threadIdx.x & 31;
+  float g00 = 0.f, g01 = 0.f, g11 = 0.f;
+#pragma unroll
+  for (int k = 0; k < PPL; k++)
+    if (lane + 32 * k < n) {
+      const float2 g = T.g[k];
+      g00 += g.x * g.x;
+      g01 += g.x * g.y;
+      g11 += g.y * g.y;
+    }
   g00 = wsum(g00);
   g01 = wsum(g01);
   g11 = wsum(g11);
@@ -135,47 +160,48 @@ __device__ __forceinline__ void level_setup(const Lvl& e, int ws, float q0, floa
 }
 
 // One Gauss-Newton right-hand side b = sum g (T - B(v + o)).
-__device__ __forceinline__ void rhs(const Lvl& e, int ws, float q0, float q1, float v0, float v1, float& b0,
+template <int PPL>
+__device__ __forceinline__ void rhs(const Lvl& e, int ws, const Tmpl<PPL>& T, float v0, float v1, float& b0,
                                     float& b1) {
   const int lane = threadIdx.x & 31, hws = ws / 2, n = ws * ws;
   b0 = 0.f;
   b1 = 0.f;
-  for (int i = lane; i < n; i += 32) {
-    const float r = (float)(i / ws - hws), c = (float)(i % ws - hws);
-    Bil st = bil_at(e.H, e.W, q0 + r, q1 + c);
-    float2 g = bil_val2(e.S, st);
-    float res = bil_val(e.A, st) - bil_val(e.B, bil_at(e.H, e.W, v0 + r, v1 + c));
-    b0 += g.x * res;
-    b1 += g.y * res;
+#pragma unroll
+  for (int k = 0; k < PPL; k++) {
+    const int i = lane + 32 * k;
+    if (i < n) {
+      const float r = (float)(i / ws - hws), c = (float)(i % ws - hws);
+      const float res = T.a[k] - bil_val(e.B, bil_at(e.H, e.W, v0 + r, v1 + c));
+      b0 += T.g[k].x * res;
+      b1 += T.g[k].y * res;
+    }
   }
   b0 = wsum(b0);
   b1 = wsum(b1);
 }
 
-__device__ __forceinline__ float level_scale(int l) {
-  float s = 1.f;
-  for (int k = 0; k < l; k++) s *= 2.f;
-  return s;
-}
-
 // Forward of one point; fills the per-level setup and the iterate history.
+template <int PPL>
 __device__ float point_forward(const Lvl* lv, int L, int ws, int K, float p0, float p1, float u0, float u1,
                                Setup* su, float2* hist, float& vf0, float& vf1) {
+  const int n = ws * ws;
   const float top = level_scale(L - 1);
   float d0 = u0 / top, d1 = u1 / top, v0 = 0.f, v1 = 0.f;
   for (int l = L - 1; l >= 0; l--) {
     const Lvl& e = lv[l];
     const float s = level_scale(l);
     const float q0 = p0 / s, q1 = p1 / s;
+    Tmpl<PPL> T;
+    load_template<PPL>(e, ws, q0, q1, T);
     float M00, M01, M11;
-    level_setup(e, ws, q0, q1, M00, M01, M11);
+    level_setup<PPL>(T, n, M00, M01, M11);
     if (su) su[l] = Setup{q0, q1, M00, M01, M11};
     v0 = q0 + d0;
     v1 = q1 + d1;
     for (int k = 0; k < K; k++) {
       if (hist) hist[l * (MAXK + 1) + k] = make_float2(v0, v1);
       float b0, b1;
-      rhs(e, ws, q0, q1, v0, v1, b0, b1);
+      rhs<PPL>(e, ws, T, v0, v1, b0, b1);
       v0 += M00 * b0 + M01 * b1;
       v1 += M01 * b0 + M11 * b1;
     }
@@ -186,16 +212,21 @@ __device__ float point_forward(const Lvl* lv, int L, int ws, int K, float p0, fl
   vf0 = v0;
   vf1 = v1;
   const Lvl& e = lv[0];
-  const int lane = threadIdx.x & 31, hws = ws / 2, n = ws * ws;
+  const int lane = threadIdx.x & 31, hws = ws / 2;
   float loss = 0.f;
-  for (int i = lane; i < n; i += 32) {
-    const float r = (float)(i / ws - hws), c = (float)(i % ws - hws);
-    float res = bil_val(e.A, bil_at(e.H, e.W, p0 + r, p1 + c)) - bil_val(e.B, bil_at(e.H, e.W, v0 + r, v1 + c));
-    loss += res * res;
+#pragma unroll
+  for (int k = 0; k < PPL; k++) {
+    const int i = lane + 32 * k;
+    if (i < n) {
+      const float r = (float)(i / ws - hws), c = (float)(i % ws - hws);
+      float res = bil_val(e.A, bil_at(e.H, e.W, p0 + r, p1 + c)) - bil_val(e.B, bil_at(e.H, e.W, v0 + r, v1 + c));
+      loss += res * res;
+    }
   }
   return wsum(loss);
 }
 
+template <int PPL>
 __global__ void __launch_bounds__(32 * WARPS) k_lkd_forward(const Lvl* __restrict__ levels, int L, int ws, int K,
                                                             int npairs, int npts, const float* __restrict__ pts,
                                                             const float* __restrict__ u0, float* __restrict__ loss,
@@ -204,8 +235,8 @@ __global__ void __launch_bounds__(32 * WARPS) k_lkd_forward(const Lvl* __restric
   if (g >= (long long)npairs * npts) return;
   const int pair = (int)(g / npts);
   float vf0, vf1;
-  float l = point_forward(levels + (size_t)pair * L, L, ws, K, pts[2 * g], pts[2 * g + 1], u0[2 * g], u0[2 * g + 1],
-                          nullptr, nullptr, vf0, vf1);
+  float l = point_forward<PPL>(levels + (size_t)pair * L, L, ws, K, pts[2 * g], pts[2 * g + 1], u0[2 * g],
+                               u0[2 * g + 1], nullptr, nullptr, vf0, vf1);
   if ((threadIdx.x & 31) == 0) {
     loss[g] = l;
     vfinal[2 * g] = vf0;
@@ -213,12 +244,69 @@ __global__ void __launch_bounds__(32 * WARPS) k_lkd_forward(const Lvl* __restric
   }
 }
 
+// Scatter accumulator of one warp: a box of image pixels in shared memory
+// (atomics there), added to the level image once at the end; samples whose
+// taps fall outside the box go to the image directly.
+constexpr int GRID_CELLS = 1024;
+struct Grid {
+  float* c;        // cells, row-major GW per row
+  int y0, x0, GH, GW;
+  int stride;      // image element stride in floats (2 for one component of a float2 image)
+  __device__ __forceinline__ bool holds(const Bil& s) const {
+    return s.y0 >= y0 && s.y0 + s.dy < y0 + GH && s.x0 >= x0 && s.x0 + s.dx < x0 + GW;
+  }
+  __device__ __forceinline__ void add(float* img, const Bil& s, float v) const {
+    if (holds(s)) {
+      float* b = c + (s.y0 - y0) * GW + (s.x0 - x0);
+      atomicAdd(b, s.w00 * v);
+      atomicAdd(b + s.dy * GW, s.w10 * v);
+      atomicAdd(b + s.dx, s.w01 * v);
+      atomicAdd(b + s.dy * GW + s.dx, s.w11 * v);
+    } else {
+      atomicAdd(img + stride * s.i00, s.w00 * v);
+      atomicAdd(img + stride * s.i10, s.w10 * v);
+      atomicAdd(img + stride * s.i01, s.w01 * v);
+      atomicAdd(img + stride * s.i11, s.w11 * v);
+    }
+  }
+};
+
+// Box of the clamped taps of samples at rows [ylo, yhi] + [-h, h] and columns
+// [xlo, xhi] + [-h, h]; GH = 0 when it does not fit in `cells`.
+__device__ __forceinline__ void grid_box(int H, int W, float ylo, float yhi, float xlo, float xhi, int h, int cells,
+                                         Grid& g) {
+  const int r0 = min(max((int)floorf(ylo) - h, 0), H - 1), r1 = min(max((int)floorf(yhi) + h + 1, 0), H - 1);
+  const int c0 = min(max((int)floorf(xlo) - h, 0), W - 1), c1 = min(max((int)floorf(xhi) + h + 1, 0), W - 1);
+  g.y0 = r0;
+  g.x0 = c0;
+  g.GH = r1 - r0 + 1;
+  g.GW = c1 - c0 + 1;
+  if (g.GH * g.GW > cells) g.GH = g.GW = 0;
+}
+
+__device__ __forceinline__ void grid_clear(Grid& g, int ncells) {
+  for (int k = threadIdx.x & 31; k < ncells; k += 32) g.c[k] = 0.f;
+  __syncwarp();
+}
+
+__device__ __forceinline__ void grid_flush(const Grid& g, float* img, int W) {
+  __syncwarp();
+  for (int k = threadIdx.x & 31; k < g.GH * g.GW; k += 32) {
+    const float v = g.c[k];
+    if (v != 0.f) atomicAdd(img + ((g.y0 + k / g.GW) * W + g.x0 + k % g.GW) * g.stride, v);
+  }
+  __syncwarp();
+}
+
+template <int PPL>
 __global__ void __launch_bounds__(32 * WARPS) k_lkd_backward(const Lvl* __restrict__ levels, int L, int ws, int K,
                                                              int npairs, int npts, const float* __restrict__ pts,
                                                              const float* __restrict__ u0,
                                                              const float* __restrict__ dloss, float* __restrict__ du0) {
   __shared__ Setup su_all[WARPS][MAXL];
   __shared__ float2 hist_all[WARPS][MAXL * (MAXK + 1)];
+  __shared__ float gB_all[WARPS][GRID_CELLS];                       // dB over the level's residual samples
+  __shared__ float gT_all[WARPS][3][(MAXW + 1) * (MAXW + 1)];      // dA, dS.x, dS.y over the template
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const long long gidx = (long long)blockIdx.x * WARPS + warp;
   if (gidx >= (long long)npairs * npts) return;
@@ -228,31 +316,62 @@ __global__ void __launch_bounds__(32 * WARPS) k_lkd_backward(const Lvl* __restri
   float2* hist = hist_all[warp];
   const float p0 = pts[2 * gidx], p1 = pts[2 * gidx + 1];
   float vf0, vf1;
-  point_forward(lv, L, ws, K, p0, p1, u0[2 * gidx], u0[2 * gidx + 1], su, hist, vf0, vf1);
+  point_forward<PPL>(lv, L, ws, K, p0, p1, u0[2 * gidx], u0[2 * gidx + 1], su, hist, vf0, vf1);
   __syncwarp();
   const float w = dloss[gidx];
   const int hws = ws / 2, n = ws * ws;
-  // Loss at level 0: r = A0(p + o) - B0(v + o), dL/dr = 2 r w.
+  constexpr int TC = (MAXW + 1) * (MAXW + 1);
   float dv0 = 0.f, dv1 = 0.f;
-  {
-    const Lvl& e = lv[0];
-    for (int i = lane; i < n; i += 32) {
-      const float r = (float)(i / ws - hws), c = (float)(i % ws - hws);
-      Bil sa = bil_at(e.H, e.W, p0 + r, p1 + c), sb = bil_at(e.H, e.W, vf0 + r, vf1 + c);
-      const float res = bil_val(e.A, sa) - bil_val(e.B, sb);
-      const float dr = 2.f * res * w;
-      bil_scatter(e.dA, sa, dr);
-      bil_scatter(e.dB, sb, -dr);
-      float2 gb = bil_grad(e.B, sb);
-      dv0 -= dr * gb.x;
-      dv1 -= dr * gb.y;
-    }
-    dv0 = wsum(dv0);
-    dv1 = wsum(dv1);
-  }
   for (int l = 0; l < L; l++) {
     const Lvl& e = lv[l];
     const Setup S = su[l];
+    // Scatter boxes: the template footprint, and every residual sample of the
+    // level's steps (and, at level 0, of the loss).
+    Grid gA{gT_all[warp][0], 0, 0, 0, 0, 1}, gS0{gT_all[warp][1], 0, 0, 0, 0, 2};
+    Grid gS1{gT_all[warp][2], 0, 0, 0, 0, 2}, gB{gB_all[warp], 0, 0, 0, 0, 1};
+    grid_box(e.H, e.W, S.q0, S.q0, S.q1, S.q1, hws, TC, gA);
+    gS0.y0 = gS1.y0 = gA.y0;
+    gS0.x0 = gS1.x0 = gA.x0;
+    gS0.GH = gS1.GH = gA.GH;
+    gS0.GW = gS1.GW = gA.GW;
+    {
+      float ylo = 1e30f, yhi = -1e30f, xlo = 1e30f, xhi = -1e30f;
+      for (int k = 0; k <= K; k++) {
+        if (k == K && l != 0) break;
+        const float2 v = hist[l * (MAXK + 1) + k];
+        ylo = fminf(ylo, v.x);
+        yhi = fmaxf(yhi, v.x);
+        xlo = fminf(xlo, v.y);
+        xhi = fmaxf(xhi, v.y);
+      }
+      grid_box(e.H, e.W, ylo, yhi, xlo, xhi, hws, GRID_CELLS, gB);
+    }
+    grid_clear(gA, gA.GH * gA.GW);
+    grid_clear(gS0, gS0.GH * gS0.GW);
+    grid_clear(gS1, gS1.GH * gS1.GW);
+    grid_clear(gB, gB.GH * gB.GW);
+    Tmpl<PPL> T;
+    load_template<PPL>(e, ws, S.q0, S.q1, T);
+    if (l == 0) {
+      // Loss at level 0: r = A0(p + o) - B0(v + o), dL/dr = 2 r w.
+#pragma unroll
+      for (int kk = 0; kk < PPL; kk++) {
+        const int i = lane + 32 * kk;
+        if (i < n) {
+          const float r = (float)(i / ws - hws), c = (float)(i % ws - hws);
+          Bil sa = bil_at(e.H, e.W, p0 + r, p1 + c), sb = bil_at(e.H, e.W, vf0 + r, vf1 + c);
+          const float res = bil_val(e.A, sa) - bil_val(e.B, sb);
+          const float dr = 2.f * res * w;
+          gA.add(e.dA, sa, dr);
+          gB.add(e.dB, sb, -dr);
+          float2 gb = bil_grad(e.B, sb);
+          dv0 -= dr * gb.x;
+          dv1 -= dr * gb.y;
+        }
+      }
+      dv0 = wsum(dv0);
+      dv1 = wsum(dv1);
+    }
     float dM00 = 0.f, dM01 = 0.f, dM10 = 0.f, dM11 = 0.f;
     float dg0[PPL], dg1[PPL], dT[PPL];
 #pragma unroll
@@ -265,21 +384,22 @@ __global__ void __launch_bounds__(32 * WARPS) k_lkd_backward(const Lvl* __restri
 #pragma unroll
       for (int kk = 0; kk < PPL; kk++) {
         const int i = lane + 32 * kk;
-        if (i >= n) break;
-        const float r = (float)(i / ws - hws), c = (float)(i % ws - hws);
-        Bil st = bil_at(e.H, e.W, S.q0 + r, S.q1 + c), sb = bil_at(e.H, e.W, vk.x + r, vk.y + c);
-        const float2 g = bil_val2(e.S, st);
-        const float res = bil_val(e.A, st) - bil_val(e.B, sb);
-        b0 += g.x * res;
-        b1 += g.y * res;
-        const float dres = g.x * db0 + g.y * db1;
-        dg0[kk] += res * db0;
-        dg1[kk] += res * db1;
-        dT[kk] += dres;
-        bil_scatter(e.dB, sb, -dres);
-        const float2 gb = bil_grad(e.B, sb);
-        pv0 -= dres * gb.x;
-        pv1 -= dres * gb.y;
+        if (i < n) {
+          const float r = (float)(i / ws - hws), c = (float)(i % ws - hws);
+          Bil sb = bil_at(e.H, e.W, vk.x + r, vk.y + c);
+          const float2 g = T.g[kk];
+          const float res = T.a[kk] - bil_val(e.B, sb);
+          b0 += g.x * res;
+          b1 += g.y * res;
+          const float dres = g.x * db0 + g.y * db1;
+          dg0[kk] += res * db0;
+          dg1[kk] += res * db1;
+          dT[kk] += dres;
+          gB.add(e.dB, sb, -dres);
+          const float2 gb = bil_grad(e.B, sb);
+          pv0 -= dres * gb.x;
+          pv1 -= dres * gb.y;
+        }
       }
       b0 = wsum(b0);
       b1 = wsum(b1);
@@ -299,14 +419,19 @@ __global__ void __launch_bounds__(32 * WARPS) k_lkd_backward(const Lvl* __restri
 #pragma unroll
     for (int kk = 0; kk < PPL; kk++) {
       const int i = lane + 32 * kk;
-      if (i >= n) break;
-      const float r = (float)(i / ws - hws), c = (float)(i % ws - hws);
-      Bil st = bil_at(e.H, e.W, S.q0 + r, S.q1 + c);
-      const float2 g = bil_val2(e.S, st);
-      const float2 dgv = make_float2(dg0[kk] + H00 * g.x + H01 * g.y, dg1[kk] + H01 * g.x + H11 * g.y);
-      bil_scatter2(e.dS, st, dgv);
-      bil_scatter(e.dA, st, dT[kk]);
+      if (i < n) {
+        const float r = (float)(i / ws - hws), c = (float)(i % ws - hws);
+        Bil st = bil_at(e.H, e.W, S.q0 + r, S.q1 + c);
+        const float2 g = T.g[kk];
+        gS0.add((float*)e.dS, st, dg0[kk] + H00 * g.x + H01 * g.y);
+        gS1.add((float*)e.dS + 1, st, dg1[kk] + H01 * g.x + H11 * g.y);
+        gA.add(e.dA, st, dT[kk]);
+      }
     }
+    grid_flush(gA, e.dA, e.W);
+    grid_flush(gS0, (float*)e.dS, e.W);
+    grid_flush(gS1, (float*)e.dS + 1, e.W);
+    grid_flush(gB, e.dB, e.W);
     // v_0 = q + d_init: the adjoint of d_init is dv.
     if (l + 1 < L) {
       dv0 *= 2.f;  // d_init(l) = 2 (v_K(l+1) - q(l+1))
@@ -543,8 +668,17 @@ extern "C" int gbt_lkd_forward(const float* I0, const float* I1, int64_t pitch, 
   if ((r = prepare(I0, I1, pitch, img_bytes, rows, cols, nlevels, npairs, false, P, st))) return r;
   long long total = (long long)npairs * npts;
   if (total > 0)
-    k_lkd_forward<<<(unsigned)((total + WARPS - 1) / WARPS), 32 * WARPS, 0, st>>>(P.table, nlevels, window, iters,
-                                                                                  npairs, npts, pts, u0, loss, vfinal);
+    switch ((window * window + 31) / 32) {
+#define GO(PPL) k_lkd_forward<PPL><<<(unsigned)((total + WARPS - 1) / WARPS), 32 * WARPS, 0, st>>>( \
+      P.table, nlevels, window, iters, npairs, npts, pts, u0, loss, vfinal)
+      case 1: GO(1); break;
+      case 2: GO(2); break;
+      case 3: GO(3); break;
+      case 4: GO(4); break;
+      case 5: case 6: GO(6); break;
+      default: GO(8); break;
+#undef GO
+    }
   return cudaGetLastError() == cudaSuccess ? GBT_OK : GBT_E_CUDA;
 }
 
@@ -561,8 +695,17 @@ extern "C" int gbt_lkd_backward(const float* I0, const float* I1, int64_t pitch,
   if ((r = prepare(I0, I1, pitch, img_bytes, rows, cols, nlevels, npairs, true, P, st))) return r;
   long long total = (long long)npairs * npts;
   if (total > 0)
-    k_lkd_backward<<<(unsigned)((total + WARPS - 1) / WARPS), 32 * WARPS, 0, st>>>(
-        P.table, nlevels, window, iters, npairs, npts, pts, u0, dloss, du0);
+    switch ((window * window + 31) / 32) {
+#define GO(PPL) k_lkd_backward<PPL><<<(unsigned)((total + WARPS - 1) / WARPS), 32 * WARPS, 0, st>>>( \
+      P.table, nlevels, window, iters, npairs, npts, pts, u0, dloss, du0)
+      case 1: GO(1); break;
+      case 2: GO(2); break;
+      case 3: GO(3); break;
+      case 4: GO(4); break;
+      case 5: case 6: GO(6); break;
+      default: GO(8); break;
+#undef GO
+    }
   float taps_f[16];
   int32_t R;
   gbt_gaussian_taps(1.f, taps_f, &R);
