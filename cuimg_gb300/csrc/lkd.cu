@@ -31,7 +31,6 @@ extern "C" int gbt_gaussian_pyramid_f32(const float* in, int64_t in_pitch, int32
 namespace gbt_lkd {
 
 constexpr int MAXW = 15;
-constexpr int MAXPIX = MAXW * MAXW;
 constexpr int MAXL = 9;
 constexpr int MAXK = 32;
 constexpr int WARPS = 4;
@@ -56,10 +55,9 @@ struct Bil {
 
 __device__ __forceinline__ Bil bil_at(int H, int W, float y, float x) {
   Bil o;
-  float fy = floorf(y), fx = floorf(x);
-  int y0 = (int)fy, x0 = (int)fx;
-  o.a = y - fy;
-  o.b = x - fx;
+  int y0 = __float2int_rd(y), x0 = __float2int_rd(x);  // floor; |y|, |x| < 2^24
+  o.a = y - (float)y0;
+  o.b = x - (float)x0;
   int y1 = min(max(y0 + 1, 0), H - 1), x1 = min(max(x0 + 1, 0), W - 1);
   y0 = min(max(y0, 0), H - 1);
   x0 = min(max(x0, 0), W - 1);
@@ -113,6 +111,8 @@ __device__ __forceinline__ float level_scale(int l) {
   return s;
 }
 
+__host__ __device__ constexpr int ppl_of(int ws) { return (ws * ws + 31) / 32; }  // window pixels per lane
+
 // The level's template at q + o for the lane's window pixels: Sobel gradient
 // and A value, fixed through the level's Gauss-Newton steps.
 template <int PPL>
@@ -121,8 +121,9 @@ struct Tmpl {
   float a[PPL];
 };
 
-template <int PPL>
-__device__ __forceinline__ void load_template(const Lvl& e, int ws, float q0, float q1, Tmpl<PPL>& T) {
+template <int WS>
+__device__ __forceinline__ void load_template(const Lvl& e, int /*window: WS*/, float q0, float q1, Tmpl<ppl_of(WS)>& T) {
+  constexpr int ws = WS, PPL = (WS * WS + 31) / 32;
   const int lane = threadIdx.x & 31, hws = ws / 2, n = ws * ws;
 #pragma unroll
   for (int k = 0; k < PPL; k++) {
@@ -160,9 +161,10 @@ __device__ __forceinline__ void level_setup(const Tmpl<PPL>& T, int n, float& M0
 }
 
 // One Gauss-Newton right-hand side b = sum g (T - B(v + o)).
-template <int PPL>
-__device__ __forceinline__ void rhs(const Lvl& e, int ws, const Tmpl<PPL>& T, float v0, float v1, float& b0,
+template <int WS>
+__device__ __forceinline__ void rhs(const Lvl& e, int /*window: WS*/, const Tmpl<ppl_of(WS)>& T, float v0, float v1, float& b0,
                                     float& b1) {
+  constexpr int ws = WS, PPL = (WS * WS + 31) / 32;
   const int lane = threadIdx.x & 31, hws = ws / 2, n = ws * ws;
   b0 = 0.f;
   b1 = 0.f;
@@ -181,9 +183,10 @@ __device__ __forceinline__ void rhs(const Lvl& e, int ws, const Tmpl<PPL>& T, fl
 }
 
 // Forward of one point; fills the per-level setup and the iterate history.
-template <int PPL>
-__device__ float point_forward(const Lvl* lv, int L, int ws, int K, float p0, float p1, float u0, float u1,
+template <int WS>
+__device__ float point_forward(const Lvl* lv, int L, int /*window: WS*/, int K, float p0, float p1, float u0, float u1,
                                Setup* su, float2* hist, float& vf0, float& vf1) {
+  constexpr int ws = WS, PPL = (WS * WS + 31) / 32;
   const int n = ws * ws;
   const float top = level_scale(L - 1);
   float d0 = u0 / top, d1 = u1 / top, v0 = 0.f, v1 = 0.f;
@@ -192,7 +195,7 @@ __device__ float point_forward(const Lvl* lv, int L, int ws, int K, float p0, fl
     const float s = level_scale(l);
     const float q0 = p0 / s, q1 = p1 / s;
     Tmpl<PPL> T;
-    load_template<PPL>(e, ws, q0, q1, T);
+    load_template<WS>(e, ws, q0, q1, T);
     float M00, M01, M11;
     level_setup<PPL>(T, n, M00, M01, M11);
     if (su) su[l] = Setup{q0, q1, M00, M01, M11};
@@ -201,7 +204,7 @@ __device__ float point_forward(const Lvl* lv, int L, int ws, int K, float p0, fl
     for (int k = 0; k < K; k++) {
       if (hist) hist[l * (MAXK + 1) + k] = make_float2(v0, v1);
       float b0, b1;
-      rhs<PPL>(e, ws, T, v0, v1, b0, b1);
+      rhs<WS>(e, ws, T, v0, v1, b0, b1);
       v0 += M00 * b0 + M01 * b1;
       v1 += M01 * b0 + M11 * b1;
     }
@@ -226,16 +229,17 @@ __device__ float point_forward(const Lvl* lv, int L, int ws, int K, float p0, fl
   return wsum(loss);
 }
 
-template <int PPL>
-__global__ void __launch_bounds__(32 * WARPS) k_lkd_forward(const Lvl* __restrict__ levels, int L, int ws, int K,
+template <int WS>
+__global__ void __launch_bounds__(32 * WARPS) k_lkd_forward(const Lvl* __restrict__ levels, int L, int /*window: WS*/, int K,
                                                             int npairs, int npts, const float* __restrict__ pts,
                                                             const float* __restrict__ u0, float* __restrict__ loss,
                                                             float* __restrict__ vfinal) {
+  constexpr int ws = WS;
   const long long g = (long long)blockIdx.x * WARPS + (threadIdx.x >> 5);
   if (g >= (long long)npairs * npts) return;
   const int pair = (int)(g / npts);
   float vf0, vf1;
-  float l = point_forward<PPL>(levels + (size_t)pair * L, L, ws, K, pts[2 * g], pts[2 * g + 1], u0[2 * g],
+  float l = point_forward<WS>(levels + (size_t)pair * L, L, ws, K, pts[2 * g], pts[2 * g + 1], u0[2 * g],
                                u0[2 * g + 1], nullptr, nullptr, vf0, vf1);
   if ((threadIdx.x & 31) == 0) {
     loss[g] = l;
@@ -298,11 +302,12 @@ __device__ __forceinline__ void grid_flush(const Grid& g, float* img, int W) {
   __syncwarp();
 }
 
-template <int PPL>
-__global__ void __launch_bounds__(32 * WARPS) k_lkd_backward(const Lvl* __restrict__ levels, int L, int ws, int K,
+template <int WS>
+__global__ void __launch_bounds__(32 * WARPS, 4) k_lkd_backward(const Lvl* __restrict__ levels, int L, int /*window: WS*/, int K,
                                                              int npairs, int npts, const float* __restrict__ pts,
                                                              const float* __restrict__ u0,
                                                              const float* __restrict__ dloss, float* __restrict__ du0) {
+  constexpr int ws = WS, PPL = (WS * WS + 31) / 32;
   __shared__ Setup su_all[WARPS][MAXL];
   __shared__ float2 hist_all[WARPS][MAXL * (MAXK + 1)];
   __shared__ float gB_all[WARPS][GRID_CELLS];                       // dB over the level's residual samples
@@ -316,7 +321,7 @@ __global__ void __launch_bounds__(32 * WARPS) k_lkd_backward(const Lvl* __restri
   float2* hist = hist_all[warp];
   const float p0 = pts[2 * gidx], p1 = pts[2 * gidx + 1];
   float vf0, vf1;
-  point_forward<PPL>(lv, L, ws, K, p0, p1, u0[2 * gidx], u0[2 * gidx + 1], su, hist, vf0, vf1);
+  point_forward<WS>(lv, L, ws, K, p0, p1, u0[2 * gidx], u0[2 * gidx + 1], su, hist, vf0, vf1);
   __syncwarp();
   const float w = dloss[gidx];
   const int hws = ws / 2, n = ws * ws;
@@ -351,7 +356,7 @@ __global__ void __launch_bounds__(32 * WARPS) k_lkd_backward(const Lvl* __restri
     grid_clear(gS1, gS1.GH * gS1.GW);
     grid_clear(gB, gB.GH * gB.GW);
     Tmpl<PPL> T;
-    load_template<PPL>(e, ws, S.q0, S.q1, T);
+    load_template<WS>(e, ws, S.q0, S.q1, T);
     if (l == 0) {
       // Loss at level 0: r = A0(p + o) - B0(v + o), dL/dr = 2 r w.
 #pragma unroll
@@ -668,15 +673,16 @@ extern "C" int gbt_lkd_forward(const float* I0, const float* I1, int64_t pitch, 
   if ((r = prepare(I0, I1, pitch, img_bytes, rows, cols, nlevels, npairs, false, P, st))) return r;
   long long total = (long long)npairs * npts;
   if (total > 0)
-    switch ((window * window + 31) / 32) {
-#define GO(PPL) k_lkd_forward<PPL><<<(unsigned)((total + WARPS - 1) / WARPS), 32 * WARPS, 0, st>>>( \
+    switch (window) {
+#define GO(WS) k_lkd_forward<WS><<<(unsigned)((total + WARPS - 1) / WARPS), 32 * WARPS, 0, st>>>( \
       P.table, nlevels, window, iters, npairs, npts, pts, u0, loss, vfinal)
-      case 1: GO(1); break;
-      case 2: GO(2); break;
       case 3: GO(3); break;
-      case 4: GO(4); break;
-      case 5: case 6: GO(6); break;
-      default: GO(8); break;
+      case 5: GO(5); break;
+      case 7: GO(7); break;
+      case 9: GO(9); break;
+      case 11: GO(11); break;
+      case 13: GO(13); break;
+      default: GO(15); break;
 #undef GO
     }
   return cudaGetLastError() == cudaSuccess ? GBT_OK : GBT_E_CUDA;
@@ -695,15 +701,16 @@ extern "C" int gbt_lkd_backward(const float* I0, const float* I1, int64_t pitch,
   if ((r = prepare(I0, I1, pitch, img_bytes, rows, cols, nlevels, npairs, true, P, st))) return r;
   long long total = (long long)npairs * npts;
   if (total > 0)
-    switch ((window * window + 31) / 32) {
-#define GO(PPL) k_lkd_backward<PPL><<<(unsigned)((total + WARPS - 1) / WARPS), 32 * WARPS, 0, st>>>( \
+    switch (window) {
+#define GO(WS) k_lkd_backward<WS><<<(unsigned)((total + WARPS - 1) / WARPS), 32 * WARPS, 0, st>>>( \
       P.table, nlevels, window, iters, npairs, npts, pts, u0, dloss, du0)
-      case 1: GO(1); break;
-      case 2: GO(2); break;
       case 3: GO(3); break;
-      case 4: GO(4); break;
-      case 5: case 6: GO(6); break;
-      default: GO(8); break;
+      case 5: GO(5); break;
+      case 7: GO(7); break;
+      case 9: GO(9); break;
+      case 11: GO(11); break;
+      case 13: GO(13); break;
+      default: GO(15); break;
 #undef GO
     }
   float taps_f[16];
