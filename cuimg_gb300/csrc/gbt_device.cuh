@@ -69,7 +69,7 @@ struct Unit {
   int birth_chunks;   // ceil(3 * TH * TW / CHUNK)
   int* birth_cnt;     // birth_chunks counts, then offsets
   // merge
-  int* act_cnt;       // max_chunks active counts, then offsets
+  int* act_cnt;       // merge actives per 32 slots (cap / 32), then offsets
   uint8_t* cmask;     // cap candidate direction masks
   int4* act_list;     // cap entries: (i, pos packed, ncand, first cand) + cand store
   int* act_cand;      // cap * 8 candidate indices

@@ -286,7 +286,7 @@ static int build(gbt_ctx* ctx, const gbt_config* cfgs, int nstreams) {
     if ((r = dalloc_t(ctx, &u.tilecode, (size_t)u.TH * u.TW + 1))) return r;
     u.birth_chunks = (u.birth_items + CHUNK - 1) / CHUNK;
     if ((r = dalloc_t(ctx, &u.birth_cnt, u.birth_chunks + 1))) return r;
-    if ((r = dalloc_t(ctx, &u.act_cnt, u.max_chunks))) return r;
+    if ((r = dalloc_t(ctx, &u.act_cnt, (size_t)u.cap / 32 + 1))) return r;
     if ((r = dalloc_t(ctx, &u.cmask, u.cap))) return r;
     if ((r = dalloc_t(ctx, &u.act_list, u.cap))) return r;
     if ((r = dalloc_t(ctx, &u.act_cand, (size_t)u.cap * 8, false))) return r;
@@ -519,7 +519,8 @@ static int enqueue_frame(gbt_ctx* ctx, bool any_det, bool any_filt) {
       k_match<Feat><<<g, MATCH_BLOCK, 0, st>>>(ctx->d_units, ctx->d_state, ctx->d_frame, ctx->d_pre, nunits);
   }
   { PROF("k_stats"); k_stats<<<(ctx->nbins + 255) / 256, 256, 0, st>>>(ctx->d_units, ctx->d_state, ctx->d_bin_prefix, nunits); }
-  n += 3;
+  { PROF("k_fuse"); k_fuse<<<(ctx->nbins + 255) / 256, 256, 0, st>>>(ctx->d_units, ctx->d_bin_prefix, nunits); }
+  n += 4;
   if (any_det) {
     CK(cudaMemsetAsync(ctx->pmask_all, 0, ctx->pmask_bytes, st));
     { PROF("k_pmask"); k_pmask<<<pgrid, CHUNK, 0, st>>>(ctx->d_units, ctx->d_state, ctx->d_frame, ctx->d_pre, nunits); }

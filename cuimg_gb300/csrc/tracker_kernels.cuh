@@ -807,37 +807,52 @@ __global__ void __launch_bounds__(256) k_stats(const Unit* __restrict__ units, U
   const int ui = find_unit(bin_prefix, nunits, t);
   const Unit& u = units[ui];
   const int local = t - bin_prefix[ui];
-  const int br = local / u.BW, bc = local % u.BW;
   int n, sr, sc;
-  bin_stats(u, st[ui], br, bc, n, sr, sc);
+  bin_stats(u, st[ui], local / u.BW, local % u.BW, n, sr, sc);
   u.st_n[local] = n;
   u.st_sp[local] = make_int2(sr, sc);
+}
+
+// Multiscale count and fused flow of every bin from the statistics k_stats
+// stored for all scales (one launch after it, so every parent bin is ready).
+__global__ void __launch_bounds__(256) k_fuse(const Unit* __restrict__ units, const int* __restrict__ bin_prefix,
+                                              int nunits) {
+  const int total = bin_prefix[nunits];
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= total) return;
+  const int ui = find_unit(bin_prefix, nunits, t);
+  const Unit& u = units[ui];
+  const int local = t - bin_prefix[ui];
+  const int br = local / u.BW, bc = local % u.BW;
+  const int n = u.st_n[local];
   unsigned msc = (unsigned)n;
   if (u.upper >= 0) {
-    int un, usr, usc;
-    bin_stats(units[u.upper], st[u.upper], br >> 1, bc >> 1, un, usr, usc);
-    msc += (unsigned)un;
+    const Unit& up = units[u.upper];
+    msc += (unsigned)up.st_n[(size_t)(br >> 1) * up.BW + (bc >> 1)];
   }
   u.msc[local] = msc;
-  // Fused flow.
   float2 flow = make_float2(-500.f, -500.f);
-  int vi = ui, vbr = br, vbc = bc, vn = n, vsr = sr, vsc = sc;
+  int vi = ui, vbr = br, vbc = bc, vn = n;
+  int2 vsp = u.st_sp[local];
   float scale = 1.f;
   while (true) {
     const Unit& v = units[vi];
     if (v.upper < 0) {
-      if (vn > 1) flow = make_float2((float)(vsr / vn) * scale, (float)(vsc / vn) * scale);
+      if (vn > 1) flow = make_float2((float)(vsp.x / vn) * scale, (float)(vsp.y / vn) * scale);
       break;
     }
     if (vn > 1) {
-      flow = make_float2((float)vsr * scale, (float)vsc * scale);
+      flow = make_float2((float)vsp.x * scale, (float)vsp.y * scale);
       break;
     }
     vi = v.upper;
     vbr >>= 1;
     vbc >>= 1;
     scale *= 2.f;
-    bin_stats(units[vi], st[vi], vbr, vbc, vn, vsr, vsc);
+    const Unit& w = units[vi];
+    const size_t wl = (size_t)vbr * w.BW + vbc;
+    vn = w.st_n[wl];
+    vsp = w.st_sp[wl];
   }
   u.flow[local] = flow;
 }
@@ -1168,8 +1183,7 @@ __global__ void __launch_bounds__(1024) k_unit_scan(const Unit* __restrict__ uni
       s.B = B;
     }
   } else {
-    const int nch = (s.n + CHUNK - 1) / CHUNK;
-    int A = scan(u.act_cnt, nch);
+    int A = scan(u.act_cnt, (s.n + 31) / 32);  // per-warp counts of k_merge_count
     if (threadIdx.x == 0) s.A = A;
   }
 }
@@ -1356,10 +1370,11 @@ __device__ __forceinline__ unsigned merge_dirs(const Unit& u, const UState& s, i
   return m;
 }
 
+// Actives are counted per warp of 32 slots (act_cnt[i / 32]); the unit scan
+// turns the counts into offsets, so neither pass needs a block-wide prefix.
 __global__ void __launch_bounds__(CHUNK) k_merge_count(const Unit* __restrict__ units, const UState* __restrict__ st,
                                                        const Frame* __restrict__ fr, const int* __restrict__ table,
                                                        int nunits) {
-  __shared__ int wt[65];
   const int f = fr->f;
   const int total = table[nunits];
   for (int g = blockIdx.x; g < total; g += gridDim.x) {
@@ -1377,16 +1392,14 @@ __global__ void __launch_bounds__(CHUNK) k_merge_count(const Unit* __restrict__ 
       }
       u.cmask[i] = (uint8_t)m;
     }
-    int tot;
-    block_prefix(m != 0, wt, tot);
-    if (threadIdx.x == 0) u.act_cnt[cc.chunk] = tot;
+    const unsigned b = __ballot_sync(0xffffffffu, m != 0);
+    if ((threadIdx.x & 31) == 0 && i < s.n) u.act_cnt[i >> 5] = __popc(b);
   }
 }
 
 __global__ void __launch_bounds__(CHUNK) k_merge_scatter(const Unit* __restrict__ units, const UState* __restrict__ st,
                                                          const Frame* __restrict__ fr, const int* __restrict__ table,
                                                          int nunits) {
-  __shared__ int wt[65];
   const int f = fr->f;
   const int total = table[nunits];
   for (int g = blockIdx.x; g < total; g += gridDim.x) {
@@ -1395,9 +1408,13 @@ __global__ void __launch_bounds__(CHUNK) k_merge_scatter(const Unit* __restrict_
     if (!filt_frame(u, f) || !u.with_merge) continue;
     const UState s = st[cc.unit];
     const int i = cc.chunk * CHUNK + threadIdx.x;
+    if ((i & ~31) >= s.n) continue;  // whole warp past the slots
+    const int w = i >> 5;
+    const int o0 = u.act_cnt[w], o1 = (w + 1) * 32 < s.n ? u.act_cnt[w + 1] : s.A;
+    if (o0 == o1) continue;  // no active in this warp
     bool act = i < s.n && u.cmask[i] != 0;
-    int tot;
-    int o = u.act_cnt[cc.chunk] + block_prefix(act, wt, tot);
+    const unsigned b = __ballot_sync(0xffffffffu, act);
+    int o = o0 + __popc(b & ((1u << (threadIdx.x & 31)) - 1u));
     if (act) {
       short2 p = u.pos[s.cur][i];
       int cand[8];
