@@ -415,13 +415,24 @@ __device__ __forceinline__ void predict(unsigned short age, short2 pos, short2 s
 // Match one live particle whose prediction (pr, pc) is inside the domain, and
 // apply the result (kernel_particle_container::move or remove).
 template <class FeatT>
+__device__ __forceinline__ void match_finish(const Unit& u, const FeatT& F, int f, int b, int i, unsigned short age,
+                                             short2 pos, int pr, int pc, const uint4& feat, int dr, int dc);
+
+template <class FeatT>
 __device__ __forceinline__ void match_one(const Unit& u, const FeatT& F, int f, int b, int i, unsigned short age,
                                           short2 pos, int pr, int pc) {
   const uint4 feat = u.feat[b][i];
   int d1r, d1c, d2r, d2c;
   gd_match(u, F, feat, pr, pc, false, d1r, d1c);
   gd_match(u, F, feat, pr + d1r, pc + d1c, true, d2r, d2c);
-  const int dr = d1r + d2r, dc = d1c + d2c;
+  match_finish(u, F, f, b, i, age, pos, pr, pc, feat, d1r + d2r, d1c + d2c);
+}
+
+// The match's acceptance and the particle update (kernel_particle_container::
+// move or remove) for a total descent (dr, dc) from the prediction.
+template <class FeatT>
+__device__ __forceinline__ void match_finish(const Unit& u, const FeatT& F, int f, int b, int i, unsigned short age,
+                                             short2 pos, int pr, int pc, const uint4& feat, int dr, int dc) {
   const int mr = (short)(pr + dr), mc = (short)(pc + dc);
   bool accept = in_dom(u, mr, mc);
   uint4 mf = make_uint4(0, 0, 0, 0);
@@ -577,6 +588,24 @@ __device__ __forceinline__ void cp_async16(void* sdst, const void* gsrc) {
   asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(gsrc) : "memory");
 }
 
+// Stages rows R0s .. R0s + MT_SR - 1 and columns C0s .. C0s + MT_SC - 1 of s1
+// and s2, skipping chunks outside the bordered images (never sampled: the taps
+// stay within 6 pixels of the domain, inside the zero border).
+__device__ __forceinline__ void mt_stage(const Unit& u, int R0s, int C0s, uint8_t* ts1, uint8_t* ts2) {
+  constexpr int CPR = MT_SC / 16;
+  for (int v = threadIdx.x; v < MT_SR * CPR; v += blockDim.x) {
+    const int row = v / CPR, ck = v % CPR;
+    const int gr = R0s + row;                    // image row
+    const int gb = C0s + CB + 16 * ck;           // byte offset inside the bordered row
+    if (gr < -RB || gr >= u.H + RB || gb < 0 || gb + 16 > FIXED_FPITCH) continue;
+    const size_t go = (size_t)(gr + RB) * FIXED_FPITCH + gb;
+    cp_async16(&ts1[row * MT_SC + 16 * ck], u.s1 + go);
+    cp_async16(&ts2[row * MT_SC + 16 * ck], u.s2 + go);
+  }
+  asm volatile("cp.async.commit_group;\n" ::: "memory");
+  asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+}
+
 __global__ void __launch_bounds__(MT_THREADS) k_match_tiled(const Unit* __restrict__ units,
                                                             const UState* __restrict__ st,
                                                             const Frame* __restrict__ fr,
@@ -592,21 +621,7 @@ __global__ void __launch_bounds__(MT_THREADS) k_match_tiled(const Unit* __restri
   const Unit& u = units[ui];
   const int local = t - tile_prefix[ui];
   const int R0s = (local / u.MTC) * MT_R - MT_MR, C0s = (local % u.MTC) * MT_C - MT_MC;
-  // Stage rows R0s .. R0s + MT_SR - 1 and columns C0s .. C0s + MT_SC - 1 of s1
-  // and s2, skipping chunks outside the bordered images (never sampled: the
-  // taps stay within 6 pixels of the domain, inside the zero border).
-  constexpr int CPR = MT_SC / 16;
-  for (int v = threadIdx.x; v < MT_SR * CPR; v += MT_THREADS) {
-    const int row = v / CPR, ck = v % CPR;
-    const int gr = R0s + row;                    // image row
-    const int gb = C0s + CB + 16 * ck;           // byte offset inside the bordered row
-    if (gr < -RB || gr >= u.H + RB || gb < 0 || gb + 16 > FIXED_FPITCH) continue;
-    const size_t go = (size_t)(gr + RB) * FIXED_FPITCH + gb;
-    cp_async16(&ts1[row * MT_SC + 16 * ck], u.s1 + go);
-    cp_async16(&ts2[row * MT_SC + 16 * ck], u.s2 + go);
-  }
-  asm volatile("cp.async.commit_group;\n" ::: "memory");
-  asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+  mt_stage(u, R0s, C0s, ts1, ts2);
   __syncthreads();
   const int f = fr->f;
   const int b = st[ui].cur;
