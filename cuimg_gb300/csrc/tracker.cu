@@ -75,6 +75,7 @@ struct gbt_ctx {
   int* d_mt_cnt = nullptr;
   int* d_mt_off = nullptr;
   int* d_mt_list = nullptr;
+  int2* d_mt_key = nullptr;  // per slot: (tile, rank in the tile) of the count pass
   int* d_post = nullptr;
   // bulk buffers cleared per frame
   void* occ_all = nullptr;
@@ -274,6 +275,7 @@ static int build(gbt_ctx* ctx, const gbt_config* cfgs, int nstreams) {
     u.MTC = (u.W + MT_C - 1) / MT_C;
     u.mt_base = ctx->mt_tiles;
     ctx->mt_tiles += u.MTR * u.MTC;
+    u.mt_pbase = (int)ctx->mt_list_cap;
     ctx->mt_list_cap += u.cap;
     for (int b = 0; b < 2; b++) {
       if ((r = dalloc_t(ctx, &u.pos[b], u.cap))) return r;
@@ -299,6 +301,7 @@ static int build(gbt_ctx* ctx, const gbt_config* cfgs, int nstreams) {
   if ((r = dalloc_t(ctx, &ctx->d_mt_cnt, ctx->mt_tiles + 1))) return r;
   if ((r = dalloc_t(ctx, &ctx->d_mt_off, ctx->mt_tiles + 1))) return r;
   if ((r = dalloc_t(ctx, &ctx->d_mt_list, ctx->mt_list_cap))) return r;
+  if ((r = dalloc_t(ctx, &ctx->d_mt_key, ctx->mt_list_cap))) return r;
   if ((r = dalloc_t(ctx, &ctx->d_post, nunits + 1))) return r;
 
   // Static tables.
@@ -501,9 +504,9 @@ static int enqueue_frame(gbt_ctx* ctx, bool any_det, bool any_filt) {
   }
   if (ctx->match_variant == 0 && ctx->fixed_fpitch) {
     CK(cudaMemsetAsync(ctx->d_mt_cnt, 0, (size_t)ctx->mt_tiles * sizeof(int), st));
-    { PROF("k_mt_count"); k_mt_bin<0><<<pgrid, CHUNK, 0, st>>>(ctx->d_units, ctx->d_state, ctx->d_pre, nunits, ctx->d_mt_cnt, nullptr); }
-    { PROF("k_mt_scan"); k_mt_scan<<<1, 1024, 0, st>>>(ctx->d_mt_cnt, ctx->mt_tiles, ctx->d_mt_off, ctx->d_mt_cnt); }
-    { PROF("k_mt_scatter"); k_mt_bin<1><<<pgrid, CHUNK, 0, st>>>(ctx->d_units, ctx->d_state, ctx->d_pre, nunits, ctx->d_mt_cnt, ctx->d_mt_list); }
+    { PROF("k_mt_count"); k_mt_bin<0><<<pgrid, CHUNK, 0, st>>>(ctx->d_units, ctx->d_state, ctx->d_pre, nunits, ctx->d_mt_cnt, ctx->d_mt_key, nullptr, nullptr); }
+    { PROF("k_mt_scan"); k_mt_scan<<<1, 1024, 0, st>>>(ctx->d_mt_cnt, ctx->mt_tiles, ctx->d_mt_off); }
+    { PROF("k_mt_scatter"); k_mt_bin<1><<<pgrid, CHUNK, 0, st>>>(ctx->d_units, ctx->d_state, ctx->d_pre, nunits, nullptr, ctx->d_mt_key, ctx->d_mt_off, ctx->d_mt_list); }
     { PROF("k_match_tiled"); k_match_tiled<<<ctx->mt_tiles, MT_THREADS, 0, st>>>(ctx->d_units, ctx->d_state, ctx->d_frame, ctx->d_mt_prefix, nunits, ctx->d_mt_off, ctx->d_mt_list); }
     n += 3;
   } else if (ctx->match_variant == 1) {

@@ -514,11 +514,13 @@ __device__ __forceinline__ int mt_tile(const Unit& u, int pr, int pc) {
   return u.mt_base + (pr / MT_R) * u.MTC + pc / MT_C;
 }
 
-// Pass 0 counts live particles per tile (and removes those predicted outside
-// the domain, as the matcher does); pass 1 scatters slot indices.
+// Pass 0 counts live particles per tile, remembering each particle's tile and
+// rank in it (and removes those predicted outside the domain, as the matcher
+// does); pass 1 places every binned slot at its tile's offset + rank.
 template <int PASS>
 __global__ void __launch_bounds__(CHUNK) k_mt_bin(const Unit* __restrict__ units, const UState* __restrict__ st,
                                                   const int* __restrict__ table, int nunits, int* __restrict__ cnt,
+                                                  int2* __restrict__ key, const int* __restrict__ off,
                                                   int* __restrict__ list) {
   const int total = table[nunits];
   for (int g = blockIdx.x; g < total; g += gridDim.x) {
@@ -527,25 +529,31 @@ __global__ void __launch_bounds__(CHUNK) k_mt_bin(const Unit* __restrict__ units
     const UState s = st[cc.unit];
     const int i = cc.chunk * CHUNK + threadIdx.x;
     if (i >= s.n) continue;
-    const int b = s.cur;
-    const unsigned short age = u.age[b][i];
-    if (age == 0) continue;
-    int pr, pc;
-    predict(age, u.pos[b][i], u.spd[b][i], pr, pc);
-    if (!in_dom(u, pr, pc)) {
-      if (PASS == 0) u.age[b][i] = 0;
+    int2* k = key + u.mt_pbase + i;
+    if (PASS == 1) {
+      const int2 tr = *k;
+      if (tr.x >= 0) list[off[tr.x] + tr.y] = i;
       continue;
     }
-    const int t = mt_tile(u, pr, pc);
-    if (PASS == 0) atomicAdd(&cnt[t], 1);
-    else list[atomicAdd(&cnt[t], 1)] = i;
+    const int b = s.cur;
+    const unsigned short age = u.age[b][i];
+    int2 tr = make_int2(-1, 0);
+    if (age != 0) {
+      int pr, pc;
+      predict(age, u.pos[b][i], u.spd[b][i], pr, pc);
+      if (!in_dom(u, pr, pc)) {
+        u.age[b][i] = 0;
+      } else {
+        tr.x = mt_tile(u, pr, pc);
+        tr.y = atomicAdd(&cnt[tr.x], 1);
+      }
+    }
+    *k = tr;
   }
 }
 
-// Exclusive scan of the tile counts into offsets (off[ntiles] = total); the
-// cursor array starts at the offsets for the scatter pass.
-__global__ void __launch_bounds__(1024) k_mt_scan(const int* __restrict__ cnt, int ntiles, int* __restrict__ off,
-                                                  int* __restrict__ cursor) {
+// Exclusive scan of the tile counts into offsets (off[ntiles] = total).
+__global__ void __launch_bounds__(1024) k_mt_scan(const int* __restrict__ cnt, int ntiles, int* __restrict__ off) {
   __shared__ int wt[65];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   int carry = 0;
@@ -572,11 +580,7 @@ __global__ void __launch_bounds__(1024) k_mt_scan(const int* __restrict__ cnt, i
       if (lane == 31) wt[64] = z;
     }
     __syncthreads();
-    if (k < ntiles) {
-      const int e = carry + wt[32 + wid] + x - v;
-      off[k] = e;
-      cursor[k] = e;
-    }
+    if (k < ntiles) off[k] = carry + wt[32 + wid] + x - v;
     carry += wt[64];
     __syncthreads();
   }
