@@ -558,6 +558,54 @@ def measure_extras(args, dev, local, peak):
     ms = e0.elapsed_time(e1) / steps
     px = sum(r * c for r, c, L in picks)
     bt.close()
+    del dvid
+    # Large combined workload: one 3840x2160 stream (5 scales) tracked frame by
+    # frame, with the LK residual and its adjoint through the Gaussian pyramid
+    # (fp32, 5 levels, 9x9, 10 steps) on every 10th frame pair, over the
+    # tracker's level-0 particles.
+    H4, W4, n4 = 2160, 3840, 21
+    v4 = synth.frames(7000, H4, W4, n4)
+    d4 = torch.from_numpy(v4).to(dev)
+    bt4 = BatchTracker([dict(rows=H4, cols=W4, nscales=5, detector_threshold=THRESHOLD,
+                             detector_frequency=DET_FREQ, filtering_frequency=FILT_FREQ)], device=local, graphs=True)
+    bt4._ensure()
+    p4 = (ctypes.c_void_p * 1)()
+    pit4 = (ctypes.c_int64 * 1)(W4)
+
+    def track4(t):
+        p4[0] = d4[t].data_ptr()
+        check(lib.gbt_run(bt4._ctx, p4, pit4, 1), bt4._ctx)
+
+    for t in range(10):
+        track4(t)
+    bt4.sync()
+    parts = bt4._particles(0, 0)
+    pts4 = torch.from_numpy(parts["pos"][parts["age"] > 0].astype(np.float32)).to(dev)[None]
+    u4 = torch.zeros_like(pts4)
+    ones4 = torch.ones(pts4.shape[:2], device=dev)
+    torch.cuda.synchronize()
+    t_trk, t_adj = 0.0, 0.0
+    for t in range(10, n4):
+        t0 = time.perf_counter()
+        track4(t)
+        bt4.sync()
+        t_trk += time.perf_counter() - t0
+        if t % 10 == 0:
+            a, b = d4[t - 1].float()[None], d4[t].float()[None]
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            lkd.forward(a, b, u4, pts4, 5, 9, 10)
+            lkd.backward(a, b, u4, pts4, ones4, 5, 9, 10)
+            torch.cuda.synchronize()
+            t_adj += time.perf_counter() - t0
+    nt = n4 - 10
+    bt4.close()
+    out["combined_4k"] = {"frames": nt, "points": int(pts4.shape[1]), "tracker_ms_per_frame": round(1000 * t_trk / nt, 3),
+                          "adjoint_pairs": sum(1 for t in range(10, n4) if t % 10 == 0),
+                          "adjoint_ms_per_pair": round(1000 * t_adj / max(1, sum(1 for t in range(10, n4) if t % 10 == 0)), 2),
+                          "frames_per_s": round(nt / (t_trk + t_adj), 1),
+                          "note": "host clock around synchronised calls; frames 10..20"}
+    del d4
     out["batched_uneven_64"] = {"streams": 64, "ms_per_step": round(ms, 3), "frames_per_s": round(64 / (ms / 1000), 1),
                                 "mpix_per_s": round(px / (ms / 1000) / 1e6, 1),
                                 "resolutions": {"%dx%d" % (c, r): sum(1 for p in picks if p[:2] == (r, c))

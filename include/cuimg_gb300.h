@@ -63,7 +63,7 @@ typedef struct {
  * H*W/6 + 4096 for FAST, 4 * ceil(H/step) * ceil(W/step) + 4096 for regular
  * and 4*H*W + 4096 for dense (neither checks for particles already at a
  * pixel the way FAST does, so the reference's counts grow without bound);
- * gbt_run reports GBT_E_CAPACITY when births overflow it. */
+ * births beyond it are dropped and gbt_sync reports GBT_E_CAPACITY. */
 #define GBT_DETECTOR_FAST 0
 #define GBT_DETECTOR_REGULAR 1
 #define GBT_DETECTOR_DENSE 2

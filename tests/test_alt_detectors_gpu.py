@@ -75,3 +75,26 @@ def test_mixed_detectors_in_one_context():
     bt.close()
     for o in oracles:
         o.destroy()
+
+
+def test_capacity_overflow_is_reported():
+    # The regular detector with step 1 and grad_th 0 adds a particle at every
+    # pixel of every detector frame; without merging or filtering the set
+    # outgrows its capacity (4 x pixels + 4096) on the fifth frame.  The
+    # births beyond it are dropped and gbt_sync reports GBT_E_CAPACITY.
+    from cuimg_gb300 import Tracker, synth
+    from cuimg_gb300._native import GbtError
+    rows, cols = 120, 160
+    frames = synth.frames(71, rows, cols, 6)
+    tr = Tracker((rows, cols), 1, detector_frequency=1, filtering_frequency=1000, with_merge=0, detector=1,
+                 detector_step=1, detector_grad_th=0)
+    for t in range(4):
+        tr.run(frames[t])
+    tr.sync()
+    assert tr.nparticles() > 3 * rows * cols
+    with pytest.raises(GbtError) as e:
+        for t in range(4, 6):
+            tr.run(frames[t])
+        tr.sync()
+    assert e.value.code == 4
+    tr.close()
