@@ -1257,6 +1257,7 @@ __global__ void __launch_bounds__(CHUNK) k_det_scatter(const Unit* __restrict__ 
           u.feat[nb][o] = F.at(r, c, u.fpitch);
           u.matches[s.n_old + k] = o;
           atomicMax(&u.idx[(size_t)r * u.W + c], stamp | (unsigned)o);
+          atomicOr(&u.occ[bin_word(u, r, c)], bin_bit(r, c));  // occ <=> a current index entry
         }
       }
     }
@@ -1372,6 +1373,9 @@ __device__ __forceinline__ unsigned merge_dirs(const Unit& u, const UState& s, i
   for (int k = 0; k < 8; k++) {
     int r = p.x + c_c8[k][0], c = p.y + c_c8[k][1];
     if (!in_dom(u, r, c)) continue;
+    // occ marks exactly the pixels whose index entry is current (matched
+    // particles, and births on detector frames): most neighbours are empty.
+    if (!(u.occ[bin_word(u, r, c)] & bin_bit(r, c))) continue;
     unsigned long long e = u.idx[(size_t)r * u.W + c];
     if (!idx_current(e, f)) continue;
     unsigned j = (unsigned)(e & 0xffffffffu);
