@@ -7,7 +7,9 @@
 // (pyrlk_tracker.hpp:910-938), every window pixel used, exactly `iters`
 // Gauss-Newton steps per level, coarse-to-fine start from twice the coarser
 // displacement (predictions.h:61-74) and from u0 / 2^(L-1) at the top,
-// floor-based bilinear sampling with clamped taps.  Loss per point = sum over
+// floor-based bilinear sampling with clamped taps (window pixel (r, c) of a
+// window centred at v is sampled at floor(v) + (r, c) with the weights of
+// frac(v), which is the sample at v + (r, c) in exact arithmetic).  Loss per point = sum over
 // the level-0 window of (A0(p + o) - B0(v + o))^2 at the final position v.
 //
 // Adjoint: gradients of sum_i dloss_i * loss_i with respect to both frames and
@@ -53,14 +55,50 @@ struct Bil {
   int dy, dx;       // 1 where the second tap row / column differs from the first, 0 at the clamp
 };
 
-__device__ __forceinline__ Bil bil_at(int H, int W, float y, float x) {
+// All pixels of a window centred at (y, x) share the fractional part of the
+// centre: their bilinear weights are computed once (the taps of window pixel
+// (r, c) are floor(y) + r .. + 1 and floor(x) + c .. + 1, exactly the taps of
+// (y + r, x + c) in exact arithmetic), and when the whole window lies inside
+// the image no tap needs clamping.
+struct Win {
+  int y0, x0;
+  float a, b, w00, w10, w01, w11;
+  bool inner;
+};
+
+__device__ __forceinline__ Win win_at(int H, int W, float y, float x, int h) {
+  Win s;
+  s.y0 = __float2int_rd(y);
+  s.x0 = __float2int_rd(x);
+  s.a = y - (float)s.y0;
+  s.b = x - (float)s.x0;
+  s.w00 = (1.f - s.a) * (1.f - s.b);
+  s.w10 = s.a * (1.f - s.b);
+  s.w01 = (1.f - s.a) * s.b;
+  s.w11 = s.a * s.b;
+  s.inner = s.y0 - h >= 0 && s.y0 + h + 1 <= H - 1 && s.x0 - h >= 0 && s.x0 + h + 1 <= W - 1;
+  return s;
+}
+
+// The sample of window pixel (r, c).
+__device__ __forceinline__ Bil bil_win(int H, int W, const Win& s, int r, int c) {
   Bil o;
-  int y0 = __float2int_rd(y), x0 = __float2int_rd(x);  // floor; |y|, |x| < 2^24
-  o.a = y - (float)y0;
-  o.b = x - (float)x0;
-  int y1 = min(max(y0 + 1, 0), H - 1), x1 = min(max(x0 + 1, 0), W - 1);
-  y0 = min(max(y0, 0), H - 1);
-  x0 = min(max(x0, 0), W - 1);
+  o.a = s.a;
+  o.b = s.b;
+  o.w00 = s.w00;
+  o.w10 = s.w10;
+  o.w01 = s.w01;
+  o.w11 = s.w11;
+  int y0 = s.y0 + r, x0 = s.x0 + c, y1, x1;
+  if (s.inner) {
+    y1 = y0 + 1;
+    x1 = x0 + 1;
+  } else {
+    y1 = min(max(y0 + 1, 0), H - 1);
+    x1 = min(max(x0 + 1, 0), W - 1);
+    y0 = min(max(y0, 0), H - 1);
+    x0 = min(max(x0, 0), W - 1);
+  }
   o.i00 = y0 * W + x0;
   o.i10 = y1 * W + x0;
   o.i01 = y0 * W + x1;
@@ -69,10 +107,6 @@ __device__ __forceinline__ Bil bil_at(int H, int W, float y, float x) {
   o.x0 = x0;
   o.dy = y1 - y0;
   o.dx = x1 - x0;
-  o.w00 = (1.f - o.a) * (1.f - o.b);
-  o.w10 = o.a * (1.f - o.b);
-  o.w01 = (1.f - o.a) * o.b;
-  o.w11 = o.a * o.b;
   return o;
 }
 
@@ -96,9 +130,9 @@ __device__ __forceinline__ void bil_scatter(float* img, const Bil& s, float v) {
   atomicAdd(img + s.i11, s.w11 * v);
 }
 
-__device__ __forceinline__ float wsum(float v) {
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-  return __shfl_sync(0xffffffffu, v, 0);
+__device__ __forceinline__ float wsum(float v) {  // every lane gets the same sum (butterfly)
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
 }
 
 struct Setup {  // per level of one point
@@ -125,13 +159,14 @@ template <int WS>
 __device__ __forceinline__ void load_template(const Lvl& e, int /*window: WS*/, float q0, float q1, Tmpl<ppl_of(WS)>& T) {
   constexpr int ws = WS, PPL = (WS * WS + 31) / 32;
   const int lane = threadIdx.x & 31, hws = ws / 2, n = ws * ws;
+  const Win wq = win_at(e.H, e.W, q0, q1, hws);
 #pragma unroll
   for (int k = 0; k < PPL; k++) {
     const int i = lane + 32 * k;
     T.g[k] = make_float2(0.f, 0.f);
     T.a[k] = 0.f;
     if (i < n) {
-      Bil st = bil_at(e.H, e.W, q0 + (float)(i / ws - hws), q1 + (float)(i % ws - hws));
+      Bil st = bil_win(e.H, e.W, wq, i / ws - hws, i % ws - hws);
       T.g[k] = bil_val2(e.S, st);
       T.a[k] = bil_val(e.A, st);
     }
@@ -168,12 +203,12 @@ __device__ __forceinline__ void rhs(const Lvl& e, int /*window: WS*/, const Tmpl
   const int lane = threadIdx.x & 31, hws = ws / 2, n = ws * ws;
   b0 = 0.f;
   b1 = 0.f;
+  const Win wv = win_at(e.H, e.W, v0, v1, hws);
 #pragma unroll
   for (int k = 0; k < PPL; k++) {
     const int i = lane + 32 * k;
     if (i < n) {
-      const float r = (float)(i / ws - hws), c = (float)(i % ws - hws);
-      const float res = T.a[k] - bil_val(e.B, bil_at(e.H, e.W, v0 + r, v1 + c));
+      const float res = T.a[k] - bil_val(e.B, bil_win(e.H, e.W, wv, i / ws - hws, i % ws - hws));
       b0 += T.g[k].x * res;
       b1 += T.g[k].y * res;
     }
@@ -217,12 +252,13 @@ __device__ float point_forward(const Lvl* lv, int L, int /*window: WS*/, int K, 
   const Lvl& e = lv[0];
   const int lane = threadIdx.x & 31, hws = ws / 2;
   float loss = 0.f;
+  const Win wp = win_at(e.H, e.W, p0, p1, hws), wv = win_at(e.H, e.W, v0, v1, hws);
 #pragma unroll
   for (int k = 0; k < PPL; k++) {
     const int i = lane + 32 * k;
     if (i < n) {
-      const float r = (float)(i / ws - hws), c = (float)(i % ws - hws);
-      float res = bil_val(e.A, bil_at(e.H, e.W, p0 + r, p1 + c)) - bil_val(e.B, bil_at(e.H, e.W, v0 + r, v1 + c));
+      const int r = i / ws - hws, c = i % ws - hws;
+      float res = bil_val(e.A, bil_win(e.H, e.W, wp, r, c)) - bil_val(e.B, bil_win(e.H, e.W, wv, r, c));
       loss += res * res;
     }
   }
@@ -359,12 +395,13 @@ __global__ void __launch_bounds__(32 * WARPS, 4) k_lkd_backward(const Lvl* __res
     load_template<WS>(e, ws, S.q0, S.q1, T);
     if (l == 0) {
       // Loss at level 0: r = A0(p + o) - B0(v + o), dL/dr = 2 r w.
+      const Win wp = win_at(e.H, e.W, p0, p1, hws), wf = win_at(e.H, e.W, vf0, vf1, hws);
 #pragma unroll
       for (int kk = 0; kk < PPL; kk++) {
         const int i = lane + 32 * kk;
         if (i < n) {
-          const float r = (float)(i / ws - hws), c = (float)(i % ws - hws);
-          Bil sa = bil_at(e.H, e.W, p0 + r, p1 + c), sb = bil_at(e.H, e.W, vf0 + r, vf1 + c);
+          const int r = i / ws - hws, c = i % ws - hws;
+          Bil sa = bil_win(e.H, e.W, wp, r, c), sb = bil_win(e.H, e.W, wf, r, c);
           const float res = bil_val(e.A, sa) - bil_val(e.B, sb);
           const float dr = 2.f * res * w;
           gA.add(e.dA, sa, dr);
@@ -386,12 +423,12 @@ __global__ void __launch_bounds__(32 * WARPS, 4) k_lkd_backward(const Lvl* __res
       const float d0 = dv0, d1 = dv1;                       // adjoint of v_{k+1}
       const float db0 = S.M00 * d0 + S.M01 * d1, db1 = S.M01 * d0 + S.M11 * d1;
       float b0 = 0.f, b1 = 0.f, pv0 = 0.f, pv1 = 0.f;
+      const Win wk = win_at(e.H, e.W, vk.x, vk.y, hws);
 #pragma unroll
       for (int kk = 0; kk < PPL; kk++) {
         const int i = lane + 32 * kk;
         if (i < n) {
-          const float r = (float)(i / ws - hws), c = (float)(i % ws - hws);
-          Bil sb = bil_at(e.H, e.W, vk.x + r, vk.y + c);
+          Bil sb = bil_win(e.H, e.W, wk, i / ws - hws, i % ws - hws);
           const float2 g = T.g[kk];
           const float res = T.a[kk] - bil_val(e.B, sb);
           b0 += g.x * res;
@@ -421,12 +458,12 @@ __global__ void __launch_bounds__(32 * WARPS, 4) k_lkd_backward(const Lvl* __res
     const float G00 = -(S.M00 * t00 + S.M01 * t10), G01 = -(S.M00 * t01 + S.M01 * t11);
     const float G10 = -(S.M01 * t00 + S.M11 * t10), G11 = -(S.M01 * t01 + S.M11 * t11);
     const float H00 = 2.f * G00, H01 = G01 + G10, H11 = 2.f * G11;
+    const Win wq = win_at(e.H, e.W, S.q0, S.q1, hws);
 #pragma unroll
     for (int kk = 0; kk < PPL; kk++) {
       const int i = lane + 32 * kk;
       if (i < n) {
-        const float r = (float)(i / ws - hws), c = (float)(i % ws - hws);
-        Bil st = bil_at(e.H, e.W, S.q0 + r, S.q1 + c);
+        Bil st = bil_win(e.H, e.W, wq, i / ws - hws, i % ws - hws);
         const float2 g = T.g[kk];
         gS0.add((float*)e.dS, st, dg0[kk] + H00 * g.x + H01 * g.y);
         gS1.add((float*)e.dS + 1, st, dg1[kk] + H01 * g.x + H11 * g.y);
