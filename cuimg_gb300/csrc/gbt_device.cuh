@@ -49,6 +49,7 @@ struct Unit {
   int BH, BW;
   unsigned long long* occ;
   unsigned long long* pmask;
+  unsigned long long* ppos;   // particle slot positions (detector frames, FAST)
   unsigned long long* idx;
   int* st_n;
   int2* st_sp;

@@ -81,6 +81,7 @@ struct gbt_ctx {
   void* occ_all = nullptr;
   size_t occ_bytes = 0;
   void* pmask_all = nullptr;
+  void* ppos_all = nullptr;
   size_t pmask_bytes = 0;
   std::vector<void*> allocs;
   // graphs, keyed by (any detector unit, any filtering unit)
@@ -240,11 +241,13 @@ static int build(gbt_ctx* ctx, const gbt_config* cfgs, int nstreams) {
   int r;
   if ((r = dalloc(ctx, &ctx->occ_all, ctx->occ_bytes, true))) return r;
   if ((r = dalloc(ctx, &ctx->pmask_all, ctx->pmask_bytes, true))) return r;
+  if ((r = dalloc(ctx, &ctx->ppos_all, ctx->pmask_bytes, true))) return r;
   size_t woff = 0;
   for (auto& u : ctx->units) {
     size_t nb = (size_t)u.BH * u.BW;
     u.occ = (unsigned long long*)ctx->occ_all + woff;
     u.pmask = (unsigned long long*)ctx->pmask_all + woff;
+    u.ppos = (unsigned long long*)ctx->ppos_all + woff;
     woff += nb;
     u.ipitch = round_up(u.W, 64);
     if ((r = dalloc(ctx, (void**)&u.img, (size_t)u.ipitch * u.H, true))) return r;
@@ -525,8 +528,9 @@ static int enqueue_frame(gbt_ctx* ctx, bool any_det, bool any_filt) {
   { PROF("k_fuse"); k_fuse<<<(ctx->nbins + 255) / 256, 256, 0, st>>>(ctx->d_units, ctx->d_bin_prefix, nunits); }
   n += 4;
   if (any_det) {
-    CK(cudaMemsetAsync(ctx->pmask_all, 0, ctx->pmask_bytes, st));
+    CK(cudaMemsetAsync(ctx->ppos_all, 0, ctx->pmask_bytes, st));
     { PROF("k_pmask"); k_pmask<<<pgrid, CHUNK, 0, st>>>(ctx->d_units, ctx->d_state, ctx->d_frame, ctx->d_pre, nunits); }
+    { PROF("k_pmask_dilate"); k_pmask_dilate<<<(ctx->nbins + 255) / 256, 256, 0, st>>>(ctx->d_units, ctx->d_frame, ctx->d_bin_prefix, nunits); }
     { PROF("k_detect"); k_detect<<<ctx->det_blocks, 256, 0, st>>>(ctx->d_units, ctx->d_frame, ctx->d_det_prefix, nunits); }
     if (ctx->any_alt_detector) {
       PROF("k_detect_alt");
@@ -538,7 +542,7 @@ static int enqueue_frame(gbt_ctx* ctx, bool any_det, bool any_filt) {
     { PROF("k_det_scatter"); k_det_scatter<<<pgrid, CHUNK, 0, st>>>(ctx->d_units, ctx->d_state, ctx->d_frame, ctx->d_pre, ctx->d_btable,
                                            nunits); }
     { PROF("k_commit"); k_commit<<<1, 1024, 0, st>>>(ctx->d_units, ctx->d_state, ctx->d_frame, ctx->d_post, nunits); }
-    n += 6;
+    n += 7;
   }
   int* table = any_det ? ctx->d_post : ctx->d_pre;
   if (any_filt) {

@@ -879,7 +879,9 @@ __global__ void __launch_bounds__(256) k_fuse(const Unit* __restrict__ units, co
 // ---------------------------------------------------------------------------
 // Detector mask, part 1: particle_mask_kernel (tracking_strategies.hpp:201-225)
 // zeroes the mask at every particle slot's position and its 8 neighbours
-// (dead slots included).  Here those pixels get a bit in `pmask`.
+// (dead slots included).  Here those pixels get a bit in `pmask`: k_pmask marks
+// every slot's position in `ppos` (one atomic per slot) and k_pmask_dilate
+// dilates that bitmap by the 3x3 box, one 64-bit bin word per thread.
 __device__ __forceinline__ bool det_frame(const Unit& u, int f) { return (f % u.det_freq) == 0; }
 __device__ __forceinline__ bool filt_frame(const Unit& u, int f) { return (f % u.filt_freq) == 0; }
 
@@ -895,13 +897,34 @@ __global__ void __launch_bounds__(CHUNK) k_pmask(const Unit* __restrict__ units,
     const UState s = st[cc.unit];
     const int i = cc.chunk * CHUNK + threadIdx.x;
     if (i >= s.n) continue;
-    short2 p = u.pos[s.cur][i];
-    for (int dr = -1; dr <= 1; dr++)
-      for (int dc = -1; dc <= 1; dc++) {
-        int r = p.x + dr, c = p.y + dc;
-        if (in_dom(u, r, c)) atomicOr(&u.pmask[bin_word(u, r, c)], bin_bit(r, c));
-      }
+    const short2 p = u.pos[s.cur][i];
+    atomicOr(&u.ppos[bin_word(u, p.x, p.y)], bin_bit(p.x, p.y));
   }
+}
+
+// Row-wise 3-pixel dilation of a bin word (bit (r&7)*8 + (c&7)) with the
+// edge columns of its left and right neighbour words.
+__device__ __forceinline__ unsigned long long dilate_row(unsigned long long w, unsigned long long wl,
+                                                         unsigned long long wr) {
+  const unsigned long long C0 = 0x0101010101010101ull, C7 = 0x8080808080808080ull;
+  return w | ((w << 1) & ~C0) | ((w >> 1) & ~C7) | ((wl >> 7) & C0) | ((wr << 7) & C7);
+}
+
+__global__ void __launch_bounds__(256) k_pmask_dilate(const Unit* __restrict__ units, const Frame* __restrict__ fr,
+                                                      const int* __restrict__ bin_prefix, int nunits) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= bin_prefix[nunits]) return;
+  const int ui = find_unit(bin_prefix, nunits, t);
+  const Unit& u = units[ui];
+  if (!det_frame(u, fr->f) || u.det_kind != GBT_DETECTOR_FAST) return;
+  const int local = t - bin_prefix[ui];
+  const int br = local / u.BW, bc = local % u.BW;
+  auto word = [&](int r, int c) -> unsigned long long {
+    return (r >= 0 && r < u.BH && c >= 0 && c < u.BW) ? u.ppos[(size_t)r * u.BW + c] : 0ull;
+  };
+  auto hrow = [&](int r) -> unsigned long long { return dilate_row(word(r, bc), word(r, bc - 1), word(r, bc + 1)); };
+  const unsigned long long h = hrow(br), hu = hrow(br - 1), hd = hrow(br + 1);
+  u.pmask[local] = h | (h << 8) | (h >> 8) | (hu >> 56) | (hd << 56);
 }
 
 // fast::compute_saliency without branches, for a pixel P of a shared tile
