@@ -63,12 +63,12 @@ struct Unit {
   int* matches;
   int cap;
   int max_chunks;
-  int* chunk_cnt;     // max_chunks survivor counts, then offsets
+  int* chunk_cnt;     // survivors per 32 slots (cap / 32), then offsets
   // detector
   int TH, TW;
   uint8_t* tilecode;  // TH * TW
   int birth_chunks;   // ceil(3 * TH * TW / CHUNK)
-  int* birth_cnt;     // birth_chunks counts, then offsets
+  int* birth_cnt;     // births per 32 items (birth_items / 32), then offsets
   // merge
   int* act_cnt;       // merge actives per 32 slots (cap / 32), then offsets
   uint8_t* cmask;     // cap candidate direction masks

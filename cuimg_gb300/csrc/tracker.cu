@@ -287,10 +287,10 @@ static int build(gbt_ctx* ctx, const gbt_config* cfgs, int nstreams) {
       if ((r = dalloc_t(ctx, &u.feat[b], u.cap))) return r;
     }
     if ((r = dalloc_t(ctx, &u.matches, (size_t)u.cap + (size_t)u.max_births))) return r;
-    if ((r = dalloc_t(ctx, &u.chunk_cnt, u.max_chunks))) return r;
+    if ((r = dalloc_t(ctx, &u.chunk_cnt, (size_t)u.cap / 32 + 1))) return r;
     if ((r = dalloc_t(ctx, &u.tilecode, (size_t)u.TH * u.TW + 1))) return r;
     u.birth_chunks = (u.birth_items + CHUNK - 1) / CHUNK;
-    if ((r = dalloc_t(ctx, &u.birth_cnt, u.birth_chunks + 1))) return r;
+    if ((r = dalloc_t(ctx, &u.birth_cnt, (size_t)u.birth_items / 32 + 2))) return r;
     if ((r = dalloc_t(ctx, &u.act_cnt, (size_t)u.cap / 32 + 1))) return r;
     if ((r = dalloc_t(ctx, &u.cmask, u.cap))) return r;
     if ((r = dalloc_t(ctx, &u.act_list, u.cap))) return r;

@@ -1145,10 +1145,12 @@ __device__ __forceinline__ bool birth_item(const Unit& u, int v, int& r, int& c)
 
 // Counts per chunk: survivors (age != 0) over the pre-compaction slots of each
 // detector-frame unit, and births over its birth items.
+// Survivors and births are counted per warp of 32 slots / items
+// (chunk_cnt[i / 32], birth_cnt[i / 32]); the unit scan turns the counts into
+// offsets, so neither pass needs a block-wide prefix.
 __global__ void __launch_bounds__(CHUNK) k_det_count(const Unit* __restrict__ units, const UState* __restrict__ st,
                                                      const Frame* __restrict__ fr, const int* __restrict__ table,
                                                      const int* __restrict__ btable, int nunits) {
-  __shared__ int wt[65];
   const int f = fr->f;
   const int ts = table[nunits], tb = btable[nunits];
   for (int g = blockIdx.x; g < ts + tb; g += gridDim.x) {
@@ -1158,16 +1160,18 @@ __global__ void __launch_bounds__(CHUNK) k_det_count(const Unit* __restrict__ un
     if (!det_frame(u, f)) continue;  // uniform per block
     const int i = cc.chunk * CHUNK + threadIdx.x;
     bool pred;
+    int lim;
     if (births) {
       int r, c;
-      pred = i < u.birth_items && birth_item(u, i, r, c);
+      lim = u.birth_items;
+      pred = i < lim && birth_item(u, i, r, c);
     } else {
       const UState s = st[cc.unit];
-      pred = i < s.n && u.age[s.cur][i] != 0;
+      lim = s.n;
+      pred = i < lim && u.age[s.cur][i] != 0;
     }
-    int total;
-    block_prefix(pred, wt, total);
-    if (threadIdx.x == 0) (births ? u.birth_cnt : u.chunk_cnt)[cc.chunk] = total;
+    const unsigned b = __ballot_sync(0xffffffffu, pred);
+    if ((threadIdx.x & 31) == 0 && i < lim) (births ? u.birth_cnt : u.chunk_cnt)[i >> 5] = __popc(b);
   }
 }
 
@@ -1215,10 +1219,9 @@ __global__ void __launch_bounds__(1024) k_unit_scan(const Unit* __restrict__ uni
     }
     return carry;
   };
-  if (which == 0) {
-    const int nch = (s.n + CHUNK - 1) / CHUNK;
-    int S = scan(u.chunk_cnt, nch);
-    int B = scan(u.birth_cnt, u.birth_chunks);
+  if (which == 0) {  // per-warp counts of k_det_count
+    int S = scan(u.chunk_cnt, (s.n + 31) / 32);
+    int B = scan(u.birth_cnt, (u.birth_items + 31) / 32);
     if (threadIdx.x == 0) {
       s.n_old = s.n;
       s.S = S;
@@ -1237,9 +1240,9 @@ __global__ void __launch_bounds__(1024) k_unit_scan(const Unit* __restrict__ uni
 __global__ void __launch_bounds__(CHUNK) k_det_scatter(const Unit* __restrict__ units, const UState* __restrict__ st,
                                                        Frame* __restrict__ fr, const int* __restrict__ table,
                                                        const int* __restrict__ btable, int nunits) {
-  __shared__ int wt[65];
   const int f = fr->f;
   const int ts = table[nunits], tb = btable[nunits];
+  const unsigned lt = (1u << (threadIdx.x & 31)) - 1u;
   for (int g = blockIdx.x; g < ts + tb; g += gridDim.x) {
     bool births = g >= ts;
     ChunkCursor cc = births ? chunk_of(btable, nunits, g - ts) : chunk_of(table, nunits, g);
@@ -1250,9 +1253,9 @@ __global__ void __launch_bounds__(CHUNK) k_det_scatter(const Unit* __restrict__ 
     const int ob = s.cur, nb = s.cur ^ 1;
     const unsigned long long stamp = (unsigned long long)stamp_compact(f) << 32;
     if (!births) {
+      if ((i & ~31) >= s.n_old) continue;  // whole warp past the slots
       bool alive = i < s.n_old && u.age[ob][i] != 0;
-      int total;
-      int o = u.chunk_cnt[cc.chunk] + block_prefix(alive, wt, total);
+      int o = u.chunk_cnt[i >> 5] + __popc(__ballot_sync(0xffffffffu, alive) & lt);
       if (i < s.n_old) u.matches[i] = alive ? o : -1;
       if (alive) {
         short2 p = u.pos[ob][i];
@@ -1263,10 +1266,10 @@ __global__ void __launch_bounds__(CHUNK) k_det_scatter(const Unit* __restrict__ 
         atomicMax(&u.idx[(size_t)p.x * u.W + p.y], stamp | (unsigned)o);
       }
     } else {
+      if ((i & ~31) >= u.birth_items) continue;  // whole warp past the items
       int r = 0, c = 0;
       bool born = i < u.birth_items && birth_item(u, i, r, c);
-      int total;
-      int k = u.birth_cnt[cc.chunk] + block_prefix(born, wt, total);
+      int k = u.birth_cnt[i >> 5] + __popc(__ballot_sync(0xffffffffu, born) & lt);
       if (born) {
         int o = s.S + k;
         if (o >= u.cap) {
