@@ -117,6 +117,19 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(self.samples)}
 
 
+def cpu_model():
+    """Host CPU description (lscpu's model name, or the architecture)."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.lower().startswith("model name"):
+                return line.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    import platform
+    return platform.machine()
+
+
 def _cpu_stream_worker(i, nframes, warmup, barrier, out):
     """One stream of the CPU tracker (oracle port, one thread) in its own
     process: frames of stream i, `warmup` untimed, the rest timed between
@@ -190,6 +203,7 @@ def bench_reference(args):
                                "filter every frame; one frame of every stream per step" % cores,
                    "streams": cores, "live_particles_per_stream": round(n)},
         "cpu_baseline": {"value": round(fps, 3), "unit": UNIT, "cores": cores, "kind": "port",
+                         "per_core": round(fps / cores, 3), "cpu": cpu_model(),
                          "sample": "%d timed frames of each of %d streams after %d warm-up frames, one process and "
                                    "core per stream" % (args.steps, cores, args.warmup)},
         "e2e": {"value": round(fps, 3), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -231,6 +245,7 @@ def bench_ours(args):
     torch.cuda.synchronize()
 
     launches = [0]  # kernels launched inside the last timed region
+    step_stats = [None]  # per-step milliseconds of the last timed region
 
     def timed_resident(bt, nstreams, steps, warmup, offset=0, sustain_s=0.0):
         stream = torch.cuda.ExternalStream(bt.cuda_stream(), device=dev)
@@ -248,16 +263,19 @@ def bench_ours(args):
         if pg:
             pg.barrier()
         torch.cuda.synchronize()
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(steps + 1)]
         k0 = bt.kernel_launches()
-        e0.record(stream)
+        ev[0].record(stream)
         for t in range(steps):
             step(offset + warmup + t)
-        e1.record(stream)
+            ev[t + 1].record(stream)
         launches[0] = bt.kernel_launches() - k0
-        e1.synchronize()
+        ev[-1].synchronize()
         torch.cuda.synchronize()
-        ms = e0.elapsed_time(e1)
+        ms = ev[0].elapsed_time(ev[-1])
+        per = sorted(ev[t].elapsed_time(ev[t + 1]) for t in range(steps))
+        step_stats[0] = {"median": round(per[len(per) // 2], 4), "p10": round(per[len(per) // 10], 4),
+                         "p90": round(per[min(len(per) - 1, (9 * len(per)) // 10)], 4)}
         # Keep the same step running so the clock sampler sees the GPU under
         # this load for longer than the (short) timed region; not timed.
         t_end, t = time.perf_counter() + sustain_s, steps
@@ -277,6 +295,7 @@ def bench_ours(args):
     with ClockSampler(local) as clk:
         ms = timed_resident(bt, B, args.steps, args.warmup, sustain_s=1.5)
     timed_launches = launches[0]
+    batched_steps = step_stats[0]
     clocks = clk.summary()
     clocks["window"] = "timed region + 1.5 s more of the same step"
     value = B * world * args.steps / (ms / 1000.0)
@@ -406,6 +425,7 @@ def bench_ours(args):
     if rank == 0 and not args.no_cpu:
         fps_cpu, wall_cpu, cores_cpu, _ = run_cpu_streams(B, args.cpu_frames, 2)
         cpu = {"value": round(fps_cpu, 3), "unit": UNIT, "cores": cores_cpu, "kind": "port",
+               "per_core": round(fps_cpu / cores_cpu, 3), "cpu": cpu_model(),
                "sample": "%d frames of each of %d 1080p streams (%.1f s wall), one process and core per stream"
                          % (args.cpu_frames, cores_cpu, wall_cpu)}
 
@@ -432,6 +452,7 @@ def bench_ours(args):
                          "avg_launch_ms": round(dom_avg_s * 1000, 5), "peak_source": peak_source},
             "kernel_time_shares": shares,
             "gpu_launches": timed_launches,
+            "step_ms": batched_steps,
             "trajectories": {"history": 20, "frames_per_s": round(traj_fps, 2),
                              "relative_to_value": round(traj_fps / value, 3)},
             "clocks": clocks,
