@@ -97,6 +97,18 @@ def test_detector_arc_lengths_and_thresholds(n_fast, th):
     o.destroy()
 
 
+def test_gpu_matches_oracle_4k():
+    # 3840x2160 with 5 scales: the largest benchmark geometry (fixed s1/s2 pitch).
+    total = _compare_run(2160, 3840, 5, 3, 33, 10)
+    assert total > 0
+
+
+def test_gpu_matches_oracle_wider_than_the_fixed_pitch():
+    # Levels wider than 4064 pixels take the runtime-pitch matcher.
+    total = _compare_run(64, 4200, 2, 4, 34, 2)
+    assert total > 0
+
+
 def test_gpu_matches_oracle_1080p():
     # The headline geometry: 1920x1080, 4 scales, detector every 10 frames.
     total = _compare_run(1080, 1920, 4, 12, 5, 10)
