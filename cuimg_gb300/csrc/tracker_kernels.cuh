@@ -552,39 +552,40 @@ __global__ void __launch_bounds__(CHUNK) k_mt_bin(const Unit* __restrict__ units
   }
 }
 
-// Exclusive scan of the tile counts into offsets (off[ntiles] = total).
+// Exclusive scan of the tile counts into offsets (off[ntiles] = total): each
+// thread scans a contiguous run of counts, the block scans the run totals.
 __global__ void __launch_bounds__(1024) k_mt_scan(const int* __restrict__ cnt, int ntiles, int* __restrict__ off) {
   __shared__ int wt[65];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  int carry = 0;
-  for (int base = 0; base < ntiles; base += 1024) {
-    const int k = base + threadIdx.x;
-    const int v = k < ntiles ? cnt[k] : 0;
-    int x = v;
+  const int per = (ntiles + 1023) / 1024, k0 = threadIdx.x * per, k1 = min(k0 + per, ntiles);
+  int run = 0;
+  for (int k = k0; k < k1; k++) run += cnt[k];
+  int x = run;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) wt[wid] = x;
+  __syncthreads();
+  if (wid == 0) {
+    const int w = wt[lane];
+    int z = w;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
-      const int y = __shfl_up_sync(0xffffffffu, x, o);
-      if (lane >= o) x += y;
+      const int y = __shfl_up_sync(0xffffffffu, z, o);
+      if (lane >= o) z += y;
     }
-    if (lane == 31) wt[wid] = x;
-    __syncthreads();
-    if (wid == 0) {
-      const int w = wt[lane];
-      int z = w;
-#pragma unroll
-      for (int o = 1; o < 32; o <<= 1) {
-        const int y = __shfl_up_sync(0xffffffffu, z, o);
-        if (lane >= o) z += y;
-      }
-      wt[32 + lane] = z - w;
-      if (lane == 31) wt[64] = z;
-    }
-    __syncthreads();
-    if (k < ntiles) off[k] = carry + wt[32 + wid] + x - v;
-    carry += wt[64];
-    __syncthreads();
+    wt[32 + lane] = z - w;
+    if (lane == 31) wt[64] = z;
   }
-  if (threadIdx.x == 0) off[ntiles] = carry;
+  __syncthreads();
+  int e = wt[32 + wid] + x - run;
+  for (int k = k0; k < k1; k++) {
+    off[k] = e;
+    e += cnt[k];
+  }
+  if (threadIdx.x == 0) off[ntiles] = wt[64];
 }
 
 __device__ __forceinline__ void cp_async16(void* sdst, const void* gsrc) {
