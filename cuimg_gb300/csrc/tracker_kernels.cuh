@@ -502,11 +502,11 @@ __global__ void __launch_bounds__(MATCH_BLOCK) k_match(const Unit* __restrict__ 
 // of the tile can touch is staged.  Particles are independent (each writes
 // only its own slot; the sparse index keeps the highest slot with atomicMax),
 // so the order inside a tile does not change any result.
-constexpr int MT_R = 32, MT_C = 128;                // tile
+constexpr int MT_R = 64, MT_C = 128;                // tile
 constexpr int MT_MR = 26, MT_MC = 32;              // staged margins
-constexpr int MT_SR = MT_R + 2 * MT_MR;            // staged rows (84)
+constexpr int MT_SR = MT_R + 2 * MT_MR;            // staged rows (116)
 constexpr int MT_SC = MT_C + 2 * MT_MC;            // staged columns (192), 16-byte chunks
-constexpr int MT_THREADS = 128;
+constexpr int MT_THREADS = 256;
 static_assert(MT_MR >= 2 * 10 + 6 && MT_MC >= 2 * 10 + 6, "staged margins cover a full descent");
 static_assert(MT_SC % 16 == 0 && MT_MC % 16 == 0, "16-byte staging");
 
@@ -611,7 +611,7 @@ __device__ __forceinline__ void mt_stage(const Unit& u, int R0s, int C0s, uint8_
   asm volatile("cp.async.wait_group 0;\n" ::: "memory");
 }
 
-__global__ void __launch_bounds__(MT_THREADS) k_match_tiled(const Unit* __restrict__ units,
+__global__ void __launch_bounds__(MT_THREADS, 4) k_match_tiled(const Unit* __restrict__ units,
                                                             const UState* __restrict__ st,
                                                             const Frame* __restrict__ fr,
                                                             const int* __restrict__ tile_prefix, int nunits,

@@ -194,7 +194,7 @@ int gbt_checkpoint_load(gbt_ctx* ctx, const void* buf, size_t len);
 
 /* Tuning knobs (results are identical for every setting; only speed
  * changes).  GBT_TUNE_MATCHER: 0 = particles binned by prediction into
- * 32 x 128 tiles, one CTA per tile matching from shared memory, 1 = one warp
+ * 64 x 128 tiles, one CTA per tile matching from shared memory, 1 = one warp
  * per particle with the sweep candidates spread over its lanes, 2 = one thread
  * per particle with ring offsets computed from each level's pitch, 3 = one
  * thread per particle with compile-time ring offsets.  0 and 3 need every
