@@ -220,7 +220,7 @@ __device__ __forceinline__ void rhs(const Lvl& e, int /*window: WS*/, const Tmpl
 // Forward of one point; fills the per-level setup and the iterate history.
 template <int WS>
 __device__ float point_forward(const Lvl* lv, int L, int /*window: WS*/, int K, float p0, float p1, float u0, float u1,
-                               Setup* su, float2* hist, float& vf0, float& vf1) {
+                               Setup* su, float4* hist, float& vf0, float& vf1) {
   constexpr int ws = WS, PPL = (WS * WS + 31) / 32;
   const int n = ws * ws;
   const float top = level_scale(L - 1);
@@ -237,13 +237,13 @@ __device__ float point_forward(const Lvl* lv, int L, int /*window: WS*/, int K, 
     v0 = q0 + d0;
     v1 = q1 + d1;
     for (int k = 0; k < K; k++) {
-      if (hist) hist[l * (MAXK + 1) + k] = make_float2(v0, v1);
       float b0, b1;
       rhs<WS>(e, ws, T, v0, v1, b0, b1);
+      if (hist) hist[l * (MAXK + 1) + k] = make_float4(v0, v1, b0, b1);  // iterate and its right-hand side
       v0 += M00 * b0 + M01 * b1;
       v1 += M01 * b0 + M11 * b1;
     }
-    if (hist) hist[l * (MAXK + 1) + K] = make_float2(v0, v1);
+    if (hist) hist[l * (MAXK + 1) + K] = make_float4(v0, v1, 0.f, 0.f);
     d0 = 2.f * (v0 - q0);
     d1 = 2.f * (v1 - q1);
   }
@@ -345,7 +345,7 @@ __global__ void __launch_bounds__(32 * WARPS, 4) k_lkd_backward(const Lvl* __res
                                                              const float* __restrict__ dloss, float* __restrict__ du0) {
   constexpr int ws = WS, PPL = (WS * WS + 31) / 32;
   __shared__ Setup su_all[WARPS][MAXL];
-  __shared__ float2 hist_all[WARPS][MAXL * (MAXK + 1)];
+  __shared__ float4 hist_all[WARPS][MAXL * (MAXK + 1)];
   __shared__ float gB_all[WARPS][GRID_CELLS];                       // dB over the level's residual samples
   __shared__ float gT_all[WARPS][3][(MAXW + 1) * (MAXW + 1)];      // dA, dS.x, dS.y over the template
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -354,7 +354,7 @@ __global__ void __launch_bounds__(32 * WARPS, 4) k_lkd_backward(const Lvl* __res
   const int pair = (int)(gidx / npts);
   const Lvl* lv = levels + (size_t)pair * L;
   Setup* su = su_all[warp];
-  float2* hist = hist_all[warp];
+  float4* hist = hist_all[warp];
   const float p0 = pts[2 * gidx], p1 = pts[2 * gidx + 1];
   float vf0, vf1;
   point_forward<WS>(lv, L, ws, K, p0, p1, u0[2 * gidx], u0[2 * gidx + 1], su, hist, vf0, vf1);
@@ -379,7 +379,7 @@ __global__ void __launch_bounds__(32 * WARPS, 4) k_lkd_backward(const Lvl* __res
       float ylo = 1e30f, yhi = -1e30f, xlo = 1e30f, xhi = -1e30f;
       for (int k = 0; k <= K; k++) {
         if (k == K && l != 0) break;
-        const float2 v = hist[l * (MAXK + 1) + k];
+        const float4 v = hist[l * (MAXK + 1) + k];
         ylo = fminf(ylo, v.x);
         yhi = fmaxf(yhi, v.x);
         xlo = fminf(xlo, v.y);
@@ -419,10 +419,11 @@ __global__ void __launch_bounds__(32 * WARPS, 4) k_lkd_backward(const Lvl* __res
 #pragma unroll
     for (int k = 0; k < PPL; k++) dg0[k] = dg1[k] = dT[k] = 0.f;
     for (int k = K - 1; k >= 0; k--) {
-      const float2 vk = hist[l * (MAXK + 1) + k];
+      const float4 vk = hist[l * (MAXK + 1) + k];  // v_k and b_k of the replayed forward
       const float d0 = dv0, d1 = dv1;                       // adjoint of v_{k+1}
       const float db0 = S.M00 * d0 + S.M01 * d1, db1 = S.M01 * d0 + S.M11 * d1;
-      float b0 = 0.f, b1 = 0.f, pv0 = 0.f, pv1 = 0.f;
+      const float b0 = vk.z, b1 = vk.w;
+      float pv0 = 0.f, pv1 = 0.f;
       const Win wk = win_at(e.H, e.W, vk.x, vk.y, hws);
 #pragma unroll
       for (int kk = 0; kk < PPL; kk++) {
@@ -431,20 +432,16 @@ __global__ void __launch_bounds__(32 * WARPS, 4) k_lkd_backward(const Lvl* __res
           Bil sb = bil_win(e.H, e.W, wk, i / ws - hws, i % ws - hws);
           const float2 g = T.g[kk];
           const float res = T.a[kk] - bil_val(e.B, sb);
-          b0 += g.x * res;
-          b1 += g.y * res;
+          const float2 gb = bil_grad(e.B, sb);
           const float dres = g.x * db0 + g.y * db1;
           dg0[kk] += res * db0;
           dg1[kk] += res * db1;
           dT[kk] += dres;
           gB.add(e.dB, sb, -dres);
-          const float2 gb = bil_grad(e.B, sb);
           pv0 -= dres * gb.x;
           pv1 -= dres * gb.y;
         }
       }
-      b0 = wsum(b0);
-      b1 = wsum(b1);
       dv0 = d0 + wsum(pv0);
       dv1 = d1 + wsum(pv1);
       dM00 += d0 * b0;
