@@ -40,6 +40,19 @@ struct gbt_ctx {
   int device = 0;
   int nsm = 0;
   cudaStream_t stream = nullptr;
+  // Frame pipeline.  The front end of a frame (its input copy, the pyramid
+  // and the blurs) runs on `pre` into the image buffers of the frame's parity
+  // while the back end of the previous frame (matcher to tick) still runs on
+  // `stream` over the other parity's images.  The back end waits for its
+  // front end (ev_front); a front end waits for the back end that last read
+  // its parity's images (ev_back).  With per-kernel timing on, both run on
+  // `stream`.
+  cudaStream_t pre = nullptr;
+  cudaEvent_t ev_front = nullptr;
+  cudaEvent_t ev_back[2] = {nullptr, nullptr};
+  cudaEvent_t ev_user = nullptr;         // caller's input writes on `stream` (gbt_run_resident)
+  Unit* d_units_v[2] = {nullptr, nullptr};  // unit tables whose images are the parity-0 / parity-1 buffers
+  std::vector<Unit> units_odd;           // host copy of the parity-1 table
   std::vector<StreamInfo> streams;
   std::vector<Unit> units;
   Unit* d_units = nullptr;
@@ -84,11 +97,14 @@ struct gbt_ctx {
   void* ppos_all = nullptr;
   size_t pmask_bytes = 0;
   std::vector<void*> allocs;
-  // graphs, keyed by (any detector unit, any filtering unit)
+  // graphs: back ends keyed by (any detector unit, any filtering unit,
+  // parity), front ends by parity
   bool use_graphs = false;
-  cudaGraphExec_t graph[4] = {nullptr, nullptr, nullptr, nullptr};
+  cudaGraphExec_t graph[8] = {};
+  cudaGraphExec_t front_graph[2] = {nullptr, nullptr};
   int launches_per_frame = 0;   // kernels of the last frame enqueued (memsets not counted)
-  int graph_launches[4] = {};   // kernels in each captured frame graph
+  int graph_launches[8] = {};   // kernels in each captured back-end graph
+  int front_launches = 0;       // kernels in a captured front-end graph
   long long kernels_total = 0;  // kernels launched by this context, graph nodes included
   int match_variant = 0;  // GBT_TUNE_MATCHER
   bool fixed_fpitch = true;  // every unit's s1/s2 pitch is FIXED_FPITCH
@@ -187,18 +203,65 @@ static void free_ctx(gbt_ctx* ctx) {
   for (auto e : ctx->event_pool) cudaEventDestroy(e);
   for (auto& g : ctx->graph)
     if (g) cudaGraphExecDestroy(g);
+  for (auto& g : ctx->front_graph)
+    if (g) cudaGraphExecDestroy(g);
   for (void* p : ctx->allocs) cudaFree(p);
   for (auto& s : ctx->streams)
     if (s.pinned) cudaFreeHost(s.pinned);
   if (ctx->h_ingest) cudaFreeHost(ctx->h_ingest);
+  for (cudaEvent_t e : {ctx->ev_front, ctx->ev_back[0], ctx->ev_back[1], ctx->ev_user})
+    if (e) cudaEventDestroy(e);
+  if (ctx->pre) cudaStreamDestroy(ctx->pre);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
   delete ctx;
+}
+
+// Unit `ui` with the image buffers of frame parity `par`.
+static Unit unit_view(const gbt_ctx* ctx, size_t ui, int par) {
+  Unit u = ctx->units[ui];
+  if (par) {
+    const Unit& o = ctx->units_odd[ui];
+    u.img = o.img;
+    u.s1 = o.s1;
+    u.s2 = o.s2;
+  }
+  return u;
+}
+
+// Uploads both parities' unit tables after a change of ctx->units.
+static int upload_units(gbt_ctx* ctx) {
+  const size_t n = ctx->units.size();
+  std::vector<Unit> v(n);
+  for (int par = 0; par < 2; par++) {
+    for (size_t i = 0; i < n; i++) v[i] = unit_view(ctx, i, par);
+    CK(cudaMemcpy(ctx->d_units_v[par], v.data(), n * sizeof(Unit), cudaMemcpyHostToDevice));
+  }
+  return GBT_OK;
+}
+
+static bool split_front(const gbt_ctx* ctx) { return !ctx->profiling; }
+static cudaStream_t front_stream(const gbt_ctx* ctx) { return split_front(ctx) ? ctx->pre : ctx->stream; }
+
+// Orders the next frame's input writes after the back end that last read the
+// images of its parity.
+static int prepare_front(gbt_ctx* ctx) {
+  if (split_front(ctx)) CK(cudaStreamWaitEvent(ctx->pre, ctx->ev_back[ctx->host_frame & 1], 0));
+  return GBT_OK;
+}
+
+static int sync_all(gbt_ctx* ctx) {
+  CK(cudaStreamSynchronize(ctx->pre));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return GBT_OK;
 }
 
 static int build(gbt_ctx* ctx, const gbt_config* cfgs, int nstreams) {
   CK(cudaSetDevice(ctx->device));
   CK(cudaDeviceGetAttribute(&ctx->nsm, cudaDevAttrMultiProcessorCount, ctx->device));
   CK(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
+  CK(cudaStreamCreateWithFlags(&ctx->pre, cudaStreamNonBlocking));
+  for (cudaEvent_t* e : {&ctx->ev_front, &ctx->ev_back[0], &ctx->ev_back[1], &ctx->ev_user})
+    CK(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
   // Units: streams in order, scales 0..L-1 of each stream contiguous.
   size_t occ_words = 0;
   for (int s = 0; s < nstreams; s++) {
@@ -255,6 +318,11 @@ static int build(gbt_ctx* ctx, const gbt_config* cfgs, int nstreams) {
     if (u.fpitch != FIXED_FPITCH) ctx->fixed_fpitch = false;
     if ((r = dalloc(ctx, (void**)&u.s1, (size_t)u.fpitch * (u.H + 2 * RB), true))) return r;
     if ((r = dalloc(ctx, (void**)&u.s2, (size_t)u.fpitch * (u.H + 2 * RB), true))) return r;
+    Unit o{};  // parity-1 images (zeroed like the parity-0 ones: the s1/s2 borders stay zero)
+    if ((r = dalloc(ctx, (void**)&o.img, (size_t)u.ipitch * u.H, true))) return r;
+    if ((r = dalloc(ctx, (void**)&o.s1, (size_t)u.fpitch * (u.H + 2 * RB), true))) return r;
+    if ((r = dalloc(ctx, (void**)&o.s2, (size_t)u.fpitch * (u.H + 2 * RB), true))) return r;
+    ctx->units_odd.push_back(o);
     if ((r = dalloc_t(ctx, &u.idx, (size_t)u.H * u.W))) return r;
     if ((r = dalloc_t(ctx, &u.st_n, nb))) return r;
     if ((r = dalloc_t(ctx, &u.st_sp, nb))) return r;
@@ -296,8 +364,10 @@ static int build(gbt_ctx* ctx, const gbt_config* cfgs, int nstreams) {
     if ((r = dalloc_t(ctx, &u.act_list, u.cap))) return r;
     if ((r = dalloc_t(ctx, &u.act_cand, (size_t)u.cap * 8, false))) return r;
   }
-  if ((r = dalloc_t(ctx, &ctx->d_units, nunits, false))) return r;
-  CK(cudaMemcpy(ctx->d_units, ctx->units.data(), nunits * sizeof(Unit), cudaMemcpyHostToDevice));
+  if ((r = dalloc_t(ctx, &ctx->d_units_v[0], nunits, false))) return r;
+  if ((r = dalloc_t(ctx, &ctx->d_units_v[1], nunits, false))) return r;
+  ctx->d_units = ctx->d_units_v[0];
+  if ((r = upload_units(ctx))) return r;
   if ((r = dalloc_t(ctx, &ctx->d_state, nunits))) return r;
   if ((r = dalloc_t(ctx, &ctx->d_frame, 1))) return r;
   if ((r = dalloc_t(ctx, &ctx->d_pre, nunits + 1))) return r;
@@ -394,6 +464,7 @@ extern "C" int gbt_create(const gbt_config* cfgs, int32_t nstreams, int32_t devi
 extern "C" int gbt_destroy(gbt_ctx* ctx) {
   if (!ctx) return GBT_E_INVALID;
   cudaSetDevice(ctx->device);
+  if (ctx->pre) cudaStreamSynchronize(ctx->pre);
   cudaStreamSynchronize(ctx->stream);
   free_ctx(ctx);
   return GBT_OK;
@@ -413,7 +484,7 @@ extern "C" int gbt_stream(gbt_ctx* ctx, void** s) {
 
 extern "C" int gbt_input_slot(gbt_ctx* ctx, int32_t stream, uint8_t** dptr, int64_t* pitch) {
   if (!ctx || stream < 0 || stream >= (int)ctx->streams.size()) return GBT_E_INVALID;
-  const Unit& u = ctx->units[ctx->streams[stream].unit0];
+  const Unit u = unit_view(ctx, ctx->streams[stream].unit0, ctx->host_frame & 1);  // the next frame's slot
   if (dptr) *dptr = u.img;
   if (pitch) *pitch = u.ipitch;
   return GBT_OK;
@@ -480,137 +551,183 @@ static void prof_collect(gbt_ctx* ctx) {
 
 #define PROF(name) ProfScope prof_scope_##__LINE__(ctx, name)
 
-// Issues the kernels of one frame on the context stream.
-static int enqueue_frame(gbt_ctx* ctx, bool any_det, bool any_filt) {
+// Front end of a frame on `st`: the pyramid (with the fused RGB ingest) and
+// the BC2S blurs, into the image buffers of parity `par`.
+static int enqueue_front(gbt_ctx* ctx, int par, cudaStream_t st, int& n) {
   const int nunits = (int)ctx->units.size();
   const int nstreams = (int)ctx->streams.size();
-  const int pgrid = std::max(1, ctx->nsm * 2);
-  cudaStream_t st = ctx->stream;
-  int n = 0;
-  CK(cudaMemsetAsync(ctx->occ_all, 0, ctx->occ_bytes, st));
-  { PROF("k_pyramid"); k_pyramid<<<ctx->pyr_tiles[0], 256, 0, st>>>(ctx->d_units, ctx->d_stream_unit0, ctx->d_pyr_prefix[0], nstreams, 0, ctx->d_ingest); }
+  const Unit* du = ctx->d_units_v[par];
+  n = 0;
+  { PROF("k_pyramid"); k_pyramid<<<ctx->pyr_tiles[0], 256, 0, st>>>(du, ctx->d_stream_unit0, ctx->d_pyr_prefix[0], nstreams, 0, ctx->d_ingest); }
   n++;
   if (ctx->pyr_tiles[1] > 0) {
     PROF("k_pyramid5");
-    k_pyramid<<<ctx->pyr_tiles[1], 256, 0, st>>>(ctx->d_units, ctx->d_stream_unit0, ctx->d_pyr_prefix[1], nstreams, 5, ctx->d_ingest);
+    k_pyramid<<<ctx->pyr_tiles[1], 256, 0, st>>>(du, ctx->d_stream_unit0, ctx->d_pyr_prefix[1], nstreams, 5, ctx->d_ingest);
     n++;
   }
   {
     PROF("k_blur");
     const int nb = (ctx->blur_tiles + BL_WARPS - 1) / BL_WARPS;
     if (ctx->blur_rows == 16)
-      k_blur<16><<<nb, 32 * BL_WARPS, 0, st>>>(ctx->d_units, ctx->d_blur_prefix, nunits);
+      k_blur<16><<<nb, 32 * BL_WARPS, 0, st>>>(du, ctx->d_blur_prefix, nunits);
     else if (ctx->blur_rows == 32)
-      k_blur<32><<<nb, 32 * BL_WARPS, 0, st>>>(ctx->d_units, ctx->d_blur_prefix, nunits);
+      k_blur<32><<<nb, 32 * BL_WARPS, 0, st>>>(du, ctx->d_blur_prefix, nunits);
     else
-      k_blur<64><<<nb, 32 * BL_WARPS, 0, st>>>(ctx->d_units, ctx->d_blur_prefix, nunits);
-  }
-  if (ctx->match_variant == 0 && ctx->fixed_fpitch) {
-    CK(cudaMemsetAsync(ctx->d_mt_cnt, 0, (size_t)ctx->mt_tiles * sizeof(int), st));
-    { PROF("k_mt_count"); k_mt_bin<0><<<pgrid, CHUNK, 0, st>>>(ctx->d_units, ctx->d_state, ctx->d_pre, nunits, ctx->d_mt_cnt, ctx->d_mt_key, nullptr, nullptr); }
-    { PROF("k_mt_scan"); k_mt_scan<<<1, 1024, 0, st>>>(ctx->d_mt_cnt, ctx->mt_tiles, ctx->d_mt_off); }
-    { PROF("k_mt_scatter"); k_mt_bin<1><<<pgrid, CHUNK, 0, st>>>(ctx->d_units, ctx->d_state, ctx->d_pre, nunits, nullptr, ctx->d_mt_key, ctx->d_mt_off, ctx->d_mt_list); }
-    { PROF("k_match_tiled"); k_match_tiled<<<ctx->mt_tiles, MT_THREADS, 0, st>>>(ctx->d_units, ctx->d_state, ctx->d_frame, ctx->d_mt_prefix, nunits, ctx->d_mt_off, ctx->d_mt_list); }
-    n += 3;
-  } else if (ctx->match_variant == 1) {
-    PROF("k_match_warp");
-    k_match_warp<<<ctx->nsm * 4, 32 * MW_WARPS, 0, st>>>(ctx->d_units, ctx->d_state, ctx->d_frame, ctx->d_pre, nunits);
-  } else {
-    PROF("k_match");
-    const dim3 g(ctx->nsm * 8);
-    if (ctx->match_variant == 3 && ctx->fixed_fpitch)
-      k_match<FeatFP<FIXED_FPITCH>>
-          <<<g, MATCH_BLOCK, 0, st>>>(ctx->d_units, ctx->d_state, ctx->d_frame, ctx->d_pre, nunits);
-    else
-      k_match<Feat><<<g, MATCH_BLOCK, 0, st>>>(ctx->d_units, ctx->d_state, ctx->d_frame, ctx->d_pre, nunits);
-  }
-  { PROF("k_stats"); k_stats<<<(ctx->nbins + 255) / 256, 256, 0, st>>>(ctx->d_units, ctx->d_state, ctx->d_bin_prefix, nunits); }
-  { PROF("k_fuse"); k_fuse<<<(ctx->nbins + 255) / 256, 256, 0, st>>>(ctx->d_units, ctx->d_bin_prefix, nunits); }
-  n += 4;
-  if (any_det) {
-    CK(cudaMemsetAsync(ctx->ppos_all, 0, ctx->pmask_bytes, st));
-    { PROF("k_pmask"); k_pmask<<<pgrid, CHUNK, 0, st>>>(ctx->d_units, ctx->d_state, ctx->d_frame, ctx->d_pre, nunits); }
-    { PROF("k_pmask_dilate"); k_pmask_dilate<<<(ctx->nbins + 255) / 256, 256, 0, st>>>(ctx->d_units, ctx->d_frame, ctx->d_bin_prefix, nunits); }
-    { PROF("k_detect"); k_detect<<<ctx->det_blocks, 256, 0, st>>>(ctx->d_units, ctx->d_frame, ctx->d_det_prefix, nunits); }
-    if (ctx->any_alt_detector) {
-      PROF("k_detect_alt");
-      k_detect_alt<<<(ctx->nbins + 255) / 256, 256, 0, st>>>(ctx->d_units, ctx->d_frame, ctx->d_bin_prefix, nunits);
-      n++;
-    }
-    { PROF("k_det_count"); k_det_count<<<pgrid, CHUNK, 0, st>>>(ctx->d_units, ctx->d_state, ctx->d_frame, ctx->d_pre, ctx->d_btable, nunits); }
-    { PROF("k_unit_scan"); k_unit_scan<<<nunits, 1024, 0, st>>>(ctx->d_units, ctx->d_state, ctx->d_frame, 0); }
-    { PROF("k_det_scatter"); k_det_scatter<<<pgrid, CHUNK, 0, st>>>(ctx->d_units, ctx->d_state, ctx->d_frame, ctx->d_pre, ctx->d_btable,
-                                           nunits); }
-    { PROF("k_commit"); k_commit<<<1, 1024, 0, st>>>(ctx->d_units, ctx->d_state, ctx->d_frame, ctx->d_post, nunits); }
-    n += 7;
-  }
-  int* table = any_det ? ctx->d_post : ctx->d_pre;
-  if (any_filt) {
-    { PROF("k_filter"); k_filter<<<pgrid, CHUNK, 0, st>>>(ctx->d_units, ctx->d_state, ctx->d_frame, table, nunits); }
-    { PROF("k_merge_count"); k_merge_count<<<pgrid, CHUNK, 0, st>>>(ctx->d_units, ctx->d_state, ctx->d_frame, table, nunits); }
-    { PROF("k_unit_scan"); k_unit_scan<<<nunits, 1024, 0, st>>>(ctx->d_units, ctx->d_state, ctx->d_frame, 1); }
-    { PROF("k_merge_scatter"); k_merge_scatter<<<pgrid, CHUNK, 0, st>>>(ctx->d_units, ctx->d_state, ctx->d_frame, table, nunits); }
-    { PROF("k_merge_resolve"); k_merge_resolve<<<nunits, 256, 0, st>>>(ctx->d_units, ctx->d_state, ctx->d_frame); }
-    n += 5;
-  }
-  if (ctx->traj_T) {
-    PROF("k_traj");
-    k_traj<<<ctx->nsm * 4, CHUNK, 0, st>>>(ctx->d_units, ctx->d_state, ctx->d_cap_table, nunits, ctx->traj_T);
+      k_blur<64><<<nb, 32 * BL_WARPS, 0, st>>>(du, ctx->d_blur_prefix, nunits);
     n++;
   }
-  { PROF("k_tick"); k_tick<<<1, 1024, 0, st>>>(ctx->d_units, ctx->d_state, ctx->d_frame, ctx->d_pre, nunits); }
-  n++;
-  ctx->launches_per_frame = n;
   CK(cudaGetLastError());
   return GBT_OK;
 }
 
+// Back end of a frame on the context stream: matching, flow statistics,
+// detection, filtering, merging, trajectories and the frame tick, over the
+// images of parity `par`.
+static int enqueue_back(gbt_ctx* ctx, bool any_det, bool any_filt, int par, int& n) {
+  const int nunits = (int)ctx->units.size();
+  const int pgrid = std::max(1, ctx->nsm * 2);
+  const Unit* du = ctx->d_units_v[par];
+  cudaStream_t st = ctx->stream;
+  n = 0;
+  CK(cudaMemsetAsync(ctx->occ_all, 0, ctx->occ_bytes, st));
+  if (ctx->match_variant == 0 && ctx->fixed_fpitch) {
+    CK(cudaMemsetAsync(ctx->d_mt_cnt, 0, (size_t)ctx->mt_tiles * sizeof(int), st));
+    { PROF("k_mt_count"); k_mt_bin<0><<<pgrid, CHUNK, 0, st>>>(du, ctx->d_state, ctx->d_pre, nunits, ctx->d_mt_cnt, ctx->d_mt_key, nullptr, nullptr); }
+    { PROF("k_mt_scan"); k_mt_scan<<<1, 1024, 0, st>>>(ctx->d_mt_cnt, ctx->mt_tiles, ctx->d_mt_off); }
+    { PROF("k_mt_scatter"); k_mt_bin<1><<<pgrid, CHUNK, 0, st>>>(du, ctx->d_state, ctx->d_pre, nunits, nullptr, ctx->d_mt_key, ctx->d_mt_off, ctx->d_mt_list); }
+    { PROF("k_match_tiled"); k_match_tiled<<<ctx->mt_tiles, MT_THREADS, 0, st>>>(du, ctx->d_state, ctx->d_frame, ctx->d_mt_prefix, nunits, ctx->d_mt_off, ctx->d_mt_list); }
+    n += 4;
+  } else if (ctx->match_variant == 1) {
+    PROF("k_match_warp");
+    k_match_warp<<<ctx->nsm * 4, 32 * MW_WARPS, 0, st>>>(du, ctx->d_state, ctx->d_frame, ctx->d_pre, nunits);
+    n++;
+  } else {
+    PROF("k_match");
+    const dim3 g(ctx->nsm * 8);
+    if (ctx->match_variant == 3 && ctx->fixed_fpitch)
+      k_match<FeatFP<FIXED_FPITCH>><<<g, MATCH_BLOCK, 0, st>>>(du, ctx->d_state, ctx->d_frame, ctx->d_pre, nunits);
+    else
+      k_match<Feat><<<g, MATCH_BLOCK, 0, st>>>(du, ctx->d_state, ctx->d_frame, ctx->d_pre, nunits);
+    n++;
+  }
+  { PROF("k_stats"); k_stats<<<(ctx->nbins + 255) / 256, 256, 0, st>>>(du, ctx->d_state, ctx->d_bin_prefix, nunits); }
+  n++;
+  if (any_det) {
+    CK(cudaMemsetAsync(ctx->ppos_all, 0, ctx->pmask_bytes, st));
+    { PROF("k_pmask"); k_pmask<<<pgrid, CHUNK, 0, st>>>(du, ctx->d_state, ctx->d_frame, ctx->d_pre, nunits); }
+    { PROF("k_pmask_dilate"); k_pmask_dilate<<<(ctx->nbins + 255) / 256, 256, 0, st>>>(du, ctx->d_frame, ctx->d_bin_prefix, nunits); }
+    { PROF("k_detect"); k_detect<<<ctx->det_blocks, 256, 0, st>>>(du, ctx->d_frame, ctx->d_det_prefix, nunits); }
+    if (ctx->any_alt_detector) {
+      PROF("k_detect_alt");
+      k_detect_alt<<<(ctx->nbins + 255) / 256, 256, 0, st>>>(du, ctx->d_frame, ctx->d_bin_prefix, nunits);
+      n++;
+    }
+    { PROF("k_det_count"); k_det_count<<<pgrid, CHUNK, 0, st>>>(du, ctx->d_state, ctx->d_frame, ctx->d_pre, ctx->d_btable, nunits); }
+    { PROF("k_unit_scan"); k_unit_scan<<<nunits, 1024, 0, st>>>(du, ctx->d_state, ctx->d_frame, 0); }
+    { PROF("k_det_scatter"); k_det_scatter<<<pgrid, CHUNK, 0, st>>>(du, ctx->d_state, ctx->d_frame, ctx->d_pre, ctx->d_btable, nunits); }
+    { PROF("k_commit"); k_commit<<<1, 1024, 0, st>>>(du, ctx->d_state, ctx->d_frame, ctx->d_post, nunits); }
+    n += 7;
+  }
+  int* table = any_det ? ctx->d_post : ctx->d_pre;
+  if (any_filt) {
+    { PROF("k_filter_merge"); k_filter_merge<<<pgrid, CHUNK, 0, st>>>(du, ctx->d_state, ctx->d_frame, table, nunits); }
+    { PROF("k_unit_scan"); k_unit_scan<<<nunits, 1024, 0, st>>>(du, ctx->d_state, ctx->d_frame, 1); }
+    { PROF("k_merge_scatter"); k_merge_scatter<<<pgrid, CHUNK, 0, st>>>(du, ctx->d_state, ctx->d_frame, table, nunits); }
+    { PROF("k_merge_resolve"); k_merge_resolve<<<nunits, 256, 0, st>>>(du, ctx->d_state, ctx->d_frame); }
+    n += 4;
+  }
+  if (ctx->traj_T) {
+    PROF("k_traj");
+    k_traj<<<ctx->nsm * 4, CHUNK, 0, st>>>(du, ctx->d_state, ctx->d_cap_table, nunits, ctx->traj_T);
+    n++;
+  }
+  { PROF("k_tick"); k_tick<<<1, 1024, 0, st>>>(du, ctx->d_state, ctx->d_frame, ctx->d_pre, nunits); }
+  n++;
+  CK(cudaGetLastError());
+  return GBT_OK;
+}
+
+// Captures (once) and launches a graph of what `issue` enqueues on `st`.
+template <class F>
+static int launch_graph(gbt_ctx* ctx, cudaGraphExec_t& exec, int& launches, cudaStream_t st, F issue) {
+  if (!exec) {
+    cudaGraph_t g;
+    int n = 0;
+    CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    int r = issue(n);
+    cudaError_t e = cudaStreamEndCapture(st, &g);
+    if (r) return r;
+    if (e != cudaSuccess) return set_err(ctx, GBT_E_CUDA, "graph capture failed: %s", cudaGetErrorString(e));
+    e = cudaGraphInstantiate(&exec, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return set_err(ctx, GBT_E_CUDA, "graph instantiate failed: %s", cudaGetErrorString(e));
+    launches = n;
+  }
+  CK(cudaGraphLaunch(exec, st));
+  return GBT_OK;
+}
+
+// Queues one frame whose input is in place (ordered on the front-end stream).
 static int run_frame(gbt_ctx* ctx) {
   bool any_det, any_filt;
   frame_kind(ctx, any_det, any_filt);
-  int key = (any_det ? 1 : 0) | (any_filt ? 2 : 0);
+  const int par = ctx->host_frame & 1;
+  const bool split = split_front(ctx);
+  cudaStream_t fs = split ? ctx->pre : ctx->stream;
+  int nf = 0, nb = 0, r;
   if (ctx->use_graphs) {
-    if (!ctx->graph[key]) {
-      cudaGraph_t g;
-      CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
-      int r = enqueue_frame(ctx, any_det, any_filt);
-      cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
-      if (r) return r;
-      if (e != cudaSuccess) return set_err(ctx, GBT_E_CUDA, "graph capture failed: %s", cudaGetErrorString(e));
-      e = cudaGraphInstantiate(&ctx->graph[key], g, 0);
-      cudaGraphDestroy(g);
-      if (e != cudaSuccess) return set_err(ctx, GBT_E_CUDA, "graph instantiate failed: %s", cudaGetErrorString(e));
-      ctx->graph_launches[key] = ctx->launches_per_frame;
-    }
-    CK(cudaGraphLaunch(ctx->graph[key], ctx->stream));
-    ctx->launches_per_frame = ctx->graph_launches[key];
+    r = launch_graph(ctx, ctx->front_graph[par], ctx->front_launches, fs,
+                     [&](int& n) { return enqueue_front(ctx, par, fs, n); });
+    nf = ctx->front_launches;
   } else {
-    int r = enqueue_frame(ctx, any_det, any_filt);
-    if (r) return r;
-    prof_collect(ctx);
+    r = enqueue_front(ctx, par, fs, nf);
   }
+  if (r) return r;
+  if (split) {
+    CK(cudaEventRecord(ctx->ev_front, fs));
+    CK(cudaStreamWaitEvent(ctx->stream, ctx->ev_front, 0));
+  }
+  const int key = (any_det ? 1 : 0) | (any_filt ? 2 : 0) | (par << 2);
+  if (ctx->use_graphs) {
+    r = launch_graph(ctx, ctx->graph[key], ctx->graph_launches[key], ctx->stream,
+                     [&](int& n) { return enqueue_back(ctx, any_det, any_filt, par, n); });
+    nb = ctx->graph_launches[key];
+  } else {
+    r = enqueue_back(ctx, any_det, any_filt, par, nb);
+  }
+  if (r) return r;
+  CK(cudaEventRecord(ctx->ev_back[par], ctx->stream));
+  if (!ctx->use_graphs) prof_collect(ctx);
+  ctx->launches_per_frame = nf + nb;
   ctx->kernels_total += ctx->launches_per_frame;
   ctx->host_frame++;
   return GBT_OK;
 }
 
+// Drops every captured graph (the next frames capture them again).
+static void drop_graphs(gbt_ctx* ctx) {
+  for (auto& g : ctx->graph)
+    if (g) {
+      cudaGraphExecDestroy(g);
+      g = nullptr;
+    }
+  for (auto& g : ctx->front_graph)
+    if (g) {
+      cudaGraphExecDestroy(g);
+      g = nullptr;
+    }
+}
+
 extern "C" int gbt_set_tuning(gbt_ctx* ctx, int32_t knob, int32_t value) {
   if (!ctx) return GBT_E_INVALID;
-  auto drop_graphs = [&]() {
-    for (auto& g : ctx->graph)
-      if (g) {
-        cudaGraphExecDestroy(g);
-        g = nullptr;
-      }
-  };
   if (knob == GBT_TUNE_MATCHER && value >= 0 && value <= 3) {
-    if (ctx->match_variant != value) drop_graphs();
+    if (ctx->match_variant != value) drop_graphs(ctx);
     ctx->match_variant = value;
     return GBT_OK;
   }
   if (knob == GBT_TUNE_BLUR_ROWS && (value == 16 || value == 32 || value == 64)) {
     const int v = value == 16 ? 0 : (value == 32 ? 1 : 2);
-    if (ctx->blur_rows != value) drop_graphs();
+    if (ctx->blur_rows != value) drop_graphs(ctx);
     ctx->blur_rows = value;
     ctx->d_blur_prefix = ctx->d_blur_prefix_v[v];
     ctx->blur_tiles = ctx->blur_tiles_v[v];
@@ -639,7 +756,10 @@ static int set_ingest(gbt_ctx* ctx, size_t s, int mode) {
   Ingest want{mode ? si.d_rgb : nullptr, mode ? si.rgb_pitch : 0, mode, 0};
   Ingest& have = ctx->h_ingest[s];
   if (have.rgb != want.rgb || have.pitch != want.pitch || have.mode != want.mode) {
-    if (!ctx->ingest_dirty) CK(cudaStreamSynchronize(ctx->stream));  // h_ingest may feed a copy in flight
+    if (!ctx->ingest_dirty) {  // h_ingest may feed a copy in flight, d_ingest a pyramid
+      int r = sync_all(ctx);
+      if (r) return r;
+    }
     have = want;
     ctx->ingest_dirty = true;
   }
@@ -649,7 +769,7 @@ static int set_ingest(gbt_ctx* ctx, size_t s, int mode) {
 static int flush_ingest(gbt_ctx* ctx) {
   if (ctx->ingest_dirty) {
     CK(cudaMemcpyAsync(ctx->d_ingest, ctx->h_ingest, sizeof(Ingest) * ctx->streams.size(), cudaMemcpyHostToDevice,
-                       ctx->stream));
+                       front_stream(ctx)));
     ctx->ingest_dirty = false;
   }
   return GBT_OK;
@@ -659,20 +779,17 @@ extern "C" int gbt_trajectories_enable(gbt_ctx* ctx, int32_t history) {
   if (!ctx || history < 1 || history > 255) return GBT_E_INVALID;
   if (ctx->traj_T) return ctx->traj_T == history ? GBT_OK : GBT_E_INVALID;
   CK(cudaSetDevice(ctx->device));
-  CK(cudaStreamSynchronize(ctx->stream));
-  int r;
+  int r = sync_all(ctx);
+  if (r) return r;
   for (auto& u : ctx->units)
     for (int b = 0; b < 2; b++) {
       if ((r = dalloc_t(ctx, &u.tpos[b], (size_t)history * u.cap))) return r;
       if ((r = dalloc_t(ctx, &u.thead[b], u.cap))) return r;
       if ((r = dalloc_t(ctx, &u.tlen[b], u.cap))) return r;
     }
-  CK(cudaMemcpy(ctx->d_units, ctx->units.data(), ctx->units.size() * sizeof(Unit), cudaMemcpyHostToDevice));
-  for (auto& g : ctx->graph)
-    if (g) {
-      cudaGraphExecDestroy(g);
-      g = nullptr;
-    }
+  int r2 = upload_units(ctx);
+  if (r2) return r2;
+  drop_graphs(ctx);
   ctx->traj_T = history;
   return GBT_OK;
 }
@@ -686,6 +803,13 @@ extern "C" int gbt_use_graphs(gbt_ctx* ctx, int32_t enable) {
 extern "C" int gbt_run_resident(gbt_ctx* ctx) {
   if (!ctx) return GBT_E_INVALID;
   CK(cudaSetDevice(ctx->device));
+  // The caller wrote the input slots on the context stream (or synchronously).
+  int r0 = prepare_front(ctx);
+  if (r0) return r0;
+  if (split_front(ctx)) {
+    CK(cudaEventRecord(ctx->ev_user, ctx->stream));
+    CK(cudaStreamWaitEvent(ctx->pre, ctx->ev_user, 0));
+  }
   for (size_t s = 0; s < ctx->streams.size(); s++) {
     int r = set_ingest(ctx, s, 0);
     if (r) return r;
@@ -698,16 +822,19 @@ extern "C" int gbt_run_resident(gbt_ctx* ctx) {
 extern "C" int gbt_run(gbt_ctx* ctx, const uint8_t* const* frames, const int64_t* pitches, int32_t location) {
   if (!ctx || !frames) return GBT_E_INVALID;
   CK(cudaSetDevice(ctx->device));
+  int r0 = prepare_front(ctx);
+  if (r0) return r0;
+  cudaStream_t in = front_stream(ctx);  // input copies go with the frame's front end
   for (size_t s = 0; s < ctx->streams.size(); s++) {
     StreamInfo& si = ctx->streams[s];
-    const Unit& u = ctx->units[si.unit0];
+    const Unit u = unit_view(ctx, si.unit0, ctx->host_frame & 1);
     const uint8_t* src = frames[s];
     int mode = 0;
     if (!src) return set_err(ctx, GBT_E_INVALID, "frame %zu is NULL", s);
     if (location == GBT_FRAMES_DEVICE) {
       int64_t p = pitches ? pitches[s] : u.W;
       if (p < u.W) return set_err(ctx, GBT_E_INVALID, "pitch %lld < cols %d", (long long)p, u.W);
-      CK(cudaMemcpy2DAsync(u.img, u.ipitch, src, p, u.W, u.H, cudaMemcpyDeviceToDevice, ctx->stream));
+      CK(cudaMemcpy2DAsync(u.img, u.ipitch, src, p, u.W, u.H, cudaMemcpyDeviceToDevice, in));
     } else if (location == GBT_FRAMES_HOST) {
       int64_t p = pitches ? pitches[s] : u.W;
       if (p < u.W) return set_err(ctx, GBT_E_INVALID, "pitch %lld < cols %d", (long long)p, u.W);
@@ -715,12 +842,12 @@ extern "C" int gbt_run(gbt_ctx* ctx, const uint8_t* const* frames, const int64_t
       bool pinned = cudaPointerGetAttributes(&at, src) == cudaSuccess && at.type == cudaMemoryTypeHost;
       cudaGetLastError();
       if (pinned) {
-        CK(cudaMemcpy2DAsync(u.img, u.ipitch, src, p, u.W, u.H, cudaMemcpyHostToDevice, ctx->stream));
+        CK(cudaMemcpy2DAsync(u.img, u.ipitch, src, p, u.W, u.H, cudaMemcpyHostToDevice, in));
       } else {
         // The staging buffer may still feed the previous frame's copy.
-        CK(cudaStreamSynchronize(ctx->stream));
+        CK(cudaStreamSynchronize(in));
         for (int r = 0; r < u.H; r++) memcpy(si.pinned + (size_t)r * u.W, src + (size_t)r * p, u.W);
-        CK(cudaMemcpy2DAsync(u.img, u.ipitch, si.pinned, u.W, u.W, u.H, cudaMemcpyHostToDevice, ctx->stream));
+        CK(cudaMemcpy2DAsync(u.img, u.ipitch, si.pinned, u.W, u.W, u.H, cudaMemcpyHostToDevice, in));
       }
     } else if (location == GBT_FRAMES_HOST_RGB || location == GBT_FRAMES_DEVICE_RGB) {
       const int64_t row = (int64_t)u.W * 3;
@@ -732,19 +859,19 @@ extern "C" int gbt_run(gbt_ctx* ctx, const uint8_t* const* frames, const int64_t
         if (r) return r;
       }
       if (location == GBT_FRAMES_DEVICE_RGB) {
-        CK(cudaMemcpy2DAsync(si.d_rgb, si.rgb_pitch, src, p, row, u.H, cudaMemcpyDeviceToDevice, ctx->stream));
+        CK(cudaMemcpy2DAsync(si.d_rgb, si.rgb_pitch, src, p, row, u.H, cudaMemcpyDeviceToDevice, in));
       } else {
         cudaPointerAttributes at;
         bool pinned = cudaPointerGetAttributes(&at, src) == cudaSuccess && at.type == cudaMemoryTypeHost;
         cudaGetLastError();
         if (!pinned) {
           // The staging buffer may still feed the previous frame's copy.
-          CK(cudaStreamSynchronize(ctx->stream));
+          CK(cudaStreamSynchronize(in));
           for (int rr = 0; rr < u.H; rr++) memcpy(si.pinned + (size_t)rr * row, src + (size_t)rr * p, row);
           src = si.pinned;
           p = row;
         }
-        CK(cudaMemcpy2DAsync(si.d_rgb, si.rgb_pitch, src, p, row, u.H, cudaMemcpyHostToDevice, ctx->stream));
+        CK(cudaMemcpy2DAsync(si.d_rgb, si.rgb_pitch, src, p, row, u.H, cudaMemcpyHostToDevice, in));
       }
       mode = ctx->rgb_mode == GBT_RGB_BT601 ? 2 : 1;
     } else {
@@ -767,7 +894,8 @@ extern "C" int gbt_set_rgb_to_gray(gbt_ctx* ctx, int32_t mode) {
 extern "C" int gbt_sync(gbt_ctx* ctx) {
   if (!ctx) return GBT_E_INVALID;
   CK(cudaSetDevice(ctx->device));
-  CK(cudaStreamSynchronize(ctx->stream));
+  int r = sync_all(ctx);
+  if (r) return r;
   Frame f;
   CK(cudaMemcpy(&f, ctx->d_frame, sizeof f, cudaMemcpyDeviceToHost));
   if (f.err & ERR_CAPACITY) return set_err(ctx, GBT_E_CAPACITY, "particle capacity exceeded");
@@ -1128,7 +1256,8 @@ extern "C" int gbt_get_stage(gbt_ctx* ctx, int32_t stream, int32_t scale, int32_
   if (ui < 0 || !out || border < 0 || border > 6) return GBT_E_INVALID;
   CK(cudaSetDevice(ctx->device));
   CK(cudaStreamSynchronize(ctx->stream));
-  const Unit& u = ctx->units[ui];
+  const int lp = (ctx->host_frame + 1) & 1;  // parity of the last frame run
+  const Unit u = unit_view(ctx, ui, lp);
   const int H = u.H, W = u.W, b = border;
   if (stage == GBT_STAGE_INPUT) {
     std::vector<uint8_t> dom((size_t)H * W);
@@ -1158,7 +1287,7 @@ extern "C" int gbt_get_stage(gbt_ctx* ctx, int32_t stream, int32_t scale, int32_
   if (stage != GBT_STAGE_CONTRAST && stage != GBT_STAGE_SALIENCY && stage != GBT_STAGE_MASK &&
       stage != GBT_STAGE_SPARSE)
     return GBT_E_INVALID;
-  k_dump<<<256, 256, 0, ctx->stream>>>(ctx->d_units, ctx->d_state, ctx->d_frame, ui, stage, ctx->dump_buf);
+  k_dump<<<256, 256, 0, ctx->stream>>>(ctx->d_units_v[lp], ctx->d_state, ctx->d_frame, ui, stage, ctx->dump_buf);
   CK(cudaGetLastError());
   CK(cudaStreamSynchronize(ctx->stream));
   size_t es = (stage == GBT_STAGE_CONTRAST || stage == GBT_STAGE_SPARSE) ? 4 : 1;
@@ -1168,6 +1297,9 @@ extern "C" int gbt_get_stage(gbt_ctx* ctx, int32_t stream, int32_t scale, int32_
 
 extern "C" int gbt_profile_enable(gbt_ctx* ctx, int32_t enable) {
   if (!ctx) return GBT_E_INVALID;
+  CK(cudaSetDevice(ctx->device));
+  int r = sync_all(ctx);  // the front end changes streams
+  if (r) return r;
   ctx->profiling = enable != 0;
   if (ctx->profiling) ctx->prof.clear();
   return GBT_OK;

@@ -270,6 +270,12 @@ struct Feat {
     }
     return d;
   }
+  __device__ __forceinline__ int s1_part(const uint4& f, int r, int c, int pitch) const {
+    const uint8_t* a = s1 + (ptrdiff_t)r * pitch + c;
+    uint32_t x = a[o1[0]] | (a[o1[1]] << 8) | (a[o1[2]] << 16) | ((uint32_t)a[o1[3]] << 24);
+    uint32_t y = a[o1[4]] | (a[o1[5]] << 8) | (a[o1[6]] << 16) | ((uint32_t)a[o1[7]] << 24);
+    return (int)(__vsadu4(x, f.x) + __vsadu4(y, f.y));
+  }
 };
 
 // The even entries of circle_r3_h (the BC2S feature ring) as constant
@@ -311,6 +317,10 @@ struct FeatFP {
     }
     return d;
   }
+  __device__ __forceinline__ int s1_part(const uint4& f, int r, int c, int) const {
+    const uint8_t* a = s1 + (r * P + c);
+    return (int)(__vsadu4(word<1, 0>(a), f.x) + __vsadu4(word<1, 4>(a), f.y));
+  }
 };
 
 // gradient_descent_match (tracking2/gradient_descent_matcher.hpp:9-76): greedy
@@ -347,29 +357,32 @@ __device__ __forceinline__ int c8_dr(int i) { return (int)((c8_pack(false) >> (2
 __device__ __forceinline__ int c8_dc(int i) { return (int)((c8_pack(true) >> (2 * i)) & 3u) - 1; }
 
 // gradient_descent_match (tracking2/gradient_descent_matcher.hpp:9-76): greedy
-// 8-neighbour descent over c8_h with the c8_it_h partial sweeps; the first
-// distance is always the s1+s2 one.  (pr, pc) is inside the domain.
-template <class FeatT>
-__device__ __forceinline__ void gd_match(const Unit& u, const FeatT& F, const uint4& f, int pr, int pc, bool with_s1,
+// 8-neighbour descent over c8_h with the c8_it_h partial sweeps from (pr, pc),
+// inside the domain.  `best` enters as the distance at (pr, pc) -- always the
+// s1+s2 one -- and leaves as the distance at the match.  Every candidate's
+// distance is computed whole: stopping at a partial sum that already reaches
+// the best would give the same descent, but the branches serialise the 8 or 16
+// independent gathers, which costs more than the loads saved.
+template <bool WITH_S1, class FeatT>
+__device__ __forceinline__ void gd_match(const Unit& u, const FeatT& F, const uint4& f, int pr, int pc, int& best,
                                          int& dr, int& dc) {
   int predr = pr, predc = pc, mr = pr, mc = pc;
-  int best = F.dist(f, pr, pc, u.fpitch, true);
   int mi = 8;
   for (int search = 0; search < 10; search++) {
     const int i0 = sweep_first(mi), n = sweep_len(mi);
-      for (int j = 0; j < n; j++) {
-        const int i = (i0 + j) & 7;
-        const int nr = predr + c8_dr(i), nc = predc + c8_dc(i);
-        if (in_dom(u, nr, nc)) {
-          const int d = F.dist(f, nr, nc, u.fpitch, with_s1);
-          if (d < best) {
-            mr = nr;
-            mc = nc;
-            mi = i;
-            best = d;
-          }
+    for (int j = 0; j < n; j++) {
+      const int i = (i0 + j) & 7;
+      const int nr = predr + c8_dr(i), nc = predc + c8_dc(i);
+      if (in_dom(u, nr, nc)) {
+        const int d = F.dist(f, nr, nc, u.fpitch, WITH_S1);
+        if (d < best) {
+          mr = nr;
+          mc = nc;
+          mi = i;
+          best = d;
         }
       }
+    }
     if ((predr == mr && predc == mc) || !in_dom(u, mr, mc)) break;
     predr = mr;
     predc = mc;
@@ -423,8 +436,16 @@ __device__ __forceinline__ void match_one(const Unit& u, const FeatT& F, int f, 
                                           short2 pos, int pr, int pc) {
   const uint4 feat = u.feat[b][i];
   int d1r, d1c, d2r, d2c;
-  gd_match(u, F, feat, pr, pc, false, d1r, d1c);
-  gd_match(u, F, feat, pr + d1r, pc + d1c, true, d2r, d2c);
+  // Step 1 compares s2-only candidates against the s1+s2 distance at the
+  // prediction.  Step 2 starts from step 1's match with its s1+s2 distance:
+  // the prediction's own when the match is the prediction (step 1 may also
+  // come back to it, ending with its s2 distance), else the s2 distance step 1
+  // ended with plus the s1 part there.
+  const int init = F.dist(feat, pr, pc, u.fpitch, true);
+  int best = init;
+  gd_match<false>(u, F, feat, pr, pc, best, d1r, d1c);
+  best = (d1r != 0 || d1c != 0) ? best + F.s1_part(feat, pr + d1r, pc + d1c, u.fpitch) : init;
+  gd_match<true>(u, F, feat, pr + d1r, pc + d1c, best, d2r, d2c);
   match_finish(u, F, f, b, i, age, pos, pr, pc, feat, d1r + d2r, d1c + d2c);
 }
 
@@ -794,27 +815,27 @@ __global__ void __launch_bounds__(32 * MW_WARPS) k_match_warp(const Unit* __rest
 // (:576-639).  The fused flow of a bin follows its chain of parent bins up to
 // the first scale with more than one particle (the root divides the speed by
 // the count), doubling per scale, so all scales are computed in one launch.
-__device__ __forceinline__ void bin_stats(const Unit& u, const UState& s, int br, int bc, int& n, int& sr, int& sc) {
-  unsigned long long w = u.occ[(size_t)br * u.BW + bc];
-  n = 0;
-  sr = 0;
-  sc = 0;
-  bool have_last = false;
-  while (w) {
-    int bit = 63 - __clzll((long long)w);
-    w &= ~(1ull << bit);
-    int r = br * 8 + (bit >> 3), c = bc * 8 + (bit & 7);
-    unsigned j = (unsigned)(u.idx[(size_t)r * u.W + c] & 0xffffffffu);
-    if (u.age[s.cur][j] >= 1) {
-      n++;
-      if (!have_last) {
-        short2 v = u.spd[s.cur][j];
-        sr = v.x;
-        sc = v.y;
-        have_last = true;
-      }
-    }
+//
+// The statistics run right after the matcher, when the occupancy bits are
+// exactly the pixels the matcher wrote this frame (births come later in the
+// frame) and the index entry of each is a particle it just moved, whose age
+// is at least 2.  So a bin's count is the population of its occupancy word and
+// its last particle is the one at the word's highest bit: one index and one
+// speed load per bin, which lets every thread read its parent bins directly.
+struct BinStat {
+  int n;
+  int2 sp;
+};
+__device__ __forceinline__ BinStat bin_stat(const Unit& u, int b, size_t bin, int br, int bc) {
+  const unsigned long long w = u.occ[bin];
+  BinStat o{__popcll(w), make_int2(0, 0)};
+  if (w) {
+    const int bit = 63 - __clzll((long long)w);
+    const unsigned j = (unsigned)(u.idx[(size_t)(br * 8 + (bit >> 3)) * u.W + bc * 8 + (bit & 7)] & 0xffffffffu);
+    const short2 v = u.spd[b][j];
+    o.sp = make_int2(v.x, v.y);
   }
+  return o;
 }
 
 __global__ void __launch_bounds__(256) k_stats(const Unit* __restrict__ units, UState* __restrict__ st,
@@ -827,52 +848,36 @@ __global__ void __launch_bounds__(256) k_stats(const Unit* __restrict__ units, U
   const int ui = find_unit(bin_prefix, nunits, t);
   const Unit& u = units[ui];
   const int local = t - bin_prefix[ui];
-  int n, sr, sc;
-  bin_stats(u, st[ui], local / u.BW, local % u.BW, n, sr, sc);
-  u.st_n[local] = n;
-  u.st_sp[local] = make_int2(sr, sc);
-}
-
-// Multiscale count and fused flow of every bin from the statistics k_stats
-// stored for all scales (one launch after it, so every parent bin is ready).
-__global__ void __launch_bounds__(256) k_fuse(const Unit* __restrict__ units, const int* __restrict__ bin_prefix,
-                                              int nunits) {
-  const int total = bin_prefix[nunits];
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= total) return;
-  const int ui = find_unit(bin_prefix, nunits, t);
-  const Unit& u = units[ui];
-  const int local = t - bin_prefix[ui];
   const int br = local / u.BW, bc = local % u.BW;
-  const int n = u.st_n[local];
-  unsigned msc = (unsigned)n;
+  const BinStat own = bin_stat(u, st[ui].cur, local, br, bc);
+  u.st_n[local] = own.n;
+  u.st_sp[local] = own.sp;
+  unsigned msc = (unsigned)own.n;
   if (u.upper >= 0) {
     const Unit& up = units[u.upper];
-    msc += (unsigned)up.st_n[(size_t)(br >> 1) * up.BW + (bc >> 1)];
+    msc += (unsigned)__popcll(up.occ[(size_t)(br >> 1) * up.BW + (bc >> 1)]);
   }
   u.msc[local] = msc;
   float2 flow = make_float2(-500.f, -500.f);
-  int vi = ui, vbr = br, vbc = bc, vn = n;
-  int2 vsp = u.st_sp[local];
+  int vi = ui, vbr = br, vbc = bc;
+  BinStat v = own;
   float scale = 1.f;
   while (true) {
-    const Unit& v = units[vi];
-    if (v.upper < 0) {
-      if (vn > 1) flow = make_float2((float)(vsp.x / vn) * scale, (float)(vsp.y / vn) * scale);
+    const Unit& x = units[vi];
+    if (x.upper < 0) {
+      if (v.n > 1) flow = make_float2((float)(v.sp.x / v.n) * scale, (float)(v.sp.y / v.n) * scale);
       break;
     }
-    if (vn > 1) {
-      flow = make_float2((float)vsp.x * scale, (float)vsp.y * scale);
+    if (v.n > 1) {
+      flow = make_float2((float)v.sp.x * scale, (float)v.sp.y * scale);
       break;
     }
-    vi = v.upper;
+    vi = x.upper;
     vbr >>= 1;
     vbc >>= 1;
     scale *= 2.f;
-    const Unit& w = units[vi];
-    const size_t wl = (size_t)vbr * w.BW + vbc;
-    vn = w.st_n[wl];
-    vsp = w.st_sp[wl];
+    const Unit& y = units[vi];
+    v = bin_stat(y, st[vi].cur, (size_t)vbr * y.BW + vbc, vbr, vbc);
   }
   u.flow[local] = flow;
 }
@@ -1345,42 +1350,27 @@ __global__ void __launch_bounds__(1024) k_commit(const Unit* __restrict__ units,
 }
 
 // ---------------------------------------------------------------------------
-// filter_bad_particles_kernel (tracking_strategies.hpp:482-523).
-__global__ void __launch_bounds__(CHUNK) k_filter(const Unit* __restrict__ units, const UState* __restrict__ st,
-                                                  const Frame* __restrict__ fr, const int* __restrict__ table,
-                                                  int nunits) {
-  const int f = fr->f;
-  const int total = table[nunits];
-  for (int g = blockIdx.x; g < total; g += gridDim.x) {
-    ChunkCursor cc = chunk_of(table, nunits, g);
-    const Unit& u = units[cc.unit];
-    if (!filt_frame(u, f)) continue;
-    const UState s = st[cc.unit];
-    const int i = cc.chunk * CHUNK + threadIdx.x;
-    if (i >= s.n) continue;
-    const int b = s.cur;
-    const unsigned short age = u.age[b][i];
-    const short2 p = u.pos[b][i];
-    const int br = p.x / 8, bc = p.y / 8;
-    const size_t w = (size_t)br * u.BW + bc;
-    const unsigned m = u.msc[w];
-    if (age > 2 && m > 0) {
-      short2 v = u.spd[b][i];
-      float2 fl = u.flow[w];
-      float dx = __fsub_rn((float)v.x, fl.x), dy = __fsub_rn((float)v.y, fl.y);
-      float nrm = __fsqrt_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)));
-      if (nrm > 10.f) {
-        u.age[b][i] = 0;
-        continue;
-      }
-    }
-    bool alone = true;
-    for (int k = 0; k < 8; k++) {
-      int nr = br + c_c8[k][0], nc = bc + c_c8[k][1];
-      if (nr >= 0 && nr < u.BH && nc >= 0 && nc < u.BW && u.msc[(size_t)nr * u.BW + nc] != 0) alone = false;
-    }
-    if (alone && m == 1) u.age[b][i] = 0;
+// filter_bad_particles_kernel (tracking_strategies.hpp:482-523): whether live
+// particle i at p survives.  It is removed when older than 2 frames and more
+// than 10 px from its bin's fused flow, or when its bin's multiscale count is
+// 1 and no c8 bin has a nonzero count.
+__device__ __forceinline__ bool filter_keeps(const Unit& u, int b, int i, unsigned short age, short2 p) {
+  const int br = p.x / 8, bc = p.y / 8;
+  const size_t w = (size_t)br * u.BW + bc;
+  const unsigned m = u.msc[w];
+  if (age > 2 && m > 0) {
+    short2 v = u.spd[b][i];
+    float2 fl = u.flow[w];
+    float dx = __fsub_rn((float)v.x, fl.x), dy = __fsub_rn((float)v.y, fl.y);
+    float nrm = __fsqrt_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)));
+    if (nrm > 10.f) return false;
   }
+  if (m != 1) return true;
+  for (int k = 0; k < 8; k++) {
+    int nr = br + c_c8[k][0], nc = bc + c_c8[k][1];
+    if (nr >= 0 && nr < u.BH && nc >= 0 && nc < u.BW && u.msc[(size_t)nr * u.BW + nc] != 0) return true;
+  }
+  return false;
 }
 
 // ---------------------------------------------------------------------------
@@ -1392,6 +1382,11 @@ __global__ void __launch_bounds__(CHUNK) k_filter(const Unit* __restrict__ units
 // Step 3: one warp per unit replays the sequential order; groups of 32 actives
 // whose positions are more than 2 pixels apart cannot interact and are
 // resolved in parallel, other groups lane by lane.
+// With FILTERED false the ages of the filter's victims are still in place
+// (the filter runs in the same launch), so a neighbour also has to pass
+// filter_keeps; the filter's decision is a function of the bin statistics
+// alone, so both passes see the same candidates.
+template <bool FILTERED>
 __device__ __forceinline__ unsigned merge_dirs(const Unit& u, const UState& s, int f, int i, short2 p,
                                                unsigned short age, int* cand, int& ncand) {
   unsigned m = 0;
@@ -1410,7 +1405,8 @@ __device__ __forceinline__ unsigned merge_dirs(const Unit& u, const UState& s, i
     if ((int)aj > (int)age + 2) {
       short2 w = u.spd[s.cur][j];
       int dx = v.x - w.x, dy = v.y - w.y;
-      if (dx * dx + dy * dy < 4) {  // sqrt(dx^2 + dy^2) < 2 with integral speeds
+      if (dx * dx + dy * dy < 4 &&  // sqrt(dx^2 + dy^2) < 2 with integral speeds
+          (FILTERED || filter_keeps(u, s.cur, (int)j, aj, make_short2((short)r, (short)c)))) {
         m |= 1u << k;
         if (cand) cand[ncand] = (int)j;
         ncand++;
@@ -1420,30 +1416,38 @@ __device__ __forceinline__ unsigned merge_dirs(const Unit& u, const UState& s, i
   return m;
 }
 
-// Actives are counted per warp of 32 slots (act_cnt[i / 32]); the unit scan
-// turns the counts into offsets, so neither pass needs a block-wide prefix.
-__global__ void __launch_bounds__(CHUNK) k_merge_count(const Unit* __restrict__ units, const UState* __restrict__ st,
-                                                       const Frame* __restrict__ fr, const int* __restrict__ table,
-                                                       int nunits) {
+// filter_bad_particles_kernel (tracking_strategies.hpp:482-523) and step 1 of
+// the merge in one pass: each live particle applies the filter to itself and,
+// when it survives, finds its qualifying directions.  Actives are counted per
+// warp of 32 slots (act_cnt[i / 32]); the unit scan turns the counts into
+// offsets, so neither pass needs a block-wide prefix.
+__global__ void __launch_bounds__(CHUNK) k_filter_merge(const Unit* __restrict__ units, const UState* __restrict__ st,
+                                                        const Frame* __restrict__ fr, const int* __restrict__ table,
+                                                        int nunits) {
   const int f = fr->f;
   const int total = table[nunits];
   for (int g = blockIdx.x; g < total; g += gridDim.x) {
     ChunkCursor cc = chunk_of(table, nunits, g);
     const Unit& u = units[cc.unit];
-    if (!filt_frame(u, f) || !u.with_merge) continue;
+    if (!filt_frame(u, f)) continue;
     const UState s = st[cc.unit];
     const int i = cc.chunk * CHUNK + threadIdx.x;
     unsigned m = 0;
     if (i < s.n) {
-      unsigned short age = u.age[s.cur][i];
+      const unsigned short age = u.age[s.cur][i];
       if (age != 0) {
-        int nc;
-        m = merge_dirs(u, s, f, i, u.pos[s.cur][i], age, nullptr, nc);
+        const short2 p = u.pos[s.cur][i];
+        if (!filter_keeps(u, s.cur, i, age, p)) {
+          u.age[s.cur][i] = 0;
+        } else if (u.with_merge) {
+          int nc;
+          m = merge_dirs<false>(u, s, f, i, p, age, nullptr, nc);
+        }
       }
-      u.cmask[i] = (uint8_t)m;
+      if (u.with_merge) u.cmask[i] = (uint8_t)m;
     }
     const unsigned b = __ballot_sync(0xffffffffu, m != 0);
-    if ((threadIdx.x & 31) == 0 && i < s.n) u.act_cnt[i >> 5] = __popc(b);
+    if (u.with_merge && (threadIdx.x & 31) == 0 && i < s.n) u.act_cnt[i >> 5] = __popc(b);
   }
 }
 
@@ -1469,7 +1473,7 @@ __global__ void __launch_bounds__(CHUNK) k_merge_scatter(const Unit* __restrict_
       short2 p = u.pos[s.cur][i];
       int cand[8];
       int nc;
-      merge_dirs(u, s, f, i, p, u.age[s.cur][i], cand, nc);
+      merge_dirs<true>(u, s, f, i, p, u.age[s.cur][i], cand, nc);
       u.act_list[o] = make_int4(i, (int)(((unsigned)(unsigned short)p.x << 16) | (unsigned short)p.y), nc, 0);
       for (int q = 0; q < nc; q++) u.act_cand[(size_t)o * 8 + q] = cand[q];
     }

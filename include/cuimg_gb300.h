@@ -111,7 +111,11 @@ int gbt_set_rgb_to_gray(gbt_ctx* ctx, int32_t mode);
  * context's input slots (gbt_input_slot); used for CUDA-graph replay. */
 int gbt_run_resident(gbt_ctx* ctx);
 
-/* Device pointer and pitch of stream `s`'s level-0 input slot. */
+/* Device pointer and pitch of stream `s`'s level-0 input slot for the next
+ * frame.  Consecutive frames alternate between two slots (the front end of
+ * one frame runs while the back end of the previous one still reads the other
+ * slot's images), so ask again before every frame; write the slot on the
+ * context stream (gbt_stream) or synchronously. */
 int gbt_input_slot(gbt_ctx* ctx, int32_t stream, uint8_t** dptr, int64_t* pitch);
 
 /* Capture the per-frame launch sequence into CUDA graphs (one per frame
@@ -122,7 +126,10 @@ int gbt_use_graphs(gbt_ctx* ctx, int32_t enable);
  * device-side check failed since the last call. */
 int gbt_sync(gbt_ctx* ctx);
 
-/* The CUDA stream (cudaStream_t) the context orders its work on. */
+/* The CUDA stream (cudaStream_t) the context orders its work on: when a
+ * frame's last kernel on it has run, the whole frame is done.  (Each frame's
+ * input copy, pyramid and blurs run on a second, internal stream, overlapping
+ * the previous frame's matching and filtering.) */
 int gbt_stream(gbt_ctx* ctx, void** cuda_stream);
 
 /* Particle set of (stream, scale): dense slot count (tombstones included,
