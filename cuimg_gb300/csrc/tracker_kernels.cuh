@@ -981,6 +981,25 @@ __device__ __forceinline__ int fast_saliency_bf(const uint8_t* P, int n_, int th
   return (xb | xd) ? ((sb > sd ? sb : sd) & 255) : 0;
 }
 
+// A necessary condition of the FAST run test for n_ >= 8: any 8 cyclically
+// consecutive ring positions hold two cyclically adjacent ones of the four
+// cardinal positions 0, 4, 8, 12, so a run of n_ >= 8 strong pixels of one
+// sign makes two adjacent cardinals strong with that sign.  Pixels that fail
+// it score 0 in fast_saliency_bf.
+template <int LD>
+__device__ __forceinline__ bool fast_pretest(const uint8_t* P, int th) {
+  const int vp = P[0];
+  unsigned B = 0, D = 0;
+#pragma unroll
+  for (int k = 0; k < 4; k++) {
+    const int d = (int)P[circle16_r(4 * k) * LD + circle16_c(4 * k)] - vp;
+    B |= (unsigned)(d > th) << k;
+    D |= (unsigned)(-d > th) << k;
+  }
+  const unsigned rb = ((B >> 1) | (B << 3)) & 15u, rd = ((D >> 1) | (D << 3)) & 15u;
+  return ((B & rb) | (D & rd)) != 0;
+}
+
 // Saliency + 3x3 tile non-maximum selection: fast_detector::update and
 // new_particles(cpu) (tracking2/fast_detector.hpp:217-262,296-313) fused.  A
 // tile q owns pixels 3q + (1,1) + [0,2]^2; it is skipped when any of them holds
@@ -993,9 +1012,11 @@ __device__ __forceinline__ int fast_saliency_bf(const uint8_t* P, int n_, int th
 //
 // A CTA covers 8 x 32 tiles: it stages their pixels (with the ring's 3-pixel
 // halo) and the occupancy / mask words of the bins they touch in shared
-// memory, lists the unoccupied tiles, and gives each listed tile to one
-// thread, which computes the saliency of its nine pixels with the branch-free
-// form above (no divergence) and selects the maximum.
+// memory.  Each thread screens the nine pixels of its tile (unoccupied tile,
+// unmasked pixel, fast_pretest) and lists the survivors -- about a quarter of
+// the pixels -- so that the full test (contrast and fast_saliency_bf) runs
+// packed over the CTA's threads; then each thread takes the first strict
+// maximum of its tile.
 constexpr int DT_R = 8, DT_C = 32;  // tiles per CTA
 constexpr int DT_PR = DT_R * 3 + 6, DT_PC = DT_C * 3 + 6;
 constexpr int DT_BR = (DT_R * 3 + 7) / 8 + 1, DT_BC = (DT_C * 3 + 7) / 8 + 1;  // bins touched
@@ -1004,8 +1025,9 @@ __global__ void __launch_bounds__(256) k_detect(const Unit* __restrict__ units, 
                                                 const int* __restrict__ blk_prefix, int nunits) {
   __shared__ uint8_t tile[DT_PR][DT_PC];
   __shared__ unsigned long long s_occ[DT_BR][DT_BC], s_pm[DT_BR][DT_BC];
-  __shared__ short list[DT_R * DT_C];
-  __shared__ int wt[65];
+  __shared__ uint8_t sal[DT_R * DT_C][9];
+  __shared__ unsigned short cand[DT_R * DT_C * 9];  // tile * 9 + pixel
+  __shared__ int ncand;
   const int f = fr->f;
   const int t = blockIdx.x;
   const int ui = find_unit(blk_prefix, nunits, t);
@@ -1027,16 +1049,18 @@ __global__ void __launch_bounds__(256) k_detect(const Unit* __restrict__ units, 
     s_occ[r][c] = ok ? u.occ[(size_t)br * u.BW + bc] : 0ull;
     s_pm[r][c] = ok ? u.pmask[(size_t)br * u.BW + bc] : 0ull;
   }
+  if (threadIdx.x == 0) ncand = 0;
   __syncthreads();
   auto bit = [&](const unsigned long long (*w)[DT_BC], int r, int c) -> bool {
     return (w[(r >> 3) - br0][(c >> 3) - bc0] >> (((r & 7) << 3) | (c & 7))) & 1ull;
   };
-  // Tiles of this CTA: occupied ones are decided now, the others are listed.
-  const int tr = TR0 + threadIdx.x / DT_C, tc = TC0 + threadIdx.x % DT_C;
+  // Screening: the thread's own tile.
+  const int lt = threadIdx.x;
+  const int tr = TR0 + lt / DT_C, tc = TC0 + lt % DT_C;
+  const int pr = 3 * tr + 1, pc = 3 * tc + 1;
   const bool valid = tr < u.TH && tc < u.TW;
   bool open = false;
   if (valid) {
-    const int pr = 3 * tr + 1, pc = 3 * tc + 1;
     bool occupied = false;
 #pragma unroll
     for (int r = 0; r < 3; r++)
@@ -1046,43 +1070,54 @@ __global__ void __launch_bounds__(256) k_detect(const Unit* __restrict__ units, 
     open = !occupied;
     if (occupied) u.tilecode[(size_t)tr * u.TW + tc] = 0xFF;
   }
-  int nopen;
-  const int slot = block_prefix(open, wt, nopen);
-  if (open) list[slot] = (short)threadIdx.x;
-  __syncthreads();
-  // One open tile per thread (packed by the list, so warps stay full): the
-  // saliency of its nine pixels, then the first strict maximum.
-  if (threadIdx.x < nopen) {
-    const int lt = list[threadIdx.x];
-    const int ttr = TR0 + lt / DT_C, ttc = TC0 + lt % DT_C;
-    const int pr = 3 * ttr + 1, pc = 3 * ttc + 1;
-    const bool inner = pr + 2 < u.H && pc + 2 < u.W;  // all nine pixels in the domain
-    const uint8_t* P0 = &tile[pr - pr0][pc - pc0];
-    int vmax = -1, mr = 0, mc = 0;
+  const bool pre = u.nfast >= 8;
+  const uint8_t* P0 = &tile[pr - pr0][pc - pc0];
 #pragma unroll
-    for (int q = 0; q < 9; q++) {
-      const int r = q / 3, c = q % 3;
-      if (!inner && !in_dom(u, pr + r, pc + c)) continue;
-      const uint8_t* P = P0 + r * DT_PC + c;
-      const int d = 2;
-      const int con = abs((int)P[d] - (int)P[-d]) + abs((int)P[-d * DT_PC] - (int)P[d * DT_PC]) +
-                      abs((int)P[-d * DT_PC - d] - (int)P[d * DT_PC + d]) +
-                      abs((int)P[-d * DT_PC + d] - (int)P[d * DT_PC - d]);
-      const int fs = fast_saliency_bf<DT_PC>(P, u.nfast, u.threshold);
-      const int v = (bit(s_pm, pr + r, pc + c) || con < 5) ? 0 : fs;
-      if (vmax < v) {  // pixel 0 always enters (v >= 0)
-        vmax = v;
-        mr = r;
-        mc = c;
-      }
-    }
-    uint8_t code = 0xFF;
-    if (vmax >= u.threshold) {
-      const int gr = pr + mr, gc = pc + mc;
-      if (gr >= 3 && gr <= u.H - 4 && gc >= 3 && gc <= u.W - 4) code = (uint8_t)(mr * 3 + mc);
-    }
-    u.tilecode[(size_t)ttr * u.TW + ttc] = code;
+  for (int q = 0; q < 9; q++) {
+    const int r = q / 3, c = q % 3;
+    sal[lt][q] = 0;
+    const bool keep = open && in_dom(u, pr + r, pc + c) && !bit(s_pm, pr + r, pc + c) &&
+                      (!pre || fast_pretest<DT_PC>(P0 + r * DT_PC + c, u.threshold));
+    const unsigned m = __ballot_sync(0xffffffffu, keep);
+    int base = 0;
+    if ((threadIdx.x & 31) == 0 && m) base = atomicAdd(&ncand, __popc(m));
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if (keep) cand[base + __popc(m & ((1u << (threadIdx.x & 31)) - 1u))] = (unsigned short)(lt * 9 + q);
   }
+  __syncthreads();
+  // Full test of the listed pixels, packed over the CTA.
+  for (int k = threadIdx.x; k < ncand; k += blockDim.x) {
+    const int e = cand[k], ct = e / 9, q = e % 9;
+    const int cpr = 3 * (TR0 + ct / DT_C) + 1 + q / 3, cpc = 3 * (TC0 + ct % DT_C) + 1 + q % 3;
+    const uint8_t* P = &tile[cpr - pr0][cpc - pc0];
+    const int d = 2;
+    const int con = abs((int)P[d] - (int)P[-d]) + abs((int)P[-d * DT_PC] - (int)P[d * DT_PC]) +
+                    abs((int)P[-d * DT_PC - d] - (int)P[d * DT_PC + d]) +
+                    abs((int)P[-d * DT_PC + d] - (int)P[d * DT_PC - d]);
+    if (con >= 5) sal[ct][q] = (uint8_t)fast_saliency_bf<DT_PC>(P, u.nfast, u.threshold);
+  }
+  __syncthreads();
+  if (!open) return;
+  // The first strict maximum of the tile (pixels outside the domain do not
+  // take part; every other pixel does, with saliency 0 where it was screened out).
+  int vmax = -1, mr = 0, mc = 0;
+#pragma unroll
+  for (int q = 0; q < 9; q++) {
+    const int r = q / 3, c = q % 3;
+    if (!in_dom(u, pr + r, pc + c)) continue;
+    const int v = sal[lt][q];
+    if (vmax < v) {
+      vmax = v;
+      mr = r;
+      mc = c;
+    }
+  }
+  uint8_t code = 0xFF;
+  if (vmax >= u.threshold) {
+    const int gr = pr + mr, gc = pc + mc;
+    if (gr >= 3 && gr <= u.H - 4 && gc >= 3 && gc <= u.W - 4) code = (uint8_t)(mr * 3 + mc);
+  }
+  u.tilecode[(size_t)tr * u.TW + tc] = code;
 }
 
 // The regular and dense detectors (regular_detector.hpp:62-103,
