@@ -630,9 +630,10 @@ static int enqueue_back(gbt_ctx* ctx, bool any_det, bool any_filt, int par, int&
   }
   int* table = any_det ? ctx->d_post : ctx->d_pre;
   if (any_filt) {
-    { PROF("k_filter_merge"); k_filter_merge<<<pgrid, CHUNK, 0, st>>>(du, ctx->d_state, ctx->d_frame, table, nunits); }
+    const int fgrid = ctx->nsm * 6;
+    { PROF("k_filter_merge"); k_filter_merge<<<fgrid, FM_THREADS, 0, st>>>(du, ctx->d_state, ctx->d_frame, table, nunits); }
     { PROF("k_unit_scan"); k_unit_scan<<<nunits, 1024, 0, st>>>(du, ctx->d_state, ctx->d_frame, 1); }
-    { PROF("k_merge_scatter"); k_merge_scatter<<<pgrid, CHUNK, 0, st>>>(du, ctx->d_state, ctx->d_frame, table, nunits); }
+    { PROF("k_merge_scatter"); k_merge_scatter<<<fgrid, FM_THREADS, 0, st>>>(du, ctx->d_state, ctx->d_frame, table, nunits); }
     { PROF("k_merge_resolve"); k_merge_resolve<<<nunits, 256, 0, st>>>(du, ctx->d_state, ctx->d_frame); }
     n += 4;
   }

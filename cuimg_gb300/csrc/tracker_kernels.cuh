@@ -549,27 +549,37 @@ __global__ void __launch_bounds__(CHUNK) k_mt_bin(const Unit* __restrict__ units
     const Unit& u = units[cc.unit];
     const UState s = st[cc.unit];
     const int i = cc.chunk * CHUNK + threadIdx.x;
-    if (i >= s.n) continue;
     int2* k = key + u.mt_pbase + i;
     if (PASS == 1) {
+      if (i >= s.n) continue;
       const int2 tr = *k;
       if (tr.x >= 0) list[off[tr.x] + tr.y] = i;
       continue;
     }
+    if ((i & ~31) >= s.n) continue;  // whole warp past the slots
     const int b = s.cur;
-    const unsigned short age = u.age[b][i];
-    int2 tr = make_int2(-1, 0);
-    if (age != 0) {
-      int pr, pc;
-      predict(age, u.pos[b][i], u.spd[b][i], pr, pc);
-      if (!in_dom(u, pr, pc)) {
-        u.age[b][i] = 0;
-      } else {
-        tr.x = mt_tile(u, pr, pc);
-        tr.y = atomicAdd(&cnt[tr.x], 1);
+    int tile = -1;
+    if (i < s.n) {
+      const unsigned short age = u.age[b][i];
+      if (age != 0) {
+        int pr, pc;
+        predict(age, u.pos[b][i], u.spd[b][i], pr, pc);
+        if (!in_dom(u, pr, pc))
+          u.age[b][i] = 0;
+        else
+          tile = mt_tile(u, pr, pc);
       }
     }
-    *k = tr;
+    // Slots follow birth order, which is raster order within a detector
+    // frame, so a warp's particles mostly share a few tiles: one atomic per
+    // distinct tile of the warp (ranks within a tile are in any order).
+    const int lane = threadIdx.x & 31;
+    const unsigned peers = __match_any_sync(0xffffffffu, tile);
+    const int leader = __ffs(peers) - 1;
+    int base = 0;
+    if (tile >= 0 && lane == leader) base = atomicAdd(&cnt[tile], __popc(peers));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    if (i < s.n) *k = tile >= 0 ? make_int2(tile, base + __popc(peers & ((1u << lane) - 1u))) : make_int2(-1, 0);
   }
 }
 
@@ -1426,13 +1436,26 @@ __device__ __forceinline__ unsigned merge_dirs(const Unit& u, const UState& s, i
                                                unsigned short age, int* cand, int& ncand) {
   unsigned m = 0;
   ncand = 0;
-  const short2 v = u.spd[s.cur][i];
+  // occ marks exactly the pixels whose index entry is current (matched
+  // particles, and births on detector frames): most neighbours are empty.  The
+  // 3x3 box touches at most four bin words (rows ra / rb, columns ca / cb).
+  const int ra = max(p.x - 1, 0), rb = min(p.x + 1, u.H - 1), ca = max(p.y - 1, 0), cb = min(p.y + 1, u.W - 1);
+  const unsigned long long wa = u.occ[bin_word(u, ra, ca)], wb = u.occ[bin_word(u, ra, cb)];
+  const unsigned long long wc = u.occ[bin_word(u, rb, ca)], wd = u.occ[bin_word(u, rb, cb)];
+  unsigned nb = 0;
+#pragma unroll
   for (int k = 0; k < 8; k++) {
-    int r = p.x + c_c8[k][0], c = p.y + c_c8[k][1];
-    if (!in_dom(u, r, c)) continue;
-    // occ marks exactly the pixels whose index entry is current (matched
-    // particles, and births on detector frames): most neighbours are empty.
-    if (!(u.occ[bin_word(u, r, c)] & bin_bit(r, c))) continue;
+    const int r = p.x + c8r(k), c = p.y + c8c(k);
+    const bool top = (r >> 3) == (ra >> 3), left = (c >> 3) == (ca >> 3);
+    const unsigned long long w = top ? (left ? wa : wb) : (left ? wc : wd);
+    if (in_dom(u, r, c) && (w & bin_bit(r, c))) nb |= 1u << k;
+  }
+  if (!nb) return 0;
+  const short2 v = u.spd[s.cur][i];
+  while (nb) {  // occupied neighbours in c8_h order
+    const int k = __ffs(nb) - 1;
+    nb &= nb - 1;
+    const int r = p.x + c8_dr(k), c = p.y + c8_dc(k);
     unsigned long long e = u.idx[(size_t)r * u.W + c];
     if (!idx_current(e, f)) continue;
     unsigned j = (unsigned)(e & 0xffffffffu);
@@ -1456,17 +1479,23 @@ __device__ __forceinline__ unsigned merge_dirs(const Unit& u, const UState& s, i
 // when it survives, finds its qualifying directions.  Actives are counted per
 // warp of 32 slots (act_cnt[i / 32]); the unit scan turns the counts into
 // offsets, so neither pass needs a block-wide prefix.
-__global__ void __launch_bounds__(CHUNK) k_filter_merge(const Unit* __restrict__ units, const UState* __restrict__ st,
-                                                        const Frame* __restrict__ fr, const int* __restrict__ table,
-                                                        int nunits) {
+// Quarter-chunk CTAs (256 threads) for the merge passes: their register
+// footprint allows six CTAs per SM, where 1024-thread CTAs get one.
+constexpr int FM_THREADS = 256;
+constexpr int FM_SUB = CHUNK / FM_THREADS;
+
+__global__ void __launch_bounds__(FM_THREADS) k_filter_merge(const Unit* __restrict__ units,
+                                                             const UState* __restrict__ st,
+                                                             const Frame* __restrict__ fr,
+                                                             const int* __restrict__ table, int nunits) {
   const int f = fr->f;
-  const int total = table[nunits];
+  const int total = table[nunits] * FM_SUB;
   for (int g = blockIdx.x; g < total; g += gridDim.x) {
-    ChunkCursor cc = chunk_of(table, nunits, g);
+    ChunkCursor cc = chunk_of(table, nunits, g / FM_SUB);
     const Unit& u = units[cc.unit];
     if (!filt_frame(u, f)) continue;
     const UState s = st[cc.unit];
-    const int i = cc.chunk * CHUNK + threadIdx.x;
+    const int i = cc.chunk * CHUNK + (g % FM_SUB) * FM_THREADS + threadIdx.x;
     unsigned m = 0;
     if (i < s.n) {
       const unsigned short age = u.age[s.cur][i];
@@ -1486,17 +1515,18 @@ __global__ void __launch_bounds__(CHUNK) k_filter_merge(const Unit* __restrict__
   }
 }
 
-__global__ void __launch_bounds__(CHUNK) k_merge_scatter(const Unit* __restrict__ units, const UState* __restrict__ st,
-                                                         const Frame* __restrict__ fr, const int* __restrict__ table,
-                                                         int nunits) {
+__global__ void __launch_bounds__(FM_THREADS) k_merge_scatter(const Unit* __restrict__ units,
+                                                              const UState* __restrict__ st,
+                                                              const Frame* __restrict__ fr,
+                                                              const int* __restrict__ table, int nunits) {
   const int f = fr->f;
-  const int total = table[nunits];
+  const int total = table[nunits] * FM_SUB;
   for (int g = blockIdx.x; g < total; g += gridDim.x) {
-    ChunkCursor cc = chunk_of(table, nunits, g);
+    ChunkCursor cc = chunk_of(table, nunits, g / FM_SUB);
     const Unit& u = units[cc.unit];
     if (!filt_frame(u, f) || !u.with_merge) continue;
     const UState s = st[cc.unit];
-    const int i = cc.chunk * CHUNK + threadIdx.x;
+    const int i = cc.chunk * CHUNK + (g % FM_SUB) * FM_THREADS + threadIdx.x;
     if ((i & ~31) >= s.n) continue;  // whole warp past the slots
     const int w = i >> 5;
     const int o0 = u.act_cnt[w], o1 = (w + 1) * 32 < s.n ? u.act_cnt[w + 1] : s.A;
