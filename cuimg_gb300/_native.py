@@ -93,6 +93,7 @@ def _declare(lib):
     lib.gbt_checkpoint_load.argtypes = [P, ctypes.c_char_p, ctypes.c_size_t]
     lib.gbt_get_trajectories.argtypes = [P, I32, I32, P, P, I32P, I32P]
     lib.gbt_read_counts.argtypes = [P, P, I32]
+    lib.gbt_read_counts_async.argtypes = [P, P, I32]
     lib.gbt_set_tuning.argtypes = [P, I32, I32]
     lib.gbt_get_tuning.argtypes = [P, I32, I32P]
     lib.gbt_profile_enable.argtypes = [P, I32]

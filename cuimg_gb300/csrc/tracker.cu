@@ -58,6 +58,7 @@ struct gbt_ctx {
   Unit* d_units = nullptr;
   UState* d_state = nullptr;
   Frame* d_frame = nullptr;
+  int* d_counts = nullptr;  // gbt_read_counts_async staging
   int host_frame = 0;
   // static work tables (device)
   int* d_stream_unit0 = nullptr;
@@ -370,6 +371,7 @@ static int build(gbt_ctx* ctx, const gbt_config* cfgs, int nstreams) {
   if ((r = upload_units(ctx))) return r;
   if ((r = dalloc_t(ctx, &ctx->d_state, nunits))) return r;
   if ((r = dalloc_t(ctx, &ctx->d_frame, 1))) return r;
+  if ((r = dalloc_t(ctx, &ctx->d_counts, nunits))) return r;
   if ((r = dalloc_t(ctx, &ctx->d_pre, nunits + 1))) return r;
   if ((r = dalloc_t(ctx, &ctx->d_mt_cnt, ctx->mt_tiles + 1))) return r;
   if ((r = dalloc_t(ctx, &ctx->d_mt_off, ctx->mt_tiles + 1))) return r;
@@ -945,6 +947,16 @@ extern "C" int gbt_read_counts(gbt_ctx* ctx, int32_t* counts, int32_t n) {
   CK(cudaMemcpyAsync(st.data(), ctx->d_state, st.size() * sizeof(UState), cudaMemcpyDeviceToHost, ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
   for (size_t i = 0; i < st.size(); i++) counts[i] = st[i].n;
+  return GBT_OK;
+}
+
+extern "C" int gbt_read_counts_async(gbt_ctx* ctx, int32_t* counts, int32_t n) {
+  if (!ctx || !counts || n < (int)ctx->units.size()) return GBT_E_INVALID;
+  CK(cudaSetDevice(ctx->device));
+  const int nunits = (int)ctx->units.size();
+  k_counts<<<(nunits + 255) / 256, 256, 0, ctx->stream>>>(ctx->d_state, nunits, ctx->d_counts);
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(counts, ctx->d_counts, (size_t)nunits * sizeof(int32_t), cudaMemcpyDeviceToHost, ctx->stream));
   return GBT_OK;
 }
 

@@ -1713,6 +1713,11 @@ __global__ void __launch_bounds__(CHUNK) k_traj(const Unit* __restrict__ units, 
 
 // Rebuilds the per-frame chunk table from the current counters (after a
 // checkpoint load).
+// Every unit's particle slot count, gathered for one host read.
+__global__ void k_counts(const UState* __restrict__ st, int nunits, int* __restrict__ out) {
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nunits; k += gridDim.x * blockDim.x) out[k] = st[k].n;
+}
+
 __global__ void __launch_bounds__(1024) k_tick_table(const Unit* __restrict__ units, const UState* __restrict__ st,
                                                      int nunits, int* __restrict__ pre_table) {
   build_table(units, st, nunits, pre_table);

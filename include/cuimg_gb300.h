@@ -172,6 +172,12 @@ int gbt_get_bins(gbt_ctx* ctx, int32_t stream, int32_t scale, float* flow, uint3
  * (units ordered stream-major, scales ascending); waits for queued work. */
 int gbt_read_counts(gbt_ctx* ctx, int32_t* counts, int32_t n);
 
+/* The same read queued on the context stream (gbt_stream) after the frames
+ * queued so far; returns at once.  `counts` is host memory (pinned, for the
+ * copy to be asynchronous) that holds the values once the stream has reached
+ * this point, so a caller can read frame t's counts while frame t + 1 runs. */
+int gbt_read_counts_async(gbt_ctx* ctx, int32_t* counts, int32_t n);
+
 /* Frame counter of (stream, scale) (generic_strategy::frame_cpt_). */
 int gbt_frame_count(gbt_ctx* ctx, int32_t stream, int32_t scale, int32_t* n);
 
