@@ -235,8 +235,8 @@ def bench_ours(args):
         tuning = autotune.tune(cfg, [[frames[s][t] for s in range(B)] for t in range(min(nfr, 11))], warmup=3, timed=8,
                                device=local)
 
-    def make(nstreams, graphs=True):
-        bt = BatchTracker(cfg[:nstreams], device=local, graphs=graphs)
+    def make(nstreams, graphs=True, groups=0):
+        bt = BatchTracker(cfg[:nstreams], device=local, graphs=graphs, groups=groups)
         bt._ensure()
         autotune.apply(bt, tuning)
         return bt
@@ -299,6 +299,7 @@ def bench_ours(args):
     clocks = clk.summary()
     clocks["window"] = "timed region + 1.5 s more of the same step"
     value = B * world * args.steps / (ms / 1000.0)
+    ngroups = bt.groups()
     bt.close()
 
     # The same with device-side trajectories (20 positions per particle).
@@ -315,7 +316,7 @@ def bench_ours(args):
     bt1.close()
 
     # Per-kernel device time (eager, CUDA events on the context stream).
-    btp = make(B, graphs=False)
+    btp = make(B, graphs=False, groups=1)  # one launch per kernel over all streams, serialised
     nprof = max(args.steps, DET_FREQ)
     for t in range(args.warmup):
         btp.run([frames[s][t % nfr] for s in range(B)])
@@ -442,7 +443,8 @@ def bench_ours(args):
             "scaling": "weak", "vs_baseline": None, "dtype": "u8", "data": "synthetic",
             "config": {"workload": "%d streams x 1920x1080 gray, 4 scales, FAST th 20, detector every 10 frames, "
                                    "filter every frame, CUDA-graph replay" % B,
-                       "streams_per_gpu": B, "live_particles_per_stream": round(live_mean),
+                       "streams_per_gpu": B, "stream_groups": ngroups,
+                       "live_particles_per_stream": round(live_mean),
                        "l2": "working set per step > L2 (inputs larger than L2)",
                        "parallelism": "replicas only (independent streams per GPU)"},
             "plain": {"value": round(plain, 2), "unit": UNIT, "streams": 1, "ms_per_frame": round(ms1 / args.steps, 4),

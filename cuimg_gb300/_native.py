@@ -70,6 +70,8 @@ def _declare(lib):
     lib.gbt_config_default.restype = None
     lib.gbt_sizes_ok.argtypes = [I32, I32, I32]
     lib.gbt_create.argtypes = [ctypes.POINTER(gbt_config), I32, I32, ctypes.POINTER(P)]
+    lib.gbt_create_ex.argtypes = [ctypes.POINTER(gbt_config), I32, I32, I32, ctypes.POINTER(P)]
+    lib.gbt_groups.argtypes = [P, ctypes.POINTER(I32)]
     lib.gbt_destroy.argtypes = [P]
     lib.gbt_last_error.argtypes = [P, ctypes.c_char_p, ctypes.c_size_t]
     lib.gbt_run.argtypes = [P, ctypes.POINTER(P), ctypes.POINTER(ctypes.c_int64), I32]

@@ -36,7 +36,7 @@ struct StreamInfo {
 
 }  // namespace
 
-struct gbt_ctx {
+struct Group {
   int device = 0;
   int nsm = 0;
   cudaStream_t stream = nullptr;
@@ -50,7 +50,6 @@ struct gbt_ctx {
   cudaStream_t pre = nullptr;
   cudaEvent_t ev_front = nullptr;
   cudaEvent_t ev_back[2] = {nullptr, nullptr};
-  cudaEvent_t ev_user = nullptr;         // caller's input writes on `stream` (gbt_run_resident)
   Unit* d_units_v[2] = {nullptr, nullptr};  // unit tables whose images are the parity-0 / parity-1 buffers
   std::vector<Unit> units_odd;           // host copy of the parity-1 table
   std::vector<StreamInfo> streams;
@@ -127,7 +126,7 @@ struct gbt_ctx {
   size_t event_next = 0;
 };
 
-static int set_err(gbt_ctx* c, int code, const char* fmt, ...) {
+static int set_err(Group* c, int code, const char* fmt, ...) {
   if (c) {
     char buf[512];
     va_list ap;
@@ -147,7 +146,7 @@ static int set_err(gbt_ctx* c, int code, const char* fmt, ...) {
                      __FILE__, __LINE__);                                                        \
   } while (0)
 
-static int dalloc(gbt_ctx* ctx, void** p, size_t bytes, bool zero) {
+static int dalloc(Group* ctx, void** p, size_t bytes, bool zero) {
   if (bytes == 0) bytes = 16;
   cudaError_t e = cudaMalloc(p, bytes);
   if (e != cudaSuccess) return set_err(ctx, GBT_E_OOM, "cudaMalloc(%zu) failed: %s", bytes, cudaGetErrorString(e));
@@ -157,11 +156,11 @@ static int dalloc(gbt_ctx* ctx, void** p, size_t bytes, bool zero) {
 }
 
 template <typename T>
-static int dalloc_t(gbt_ctx* ctx, T** p, size_t n, bool zero = true) {
+static int dalloc_t(Group* ctx, T** p, size_t n, bool zero = true) {
   return dalloc(ctx, (void**)p, n * sizeof(T), zero);
 }
 
-static int upload_table(gbt_ctx* ctx, int** d, const std::vector<int>& h) {
+static int upload_table(Group* ctx, int** d, const std::vector<int>& h) {
   int r = dalloc_t(ctx, d, h.size(), false);
   if (r) return r;
   CK(cudaMemcpy(*d, h.data(), h.size() * sizeof(int), cudaMemcpyHostToDevice));
@@ -198,7 +197,7 @@ extern "C" int gbt_sizes_ok(int32_t rows, int32_t cols, int32_t nscales) {
   return 1;
 }
 
-static void free_ctx(gbt_ctx* ctx) {
+static void free_ctx(Group* ctx) {
   if (!ctx) return;
   if (ctx->device >= 0) cudaSetDevice(ctx->device);
   for (auto e : ctx->event_pool) cudaEventDestroy(e);
@@ -210,7 +209,7 @@ static void free_ctx(gbt_ctx* ctx) {
   for (auto& s : ctx->streams)
     if (s.pinned) cudaFreeHost(s.pinned);
   if (ctx->h_ingest) cudaFreeHost(ctx->h_ingest);
-  for (cudaEvent_t e : {ctx->ev_front, ctx->ev_back[0], ctx->ev_back[1], ctx->ev_user})
+  for (cudaEvent_t e : {ctx->ev_front, ctx->ev_back[0], ctx->ev_back[1]})
     if (e) cudaEventDestroy(e);
   if (ctx->pre) cudaStreamDestroy(ctx->pre);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
@@ -218,7 +217,7 @@ static void free_ctx(gbt_ctx* ctx) {
 }
 
 // Unit `ui` with the image buffers of frame parity `par`.
-static Unit unit_view(const gbt_ctx* ctx, size_t ui, int par) {
+static Unit unit_view(const Group* ctx, size_t ui, int par) {
   Unit u = ctx->units[ui];
   if (par) {
     const Unit& o = ctx->units_odd[ui];
@@ -230,7 +229,7 @@ static Unit unit_view(const gbt_ctx* ctx, size_t ui, int par) {
 }
 
 // Uploads both parities' unit tables after a change of ctx->units.
-static int upload_units(gbt_ctx* ctx) {
+static int upload_units(Group* ctx) {
   const size_t n = ctx->units.size();
   std::vector<Unit> v(n);
   for (int par = 0; par < 2; par++) {
@@ -240,28 +239,28 @@ static int upload_units(gbt_ctx* ctx) {
   return GBT_OK;
 }
 
-static bool split_front(const gbt_ctx* ctx) { return !ctx->profiling; }
-static cudaStream_t front_stream(const gbt_ctx* ctx) { return split_front(ctx) ? ctx->pre : ctx->stream; }
+static bool split_front(const Group* ctx) { return !ctx->profiling; }
+static cudaStream_t front_stream(const Group* ctx) { return split_front(ctx) ? ctx->pre : ctx->stream; }
 
 // Orders the next frame's input writes after the back end that last read the
 // images of its parity.
-static int prepare_front(gbt_ctx* ctx) {
+static int prepare_front(Group* ctx) {
   if (split_front(ctx)) CK(cudaStreamWaitEvent(ctx->pre, ctx->ev_back[ctx->host_frame & 1], 0));
   return GBT_OK;
 }
 
-static int sync_all(gbt_ctx* ctx) {
+static int sync_all(Group* ctx) {
   CK(cudaStreamSynchronize(ctx->pre));
   CK(cudaStreamSynchronize(ctx->stream));
   return GBT_OK;
 }
 
-static int build(gbt_ctx* ctx, const gbt_config* cfgs, int nstreams) {
+static int build(Group* ctx, const gbt_config* cfgs, int nstreams) {
   CK(cudaSetDevice(ctx->device));
   CK(cudaDeviceGetAttribute(&ctx->nsm, cudaDevAttrMultiProcessorCount, ctx->device));
   CK(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
   CK(cudaStreamCreateWithFlags(&ctx->pre, cudaStreamNonBlocking));
-  for (cudaEvent_t* e : {&ctx->ev_front, &ctx->ev_back[0], &ctx->ev_back[1], &ctx->ev_user})
+  for (cudaEvent_t* e : {&ctx->ev_front, &ctx->ev_back[0], &ctx->ev_back[1]})
     CK(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
   // Units: streams in order, scales 0..L-1 of each stream contiguous.
   size_t occ_words = 0;
@@ -440,7 +439,7 @@ static int build(gbt_ctx* ctx, const gbt_config* cfgs, int nstreams) {
   return GBT_OK;
 }
 
-extern "C" int gbt_create(const gbt_config* cfgs, int32_t nstreams, int32_t device, gbt_ctx** out) {
+static int grp_create(const gbt_config* cfgs, int32_t nstreams, int32_t device, Group** out) {
   if (!out) return GBT_E_INVALID;
   *out = nullptr;
   if (!cfgs || nstreams < 1) return GBT_E_INVALID;
@@ -451,7 +450,7 @@ extern "C" int gbt_create(const gbt_config* cfgs, int32_t nstreams, int32_t devi
         c.detector > GBT_DETECTOR_DENSE || c.detector_step < 1)
       return GBT_E_INVALID;
   }
-  gbt_ctx* ctx = new gbt_ctx;
+  Group* ctx = new Group;
   ctx->device = device;
   int r = build(ctx, cfgs, nstreams);
   if (r) {
@@ -463,7 +462,7 @@ extern "C" int gbt_create(const gbt_config* cfgs, int32_t nstreams, int32_t devi
   return GBT_OK;
 }
 
-extern "C" int gbt_destroy(gbt_ctx* ctx) {
+static int grp_destroy(Group* ctx) {
   if (!ctx) return GBT_E_INVALID;
   cudaSetDevice(ctx->device);
   if (ctx->pre) cudaStreamSynchronize(ctx->pre);
@@ -472,19 +471,7 @@ extern "C" int gbt_destroy(gbt_ctx* ctx) {
   return GBT_OK;
 }
 
-extern "C" int gbt_last_error(gbt_ctx* ctx, char* buf, size_t len) {
-  if (!ctx || !buf || !len) return GBT_E_INVALID;
-  snprintf(buf, len, "%s", ctx->err.c_str());
-  return GBT_OK;
-}
-
-extern "C" int gbt_stream(gbt_ctx* ctx, void** s) {
-  if (!ctx || !s) return GBT_E_INVALID;
-  *s = (void*)ctx->stream;
-  return GBT_OK;
-}
-
-extern "C" int gbt_input_slot(gbt_ctx* ctx, int32_t stream, uint8_t** dptr, int64_t* pitch) {
+static int grp_input_slot(Group* ctx, int32_t stream, uint8_t** dptr, int64_t* pitch) {
   if (!ctx || stream < 0 || stream >= (int)ctx->streams.size()) return GBT_E_INVALID;
   const Unit u = unit_view(ctx, ctx->streams[stream].unit0, ctx->host_frame & 1);  // the next frame's slot
   if (dptr) *dptr = u.img;
@@ -493,7 +480,7 @@ extern "C" int gbt_input_slot(gbt_ctx* ctx, int32_t stream, uint8_t** dptr, int6
 }
 
 // Frame kind of the frame about to run.
-static void frame_kind(gbt_ctx* ctx, bool& any_det, bool& any_filt) {
+static void frame_kind(Group* ctx, bool& any_det, bool& any_filt) {
   any_det = any_filt = false;
   for (auto& s : ctx->streams) {
     if (ctx->host_frame % s.cfg.detector_frequency == 0) any_det = true;
@@ -501,7 +488,7 @@ static void frame_kind(gbt_ctx* ctx, bool& any_det, bool& any_filt) {
   }
 }
 
-static cudaEvent_t next_event(gbt_ctx* ctx) {
+static cudaEvent_t next_event(Group* ctx) {
   if (ctx->event_next == ctx->event_pool.size()) {
     cudaEvent_t e;
     cudaEventCreate(&e);
@@ -510,10 +497,10 @@ static cudaEvent_t next_event(gbt_ctx* ctx) {
   return ctx->event_pool[ctx->event_next++];
 }
 
-static int prof_slot(gbt_ctx* ctx, const char* name) {
+static int prof_slot(Group* ctx, const char* name) {
   for (size_t i = 0; i < ctx->prof.size(); i++)
     if (ctx->prof[i].name == name) return (int)i;
-  gbt_ctx::Prof p;
+  Group::Prof p;
   p.name = name;
   ctx->prof.push_back(p);
   return (int)ctx->prof.size() - 1;
@@ -521,10 +508,10 @@ static int prof_slot(gbt_ctx* ctx, const char* name) {
 
 // Brackets one launch with events when profiling (never inside a capture).
 struct ProfScope {
-  gbt_ctx* ctx;
+  Group* ctx;
   int slot = -1;
   cudaEvent_t a = nullptr;
-  ProfScope(gbt_ctx* c, const char* name) : ctx(c) {
+  ProfScope(Group* c, const char* name) : ctx(c) {
     if (!ctx->profiling) return;
     slot = prof_slot(ctx, name);
     a = next_event(ctx);
@@ -538,7 +525,7 @@ struct ProfScope {
   }
 };
 
-static void prof_collect(gbt_ctx* ctx) {
+static void prof_collect(Group* ctx) {
   if (ctx->pending.empty()) return;
   cudaStreamSynchronize(ctx->stream);
   for (auto& p : ctx->pending) {
@@ -555,7 +542,7 @@ static void prof_collect(gbt_ctx* ctx) {
 
 // Front end of a frame on `st`: the pyramid (with the fused RGB ingest) and
 // the BC2S blurs, into the image buffers of parity `par`.
-static int enqueue_front(gbt_ctx* ctx, int par, cudaStream_t st, int& n) {
+static int enqueue_front(Group* ctx, int par, cudaStream_t st, int& n) {
   const int nunits = (int)ctx->units.size();
   const int nstreams = (int)ctx->streams.size();
   const Unit* du = ctx->d_units_v[par];
@@ -585,7 +572,7 @@ static int enqueue_front(gbt_ctx* ctx, int par, cudaStream_t st, int& n) {
 // Back end of a frame on the context stream: matching, flow statistics,
 // detection, filtering, merging, trajectories and the frame tick, over the
 // images of parity `par`.
-static int enqueue_back(gbt_ctx* ctx, bool any_det, bool any_filt, int par, int& n) {
+static int enqueue_back(Group* ctx, bool any_det, bool any_filt, int par, int& n) {
   const int nunits = (int)ctx->units.size();
   const int pgrid = std::max(1, ctx->nsm * 2);
   const Unit* du = ctx->d_units_v[par];
@@ -652,7 +639,7 @@ static int enqueue_back(gbt_ctx* ctx, bool any_det, bool any_filt, int par, int&
 
 // Captures (once) and launches a graph of what `issue` enqueues on `st`.
 template <class F>
-static int launch_graph(gbt_ctx* ctx, cudaGraphExec_t& exec, int& launches, cudaStream_t st, F issue) {
+static int launch_graph(Group* ctx, cudaGraphExec_t& exec, int& launches, cudaStream_t st, F issue) {
   if (!exec) {
     cudaGraph_t g;
     int n = 0;
@@ -671,7 +658,7 @@ static int launch_graph(gbt_ctx* ctx, cudaGraphExec_t& exec, int& launches, cuda
 }
 
 // Queues one frame whose input is in place (ordered on the front-end stream).
-static int run_frame(gbt_ctx* ctx) {
+static int run_frame(Group* ctx) {
   bool any_det, any_filt;
   frame_kind(ctx, any_det, any_filt);
   const int par = ctx->host_frame & 1;
@@ -708,7 +695,7 @@ static int run_frame(gbt_ctx* ctx) {
 }
 
 // Drops every captured graph (the next frames capture them again).
-static void drop_graphs(gbt_ctx* ctx) {
+static void drop_graphs(Group* ctx) {
   for (auto& g : ctx->graph)
     if (g) {
       cudaGraphExecDestroy(g);
@@ -721,7 +708,7 @@ static void drop_graphs(gbt_ctx* ctx) {
     }
 }
 
-extern "C" int gbt_set_tuning(gbt_ctx* ctx, int32_t knob, int32_t value) {
+static int grp_set_tuning(Group* ctx, int32_t knob, int32_t value) {
   if (!ctx) return GBT_E_INVALID;
   if (knob == GBT_TUNE_MATCHER && value >= 0 && value <= 3) {
     if (ctx->match_variant != value) drop_graphs(ctx);
@@ -739,7 +726,7 @@ extern "C" int gbt_set_tuning(gbt_ctx* ctx, int32_t knob, int32_t value) {
   return GBT_E_INVALID;
 }
 
-extern "C" int gbt_get_tuning(gbt_ctx* ctx, int32_t knob, int32_t* value) {
+static int grp_get_tuning(Group* ctx, int32_t knob, int32_t* value) {
   if (!ctx || !value) return GBT_E_INVALID;
   if (knob == GBT_TUNE_MATCHER) {
     *value = ctx->match_variant;
@@ -754,7 +741,7 @@ extern "C" int gbt_get_tuning(gbt_ctx* ctx, int32_t knob, int32_t* value) {
 
 // Uploads the per-stream ingest modes when they changed (ordered on the
 // context stream before the frame's kernels).
-static int set_ingest(gbt_ctx* ctx, size_t s, int mode) {
+static int set_ingest(Group* ctx, size_t s, int mode) {
   StreamInfo& si = ctx->streams[s];
   Ingest want{mode ? si.d_rgb : nullptr, mode ? si.rgb_pitch : 0, mode, 0};
   Ingest& have = ctx->h_ingest[s];
@@ -769,7 +756,7 @@ static int set_ingest(gbt_ctx* ctx, size_t s, int mode) {
   return GBT_OK;
 }
 
-static int flush_ingest(gbt_ctx* ctx) {
+static int flush_ingest(Group* ctx) {
   if (ctx->ingest_dirty) {
     CK(cudaMemcpyAsync(ctx->d_ingest, ctx->h_ingest, sizeof(Ingest) * ctx->streams.size(), cudaMemcpyHostToDevice,
                        front_stream(ctx)));
@@ -778,7 +765,7 @@ static int flush_ingest(gbt_ctx* ctx) {
   return GBT_OK;
 }
 
-extern "C" int gbt_trajectories_enable(gbt_ctx* ctx, int32_t history) {
+static int grp_trajectories_enable(Group* ctx, int32_t history) {
   if (!ctx || history < 1 || history > 255) return GBT_E_INVALID;
   if (ctx->traj_T) return ctx->traj_T == history ? GBT_OK : GBT_E_INVALID;
   CK(cudaSetDevice(ctx->device));
@@ -797,22 +784,19 @@ extern "C" int gbt_trajectories_enable(gbt_ctx* ctx, int32_t history) {
   return GBT_OK;
 }
 
-extern "C" int gbt_use_graphs(gbt_ctx* ctx, int32_t enable) {
+static int grp_use_graphs(Group* ctx, int32_t enable) {
   if (!ctx) return GBT_E_INVALID;
   ctx->use_graphs = enable != 0;
   return GBT_OK;
 }
 
-extern "C" int gbt_run_resident(gbt_ctx* ctx) {
+// `user`: the caller's input writes (recorded on the stream it wrote them on).
+static int grp_run_resident(Group* ctx, cudaEvent_t user) {
   if (!ctx) return GBT_E_INVALID;
   CK(cudaSetDevice(ctx->device));
-  // The caller wrote the input slots on the context stream (or synchronously).
   int r0 = prepare_front(ctx);
   if (r0) return r0;
-  if (split_front(ctx)) {
-    CK(cudaEventRecord(ctx->ev_user, ctx->stream));
-    CK(cudaStreamWaitEvent(ctx->pre, ctx->ev_user, 0));
-  }
+  if (user) CK(cudaStreamWaitEvent(front_stream(ctx), user, 0));
   for (size_t s = 0; s < ctx->streams.size(); s++) {
     int r = set_ingest(ctx, s, 0);
     if (r) return r;
@@ -822,7 +806,7 @@ extern "C" int gbt_run_resident(gbt_ctx* ctx) {
   return run_frame(ctx);
 }
 
-extern "C" int gbt_run(gbt_ctx* ctx, const uint8_t* const* frames, const int64_t* pitches, int32_t location) {
+static int grp_run(Group* ctx, const uint8_t* const* frames, const int64_t* pitches, int32_t location) {
   if (!ctx || !frames) return GBT_E_INVALID;
   CK(cudaSetDevice(ctx->device));
   int r0 = prepare_front(ctx);
@@ -888,13 +872,13 @@ extern "C" int gbt_run(gbt_ctx* ctx, const uint8_t* const* frames, const int64_t
   return run_frame(ctx);
 }
 
-extern "C" int gbt_set_rgb_to_gray(gbt_ctx* ctx, int32_t mode) {
+static int grp_set_rgb_to_gray(Group* ctx, int32_t mode) {
   if (!ctx || (mode != GBT_RGB_CHANNEL0 && mode != GBT_RGB_BT601)) return GBT_E_INVALID;
   ctx->rgb_mode = mode;
   return GBT_OK;
 }
 
-extern "C" int gbt_sync(gbt_ctx* ctx) {
+static int grp_sync(Group* ctx) {
   if (!ctx) return GBT_E_INVALID;
   CK(cudaSetDevice(ctx->device));
   int r = sync_all(ctx);
@@ -905,31 +889,31 @@ extern "C" int gbt_sync(gbt_ctx* ctx) {
   return GBT_OK;
 }
 
-extern "C" int gbt_kernel_launches(gbt_ctx* ctx, int64_t* total) {
+static int grp_kernel_launches(Group* ctx, int64_t* total) {
   if (!ctx || !total) return GBT_E_INVALID;
   *total = ctx->kernels_total;
   return GBT_OK;
 }
 
-extern "C" int gbt_kernels_per_frame(gbt_ctx* ctx, int32_t* n) {
+static int grp_kernels_per_frame(Group* ctx, int32_t* n) {
   if (!ctx || !n) return GBT_E_INVALID;
   *n = ctx->launches_per_frame;
   return GBT_OK;
 }
 
-static int unit_of(gbt_ctx* ctx, int stream, int scale) {
+static int unit_of(Group* ctx, int stream, int scale) {
   if (!ctx || stream < 0 || stream >= (int)ctx->streams.size()) return -1;
   if (scale < 0 || scale >= ctx->streams[stream].cfg.nscales) return -1;
   return ctx->streams[stream].unit0 + scale;
 }
 
-static int read_state(gbt_ctx* ctx, int ui, UState* s) {
+static int read_state(Group* ctx, int ui, UState* s) {
   CK(cudaStreamSynchronize(ctx->stream));
   CK(cudaMemcpy(s, ctx->d_state + ui, sizeof(UState), cudaMemcpyDeviceToHost));
   return GBT_OK;
 }
 
-extern "C" int gbt_nparticles(gbt_ctx* ctx, int32_t stream, int32_t scale, int32_t* n) {
+static int grp_nparticles(Group* ctx, int32_t stream, int32_t scale, int32_t* n) {
   int ui = unit_of(ctx, stream, scale);
   if (ui < 0 || !n) return GBT_E_INVALID;
   CK(cudaSetDevice(ctx->device));
@@ -940,7 +924,7 @@ extern "C" int gbt_nparticles(gbt_ctx* ctx, int32_t stream, int32_t scale, int32
   return GBT_OK;
 }
 
-extern "C" int gbt_read_counts(gbt_ctx* ctx, int32_t* counts, int32_t n) {
+static int grp_read_counts(Group* ctx, int32_t* counts, int32_t n) {
   if (!ctx || !counts || n < (int)ctx->units.size()) return GBT_E_INVALID;
   CK(cudaSetDevice(ctx->device));
   std::vector<UState> st(ctx->units.size());
@@ -950,23 +934,13 @@ extern "C" int gbt_read_counts(gbt_ctx* ctx, int32_t* counts, int32_t n) {
   return GBT_OK;
 }
 
-extern "C" int gbt_read_counts_async(gbt_ctx* ctx, int32_t* counts, int32_t n) {
-  if (!ctx || !counts || n < (int)ctx->units.size()) return GBT_E_INVALID;
-  CK(cudaSetDevice(ctx->device));
-  const int nunits = (int)ctx->units.size();
-  k_counts<<<(nunits + 255) / 256, 256, 0, ctx->stream>>>(ctx->d_state, nunits, ctx->d_counts);
-  CK(cudaGetLastError());
-  CK(cudaMemcpyAsync(counts, ctx->d_counts, (size_t)nunits * sizeof(int32_t), cudaMemcpyDeviceToHost, ctx->stream));
-  return GBT_OK;
-}
-
-extern "C" int gbt_frame_count(gbt_ctx* ctx, int32_t stream, int32_t scale, int32_t* n) {
+static int grp_frame_count(Group* ctx, int32_t stream, int32_t scale, int32_t* n) {
   if (unit_of(ctx, stream, scale) < 0 || !n) return GBT_E_INVALID;
   *n = ctx->host_frame;
   return GBT_OK;
 }
 
-extern "C" int gbt_get_particles(gbt_ctx* ctx, int32_t stream, int32_t scale, float* speed, int16_t* pos,
+static int grp_get_particles(Group* ctx, int32_t stream, int32_t scale, float* speed, int16_t* pos,
                                  uint16_t* age, uint8_t* features, int32_t* matches, int32_t* nmatches,
                                  int32_t* compact_has_run) {
   int ui = unit_of(ctx, stream, scale);
@@ -995,7 +969,7 @@ extern "C" int gbt_get_particles(gbt_ctx* ctx, int32_t stream, int32_t scale, fl
   return GBT_OK;
 }
 
-extern "C" int gbt_get_trajectories(gbt_ctx* ctx, int32_t stream, int32_t scale, int16_t* xy, uint8_t* len,
+static int grp_get_trajectories(Group* ctx, int32_t stream, int32_t scale, int16_t* xy, uint8_t* len,
                                     int32_t* n, int32_t* history) {
   int ui = unit_of(ctx, stream, scale);
   if (ui < 0 || !n || !ctx->traj_T) return GBT_E_INVALID;
@@ -1052,14 +1026,14 @@ size_t unit_blob_bytes(const UState& s, int T) {
 }
 }  // namespace
 
-static int read_all_states(gbt_ctx* ctx, std::vector<UState>& st) {
+static int read_all_states(Group* ctx, std::vector<UState>& st) {
   st.resize(ctx->units.size());
   CK(cudaStreamSynchronize(ctx->stream));
   CK(cudaMemcpy(st.data(), ctx->d_state, st.size() * sizeof(UState), cudaMemcpyDeviceToHost));
   return GBT_OK;
 }
 
-extern "C" int gbt_checkpoint_size(gbt_ctx* ctx, size_t* bytes) {
+static int grp_checkpoint_size(Group* ctx, size_t* bytes) {
   if (!ctx || !bytes) return GBT_E_INVALID;
   CK(cudaSetDevice(ctx->device));
   std::vector<UState> st;
@@ -1071,11 +1045,11 @@ extern "C" int gbt_checkpoint_size(gbt_ctx* ctx, size_t* bytes) {
   return GBT_OK;
 }
 
-extern "C" int gbt_checkpoint_save(gbt_ctx* ctx, void* buf, size_t cap, size_t* written) {
+static int grp_checkpoint_save(Group* ctx, void* buf, size_t cap, size_t* written) {
   if (!ctx || !buf) return GBT_E_INVALID;
   CK(cudaSetDevice(ctx->device));
   size_t need;
-  int r = gbt_checkpoint_size(ctx, &need);
+  int r = grp_checkpoint_size(ctx, &need);
   if (r) return r;
   if (cap < need) return set_err(ctx, GBT_E_INVALID, "checkpoint needs %zu bytes", need);
   std::vector<UState> st;
@@ -1126,7 +1100,7 @@ extern "C" int gbt_checkpoint_save(gbt_ctx* ctx, void* buf, size_t cap, size_t* 
   return GBT_OK;
 }
 
-extern "C" int gbt_checkpoint_load(gbt_ctx* ctx, const void* buf, size_t len) {
+static int grp_checkpoint_load(Group* ctx, const void* buf, size_t len) {
   if (!ctx || !buf || len < sizeof(CkHeader)) return GBT_E_INVALID;
   CK(cudaSetDevice(ctx->device));
   const uint8_t* p = (const uint8_t*)buf;
@@ -1161,7 +1135,7 @@ extern "C" int gbt_checkpoint_load(gbt_ctx* ctx, const void* buf, size_t len) {
     }
   }
   if (T && ctx->traj_T != T) {
-    int r = gbt_trajectories_enable(ctx, T);
+    int r = grp_trajectories_enable(ctx, T);
     if (r) return r;
   }
   CK(cudaStreamSynchronize(ctx->stream));
@@ -1208,7 +1182,7 @@ extern "C" int gbt_checkpoint_load(gbt_ctx* ctx, const void* buf, size_t len) {
   return GBT_OK;
 }
 
-extern "C" int gbt_bins(gbt_ctx* ctx, int32_t stream, int32_t scale, int32_t* rows, int32_t* cols) {
+static int grp_bins(Group* ctx, int32_t stream, int32_t scale, int32_t* rows, int32_t* cols) {
   int ui = unit_of(ctx, stream, scale);
   if (ui < 0) return GBT_E_INVALID;
   if (rows) *rows = ctx->units[ui].BH;
@@ -1216,7 +1190,7 @@ extern "C" int gbt_bins(gbt_ctx* ctx, int32_t stream, int32_t scale, int32_t* ro
   return GBT_OK;
 }
 
-extern "C" int gbt_get_bins(gbt_ctx* ctx, int32_t stream, int32_t scale, float* flow, uint32_t* count,
+static int grp_get_bins(Group* ctx, int32_t stream, int32_t scale, float* flow, uint32_t* count,
                             int32_t* stat_n, int32_t* stat_speed) {
   int ui = unit_of(ctx, stream, scale);
   if (ui < 0) return GBT_E_INVALID;
@@ -1264,7 +1238,7 @@ __global__ void k_dump(const Unit* __restrict__ units, const UState* __restrict_
 }
 }  // namespace gbt
 
-extern "C" int gbt_get_stage(gbt_ctx* ctx, int32_t stream, int32_t scale, int32_t stage, int32_t border, void* out) {
+static int grp_get_stage(Group* ctx, int32_t stream, int32_t scale, int32_t stage, int32_t border, void* out) {
   int ui = unit_of(ctx, stream, scale);
   if (ui < 0 || !out || border < 0 || border > 6) return GBT_E_INVALID;
   CK(cudaSetDevice(ctx->device));
@@ -1308,7 +1282,7 @@ extern "C" int gbt_get_stage(gbt_ctx* ctx, int32_t stream, int32_t scale, int32_
   return GBT_OK;
 }
 
-extern "C" int gbt_profile_enable(gbt_ctx* ctx, int32_t enable) {
+static int grp_profile_enable(Group* ctx, int32_t enable) {
   if (!ctx) return GBT_E_INVALID;
   CK(cudaSetDevice(ctx->device));
   int r = sync_all(ctx);  // the front end changes streams
@@ -1318,11 +1292,492 @@ extern "C" int gbt_profile_enable(gbt_ctx* ctx, int32_t enable) {
   return GBT_OK;
 }
 
-extern "C" int gbt_profile_read(gbt_ctx* ctx, int32_t i, char* name, size_t len, double* total_ms, int32_t* launches) {
+static int grp_profile_read(Group* ctx, int32_t i, char* name, size_t len, double* total_ms, int32_t* launches) {
   if (!ctx) return -1;
   if (i < 0 || i >= (int)ctx->prof.size()) return (int)ctx->prof.size();
   if (name && len) snprintf(name, len, "%s", ctx->prof[i].name.c_str());
   if (total_ms) *total_ms = ctx->prof[i].ms;
   if (launches) *launches = ctx->prof[i].launches;
   return (int)ctx->prof.size();
+}
+
+// ---------------------------------------------------------------------------
+// The context: its streams split into groups, each a complete tracker over its
+// streams (units, work tables, CUDA streams, graphs).  Groups share nothing,
+// so the latency-bound stages of one group (scans, the merge replay, the tick)
+// run while another group's matcher or blurs fill the GPU.  The stream callers
+// see (gbt_stream) is `join`: every call that queues work ends with `join`
+// waiting for each group's context stream, and input the caller writes on
+// `join` is waited for by the groups.  Results do not depend on the grouping.
+struct gbt_ctx {
+  int device = 0;
+  std::vector<Group*> g;
+  std::vector<int> grp, local;             // per stream: its group and its index there
+  std::vector<std::vector<int>> members;   // per group: its streams, ascending
+  std::vector<int> nscales, unit0;         // per stream: scales, first unit (context order)
+  std::vector<int> gunit0;                 // per stream: first unit inside its group
+  int nunits = 0;
+  cudaStream_t join = nullptr;
+  std::vector<cudaEvent_t> ev;             // per group: its latest queued work
+  cudaEvent_t ev_join = nullptr;
+  bool profiling = false;                  // per-kernel timing: groups run one after another
+  std::string err;
+};
+
+#define CKO(call)                                                                              \
+  do {                                                                                         \
+    cudaError_t e_ = (call);                                                                   \
+    if (e_ != cudaSuccess) {                                                                   \
+      c->err = std::string(#call) + " failed: " + cudaGetErrorString(e_);                      \
+      return GBT_E_CUDA;                                                                       \
+    }                                                                                          \
+  } while (0)
+
+static int adopt(gbt_ctx* c, Group* g, int r) {
+  if (r && g) c->err = g->err;
+  return r;
+}
+
+static int join_groups(gbt_ctx* c) {
+  for (size_t k = 0; k < c->g.size(); k++) {
+    CKO(cudaEventRecord(c->ev[k], c->g[k]->stream));
+    CKO(cudaStreamWaitEvent(c->join, c->ev[k], 0));
+  }
+  return GBT_OK;
+}
+
+// With per-kernel timing on, group k's work waits for group k - 1's, so that
+// every event pair times one kernel alone.
+static int serialize_group(gbt_ctx* c, size_t k) {
+  if (!c->profiling || k == 0) return GBT_OK;
+  CKO(cudaEventRecord(c->ev[k - 1], c->g[k - 1]->stream));
+  CKO(cudaStreamWaitEvent(c->g[k]->stream, c->ev[k - 1], 0));
+  return GBT_OK;
+}
+
+static void free_outer(gbt_ctx* c) {
+  if (!c) return;
+  cudaSetDevice(c->device);
+  for (Group* g : c->g) grp_destroy(g);
+  for (cudaEvent_t e : c->ev)
+    if (e) cudaEventDestroy(e);
+  if (c->ev_join) cudaEventDestroy(c->ev_join);
+  if (c->join) cudaStreamDestroy(c->join);
+  delete c;
+}
+
+// Streams to groups: longest-processing-time-first by pixels per frame, ties
+// to the lower group; each group keeps its streams in ascending order.
+static void partition(const gbt_config* cfgs, int n, int G, std::vector<std::vector<int>>& members) {
+  std::vector<int> order(n);
+  for (int s = 0; s < n; s++) order[s] = s;
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+    return (long long)cfgs[a].rows * cfgs[a].cols > (long long)cfgs[b].rows * cfgs[b].cols;
+  });
+  std::vector<long long> load(G, 0);
+  members.assign(G, {});
+  for (int s : order) {
+    int k = 0;
+    for (int j = 1; j < G; j++)
+      if (load[j] < load[k]) k = j;
+    members[k].push_back(s);
+    load[k] += (long long)cfgs[s].rows * cfgs[s].cols;
+  }
+  for (auto& m : members) std::sort(m.begin(), m.end());
+}
+
+extern "C" int gbt_create_ex(const gbt_config* cfgs, int32_t nstreams, int32_t device, int32_t groups,
+                             gbt_ctx** out) {
+  if (!out) return GBT_E_INVALID;
+  *out = nullptr;
+  if (!cfgs || nstreams < 1) return GBT_E_INVALID;
+  int G = groups > 0 ? groups : 4;
+  G = std::max(1, std::min(G, (int)nstreams));
+  gbt_ctx* c = new gbt_ctx;
+  c->device = device;
+  partition(cfgs, nstreams, G, c->members);
+  c->grp.assign(nstreams, 0);
+  c->local.assign(nstreams, 0);
+  c->nscales.assign(nstreams, 0);
+  c->unit0.assign(nstreams, 0);
+  c->gunit0.assign(nstreams, 0);
+  for (int s = 0; s < nstreams; s++) {
+    c->nscales[s] = cfgs[s].nscales;
+    c->unit0[s] = c->nunits;
+    c->nunits += cfgs[s].nscales;
+  }
+  for (int k = 0; k < G; k++) {
+    std::vector<gbt_config> sub;
+    int u = 0;
+    for (size_t i = 0; i < c->members[k].size(); i++) {
+      const int s = c->members[k][i];
+      c->grp[s] = k;
+      c->local[s] = (int)i;
+      c->gunit0[s] = u;
+      u += cfgs[s].nscales;
+      sub.push_back(cfgs[s]);
+    }
+    Group* g = nullptr;
+    int r = grp_create(sub.data(), (int32_t)sub.size(), device, &g);
+    if (r) {
+      free_outer(c);
+      return r;
+    }
+    c->g.push_back(g);
+  }
+  cudaError_t e = cudaSetDevice(device);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->join, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming);
+  c->ev.assign(G, nullptr);
+  for (int k = 0; k < G && e == cudaSuccess; k++) e = cudaEventCreateWithFlags(&c->ev[k], cudaEventDisableTiming);
+  if (e != cudaSuccess) {
+    fprintf(stderr, "gbt_create: %s\n", cudaGetErrorString(e));
+    free_outer(c);
+    return GBT_E_CUDA;
+  }
+  *out = c;
+  return GBT_OK;
+}
+
+extern "C" int gbt_create(const gbt_config* cfgs, int32_t nstreams, int32_t device, gbt_ctx** out) {
+  return gbt_create_ex(cfgs, nstreams, device, 0, out);
+}
+
+extern "C" int gbt_groups(gbt_ctx* c, int32_t* groups) {
+  if (!c || !groups) return GBT_E_INVALID;
+  *groups = (int32_t)c->g.size();
+  return GBT_OK;
+}
+
+extern "C" int gbt_destroy(gbt_ctx* c) {
+  if (!c) return GBT_E_INVALID;
+  cudaSetDevice(c->device);
+  if (c->join) cudaStreamSynchronize(c->join);
+  free_outer(c);
+  return GBT_OK;
+}
+
+extern "C" int gbt_last_error(gbt_ctx* c, char* buf, size_t len) {
+  if (!c || !buf || !len) return GBT_E_INVALID;
+  snprintf(buf, len, "%s", c->err.c_str());
+  return GBT_OK;
+}
+
+extern "C" int gbt_stream(gbt_ctx* c, void** s) {
+  if (!c || !s) return GBT_E_INVALID;
+  *s = (void*)c->join;
+  return GBT_OK;
+}
+
+static bool stream_ok(const gbt_ctx* c, int32_t s) { return c && s >= 0 && s < (int32_t)c->grp.size(); }
+
+extern "C" int gbt_input_slot(gbt_ctx* c, int32_t stream, uint8_t** dptr, int64_t* pitch) {
+  if (!stream_ok(c, stream)) return GBT_E_INVALID;
+  Group* g = c->g[c->grp[stream]];
+  return adopt(c, g, grp_input_slot(g, c->local[stream], dptr, pitch));
+}
+
+extern "C" int gbt_set_tuning(gbt_ctx* c, int32_t knob, int32_t value) {
+  if (!c) return GBT_E_INVALID;
+  for (Group* g : c->g) {
+    int r = grp_set_tuning(g, knob, value);
+    if (r) return adopt(c, g, r);
+  }
+  return GBT_OK;
+}
+
+extern "C" int gbt_get_tuning(gbt_ctx* c, int32_t knob, int32_t* value) {
+  if (!c) return GBT_E_INVALID;
+  return adopt(c, c->g[0], grp_get_tuning(c->g[0], knob, value));
+}
+
+extern "C" int gbt_trajectories_enable(gbt_ctx* c, int32_t history) {
+  if (!c) return GBT_E_INVALID;
+  for (Group* g : c->g) {
+    int r = grp_trajectories_enable(g, history);
+    if (r) return adopt(c, g, r);
+  }
+  return GBT_OK;
+}
+
+extern "C" int gbt_use_graphs(gbt_ctx* c, int32_t enable) {
+  if (!c) return GBT_E_INVALID;
+  for (Group* g : c->g) grp_use_graphs(g, enable);
+  return GBT_OK;
+}
+
+extern "C" int gbt_set_rgb_to_gray(gbt_ctx* c, int32_t mode) {
+  if (!c) return GBT_E_INVALID;
+  for (Group* g : c->g) {
+    int r = grp_set_rgb_to_gray(g, mode);
+    if (r) return adopt(c, g, r);
+  }
+  return GBT_OK;
+}
+
+extern "C" int gbt_run_resident(gbt_ctx* c) {
+  if (!c) return GBT_E_INVALID;
+  CKO(cudaSetDevice(c->device));
+  CKO(cudaEventRecord(c->ev_join, c->join));  // the caller's slot writes on gbt_stream
+  for (size_t k = 0; k < c->g.size(); k++) {
+    int r = serialize_group(c, k);
+    if (!r) r = adopt(c, c->g[k], grp_run_resident(c->g[k], c->ev_join));
+    if (r) return r;
+  }
+  return join_groups(c);
+}
+
+extern "C" int gbt_run(gbt_ctx* c, const uint8_t* const* frames, const int64_t* pitches, int32_t location) {
+  if (!c || !frames) return GBT_E_INVALID;
+  CKO(cudaSetDevice(c->device));
+  for (size_t k = 0; k < c->g.size(); k++) {
+    const auto& m = c->members[k];
+    std::vector<const uint8_t*> f(m.size());
+    std::vector<int64_t> p(m.size());
+    for (size_t i = 0; i < m.size(); i++) {
+      f[i] = frames[m[i]];
+      if (pitches) p[i] = pitches[m[i]];
+    }
+    int r = serialize_group(c, k);
+    if (!r) r = adopt(c, c->g[k], grp_run(c->g[k], f.data(), pitches ? p.data() : nullptr, location));
+    if (r) return r;
+  }
+  return join_groups(c);
+}
+
+extern "C" int gbt_sync(gbt_ctx* c) {
+  if (!c) return GBT_E_INVALID;
+  int first = GBT_OK;
+  for (Group* g : c->g) {
+    int r = grp_sync(g);
+    if (r && !first) first = adopt(c, g, r);
+  }
+  CKO(cudaStreamSynchronize(c->join));
+  return first;
+}
+
+extern "C" int gbt_kernel_launches(gbt_ctx* c, int64_t* total) {
+  if (!c || !total) return GBT_E_INVALID;
+  int64_t t = 0;
+  for (Group* g : c->g) {
+    int64_t x = 0;
+    grp_kernel_launches(g, &x);
+    t += x;
+  }
+  *total = t;
+  return GBT_OK;
+}
+
+extern "C" int gbt_kernels_per_frame(gbt_ctx* c, int32_t* n) {
+  if (!c || !n) return GBT_E_INVALID;
+  int32_t t = 0;
+  for (Group* g : c->g) {
+    int32_t x = 0;
+    grp_kernels_per_frame(g, &x);
+    t += x;
+  }
+  *n = t;
+  return GBT_OK;
+}
+
+#define DISPATCH(call_with_local)                        \
+  if (!stream_ok(c, stream)) return GBT_E_INVALID;       \
+  Group* g = c->g[c->grp[stream]];                       \
+  const int32_t ls = c->local[stream];                   \
+  return adopt(c, g, call_with_local)
+
+extern "C" int gbt_nparticles(gbt_ctx* c, int32_t stream, int32_t scale, int32_t* n) {
+  DISPATCH(grp_nparticles(g, ls, scale, n));
+}
+
+extern "C" int gbt_frame_count(gbt_ctx* c, int32_t stream, int32_t scale, int32_t* n) {
+  DISPATCH(grp_frame_count(g, ls, scale, n));
+}
+
+extern "C" int gbt_get_particles(gbt_ctx* c, int32_t stream, int32_t scale, float* speed, int16_t* pos,
+                                 uint16_t* age, uint8_t* features, int32_t* matches, int32_t* nmatches,
+                                 int32_t* compact_has_run) {
+  DISPATCH(grp_get_particles(g, ls, scale, speed, pos, age, features, matches, nmatches, compact_has_run));
+}
+
+extern "C" int gbt_get_trajectories(gbt_ctx* c, int32_t stream, int32_t scale, int16_t* xy, uint8_t* len,
+                                    int32_t* n, int32_t* history) {
+  DISPATCH(grp_get_trajectories(g, ls, scale, xy, len, n, history));
+}
+
+extern "C" int gbt_bins(gbt_ctx* c, int32_t stream, int32_t scale, int32_t* rows, int32_t* cols) {
+  DISPATCH(grp_bins(g, ls, scale, rows, cols));
+}
+
+extern "C" int gbt_get_bins(gbt_ctx* c, int32_t stream, int32_t scale, float* flow, uint32_t* count,
+                            int32_t* stat_n, int32_t* stat_speed) {
+  DISPATCH(grp_get_bins(g, ls, scale, flow, count, stat_n, stat_speed));
+}
+
+extern "C" int gbt_get_stage(gbt_ctx* c, int32_t stream, int32_t scale, int32_t stage, int32_t border, void* out) {
+  DISPATCH(grp_get_stage(g, ls, scale, stage, border, out));
+}
+
+extern "C" int gbt_read_counts(gbt_ctx* c, int32_t* counts, int32_t n) {
+  if (!c || !counts || n < c->nunits) return GBT_E_INVALID;
+  for (size_t k = 0; k < c->g.size(); k++) {
+    Group* g = c->g[k];
+    std::vector<int32_t> tmp(g->units.size());
+    int r = grp_read_counts(g, tmp.data(), (int32_t)tmp.size());
+    if (r) return adopt(c, g, r);
+    for (int s : c->members[k])
+      for (int l = 0; l < c->nscales[s]; l++) counts[c->unit0[s] + l] = tmp[c->gunit0[s] + l];
+  }
+  return GBT_OK;
+}
+
+extern "C" int gbt_read_counts_async(gbt_ctx* c, int32_t* counts, int32_t n) {
+  if (!c || !counts || n < c->nunits) return GBT_E_INVALID;
+  CKO(cudaSetDevice(c->device));
+  for (size_t k = 0; k < c->g.size(); k++) {
+    Group* g = c->g[k];
+    const int nu = (int)g->units.size();
+    k_counts<<<(nu + 255) / 256, 256, 0, g->stream>>>(g->d_state, nu, g->d_counts);
+    CKO(cudaGetLastError());
+    for (int s : c->members[k])
+      CKO(cudaMemcpyAsync(counts + c->unit0[s], g->d_counts + c->gunit0[s], (size_t)c->nscales[s] * sizeof(int32_t),
+                          cudaMemcpyDeviceToHost, g->stream));
+  }
+  return join_groups(c);
+}
+
+// Checkpoint of a grouped context: a header with the grouping, then each
+// group's blob (its own header, configurations and units) with its size.
+namespace {
+const char CKG_MAGIC[8] = {'G', 'B', 'T', 'C', 'K', 'P', 'G', '1'};
+struct CkgHeader {
+  char magic[8];
+  int32_t version, ngroups, nstreams, pad;
+};
+}  // namespace
+
+extern "C" int gbt_checkpoint_size(gbt_ctx* c, size_t* bytes) {
+  if (!c || !bytes) return GBT_E_INVALID;
+  size_t b = sizeof(CkgHeader) + c->grp.size() * sizeof(int32_t) + c->g.size() * sizeof(uint64_t);
+  for (Group* g : c->g) {
+    size_t x = 0;
+    int r = grp_checkpoint_size(g, &x);
+    if (r) return adopt(c, g, r);
+    b += x;
+  }
+  *bytes = b;
+  return GBT_OK;
+}
+
+extern "C" int gbt_checkpoint_save(gbt_ctx* c, void* buf, size_t cap, size_t* written) {
+  if (!c || !buf) return GBT_E_INVALID;
+  size_t need = 0;
+  int r = gbt_checkpoint_size(c, &need);
+  if (r) return r;
+  if (cap < need) return GBT_E_INVALID;
+  uint8_t* p = (uint8_t*)buf;
+  CkgHeader h{};
+  memcpy(h.magic, CKG_MAGIC, 8);
+  h.version = 1;
+  h.ngroups = (int32_t)c->g.size();
+  h.nstreams = (int32_t)c->grp.size();
+  memcpy(p, &h, sizeof h);
+  p += sizeof h;
+  for (int s = 0; s < h.nstreams; s++) {
+    const int32_t k = c->grp[s];
+    memcpy(p, &k, sizeof k);
+    p += sizeof k;
+  }
+  for (Group* g : c->g) {
+    size_t x = 0, w = 0;
+    if ((r = grp_checkpoint_size(g, &x))) return adopt(c, g, r);
+    const uint64_t x64 = x;
+    memcpy(p, &x64, sizeof x64);
+    p += sizeof x64;
+    if ((r = grp_checkpoint_save(g, p, x, &w))) return adopt(c, g, r);
+    p += x;
+  }
+  if (written) *written = (size_t)(p - (uint8_t*)buf);
+  return GBT_OK;
+}
+
+extern "C" int gbt_checkpoint_load(gbt_ctx* c, const void* buf, size_t len) {
+  if (!c || !buf || len < sizeof(CkgHeader)) return GBT_E_INVALID;
+  const uint8_t* p = (const uint8_t*)buf;
+  const uint8_t* end = p + len;
+  CkgHeader h;
+  memcpy(&h, p, sizeof h);
+  p += sizeof h;
+  if (memcmp(h.magic, CKG_MAGIC, 8) != 0 || h.version != 1 || h.ngroups != (int32_t)c->g.size() ||
+      h.nstreams != (int32_t)c->grp.size() || (size_t)(end - p) < (size_t)h.nstreams * sizeof(int32_t)) {
+    c->err = "checkpoint does not belong to a context of this shape";
+    return GBT_E_INVALID;
+  }
+  for (int s = 0; s < h.nstreams; s++) {
+    int32_t k;
+    memcpy(&k, p, sizeof k);
+    p += sizeof k;
+    if (k != c->grp[s]) {
+      c->err = "checkpoint groups its streams differently";
+      return GBT_E_INVALID;
+    }
+  }
+  // Every group's blob is checked by its own loader before it changes anything;
+  // first make sure all the blobs are there.
+  std::vector<std::pair<const uint8_t*, size_t>> blobs;
+  for (size_t k = 0; k < c->g.size(); k++) {
+    uint64_t x;
+    if ((size_t)(end - p) < sizeof x) return GBT_E_INVALID;
+    memcpy(&x, p, sizeof x);
+    p += sizeof x;
+    if ((uint64_t)(end - p) < x) return GBT_E_INVALID;
+    blobs.push_back({p, (size_t)x});
+    p += x;
+  }
+  for (size_t k = 0; k < c->g.size(); k++) {
+    int r = grp_checkpoint_load(c->g[k], blobs[k].first, blobs[k].second);
+    if (r) return adopt(c, c->g[k], r);
+  }
+  return GBT_OK;
+}
+
+extern "C" int gbt_profile_enable(gbt_ctx* c, int32_t enable) {
+  if (!c) return GBT_E_INVALID;
+  for (Group* g : c->g) {
+    int r = grp_profile_enable(g, enable);
+    if (r) return adopt(c, g, r);
+  }
+  c->profiling = enable != 0;
+  return GBT_OK;
+}
+
+// Per-kernel entries of all groups, merged by kernel name (first-seen order).
+extern "C" int gbt_profile_read(gbt_ctx* c, int32_t i, char* name, size_t len, double* total_ms, int32_t* launches) {
+  if (!c) return -1;
+  std::vector<std::string> names;
+  std::vector<double> ms;
+  std::vector<int> cnt;
+  char nb[128];
+  for (Group* g : c->g) {
+    double t;
+    int32_t n;
+    const int m = grp_profile_read(g, -1, nullptr, 0, nullptr, nullptr);
+    for (int k = 0; k < m; k++) {
+      grp_profile_read(g, k, nb, sizeof nb, &t, &n);
+      size_t j = 0;
+      while (j < names.size() && names[j] != nb) j++;
+      if (j == names.size()) {
+        names.push_back(nb);
+        ms.push_back(0);
+        cnt.push_back(0);
+      }
+      ms[j] += t;
+      cnt[j] += n;
+    }
+  }
+  if (i < 0 || i >= (int)names.size()) return (int)names.size();
+  if (name && len) snprintf(name, len, "%s", names[i].c_str());
+  if (total_ms) *total_ms = ms[i];
+  if (launches) *launches = cnt[i];
+  return (int)names.size();
 }

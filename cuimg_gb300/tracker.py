@@ -148,7 +148,8 @@ class _ScaleSetter:
 class BatchTracker:
     """Many independent streams advanced one frame per run() call."""
 
-    def __init__(self, configs, device=0, graphs=False):
+    def __init__(self, configs, device=0, graphs=False, groups=0):
+        """groups: stream groups (gbt_create_ex; 0 = the library's default)."""
         self._lib = cuda_lib()
         self._cfgs = []
         for c in configs:
@@ -160,6 +161,7 @@ class BatchTracker:
             self._cfgs.append(cfg)
         self._device = device
         self._graphs = graphs
+        self._groups = groups
         self._ctx = None
         self.nstreams = len(self._cfgs)
 
@@ -175,7 +177,7 @@ class BatchTracker:
         if self._ctx is None:
             arr = (gbt_config * self.nstreams)(*self._cfgs)
             ctx = ctypes.c_void_p()
-            code = self._lib.gbt_create(arr, self.nstreams, self._device, ctypes.byref(ctx))
+            code = self._lib.gbt_create_ex(arr, self.nstreams, self._device, self._groups, ctypes.byref(ctx))
             if code:
                 raise GbtError(code, "gbt_create failed (sizes ok: %s)" % [
                     sizes_ok(c.rows, c.cols, c.nscales) for c in self._cfgs])
@@ -250,6 +252,12 @@ class BatchTracker:
     def kernels_per_frame(self):
         n = ctypes.c_int32()
         check(self._lib.gbt_kernels_per_frame(self._ensure(), ctypes.byref(n)), self._ctx)
+        return n.value
+
+    def groups(self):
+        """Stream groups of the context (each runs on its own CUDA streams)."""
+        n = ctypes.c_int32()
+        check(self._lib.gbt_groups(self._ensure(), ctypes.byref(n)), self._ctx)
         return n.value
 
     def kernel_launches(self):

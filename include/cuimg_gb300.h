@@ -81,6 +81,15 @@ int gbt_sizes_ok(int32_t rows, int32_t cols, int32_t nscales);
  * its own configuration and resolution) by one frame per gbt_run call.
  * Replaces constructing one tracker<F> per stream (tracker.hpp:11-26). */
 int gbt_create(const gbt_config* cfgs, int32_t nstreams, int32_t device, gbt_ctx** out);
+
+/* The same with the number of stream groups chosen by the caller (0: the
+ * default, min(4, nstreams)).  The streams are split into groups balanced by
+ * pixels per frame; each group is a complete tracker over its streams with its
+ * own device buffers, CUDA streams and graphs, so the latency-bound stages of
+ * one group run while another group's matcher or blurs fill the GPU.  Results
+ * do not depend on the grouping.  No counterpart in the reference. */
+int gbt_create_ex(const gbt_config* cfgs, int32_t nstreams, int32_t device, int32_t groups, gbt_ctx** out);
+int gbt_groups(gbt_ctx* ctx, int32_t* groups);
 int gbt_destroy(gbt_ctx* ctx);
 
 /* Message of the last error on this context (NUL-terminated). */
@@ -126,10 +135,12 @@ int gbt_use_graphs(gbt_ctx* ctx, int32_t enable);
  * device-side check failed since the last call. */
 int gbt_sync(gbt_ctx* ctx);
 
-/* The CUDA stream (cudaStream_t) the context orders its work on: when a
- * frame's last kernel on it has run, the whole frame is done.  (Each frame's
- * input copy, pyramid and blurs run on a second, internal stream, overlapping
- * the previous frame's matching and filtering.) */
+/* The CUDA stream (cudaStream_t) that follows the context's work: after every
+ * call that queues work it waits for all of that work, so an event recorded
+ * on it (or work queued on it) comes after the frames queued so far, and input
+ * the caller writes on it is waited for.  (Each stream group works on its own
+ * internal streams; a frame's input copy, pyramid and blurs overlap the
+ * previous frame's matching and filtering.) */
 int gbt_stream(gbt_ctx* ctx, void** cuda_stream);
 
 /* Particle set of (stream, scale): dense slot count (tombstones included,

@@ -124,11 +124,14 @@ def test_graph_replay_matches_oracle():
     _compare_run(240, 320, 3, 14, 4, detf=3, graphs=True)
 
 
-def test_batched_uneven_streams_match_per_stream_oracles():
+@pytest.mark.parametrize("groups", [1, 2, 0])
+def test_batched_uneven_streams_match_per_stream_oracles(groups):
+    # groups: the context's stream groups (0 = the default, here one per stream).
     from cuimg_gb300 import BatchTracker, synth
     shapes = [(240, 320, 3), (480, 640, 3), (135, 201, 2), (360, 480, 4)]
     cfgs = [dict(rows=r, cols=c, nscales=L, detector_threshold=20, detector_frequency=4) for r, c, L in shapes]
-    bt = BatchTracker(cfgs, graphs=True)
+    bt = BatchTracker(cfgs, graphs=True, groups=groups)
+    assert bt.groups() == (groups or 4)
     streams = [synth.Stream(100 + i, r, c) for i, (r, c, L) in enumerate(shapes)]
     oracles = [tracker_oracle(r, c, L, 20, 4, 1) for r, c, L in shapes]
     for t in range(9):
@@ -138,6 +141,27 @@ def test_batched_uneven_streams_match_per_stream_oracles():
             oracles[i].run(frames[i])
             bad = diff_snapshots(snapshot(oracles[i], L), bt.snapshot(i), detector_frame=(t % 4 == 0))
             assert not bad, "stream %d frame %d: %s" % (i, t, bad)
+    bt.close()
+
+
+def test_counts_read_sync_and_async_agree_across_groups():
+    import ctypes
+    from cuimg_gb300 import BatchTracker, synth
+    from cuimg_gb300._native import check
+    shapes = [(240, 320, 3), (120, 160, 2), (480, 640, 4)]
+    cfgs = [dict(rows=r, cols=c, nscales=L, detector_threshold=20, detector_frequency=3) for r, c, L in shapes]
+    bt = BatchTracker(cfgs, graphs=True, groups=2)
+    streams = [synth.Stream(300 + i, r, c) for i, (r, c, L) in enumerate(shapes)]
+    for t in range(7):
+        bt.run([s.frame(t) for s in streams])
+    n = sum(L for _, _, L in shapes)
+    a = np.zeros(n, np.int32)
+    b = np.full(n, -1, np.int32)
+    check(bt._lib.gbt_read_counts(bt._ctx, a.ctypes.data, n), bt._ctx)
+    check(bt._lib.gbt_read_counts_async(bt._ctx, b.ctypes.data, n), bt._ctx)
+    bt.sync()
+    want = [bt.nparticles(s, l) for s, (_, _, L) in enumerate(shapes) for l in range(L)]
+    assert a.tolist() == want and b.tolist() == want
     bt.close()
 
 
