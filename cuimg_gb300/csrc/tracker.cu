@@ -107,6 +107,7 @@ struct Group {
   int front_launches = 0;       // kernels in a captured front-end graph
   long long kernels_total = 0;  // kernels launched by this context, graph nodes included
   int match_variant = 0;  // GBT_TUNE_MATCHER
+  int mt_shape = 3;       // GBT_TUNE_MATCH_TILE: tiled matcher threads and particle assignment
   bool fixed_fpitch = true;  // every unit's s1/s2 pitch is FIXED_FPITCH
   bool any_alt_detector = false;  // a stream uses the regular or the dense detector
   std::string err;
@@ -584,7 +585,15 @@ static int enqueue_back(Group* ctx, bool any_det, bool any_filt, int par, int& n
     { PROF("k_mt_count"); k_mt_bin<0><<<pgrid, CHUNK, 0, st>>>(du, ctx->d_state, ctx->d_pre, nunits, ctx->d_mt_cnt, ctx->d_mt_key, nullptr, nullptr); }
     { PROF("k_mt_scan"); k_mt_scan<<<1, 1024, 0, st>>>(ctx->d_mt_cnt, ctx->mt_tiles, ctx->d_mt_off); }
     { PROF("k_mt_scatter"); k_mt_bin<1><<<pgrid, CHUNK, 0, st>>>(du, ctx->d_state, ctx->d_pre, nunits, nullptr, ctx->d_mt_key, ctx->d_mt_off, ctx->d_mt_list); }
-    { PROF("k_match_tiled"); k_match_tiled<<<ctx->mt_tiles, MT_THREADS, 0, st>>>(du, ctx->d_state, ctx->d_frame, ctx->d_mt_prefix, nunits, ctx->d_mt_off, ctx->d_mt_list); }
+    PROF("k_match_tiled");
+    if (ctx->mt_shape == 1)
+      k_match_tiled<128, true, 8><<<ctx->mt_tiles, 128, 0, st>>>(du, ctx->d_state, ctx->d_frame, ctx->d_mt_prefix, nunits, ctx->d_mt_off, ctx->d_mt_list);
+    else if (ctx->mt_shape == 2)
+      k_match_tiled<64, true, 10><<<ctx->mt_tiles, 64, 0, st>>>(du, ctx->d_state, ctx->d_frame, ctx->d_mt_prefix, nunits, ctx->d_mt_off, ctx->d_mt_list);
+    else if (ctx->mt_shape == 3)
+      k_match_tiled<256, true, 4><<<ctx->mt_tiles, 256, 0, st>>>(du, ctx->d_state, ctx->d_frame, ctx->d_mt_prefix, nunits, ctx->d_mt_off, ctx->d_mt_list);
+    else
+      k_match_tiled<MT_THREADS, false, 4><<<ctx->mt_tiles, MT_THREADS, 0, st>>>(du, ctx->d_state, ctx->d_frame, ctx->d_mt_prefix, nunits, ctx->d_mt_off, ctx->d_mt_list);
     n += 4;
   } else if (ctx->match_variant == 1) {
     PROF("k_match_warp");
@@ -723,6 +732,11 @@ static int grp_set_tuning(Group* ctx, int32_t knob, int32_t value) {
     ctx->blur_tiles = ctx->blur_tiles_v[v];
     return GBT_OK;
   }
+  if (knob == GBT_TUNE_MATCH_TILE && value >= 0 && value <= 3) {
+    if (ctx->mt_shape != value) drop_graphs(ctx);
+    ctx->mt_shape = value;
+    return GBT_OK;
+  }
   return GBT_E_INVALID;
 }
 
@@ -734,6 +748,10 @@ static int grp_get_tuning(Group* ctx, int32_t knob, int32_t* value) {
   }
   if (knob == GBT_TUNE_BLUR_ROWS) {
     *value = ctx->blur_rows;
+    return GBT_OK;
+  }
+  if (knob == GBT_TUNE_MATCH_TILE) {
+    *value = ctx->mt_shape;
     return GBT_OK;
   }
   return GBT_E_INVALID;

@@ -433,8 +433,7 @@ __device__ __forceinline__ void match_finish(const Unit& u, const FeatT& F, int 
 
 template <class FeatT>
 __device__ __forceinline__ void match_one(const Unit& u, const FeatT& F, int f, int b, int i, unsigned short age,
-                                          short2 pos, int pr, int pc) {
-  const uint4 feat = u.feat[b][i];
+                                          short2 pos, int pr, int pc, const uint4& feat) {
   int d1r, d1c, d2r, d2c;
   // Step 1 compares s2-only candidates against the s1+s2 distance at the
   // prediction.  Step 2 starts from step 1's match with its s1+s2 distance:
@@ -509,7 +508,7 @@ __global__ void __launch_bounds__(MATCH_BLOCK) k_match(const Unit* __restrict__ 
     }
     FeatT F;
     F.init(u);
-    match_one(u, F, f, b, i, age, pos, pr, pc);
+    match_one(u, F, f, b, i, age, pos, pr, pc, u.feat[b][i]);
   }
 }
 
@@ -627,7 +626,7 @@ __device__ __forceinline__ void cp_async16(void* sdst, const void* gsrc) {
 // Stages rows R0s .. R0s + MT_SR - 1 and columns C0s .. C0s + MT_SC - 1 of s1
 // and s2, skipping chunks outside the bordered images (never sampled: the taps
 // stay within 6 pixels of the domain, inside the zero border).
-__device__ __forceinline__ void mt_stage(const Unit& u, int R0s, int C0s, uint8_t* ts1, uint8_t* ts2) {
+__device__ __forceinline__ void mt_stage_issue(const Unit& u, int R0s, int C0s, uint8_t* ts1, uint8_t* ts2) {
   constexpr int CPR = MT_SC / 16;
   for (int v = threadIdx.x; v < MT_SR * CPR; v += blockDim.x) {
     const int row = v / CPR, ck = v % CPR;
@@ -639,17 +638,21 @@ __device__ __forceinline__ void mt_stage(const Unit& u, int R0s, int C0s, uint8_
     cp_async16(&ts2[row * MT_SC + 16 * ck], u.s2 + go);
   }
   asm volatile("cp.async.commit_group;\n" ::: "memory");
-  asm volatile("cp.async.wait_group 0;\n" ::: "memory");
 }
 
-__global__ void __launch_bounds__(MT_THREADS, 4) k_match_tiled(const Unit* __restrict__ units,
-                                                            const UState* __restrict__ st,
-                                                            const Frame* __restrict__ fr,
-                                                            const int* __restrict__ tile_prefix, int nunits,
-                                                            const int* __restrict__ off,
-                                                            const int* __restrict__ list) {
+// THREADS per CTA; with DYN the threads take the tile's particles one at a
+// time from a shared counter (a thread that finishes a short descent takes the
+// next particle) instead of every THREADS-th one.
+template <int THREADS, bool DYN, int MINB>
+__global__ void __launch_bounds__(THREADS, MINB) k_match_tiled(const Unit* __restrict__ units,
+                                                               const UState* __restrict__ st,
+                                                               const Frame* __restrict__ fr,
+                                                               const int* __restrict__ tile_prefix, int nunits,
+                                                               const int* __restrict__ off,
+                                                               const int* __restrict__ list) {
   __shared__ __align__(16) uint8_t ts1[MT_SR * MT_SC];
   __shared__ __align__(16) uint8_t ts2[MT_SR * MT_SC];
+  __shared__ int next;
   const int t = blockIdx.x;
   const int n0 = off[t], n1 = off[t + 1];
   if (n0 == n1) return;
@@ -657,20 +660,40 @@ __global__ void __launch_bounds__(MT_THREADS, 4) k_match_tiled(const Unit* __res
   const Unit& u = units[ui];
   const int local = t - tile_prefix[ui];
   const int R0s = (local / u.MTC) * MT_R - MT_MR, C0s = (local % u.MTC) * MT_C - MT_MC;
-  mt_stage(u, R0s, C0s, ts1, ts2);
-  __syncthreads();
+  if (DYN && threadIdx.x == 0) next = n0 + THREADS;
+  mt_stage_issue(u, R0s, C0s, ts1, ts2);
+  // The thread's first particle is read while the tile arrives.
   const int f = fr->f;
   const int b = st[ui].cur;
+  int k = n0 + threadIdx.x;
+  int i = 0;
+  unsigned short age = 0;
+  short2 pos = make_short2(0, 0), spd = make_short2(0, 0);
+  uint4 feat = make_uint4(0, 0, 0, 0);
+  if (k < n1) {
+    i = list[k];
+    age = u.age[b][i];
+    pos = u.pos[b][i];
+    spd = u.spd[b][i];
+    feat = u.feat[b][i];
+  }
+  asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+  __syncthreads();
   FeatFP<MT_SC> F;
   F.s1 = ts1 - (R0s * MT_SC + C0s);  // F.s1 + (r * MT_SC + c) is staged pixel (r, c)
   F.s2 = ts2 - (R0s * MT_SC + C0s);
-  for (int k = n0 + threadIdx.x; k < n1; k += MT_THREADS) {
-    const int i = list[k];
-    const unsigned short age = u.age[b][i];
-    const short2 pos = u.pos[b][i];
+  while (k < n1) {
     int pr, pc;
-    predict(age, pos, u.spd[b][i], pr, pc);
-    match_one(u, F, f, b, i, age, pos, pr, pc);
+    predict(age, pos, spd, pr, pc);
+    match_one(u, F, f, b, i, age, pos, pr, pc, feat);
+    k = DYN ? atomicAdd(&next, 1) : k + THREADS;
+    if (k < n1) {
+      i = list[k];
+      age = u.age[b][i];
+      pos = u.pos[b][i];
+      spd = u.spd[b][i];
+      feat = u.feat[b][i];
+    }
   }
 }
 

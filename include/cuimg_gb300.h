@@ -224,11 +224,15 @@ int gbt_checkpoint_load(gbt_ctx* ctx, const void* buf, size_t len);
  * thread per particle with compile-time ring offsets.  0 and 3 need every
  * stream to be at most 4064 pixels wide (fixed s1/s2 pitch) and fall back to 2
  * otherwise.
- * GBT_TUNE_BLUR_ROWS: height of the strip one warp walks in the BC2S blur.  The package's
+ * GBT_TUNE_BLUR_ROWS: height of the strip one warp walks in the BC2S blur.
+ * GBT_TUNE_MATCH_TILE (matcher 0 only): 0 = 256 threads per tile CTA, each
+ * taking every 256th particle of the tile; 1 / 2 / 3 = 128 / 64 / 256 threads
+ * taking the tile's particles one at a time from a shared counter.  The package's
  * autotuner (cuimg_gb300/autotune.py) times the settings on the caller's
  * workload and caches the winner. */
 #define GBT_TUNE_MATCHER 0
 #define GBT_TUNE_BLUR_ROWS 1   /* rows per warp strip of the BC2S blur: 16, 32 or 64 */
+#define GBT_TUNE_MATCH_TILE 2  /* tiled matcher CTA shape: 0..3 */
 int gbt_set_tuning(gbt_ctx* ctx, int32_t knob, int32_t value);
 int gbt_get_tuning(gbt_ctx* ctx, int32_t knob, int32_t* value);
 
