@@ -165,6 +165,47 @@ def test_counts_read_sync_and_async_agree_across_groups():
     bt.close()
 
 
+@pytest.mark.parametrize("graphs", [True, False])
+def test_resident_input_slots_alternate_and_match_gbt_run(graphs):
+    # Frames written by the caller into the input slots (on the context stream)
+    # and run with gbt_run_resident give the same tracks as gbt_run; the slot
+    # of the next frame alternates between two buffers (frame pipeline).
+    torch = pytest.importorskip("torch")
+    from cuimg_gb300 import BatchTracker, synth
+    shapes = [(240, 320, 3), (120, 160, 2), (200, 300, 3)]
+    cfgs = [dict(rows=r, cols=c, nscales=L, detector_threshold=20, detector_frequency=3) for r, c, L in shapes]
+    a = BatchTracker(cfgs, graphs=graphs, groups=2)
+    b = BatchTracker(cfgs, graphs=graphs, groups=2)
+    streams = [synth.Stream(500 + i, r, c) for i, (r, c, L) in enumerate(shapes)]
+    stream = torch.cuda.ExternalStream(b.cuda_stream())
+    import ctypes
+    from cuimg_gb300._native import cuda_lib
+    memcpy2d = cuda_lib().cudaMemcpy2DAsync  # the runtime the library links
+    memcpy2d.argtypes = [ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_size_t,
+                         ctypes.c_size_t, ctypes.c_int, ctypes.c_void_p]
+    slots = []
+    for t in range(8):
+        frames = [s.frame(t) for s in streams]
+        a.run(frames)
+        with torch.cuda.stream(stream):
+            for k, f in enumerate(frames):
+                ptr, pitch = b.input_slot(k)
+                if k == 0:
+                    slots.append(ptr)
+                h, w = f.shape
+                src = torch.from_numpy(f).to("cuda")
+                torch.cuda.current_stream().synchronize()
+                # Into the pitched slot, ordered on the context stream (cudaMemcpyDeviceToDevice = 3).
+                assert memcpy2d(ptr, pitch, src.data_ptr(), w, w, h, 3, stream.cuda_stream) == 0
+        b.run_resident()
+        for k, (r, c, L) in enumerate(shapes):
+            bad = diff_snapshots(a.snapshot(k), b.snapshot(k), detector_frame=(t % 3 == 0))
+            assert not bad, "stream %d frame %d: %s" % (k, t, bad)
+    assert slots[0] != slots[1] and slots[0] == slots[2]
+    a.close()
+    b.close()
+
+
 def test_rgb_input_tracks_channel_zero():
     from cuimg_gb300 import synth
     s = synth.Stream(7, 120, 160)
