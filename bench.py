@@ -553,13 +553,23 @@ def measure_extras(args, dev, local, peak):
                              "f32_5lvl_9x9_10it": {"ms": round(ms, 3), "points_per_s": round(P * n / (ms / 1000))},
                              "u8_3lvl_11x11_30it_top25": {"ms": round(ms8, 3),
                                                           "points_per_s": round(P * n / (ms8 / 1000))}}
-    # Adjoint: forward + backward (pyramids recomputed) on the same batch.
+    # Adjoint: forward recording the tape, backward reading it (pyramids
+    # recomputed by both); the backward without a tape replays the forward.
     U0 = torch.from_numpy(rng.uniform(-2, 2, (P, n, 2)).astype(np.float32)).to(dev)
     ones = torch.ones((P, n), device=dev)
-    msf = _events_ms(lambda: lkd.forward(A, Bt, U0, X, 5, 9, 10), 3, stream)
-    msb = _events_ms(lambda: lkd.backward(A, Bt, U0, X, ones, 5, 9, 10), 3, stream)
+    tape = [None]
+
+    def fwd():
+        tape[0] = lkd.forward(A, Bt, U0, X, 5, 9, 10, tape=True)[2]
+
+    msf = _events_ms(fwd, 3, stream)
+    msb = _events_ms(lambda: lkd.backward(A, Bt, U0, X, ones, 5, 9, 10, tape=tape[0]), 3, stream)
+    msr = _events_ms(lambda: lkd.backward(A, Bt, U0, X, ones, 5, 9, 10), 3, stream)
     out["lk_adjoint_640x480_x16"] = {"forward_ms": round(msf, 3), "backward_ms": round(msb, 3),
+                                     "backward_replay_ms": round(msr, 3),
+                                     "tape_bytes": tape[0].numel(),
                                      "pairs_per_s": round(P / ((msf + msb) / 1000), 1)}
+    del tape
     del A, Bt, X, A8, B8, U0, x, y
     # Batched uneven streams: 64 streams drawn from five resolutions.
     shapes = [(240, 320, 3), (480, 640, 3), (720, 1280, 4), (1080, 1920, 4), (2160, 3840, 5)]
@@ -639,8 +649,8 @@ def measure_extras(args, dev, local, peak):
             a, b = d4[t - 1].float()[None], d4[t].float()[None]
             torch.cuda.synchronize()
             t0 = time.perf_counter()
-            lkd.forward(a, b, u4, pts4, 5, 9, 10)
-            lkd.backward(a, b, u4, pts4, ones4, 5, 9, 10)
+            tp = lkd.forward(a, b, u4, pts4, 5, 9, 10, tape=True)[2]
+            lkd.backward(a, b, u4, pts4, ones4, 5, 9, 10, tape=tp)
             torch.cuda.synchronize()
             t_adj += time.perf_counter() - t0
     nt = n4 - 10

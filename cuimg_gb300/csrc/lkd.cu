@@ -220,7 +220,7 @@ __device__ __forceinline__ void rhs(const Lvl& e, int /*window: WS*/, const Tmpl
 // Forward of one point; fills the per-level setup and the iterate history.
 template <int WS>
 __device__ float point_forward(const Lvl* lv, int L, int /*window: WS*/, int K, float p0, float p1, float u0, float u1,
-                               Setup* su, float4* hist, float& vf0, float& vf1) {
+                               Setup* su, float4* hist, int hs, float& vf0, float& vf1) {
   constexpr int ws = WS, PPL = (WS * WS + 31) / 32;
   const int n = ws * ws;
   const float top = level_scale(L - 1);
@@ -239,11 +239,11 @@ __device__ float point_forward(const Lvl* lv, int L, int /*window: WS*/, int K, 
     for (int k = 0; k < K; k++) {
       float b0, b1;
       rhs<WS>(e, ws, T, v0, v1, b0, b1);
-      if (hist) hist[l * (MAXK + 1) + k] = make_float4(v0, v1, b0, b1);  // iterate and its right-hand side
+      if (hist) hist[l * hs + k] = make_float4(v0, v1, b0, b1);  // iterate and its right-hand side
       v0 += M00 * b0 + M01 * b1;
       v1 += M01 * b0 + M11 * b1;
     }
-    if (hist) hist[l * (MAXK + 1) + K] = make_float4(v0, v1, 0.f, 0.f);
+    if (hist) hist[l * hs + K] = make_float4(v0, v1, 0.f, 0.f);
     d0 = 2.f * (v0 - q0);
     d1 = 2.f * (v1 - q1);
   }
@@ -265,22 +265,50 @@ __device__ float point_forward(const Lvl* lv, int L, int /*window: WS*/, int K, 
   return wsum(loss);
 }
 
+// Tape of one point (gbt_lkd_forward_tape / gbt_lkd_backward_tape): the
+// iterate history hist[L][K + 1] (float4: v, then the step's right-hand side
+// b), the per-level setup su[L], the final position; stride tape_stride.
+__host__ __device__ inline long long tape_stride(int L, int K) {
+  return ((long long)16 * L * (K + 1) + (long long)sizeof(Setup) * L + 8 + 15) / 16 * 16;
+}
+struct TapeView {
+  float4* hist;
+  Setup* su;
+  float* vf;
+};
+__device__ __forceinline__ TapeView tape_at(void* tape, long long g, int L, int K) {
+  char* b = (char*)tape + g * tape_stride(L, K);
+  TapeView t;
+  t.hist = (float4*)b;
+  t.su = (Setup*)(b + 16 * L * (K + 1));
+  t.vf = (float*)(b + 16 * L * (K + 1) + sizeof(Setup) * L);
+  return t;
+}
+
 template <int WS>
 __global__ void __launch_bounds__(32 * WARPS) k_lkd_forward(const Lvl* __restrict__ levels, int L, int /*window: WS*/, int K,
                                                             int npairs, int npts, const float* __restrict__ pts,
                                                             const float* __restrict__ u0, float* __restrict__ loss,
-                                                            float* __restrict__ vfinal) {
+                                                            float* __restrict__ vfinal, void* __restrict__ tape) {
   constexpr int ws = WS;
   const long long g = (long long)blockIdx.x * WARPS + (threadIdx.x >> 5);
   if (g >= (long long)npairs * npts) return;
   const int pair = (int)(g / npts);
   float vf0, vf1;
+  // Every lane holds the same values; the tape stores of the 32 lanes go to
+  // one address each.
+  TapeView t{nullptr, nullptr, nullptr};
+  if (tape) t = tape_at(tape, g, L, K);
   float l = point_forward<WS>(levels + (size_t)pair * L, L, ws, K, pts[2 * g], pts[2 * g + 1], u0[2 * g],
-                               u0[2 * g + 1], nullptr, nullptr, vf0, vf1);
+                               u0[2 * g + 1], t.su, t.hist, K + 1, vf0, vf1);
   if ((threadIdx.x & 31) == 0) {
     loss[g] = l;
     vfinal[2 * g] = vf0;
     vfinal[2 * g + 1] = vf1;
+    if (tape) {
+      t.vf[0] = vf0;
+      t.vf[1] = vf1;
+    }
   }
 }
 
@@ -342,7 +370,8 @@ template <int WS>
 __global__ void __launch_bounds__(32 * WARPS, 4) k_lkd_backward(const Lvl* __restrict__ levels, int L, int /*window: WS*/, int K,
                                                              int npairs, int npts, const float* __restrict__ pts,
                                                              const float* __restrict__ u0,
-                                                             const float* __restrict__ dloss, float* __restrict__ du0) {
+                                                             const float* __restrict__ dloss, float* __restrict__ du0,
+                                                             const void* __restrict__ tape) {
   constexpr int ws = WS, PPL = (WS * WS + 31) / 32;
   __shared__ Setup su_all[WARPS][MAXL];
   __shared__ float4 hist_all[WARPS][MAXL * (MAXK + 1)];
@@ -357,7 +386,16 @@ __global__ void __launch_bounds__(32 * WARPS, 4) k_lkd_backward(const Lvl* __res
   float4* hist = hist_all[warp];
   const float p0 = pts[2 * gidx], p1 = pts[2 * gidx + 1];
   float vf0, vf1;
-  point_forward<WS>(lv, L, ws, K, p0, p1, u0[2 * gidx], u0[2 * gidx + 1], su, hist, vf0, vf1);
+  if (tape) {
+    // The forward's record of this point instead of a replay.
+    const TapeView t = tape_at(const_cast<void*>(tape), gidx, L, K);
+    for (int q = lane; q < L * (K + 1); q += 32) hist[(q / (K + 1)) * (MAXK + 1) + q % (K + 1)] = t.hist[q];
+    if (lane < L) su[lane] = t.su[lane];
+    vf0 = t.vf[0];
+    vf1 = t.vf[1];
+  } else {
+    point_forward<WS>(lv, L, ws, K, p0, p1, u0[2 * gidx], u0[2 * gidx + 1], su, hist, MAXK + 1, vf0, vf1);
+  }
   __syncwarp();
   const float w = dloss[gidx];
   const int hws = ws / 2, n = ws * ws;
@@ -695,10 +733,15 @@ int check_args(const float* I0, const float* I1, int rows, int cols, int L, int 
 
 }  // namespace
 
-extern "C" int gbt_lkd_forward(const float* I0, const float* I1, int64_t pitch, int64_t img_bytes, int32_t rows,
-                               int32_t cols, int32_t nlevels, int32_t window, int32_t iters, int32_t npairs,
-                               const float* pts, const float* u0, int32_t npts, float* loss, float* vfinal,
-                               void* stream) {
+extern "C" int64_t gbt_lkd_tape_bytes(int32_t nlevels, int32_t iters, int32_t npairs, int32_t npts) {
+  if (nlevels < 1 || nlevels > MAXL || iters < 0 || iters > MAXK || npairs < 1 || npts < 0) return -1;
+  return tape_stride(nlevels, iters) * npairs * npts;
+}
+
+extern "C" int gbt_lkd_forward_tape(const float* I0, const float* I1, int64_t pitch, int64_t img_bytes, int32_t rows,
+                                    int32_t cols, int32_t nlevels, int32_t window, int32_t iters, int32_t npairs,
+                                    const float* pts, const float* u0, int32_t npts, float* loss, float* vfinal,
+                                    void* tape, void* stream) {
   int r = check_args(I0, I1, rows, cols, nlevels, window, iters, npairs, npts);
   if (r) return r;
   if (npts > 0 && (!pts || !u0 || !loss || !vfinal)) return GBT_E_INVALID;
@@ -709,7 +752,7 @@ extern "C" int gbt_lkd_forward(const float* I0, const float* I1, int64_t pitch, 
   if (total > 0)
     switch (window) {
 #define GO(WS) k_lkd_forward<WS><<<(unsigned)((total + WARPS - 1) / WARPS), 32 * WARPS, 0, st>>>( \
-      P.table, nlevels, window, iters, npairs, npts, pts, u0, loss, vfinal)
+      P.table, nlevels, window, iters, npairs, npts, pts, u0, loss, vfinal, tape)
       case 3: GO(3); break;
       case 5: GO(5); break;
       case 7: GO(7); break;
@@ -722,10 +765,18 @@ extern "C" int gbt_lkd_forward(const float* I0, const float* I1, int64_t pitch, 
   return cudaGetLastError() == cudaSuccess ? GBT_OK : GBT_E_CUDA;
 }
 
-extern "C" int gbt_lkd_backward(const float* I0, const float* I1, int64_t pitch, int64_t img_bytes, int32_t rows,
-                                int32_t cols, int32_t nlevels, int32_t window, int32_t iters, int32_t npairs,
-                                const float* pts, const float* u0, int32_t npts, const float* dloss, float* dI0,
-                                float* dI1, float* du0, void* stream) {
+extern "C" int gbt_lkd_forward(const float* I0, const float* I1, int64_t pitch, int64_t img_bytes, int32_t rows,
+                               int32_t cols, int32_t nlevels, int32_t window, int32_t iters, int32_t npairs,
+                               const float* pts, const float* u0, int32_t npts, float* loss, float* vfinal,
+                               void* stream) {
+  return gbt_lkd_forward_tape(I0, I1, pitch, img_bytes, rows, cols, nlevels, window, iters, npairs, pts, u0, npts,
+                              loss, vfinal, nullptr, stream);
+}
+
+extern "C" int gbt_lkd_backward_tape(const float* I0, const float* I1, int64_t pitch, int64_t img_bytes, int32_t rows,
+                                     int32_t cols, int32_t nlevels, int32_t window, int32_t iters, int32_t npairs,
+                                     const float* pts, const float* u0, int32_t npts, const float* dloss, float* dI0,
+                                     float* dI1, float* du0, const void* tape, void* stream) {
   int r = check_args(I0, I1, rows, cols, nlevels, window, iters, npairs, npts);
   if (r) return r;
   if (!dI0 || !dI1) return GBT_E_INVALID;
@@ -737,7 +788,7 @@ extern "C" int gbt_lkd_backward(const float* I0, const float* I1, int64_t pitch,
   if (total > 0)
     switch (window) {
 #define GO(WS) k_lkd_backward<WS><<<(unsigned)((total + WARPS - 1) / WARPS), 32 * WARPS, 0, st>>>( \
-      P.table, nlevels, window, iters, npairs, npts, pts, u0, dloss, du0)
+      P.table, nlevels, window, iters, npairs, npts, pts, u0, dloss, du0, tape)
       case 3: GO(3); break;
       case 5: GO(5); break;
       case 7: GO(7); break;
@@ -770,4 +821,12 @@ extern "C" int gbt_lkd_backward(const float* I0, const float* I1, int64_t pitch,
   cudaMemcpyAsync(dI0, P.dA, (size_t)npairs * rows * cols * 4, cudaMemcpyDeviceToDevice, st);
   cudaMemcpyAsync(dI1, P.dB, (size_t)npairs * rows * cols * 4, cudaMemcpyDeviceToDevice, st);
   return cudaGetLastError() == cudaSuccess ? GBT_OK : GBT_E_CUDA;
+}
+
+extern "C" int gbt_lkd_backward(const float* I0, const float* I1, int64_t pitch, int64_t img_bytes, int32_t rows,
+                                int32_t cols, int32_t nlevels, int32_t window, int32_t iters, int32_t npairs,
+                                const float* pts, const float* u0, int32_t npts, const float* dloss, float* dI0,
+                                float* dI1, float* du0, void* stream) {
+  return gbt_lkd_backward_tape(I0, I1, pitch, img_bytes, rows, cols, nlevels, window, iters, npairs, pts, u0, npts,
+                               dloss, dI0, dI1, du0, nullptr, stream);
 }

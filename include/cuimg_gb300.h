@@ -334,6 +334,21 @@ int gbt_lkd_backward(const float* I0, const float* I1, int64_t pitch, int64_t im
                      const float* pts, const float* u0, int32_t npts, const float* dloss, float* dI0,
                      float* dI1, float* du0, void* stream);
 
+/* The same pair with a tape (no counterpart in the reference): the forward
+ * records, per point, every level's normal-matrix inverse and the iterates
+ * with their right-hand sides (gbt_lkd_tape_bytes of device memory); the
+ * backward given that tape reads them instead of replaying the forward.  The
+ * tape belongs to the same images, points, u0 and configuration. */
+int64_t gbt_lkd_tape_bytes(int32_t nlevels, int32_t iters, int32_t npairs, int32_t npts);
+int gbt_lkd_forward_tape(const float* I0, const float* I1, int64_t pitch, int64_t img_bytes, int32_t rows,
+                         int32_t cols, int32_t nlevels, int32_t window, int32_t iters, int32_t npairs,
+                         const float* pts, const float* u0, int32_t npts, float* loss, float* vfinal, void* tape,
+                         void* stream);
+int gbt_lkd_backward_tape(const float* I0, const float* I1, int64_t pitch, int64_t img_bytes, int32_t rows,
+                          int32_t cols, int32_t nlevels, int32_t window, int32_t iters, int32_t npairs,
+                          const float* pts, const float* u0, int32_t npts, const float* dloss, float* dI0,
+                          float* dI1, float* du0, const void* tape, void* stream);
+
 /* Allocation-free variant of gbt_lk_track_batch (no counterpart in the
  * reference).  For callers that must not allocate device memory (their own
  * device pool or budget, a plugin that may not touch the CUDA heap): same

@@ -90,6 +90,26 @@ def test_adjoint_config_scale_batch_and_directional_derivative():
     assert abs(an - fd) / abs(fd) < RTOL_GRAD, (an, fd)
 
 
+def test_backward_from_the_tape_equals_the_replay():
+    # The tape the forward records replaces the backward's replay: same
+    # gradients up to the order of the float atomics.
+    torch = _torch()
+    from cuimg_gb300 import lkd
+    for L, ws, K, seed in ((3, 7, 4, 21), (2, 9, 6, 22), (5, 9, 10, 23)):
+        H, W = (48, 64) if L < 5 else (96, 128)
+        I0, I1, pts, u0 = _problem(seed, H, W, 40, 14)
+        t = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()
+        wts = t(np.linspace(0.5, 1.5, 40).astype(np.float32))
+        loss, vf, tape = lkd.forward(t(I0), t(I1), t(u0), t(pts), L, ws, K, tape=True)
+        assert tape.numel() == lkd.tape_bytes(L, K, 1, 40)
+        l2, v2 = lkd.forward(t(I0), t(I1), t(u0), t(pts), L, ws, K)
+        assert torch.equal(loss, l2) and torch.equal(vf, v2)
+        a = lkd.backward(t(I0), t(I1), t(u0), t(pts), wts, L, ws, K, tape=tape)
+        b = lkd.backward(t(I0), t(I1), t(u0), t(pts), wts, L, ws, K)
+        for got, want in zip(a, b):
+            torch.testing.assert_close(got, want, rtol=1e-5, atol=1e-6 * float(want.abs().max()))
+
+
 def test_autograd_function_routes_to_the_adjoint():
     torch = _torch()
     from cuimg_gb300 import lkd
