@@ -316,6 +316,7 @@ __global__ void __launch_bounds__(32 * WARPS) k_lkd_forward(const Lvl* __restric
 // (atomics there), added to the level image once at the end; samples whose
 // taps fall outside the box go to the image directly.
 constexpr int GRID_CELLS = 1024;
+constexpr int BW_MINB = 5;  // backward CTAs per SM the registers are sized for
 struct Grid {
   float* c;        // cells, row-major GW per row
   int y0, x0, GH, GW;
@@ -366,15 +367,15 @@ __device__ __forceinline__ void grid_flush(const Grid& g, float* img, int W) {
   __syncwarp();
 }
 
-template <int WS>
-__global__ void __launch_bounds__(32 * WARPS, 4) k_lkd_backward(const Lvl* __restrict__ levels, int L, int /*window: WS*/, int K,
+template <int WS, bool TAPE>
+__global__ void __launch_bounds__(32 * WARPS, BW_MINB) k_lkd_backward(const Lvl* __restrict__ levels, int L, int /*window: WS*/, int K,
                                                              int npairs, int npts, const float* __restrict__ pts,
                                                              const float* __restrict__ u0,
                                                              const float* __restrict__ dloss, float* __restrict__ du0,
                                                              const void* __restrict__ tape) {
   constexpr int ws = WS, PPL = (WS * WS + 31) / 32;
   __shared__ Setup su_all[WARPS][MAXL];
-  __shared__ float4 hist_all[WARPS][MAXL * (MAXK + 1)];
+  extern __shared__ float4 hist_dyn[];  // WARPS x L x (K + 1): the iterate history
   __shared__ float gB_all[WARPS][GRID_CELLS];                       // dB over the level's residual samples
   __shared__ float gT_all[WARPS][3][(MAXW + 1) * (MAXW + 1)];      // dA, dS.x, dS.y over the template
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -383,18 +384,19 @@ __global__ void __launch_bounds__(32 * WARPS, 4) k_lkd_backward(const Lvl* __res
   const int pair = (int)(gidx / npts);
   const Lvl* lv = levels + (size_t)pair * L;
   Setup* su = su_all[warp];
-  float4* hist = hist_all[warp];
+  const int HS = K + 1;
+  float4* hist = hist_dyn + (size_t)warp * L * HS;
   const float p0 = pts[2 * gidx], p1 = pts[2 * gidx + 1];
   float vf0, vf1;
-  if (tape) {
+  if (TAPE) {
     // The forward's record of this point instead of a replay.
     const TapeView t = tape_at(const_cast<void*>(tape), gidx, L, K);
-    for (int q = lane; q < L * (K + 1); q += 32) hist[(q / (K + 1)) * (MAXK + 1) + q % (K + 1)] = t.hist[q];
+    for (int q = lane; q < L * HS; q += 32) hist[q] = t.hist[q];
     if (lane < L) su[lane] = t.su[lane];
     vf0 = t.vf[0];
     vf1 = t.vf[1];
   } else {
-    point_forward<WS>(lv, L, ws, K, p0, p1, u0[2 * gidx], u0[2 * gidx + 1], su, hist, MAXK + 1, vf0, vf1);
+    point_forward<WS>(lv, L, ws, K, p0, p1, u0[2 * gidx], u0[2 * gidx + 1], su, hist, HS, vf0, vf1);
   }
   __syncwarp();
   const float w = dloss[gidx];
@@ -417,7 +419,7 @@ __global__ void __launch_bounds__(32 * WARPS, 4) k_lkd_backward(const Lvl* __res
       float ylo = 1e30f, yhi = -1e30f, xlo = 1e30f, xhi = -1e30f;
       for (int k = 0; k <= K; k++) {
         if (k == K && l != 0) break;
-        const float4 v = hist[l * (MAXK + 1) + k];
+        const float4 v = hist[l * HS + k];
         ylo = fminf(ylo, v.x);
         yhi = fmaxf(yhi, v.x);
         xlo = fminf(xlo, v.y);
@@ -457,7 +459,7 @@ __global__ void __launch_bounds__(32 * WARPS, 4) k_lkd_backward(const Lvl* __res
 #pragma unroll
     for (int k = 0; k < PPL; k++) dg0[k] = dg1[k] = dT[k] = 0.f;
     for (int k = K - 1; k >= 0; k--) {
-      const float4 vk = hist[l * (MAXK + 1) + k];  // v_k and b_k of the replayed forward
+      const float4 vk = hist[l * HS + k];  // v_k and b_k of the forward
       const float d0 = dv0, d1 = dv1;                       // adjoint of v_{k+1}
       const float db0 = S.M00 * d0 + S.M01 * d1, db1 = S.M01 * d0 + S.M11 * d1;
       const float b0 = vk.z, b1 = vk.w;
@@ -785,10 +787,16 @@ extern "C" int gbt_lkd_backward_tape(const float* I0, const float* I1, int64_t p
   Plan P;
   if ((r = prepare(I0, I1, pitch, img_bytes, rows, cols, nlevels, npairs, true, P, st))) return r;
   long long total = (long long)npairs * npts;
+  const size_t hbytes = (size_t)WARPS * nlevels * (iters + 1) * sizeof(float4);
   if (total > 0)
     switch (window) {
-#define GO(WS) k_lkd_backward<WS><<<(unsigned)((total + WARPS - 1) / WARPS), 32 * WARPS, 0, st>>>( \
-      P.table, nlevels, window, iters, npairs, npts, pts, u0, dloss, du0, tape)
+#define GO(WS)                                                                                            \
+  if (tape)                                                                                               \
+    k_lkd_backward<WS, true><<<(unsigned)((total + WARPS - 1) / WARPS), 32 * WARPS, hbytes, st>>>(       \
+        P.table, nlevels, window, iters, npairs, npts, pts, u0, dloss, du0, tape);                        \
+  else                                                                                                    \
+    k_lkd_backward<WS, false><<<(unsigned)((total + WARPS - 1) / WARPS), 32 * WARPS, hbytes, st>>>(      \
+        P.table, nlevels, window, iters, npairs, npts, pts, u0, dloss, du0, tape)
       case 3: GO(3); break;
       case 5: GO(5); break;
       case 7: GO(7); break;
