@@ -544,15 +544,19 @@ def measure_extras(args, dev, local, peak):
         f0[p], f1[p] = st.frame_f32(0), st.frame_f32(1)
     pts = np.stack([rng.uniform(30, H - 30, (P, n)), rng.uniform(30, W - 30, (P, n))], -1).astype(np.float32)
     A, Bt, X = torch.from_numpy(f0).to(dev), torch.from_numpy(f1).to(dev), torch.from_numpy(pts).to(dev)
-    prm = lk.params(window=9, npix=81, max_iter=10)
+    # Warps per CTA of the LK kernel chosen by the autotuner on each batch.
+    prm = autotune.tune_lk(A, Bt, X, 5, lk.params(window=9, npix=81, max_iter=10))
     ms = _events_ms(lambda: lk.track(A, Bt, X, nlevels=5, prm=prm), 3, stream)
     A8 = A.clamp(0, 255).to(torch.uint8)
     B8 = Bt.clamp(0, 255).to(torch.uint8)
-    ms8 = _events_ms(lambda: lk.track(A8, B8, X, nlevels=3, prm=lk.params()), 3, stream)
+    prm8 = autotune.tune_lk(A8, B8, X, 3, lk.params())
+    ms8 = _events_ms(lambda: lk.track(A8, B8, X, nlevels=3, prm=prm8), 3, stream)
     out["lk_640x480_x16"] = {"points": P * n,
-                             "f32_5lvl_9x9_10it": {"ms": round(ms, 3), "points_per_s": round(P * n / (ms / 1000))},
+                             "f32_5lvl_9x9_10it": {"ms": round(ms, 3), "points_per_s": round(P * n / (ms / 1000)),
+                                                   "warps_per_block": prm.warps_per_block},
                              "u8_3lvl_11x11_30it_top25": {"ms": round(ms8, 3),
-                                                          "points_per_s": round(P * n / (ms8 / 1000))}}
+                                                          "points_per_s": round(P * n / (ms8 / 1000)),
+                                                          "warps_per_block": prm8.warps_per_block}}
     # Adjoint: forward recording the tape, backward reading it (pyramids
     # recomputed by both); the backward without a tape replays the forward.
     U0 = torch.from_numpy(rng.uniform(-2, 2, (P, n, 2)).astype(np.float32)).to(dev)

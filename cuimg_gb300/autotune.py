@@ -98,3 +98,45 @@ def apply(bt, choice):
     for knob, value in choice.items():
         bt.set_tuning(int(knob), int(value))
     return bt
+
+
+LK_WARPS = (2, 4, 8)
+
+
+def tune_lk(prev, cur, points, nlevels, prm, reps=3, cache_path=DEFAULT_CACHE, force=False):
+    """Warps per CTA of the LK tracking kernel for this workload: each setting
+    timed with CUDA events over `reps` calls of lk.track on the caller's own
+    batch, the fastest cached by GPU name, batch geometry and LK parameters.
+    Returns params equal to `prm` with warps_per_block set."""
+    import torch
+
+    from . import lk
+    dev = prev.device.index or 0
+    key = "lk|%s|%s|%s|%d|%d|%d|%d|%d" % (_gpu_name(dev), "x".join(map(str, prev.shape)), str(prev.dtype),
+                                         points.shape[-2], nlevels, prm.window, prm.npix, prm.max_iter)
+    cache = {}
+    if os.path.exists(cache_path):
+        try:
+            with open(cache_path) as f:
+                cache = json.load(f)
+        except (OSError, ValueError):
+            cache = {}
+    best = cache.get(key) if not force else None
+    if best is None:
+        times = {}
+        for w in LK_WARPS:
+            p = lk.params(prm.window, prm.npix, prm.max_iter, prm.eps, prm.max_err, w)
+            lk.track(prev, cur, points, nlevels=nlevels, prm=p)  # warm-up
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            for _ in range(reps):
+                lk.track(prev, cur, points, nlevels=nlevels, prm=p)
+            e1.record()
+            e1.synchronize()
+            times[w] = e0.elapsed_time(e1)
+        best = min(times, key=times.get)
+        cache[key] = best
+        os.makedirs(os.path.dirname(cache_path), exist_ok=True)
+        with open(cache_path, "w") as f:
+            json.dump(cache, f, indent=1, sort_keys=True)
+    return lk.params(prm.window, prm.npix, prm.max_iter, prm.eps, prm.max_err, int(best))

@@ -231,14 +231,14 @@ __device__ bool lk_match(const Level& lv, const Params& P, WarpSmem& S, float py
   return ok;
 }
 
-template <int PPL>
-__global__ void __launch_bounds__(32 * WARPS) k_lk_track(const Level* __restrict__ levels, Params P, int npairs,
+template <int PPL, int NW>
+__global__ void __launch_bounds__(32 * NW) k_lk_track(const Level* __restrict__ levels, Params P, int npairs,
                                                          int npts, const float* __restrict__ pts,
                                                          float* __restrict__ out, int* __restrict__ status,
                                                          float* __restrict__ err) {
-  __shared__ WarpSmem smem[WARPS];
+  __shared__ WarpSmem smem[NW];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const long long g = (long long)blockIdx.x * WARPS + warp;
+  const long long g = (long long)blockIdx.x * NW + warp;
   if (g >= (long long)npairs * npts) return;
   const int pair = (int)(g / npts);
   const Level* lv = levels + (size_t)pair * P.L;
@@ -292,6 +292,34 @@ __global__ void __launch_bounds__(32 * WARPS) k_lk_track(const Level* __restrict
     status[g] = st;
     err[g] = oe;
   }
+}
+
+// One warp per point; the window pixels per lane (PPL) and the warps per CTA
+// (NW, a tuning choice) are compile-time.
+template <int NW>
+void launch_lk_nw(const Level* table, const Params& P, int ppl, int npairs, int npts, const float* pts, float* out,
+                  int* status, float* err, cudaStream_t st) {
+  const long long blocks = ((long long)npairs * npts + NW - 1) / NW;
+  auto go = [&](auto kern) { kern<<<(unsigned)blocks, 32 * NW, 0, st>>>(table, P, npairs, npts, pts, out, status, err); };
+  switch (ppl) {
+    case 1: go(k_lk_track<1, NW>); break;
+    case 2: go(k_lk_track<2, NW>); break;
+    case 3: go(k_lk_track<3, NW>); break;
+    case 4: go(k_lk_track<4, NW>); break;
+    case 5: case 6: go(k_lk_track<6, NW>); break;
+    default: go(k_lk_track<8, NW>); break;
+  }
+}
+
+inline void launch_lk(const Level* table, const Params& P, const gbt_lk_params* prm, int npairs, int npts,
+                      const float* pts, float* out, int* status, float* err, cudaStream_t st) {
+  const int ppl = (prm->window * prm->window + 31) / 32;
+  if (prm->warps_per_block == 2)
+    launch_lk_nw<2>(table, P, ppl, npairs, npts, pts, out, status, err, st);
+  else if (prm->warps_per_block == 4)
+    launch_lk_nw<4>(table, P, ppl, npairs, npts, pts, out, status, err, st);
+  else
+    launch_lk_nw<8>(table, P, ppl, npairs, npts, pts, out, status, err, st);
 }
 
 // Level images (fp32) of a uint8 frame: level 0 converted, then 2x2 floor means.
@@ -351,6 +379,7 @@ extern "C" void gbt_lk_params_default(gbt_lk_params* p) {
   p->max_iter = 30;
   p->eps = 0.1f;
   p->max_err = 300.f;
+  p->warps_per_block = 0;
 }
 
 // Bytes of scratch gbt_lk_track_batch needs for `npairs` pairs.
@@ -373,7 +402,8 @@ static int lk_run(const void* prev, const void* cur, int64_t pitch, int64_t img_
   if (!prev || !cur || !prm || !scratch) return GBT_E_INVALID;
   if (npts > 0 && (!pts || !out || !status || !err)) return GBT_E_INVALID;
   if (rows < 16 || cols < 16 || nlevels < 1 || npairs < 1 || npts < 0) return GBT_E_INVALID;
-  if (prm->window < 3 || prm->window > MAXW || !(prm->window & 1) || prm->npix < 1 || prm->max_iter < 0)
+  if (prm->window < 3 || prm->window > MAXW || !(prm->window & 1) || prm->npix < 1 || prm->max_iter < 0 ||
+      (prm->warps_per_block != 0 && prm->warps_per_block != 2 && prm->warps_per_block != 4 && prm->warps_per_block != 8))
     return GBT_E_INVALID;
   if ((rows >> (nlevels - 1)) < 8 || (cols >> (nlevels - 1)) < 8) return GBT_E_INVALID;
   if (scratch_bytes < gbt_lk_scratch_bytes(rows, cols, nlevels, npairs)) return GBT_E_INVALID;
@@ -447,16 +477,7 @@ static int lk_run(const void* prev, const void* cur, int64_t pitch, int64_t img_
   Params P{prm->window, prm->npix, prm->max_iter, nlevels, prm->eps, prm->max_err, is_u8};
   long long total = (long long)npairs * npts;
   if (total > 0) {
-    long long blocks = (total + WARPS - 1) / WARPS;
-    auto go = [&](auto kern) { kern<<<(unsigned)blocks, 32 * WARPS, 0, st>>>(table, P, npairs, npts, pts, out, status, err); };
-    switch ((prm->window * prm->window + 31) / 32) {
-      case 1: go(k_lk_track<1>); break;
-      case 2: go(k_lk_track<2>); break;
-      case 3: go(k_lk_track<3>); break;
-      case 4: go(k_lk_track<4>); break;
-      case 5: case 6: go(k_lk_track<6>); break;
-      default: go(k_lk_track<8>); break;
-    }
+    launch_lk(table, P, prm, npairs, npts, pts, out, status, err, st);
   }
   // The host table must outlive the asynchronous copy.
   cudaStreamSynchronize(st);
@@ -558,7 +579,8 @@ extern "C" int gbt_lk_track_batch_noalloc(const void* prev, const void* cur, int
   if (npts > 0 && (!pts || !out || !status || !err)) return GBT_E_INVALID;
   if (rows < 16 || cols < 16 || nlevels < 1 || nlevels > NOALLOC_MAX_LEVELS || npairs < 1 || npts < 0)
     return GBT_E_INVALID;
-  if (prm->window < 3 || prm->window > MAXW || !(prm->window & 1) || prm->npix < 1 || prm->max_iter < 0)
+  if (prm->window < 3 || prm->window > MAXW || !(prm->window & 1) || prm->npix < 1 || prm->max_iter < 0 ||
+      (prm->warps_per_block != 0 && prm->warps_per_block != 2 && prm->warps_per_block != 4 && prm->warps_per_block != 8))
     return GBT_E_INVALID;
   if ((rows >> (nlevels - 1)) < 8 || (cols >> (nlevels - 1)) < 8) return GBT_E_INVALID;
   const int64_t need = gbt_lk_scratch_bytes(rows, cols, nlevels, npairs);
@@ -625,16 +647,7 @@ extern "C" int gbt_lk_track_batch_noalloc(const void* prev, const void* cur, int
   Params P{prm->window, prm->npix, prm->max_iter, nlevels, prm->eps, prm->max_err, is_u8};
   long long total = (long long)npairs * npts;
   if (total > 0) {
-    long long blocks = (total + WARPS - 1) / WARPS;
-    auto go = [&](auto kern) { kern<<<(unsigned)blocks, 32 * WARPS, 0, st>>>(table, P, npairs, npts, pts, out, status, err); };
-    switch ((prm->window * prm->window + 31) / 32) {
-      case 1: go(k_lk_track<1>); break;
-      case 2: go(k_lk_track<2>); break;
-      case 3: go(k_lk_track<3>); break;
-      case 4: go(k_lk_track<4>); break;
-      case 5: case 6: go(k_lk_track<6>); break;
-      default: go(k_lk_track<8>); break;
-    }
+    launch_lk(table, P, prm, npairs, npts, pts, out, status, err, st);
   }
   return cudaGetLastError() == cudaSuccess ? GBT_OK : GBT_E_CUDA;
 }

@@ -15,11 +15,13 @@ from ._native import check, cuda_lib
 
 class gbt_lk_params(ctypes.Structure):
     _fields_ = [("window", ctypes.c_int32), ("npix", ctypes.c_int32), ("max_iter", ctypes.c_int32),
-                ("eps", ctypes.c_float), ("max_err", ctypes.c_float)]
+                ("eps", ctypes.c_float), ("max_err", ctypes.c_float), ("warps_per_block", ctypes.c_int32)]
 
 
-def params(window=11, npix=25, max_iter=30, eps=0.1, max_err=300.0):
-    return gbt_lk_params(window, npix, max_iter, eps, max_err)
+def params(window=11, npix=25, max_iter=30, eps=0.1, max_err=300.0, warps_per_block=0):
+    """warps_per_block: CTA size of the tracking kernel (2, 4, 8; 0 = 8), speed only;
+    cuimg_gb300.autotune.tune_lk picks it for a workload."""
+    return gbt_lk_params(window, npix, max_iter, eps, max_err, warps_per_block)
 
 
 def _declare(lib):

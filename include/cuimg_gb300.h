@@ -293,6 +293,8 @@ typedef struct {
   int32_t max_iter;  /* Gauss-Newton iterations at most */
   float eps;         /* stop when the step norm falls below eps */
   float max_err;     /* accept when the mean residual is below max_err */
+  int32_t warps_per_block;  /* CTA size of the tracking kernel (one warp per point): 2, 4 or 8;
+                               0 = 8.  Speed only (the package's autotuner picks it). */
 } gbt_lk_params;
 
 void gbt_lk_params_default(gbt_lk_params* p);

@@ -103,3 +103,22 @@ def test_lk_edge_points_and_empty():
     assert st.cpu().numpy()[0][:5].sum() == 0  # outside domain - border(3)
     out, st, err = lk.track(A, B, torch.zeros((0, 2)).cuda(), nlevels=2)
     assert out.numel() == 0
+
+
+def test_lk_block_sizes_give_identical_tracks():
+    # warps_per_block (the autotuned CTA size) changes speed only.
+    torch = _torch()
+    from cuimg_gb300 import autotune, lk, synth
+    H, W, n = 240, 320, 500
+    rng = np.random.default_rng(5)
+    s = synth.Stream(41, H, W)
+    A = torch.from_numpy(np.stack([s.frame_f32(0), s.frame_f32(2)])).cuda()
+    B = torch.from_numpy(np.stack([s.frame_f32(1), s.frame_f32(3)])).cuda()
+    X = torch.from_numpy(np.stack([_points(rng, H, W, n, 20), _points(rng, H, W, n, 20)])).cuda()
+    runs = [lk.track(A, B, X, nlevels=3, prm=lk.params(window=9, npix=81, max_iter=10, warps_per_block=w))
+            for w in (2, 4, 8, 0)]
+    for other in runs[1:]:
+        for a, b in zip(runs[0], other):
+            assert torch.equal(a, b)
+    p = autotune.tune_lk(A, B, X, 3, lk.params(window=9, npix=81, max_iter=10), force=True)
+    assert p.warps_per_block in autotune.LK_WARPS
