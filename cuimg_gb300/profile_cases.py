@@ -2,7 +2,7 @@
 
     python -m cuimg_gb300.profile_cases gaussian   # 8 fp32 1920x1080 images, sigma 4
     python -m cuimg_gb300.profile_cases lk         # 4 fp32 640x480 pairs, 5 levels, 20k points each
-    python -m cuimg_gb300.profile_cases adjoint    # LK residual forward + backward, same batch
+    python -m cuimg_gb300.profile_cases adjoint    # LK residual forward (tape) + backward, same batch
     python -m cuimg_gb300.profile_cases tracker    # 4 streams of 1920x1080, 6 frames
     python -m cuimg_gb300.profile_cases tracker_det  # the same with the detector every third frame
 
@@ -65,8 +65,8 @@ def adjoint(reps=2):
     A, B, X, U = _lk_batch()
     ones = torch.ones(X.shape[:2], device="cuda")
     for _ in range(reps):
-        lkd.forward(A, B, U, X, 5, 9, 10)
-        lkd.backward(A, B, U, X, ones, 5, 9, 10)
+        tape = lkd.forward(A, B, U, X, 5, 9, 10, tape=True)[2]
+        lkd.backward(A, B, U, X, ones, 5, 9, 10, tape=tape)
     torch.cuda.synchronize()
 
 
