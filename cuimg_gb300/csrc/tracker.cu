@@ -621,7 +621,7 @@ static int enqueue_back(Group* ctx, bool any_det, bool any_filt, int par, int& n
       n++;
     }
     { PROF("k_det_count"); k_det_count<<<pgrid, CHUNK, 0, st>>>(du, ctx->d_state, ctx->d_frame, ctx->d_pre, ctx->d_btable, nunits); }
-    { PROF("k_unit_scan"); k_unit_scan<<<nunits, 1024, 0, st>>>(du, ctx->d_state, ctx->d_frame, 0); }
+    { PROF("k_unit_scan"); k_unit_scan<<<nunits, 1024, 0, st>>>(du, ctx->d_state, ctx->d_frame); }
     { PROF("k_det_scatter"); k_det_scatter<<<pgrid, CHUNK, 0, st>>>(du, ctx->d_state, ctx->d_frame, ctx->d_pre, ctx->d_btable, nunits); }
     { PROF("k_commit"); k_commit<<<1, 1024, 0, st>>>(du, ctx->d_state, ctx->d_frame, ctx->d_post, nunits); }
     n += 7;
@@ -630,10 +630,8 @@ static int enqueue_back(Group* ctx, bool any_det, bool any_filt, int par, int& n
   if (any_filt) {
     const int fgrid = ctx->nsm * 6;
     { PROF("k_filter_merge"); k_filter_merge<<<fgrid, FM_THREADS, 0, st>>>(du, ctx->d_state, ctx->d_frame, table, nunits); }
-    { PROF("k_unit_scan"); k_unit_scan<<<nunits, 1024, 0, st>>>(du, ctx->d_state, ctx->d_frame, 1); }
-    { PROF("k_merge_scatter"); k_merge_scatter<<<fgrid, FM_THREADS, 0, st>>>(du, ctx->d_state, ctx->d_frame, table, nunits); }
-    { PROF("k_merge_resolve"); k_merge_resolve<<<nunits, 256, 0, st>>>(du, ctx->d_state, ctx->d_frame); }
-    n += 4;
+    { PROF("k_merge_unit"); k_merge_unit<<<nunits, MU_THREADS, 0, st>>>(du, ctx->d_state, ctx->d_frame); }
+    n += 2;
   }
   if (ctx->traj_T) {
     PROF("k_traj");

@@ -1252,12 +1252,12 @@ __global__ void __launch_bounds__(CHUNK) k_det_count(const Unit* __restrict__ un
 // Per-unit exclusive scans of chunk counts.  which: 0 = detector (survivors
 // and births), 1 = merge actives.
 __global__ void __launch_bounds__(1024) k_unit_scan(const Unit* __restrict__ units, UState* __restrict__ st,
-                                                    const Frame* __restrict__ fr, int which) {
+                                                    const Frame* __restrict__ fr) {
   __shared__ int wt[65];
   const int ui = blockIdx.x;
   const Unit& u = units[ui];
   const int f = fr->f;
-  if (which == 0 ? !det_frame(u, f) : !filt_frame(u, f)) return;
+  if (!det_frame(u, f)) return;
   UState& s = st[ui];
   auto scan = [&](int* cnt, int nch) -> int {
     int carry = 0;
@@ -1293,17 +1293,13 @@ __global__ void __launch_bounds__(1024) k_unit_scan(const Unit* __restrict__ uni
     }
     return carry;
   };
-  if (which == 0) {  // per-warp counts of k_det_count
-    int S = scan(u.chunk_cnt, (s.n + 31) / 32);
-    int B = scan(u.birth_cnt, (u.birth_items + 31) / 32);
-    if (threadIdx.x == 0) {
-      s.n_old = s.n;
-      s.S = S;
-      s.B = B;
-    }
-  } else {
-    int A = scan(u.act_cnt, (s.n + 31) / 32);  // per-warp counts of k_merge_count
-    if (threadIdx.x == 0) s.A = A;
+  // per-warp counts of k_det_count
+  int S = scan(u.chunk_cnt, (s.n + 31) / 32);
+  int B = scan(u.birth_cnt, (u.birth_items + 31) / 32);
+  if (threadIdx.x == 0) {
+    s.n_old = s.n;
+    s.S = S;
+    s.B = B;
   }
 }
 
@@ -1500,8 +1496,7 @@ __device__ __forceinline__ unsigned merge_dirs(const Unit& u, const UState& s, i
 // filter_bad_particles_kernel (tracking_strategies.hpp:482-523) and step 1 of
 // the merge in one pass: each live particle applies the filter to itself and,
 // when it survives, finds its qualifying directions.  Actives are counted per
-// warp of 32 slots (act_cnt[i / 32]); the unit scan turns the counts into
-// offsets, so neither pass needs a block-wide prefix.
+// warp of 32 slots (act_cnt[i / 32]) for k_merge_unit.
 // Quarter-chunk CTAs (256 threads) for the merge passes: their register
 // footprint allows six CTAs per SM, where 1024-thread CTAs get one.
 constexpr int FM_THREADS = 256;
@@ -1538,36 +1533,6 @@ __global__ void __launch_bounds__(FM_THREADS) k_filter_merge(const Unit* __restr
   }
 }
 
-__global__ void __launch_bounds__(FM_THREADS) k_merge_scatter(const Unit* __restrict__ units,
-                                                              const UState* __restrict__ st,
-                                                              const Frame* __restrict__ fr,
-                                                              const int* __restrict__ table, int nunits) {
-  const int f = fr->f;
-  const int total = table[nunits] * FM_SUB;
-  for (int g = blockIdx.x; g < total; g += gridDim.x) {
-    ChunkCursor cc = chunk_of(table, nunits, g / FM_SUB);
-    const Unit& u = units[cc.unit];
-    if (!filt_frame(u, f) || !u.with_merge) continue;
-    const UState s = st[cc.unit];
-    const int i = cc.chunk * CHUNK + (g % FM_SUB) * FM_THREADS + threadIdx.x;
-    if ((i & ~31) >= s.n) continue;  // whole warp past the slots
-    const int w = i >> 5;
-    const int o0 = u.act_cnt[w], o1 = (w + 1) * 32 < s.n ? u.act_cnt[w + 1] : s.A;
-    if (o0 == o1) continue;  // no active in this warp
-    bool act = i < s.n && u.cmask[i] != 0;
-    const unsigned b = __ballot_sync(0xffffffffu, act);
-    int o = o0 + __popc(b & ((1u << (threadIdx.x & 31)) - 1u));
-    if (act) {
-      short2 p = u.pos[s.cur][i];
-      int cand[8];
-      int nc;
-      merge_dirs<true>(u, s, f, i, p, u.age[s.cur][i], cand, nc);
-      u.act_list[o] = make_int4(i, (int)(((unsigned)(unsigned short)p.x << 16) | (unsigned short)p.y), nc, 0);
-      for (int q = 0; q < nc; q++) u.act_cand[(size_t)o * 8 + q] = cand[q];
-    }
-  }
-}
-
 // Liveness of the particles a batch of actives touches, in a shared-memory
 // open-addressing table (key = slot + 1, top bit = killed).  Falls back to the
 // global age array when the table would overflow.
@@ -1584,21 +1549,98 @@ __device__ __forceinline__ int mr_find(unsigned* tab, unsigned key) {
   return -1;
 }
 
-__global__ void __launch_bounds__(256) k_merge_resolve(const Unit* __restrict__ units, const UState* __restrict__ st,
-                                                       const Frame* __restrict__ fr) {
+// Block-wide exclusive prefix sum of one int per thread (blockDim.x a multiple
+// of 32, at most 1024); `total` gets the sum.
+__device__ __forceinline__ int block_scan(int v, int* warp_tot, int& total) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  int x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) warp_tot[wid] = x;
+  __syncthreads();
+  if (wid == 0) {
+    const int w = lane < (int)(blockDim.x >> 5) ? warp_tot[lane] : 0;
+    int z = w;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, z, o);
+      if (lane >= o) z += y;
+    }
+    warp_tot[32 + lane] = z - w;
+    if (lane == 31) warp_tot[64] = z;
+  }
+  __syncthreads();
+  const int r = warp_tot[32 + wid] + x - v;
+  total = warp_tot[64];
+  __syncthreads();
+  return r;
+}
+
+// Steps 2 and 3 of the merge for one unit per CTA.  Step 2: the actives in
+// slot order -- warps of 32 slots taken 1024 at a time, their active counts
+// (act_cnt, from k_filter_merge) scanned across the CTA, and each warp with
+// actives expanded by one thread into act_list / act_cand (its qualifying
+// neighbours recomputed, with the post-filter ages).  Step 3: the ordered
+// replay described above.
+constexpr int MU_THREADS = 1024;
+static_assert(MR_HASH >= 2 * MU_THREADS, "the active-warp lists fit in the liveness table");
+
+__global__ void __launch_bounds__(MU_THREADS) k_merge_unit(const Unit* __restrict__ units, UState* __restrict__ st,
+                                                          const Frame* __restrict__ fr) {
   __shared__ int4 ent[MR_NB];
   __shared__ int cnd[MR_NB][8];
   __shared__ unsigned tab[MR_HASH];
   __shared__ int tab_fill, tab_over;
+  __shared__ int wt[65];
   const int ui = blockIdx.x;
   const Unit& u = units[ui];
   const int f = fr->f;
   if (!filt_frame(u, f) || !u.with_merge) return;
   const UState s = st[ui];
+  int A = 0;
+  const int nw = (s.n + 31) >> 5;
+  const int lane0 = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  int* wl = (int*)tab;             // slot warps with actives (the table is free until step 3)
+  int* wo = (int*)tab + MU_THREADS;  // and their first position in the ordered list
+  for (int w0 = 0; w0 < nw; w0 += blockDim.x) {
+    const int w = w0 + threadIdx.x;
+    const int c = w < nw ? u.act_cnt[w] : 0;
+    int tot, nact;
+    const int off = A + block_scan(c, wt, tot);
+    const int k = block_prefix(c > 0, wt, nact);
+    if (c > 0) {
+      wl[k] = w;
+      wo[k] = off;
+    }
+    __syncthreads();
+    // One warp of threads per listed slot warp: a lane per slot.
+    for (int q = wid; q < nact; q += (int)(blockDim.x >> 5)) {
+      const int i = 32 * wl[q] + lane0;
+      const bool act = i < s.n && u.cmask[i] != 0;
+      const unsigned bal = __ballot_sync(0xffffffffu, act);
+      if (act) {
+        const int o = wo[q] + __popc(bal & ((1u << lane0) - 1u));
+        const short2 p = u.pos[s.cur][i];
+        int cand[8];
+        int nc;
+        merge_dirs<true>(u, s, f, i, p, u.age[s.cur][i], cand, nc);
+        u.act_list[o] = make_int4(i, (int)(((unsigned)(unsigned short)p.x << 16) | (unsigned short)p.y), nc, 0);
+        for (int r = 0; r < nc; r++) u.act_cand[(size_t)o * 8 + r] = cand[r];
+      }
+    }
+    A += tot;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) st[ui].A = A;
+  __threadfence_block();
+  __syncthreads();
   unsigned short* age = u.age[s.cur];
   const int lane = threadIdx.x & 31;
-  for (int base = 0; base < s.A; base += MR_NB) {
-    const int nb = min(MR_NB, s.A - base);
+  for (int base = 0; base < A; base += MR_NB) {
+    const int nb = min(MR_NB, A - base);
     for (int k = threadIdx.x; k < MR_HASH; k += blockDim.x) tab[k] = 0;
     if (threadIdx.x == 0) {
       tab_fill = 0;
