@@ -108,6 +108,7 @@ struct Group {
   long long kernels_total = 0;  // kernels launched by this context, graph nodes included
   int match_variant = 0;  // GBT_TUNE_MATCHER
   int mt_shape = 3;       // GBT_TUNE_MATCH_TILE: tiled matcher threads and particle assignment
+  int fm_grid = 0;        // k_filter_merge CTAs: the ones all SMs hold at once
   bool fixed_fpitch = true;  // every unit's s1/s2 pitch is FIXED_FPITCH
   bool any_alt_detector = false;  // a stream uses the regular or the dense detector
   std::string err;
@@ -259,6 +260,11 @@ static int sync_all(Group* ctx) {
 static int build(Group* ctx, const gbt_config* cfgs, int nstreams) {
   CK(cudaSetDevice(ctx->device));
   CK(cudaDeviceGetAttribute(&ctx->nsm, cudaDevAttrMultiProcessorCount, ctx->device));
+  {
+    int per_sm = 0;
+    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_filter_merge, FM_THREADS, 0));
+    ctx->fm_grid = ctx->nsm * std::max(1, per_sm);
+  }
   CK(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
   CK(cudaStreamCreateWithFlags(&ctx->pre, cudaStreamNonBlocking));
   for (cudaEvent_t* e : {&ctx->ev_front, &ctx->ev_back[0], &ctx->ev_back[1]})
@@ -628,7 +634,7 @@ static int enqueue_back(Group* ctx, bool any_det, bool any_filt, int par, int& n
   }
   int* table = any_det ? ctx->d_post : ctx->d_pre;
   if (any_filt) {
-    const int fgrid = ctx->nsm * 6;
+    const int fgrid = ctx->fm_grid;
     { PROF("k_filter_merge"); k_filter_merge<<<fgrid, FM_THREADS, 0, st>>>(du, ctx->d_state, ctx->d_frame, table, nunits); }
     { PROF("k_merge_unit"); k_merge_unit<<<nunits, MU_THREADS, 0, st>>>(du, ctx->d_state, ctx->d_frame); }
     n += 2;

@@ -1418,6 +1418,22 @@ __global__ void __launch_bounds__(1024) k_commit(const Unit* __restrict__ units,
 // particle i at p survives.  It is removed when older than 2 frames and more
 // than 10 px from its bin's fused flow, or when its bin's multiscale count is
 // 1 and no c8 bin has a nonzero count.
+// The decision from the bin's count m, its flow fl and the particle's speed v.
+__device__ __forceinline__ bool filter_decide(const Unit& u, unsigned short age, unsigned m, float2 fl, short2 v,
+                                              int br, int bc) {
+  if (age > 2 && m > 0) {
+    float dx = __fsub_rn((float)v.x, fl.x), dy = __fsub_rn((float)v.y, fl.y);
+    float nrm = __fsqrt_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)));
+    if (nrm > 10.f) return false;
+  }
+  if (m != 1) return true;
+  for (int k = 0; k < 8; k++) {
+    int nr = br + c_c8[k][0], nc = bc + c_c8[k][1];
+    if (nr >= 0 && nr < u.BH && nc >= 0 && nc < u.BW && u.msc[(size_t)nr * u.BW + nc] != 0) return true;
+  }
+  return false;
+}
+
 __device__ __forceinline__ bool filter_keeps(const Unit& u, int b, int i, unsigned short age, short2 p) {
   const int br = p.x / 8, bc = p.y / 8;
   const size_t w = (size_t)br * u.BW + bc;
@@ -1450,17 +1466,26 @@ __device__ __forceinline__ bool filter_keeps(const Unit& u, int b, int i, unsign
 // (the filter runs in the same launch), so a neighbour also has to pass
 // filter_keeps; the filter's decision is a function of the bin statistics
 // alone, so both passes see the same candidates.
+// occ marks exactly the pixels whose index entry is current (matched
+// particles, and births on detector frames): most neighbours are empty.  The
+// 3x3 box around p touches at most four bin words (rows ra / rb, columns ca /
+// cb), loaded by box_words.
+struct BoxWords {
+  unsigned long long a, b, c, d;
+};
+__device__ __forceinline__ BoxWords box_words(const Unit& u, short2 p) {
+  const int ra = max(p.x - 1, 0), rb = min(p.x + 1, u.H - 1), ca = max(p.y - 1, 0), cb = min(p.y + 1, u.W - 1);
+  return BoxWords{u.occ[bin_word(u, ra, ca)], u.occ[bin_word(u, ra, cb)], u.occ[bin_word(u, rb, ca)],
+                  u.occ[bin_word(u, rb, cb)]};
+}
+
 template <bool FILTERED>
-__device__ __forceinline__ unsigned merge_dirs(const Unit& u, const UState& s, int f, int i, short2 p,
-                                               unsigned short age, int* cand, int& ncand) {
+__device__ __forceinline__ unsigned merge_dirs_w(const Unit& u, const UState& s, int f, short2 p, short2 v,
+                                                 unsigned short age, const BoxWords& bw, int* cand, int& ncand) {
   unsigned m = 0;
   ncand = 0;
-  // occ marks exactly the pixels whose index entry is current (matched
-  // particles, and births on detector frames): most neighbours are empty.  The
-  // 3x3 box touches at most four bin words (rows ra / rb, columns ca / cb).
-  const int ra = max(p.x - 1, 0), rb = min(p.x + 1, u.H - 1), ca = max(p.y - 1, 0), cb = min(p.y + 1, u.W - 1);
-  const unsigned long long wa = u.occ[bin_word(u, ra, ca)], wb = u.occ[bin_word(u, ra, cb)];
-  const unsigned long long wc = u.occ[bin_word(u, rb, ca)], wd = u.occ[bin_word(u, rb, cb)];
+  const int ra = max(p.x - 1, 0), ca = max(p.y - 1, 0);
+  const unsigned long long wa = bw.a, wb = bw.b, wc = bw.c, wd = bw.d;
   unsigned nb = 0;
 #pragma unroll
   for (int k = 0; k < 8; k++) {
@@ -1470,7 +1495,6 @@ __device__ __forceinline__ unsigned merge_dirs(const Unit& u, const UState& s, i
     if (in_dom(u, r, c) && (w & bin_bit(r, c))) nb |= 1u << k;
   }
   if (!nb) return 0;
-  const short2 v = u.spd[s.cur][i];
   while (nb) {  // occupied neighbours in c8_h order
     const int k = __ffs(nb) - 1;
     nb &= nb - 1;
@@ -1491,6 +1515,12 @@ __device__ __forceinline__ unsigned merge_dirs(const Unit& u, const UState& s, i
     }
   }
   return m;
+}
+
+template <bool FILTERED>
+__device__ __forceinline__ unsigned merge_dirs(const Unit& u, const UState& s, int f, int i, short2 p,
+                                               unsigned short age, int* cand, int& ncand) {
+  return merge_dirs_w<FILTERED>(u, s, f, p, u.spd[s.cur][i], age, box_words(u, p), cand, ncand);
 }
 
 // filter_bad_particles_kernel (tracking_strategies.hpp:482-523) and step 1 of
@@ -1518,12 +1548,20 @@ __global__ void __launch_bounds__(FM_THREADS) k_filter_merge(const Unit* __restr
     if (i < s.n) {
       const unsigned short age = u.age[s.cur][i];
       if (age != 0) {
+        // Everything that depends only on the slot and its position, loaded
+        // together: the bin's count and flow, the speed, the box's occupancy.
         const short2 p = u.pos[s.cur][i];
-        if (!filter_keeps(u, s.cur, i, age, p)) {
+        const int br = p.x / 8, bc = p.y / 8;
+        const size_t w = (size_t)br * u.BW + bc;
+        const unsigned mc = u.msc[w];
+        const float2 fl = u.flow[w];
+        const short2 v = u.spd[s.cur][i];
+        const BoxWords bw = box_words(u, p);
+        if (!filter_decide(u, age, mc, fl, v, br, bc)) {
           u.age[s.cur][i] = 0;
         } else if (u.with_merge) {
           int nc;
-          m = merge_dirs<false>(u, s, f, i, p, age, nullptr, nc);
+          m = merge_dirs_w<false>(u, s, f, p, v, age, bw, nullptr, nc);
         }
       }
       if (u.with_merge) u.cmask[i] = (uint8_t)m;
