@@ -74,7 +74,7 @@ def tracker(frames=6):
     from . import BatchTracker, synth
     cfg = [dict(rows=1080, cols=1920, nscales=4, detector_threshold=20, detector_frequency=10)] * 4
     vids = [synth.frames(1000 + i, 1080, 1920, frames) for i in range(4)]
-    bt = BatchTracker(cfg, graphs=False)
+    bt = BatchTracker(cfg, graphs=False, groups=1)  # one launch per stage over all four streams
     for t in range(frames):
         bt.run([v[t] for v in vids])
     bt.sync()
@@ -86,7 +86,7 @@ def tracker_det(frames=8):
     from . import BatchTracker, synth
     cfg = [dict(rows=1080, cols=1920, nscales=4, detector_threshold=20, detector_frequency=3)] * 4
     vids = [synth.frames(1000 + i, 1080, 1920, frames) for i in range(4)]
-    bt = BatchTracker(cfg, graphs=False)
+    bt = BatchTracker(cfg, graphs=False, groups=1)  # one launch per stage over all four streams
     for t in range(frames):
         bt.run([v[t] for v in vids])
     bt.sync()
