@@ -73,7 +73,7 @@ struct Unit {
   int* act_cnt;       // merge actives per 32 slots (cap / 32), then offsets
   uint8_t* cmask;     // cap candidate direction masks
   int4* act_list;     // cap entries: (i, pos packed, ncand, first cand) + cand store
-  int* act_cand;      // cap * 8 candidate indices
+  int* act_cand;      // cap * 8: an active slot's candidate slots, in c8_h order
   // matcher tiles (k_match_tiled)
   int MTR, MTC;       // tiles per column / row
   int mt_base;        // first tile of this unit in the context-wide tile arrays

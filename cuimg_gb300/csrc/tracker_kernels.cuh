@@ -1526,7 +1526,8 @@ __device__ __forceinline__ unsigned merge_dirs(const Unit& u, const UState& s, i
 // filter_bad_particles_kernel (tracking_strategies.hpp:482-523) and step 1 of
 // the merge in one pass: each live particle applies the filter to itself and,
 // when it survives, finds its qualifying directions.  Actives are counted per
-// warp of 32 slots (act_cnt[i / 32]) for k_merge_unit.
+// warp of 32 slots (act_cnt[i / 32]) and their candidates stored at their slot
+// (act_cand[8 i ..]) for k_merge_unit.
 // Quarter-chunk CTAs (256 threads) for the merge passes: their register
 // footprint allows six CTAs per SM, where 1024-thread CTAs get one.
 constexpr int FM_THREADS = 256;
@@ -1560,8 +1561,10 @@ __global__ void __launch_bounds__(FM_THREADS) k_filter_merge(const Unit* __restr
         if (!filter_decide(u, age, mc, fl, v, br, bc)) {
           u.age[s.cur][i] = 0;
         } else if (u.with_merge) {
-          int nc;
-          m = merge_dirs_w<false>(u, s, f, p, v, age, bw, nullptr, nc);
+          // An active's candidates (c8_h order) go to act_cand at its slot.
+          int cand[8], nc;
+          m = merge_dirs_w<false>(u, s, f, p, v, age, bw, cand, nc);
+          for (int q = 0; q < nc; q++) u.act_cand[(size_t)i * 8 + q] = cand[q];
         }
       }
       if (u.with_merge) u.cmask[i] = (uint8_t)m;
@@ -1620,9 +1623,9 @@ __device__ __forceinline__ int block_scan(int v, int* warp_tot, int& total) {
 // Steps 2 and 3 of the merge for one unit per CTA.  Step 2: the actives in
 // slot order -- warps of 32 slots taken 1024 at a time, their active counts
 // (act_cnt, from k_filter_merge) scanned across the CTA, and each warp with
-// actives expanded by one thread into act_list / act_cand (its qualifying
-// neighbours recomputed, with the post-filter ages).  Step 3: the ordered
-// replay described above.
+// actives expanded by a warp of threads into act_list (slot, position, number
+// of candidates; the candidates themselves are at the slot in act_cand).
+// Step 3: the ordered replay described above.
 constexpr int MU_THREADS = 1024;
 static_assert(MR_HASH >= 2 * MU_THREADS, "the active-warp lists fit in the liveness table");
 
@@ -1660,13 +1663,11 @@ __global__ void __launch_bounds__(MU_THREADS) k_merge_unit(const Unit* __restric
       const bool act = i < s.n && u.cmask[i] != 0;
       const unsigned bal = __ballot_sync(0xffffffffu, act);
       if (act) {
+        // One candidate per direction bit, stored at the slot by k_filter_merge.
         const int o = wo[q] + __popc(bal & ((1u << lane0) - 1u));
         const short2 p = u.pos[s.cur][i];
-        int cand[8];
-        int nc;
-        merge_dirs<true>(u, s, f, i, p, u.age[s.cur][i], cand, nc);
-        u.act_list[o] = make_int4(i, (int)(((unsigned)(unsigned short)p.x << 16) | (unsigned short)p.y), nc, 0);
-        for (int r = 0; r < nc; r++) u.act_cand[(size_t)o * 8 + r] = cand[r];
+        u.act_list[o] = make_int4(i, (int)(((unsigned)(unsigned short)p.x << 16) | (unsigned short)p.y),
+                                  __popc((unsigned)u.cmask[i]), 0);
       }
     }
     A += tot;
@@ -1688,7 +1689,7 @@ __global__ void __launch_bounds__(MU_THREADS) k_merge_unit(const Unit* __restric
     for (int k = threadIdx.x; k < nb; k += blockDim.x) {
       int4 e = u.act_list[base + k];
       ent[k] = e;
-      for (int q = 0; q < e.z; q++) cnd[k][q] = u.act_cand[(size_t)(base + k) * 8 + q];
+      for (int q = 0; q < e.z; q++) cnd[k][q] = u.act_cand[(size_t)e.x * 8 + q];
     }
     __syncthreads();
     // Register every touched slot with its current liveness (killed bit set
