@@ -20,6 +20,7 @@
 //                 age (uint16), feature (16 bytes).
 #pragma once
 #include <cstdint>
+#include <cuda.h>  // CUtensorMap (the type only; the library does not link the driver API)
 #include <cuda_runtime.h>
 
 namespace gbt {
@@ -114,6 +115,7 @@ struct Frame {
 
 constexpr int ERR_CAPACITY = 1;
 constexpr int ERR_MERGE_OVERFLOW = 2;
+constexpr int ERR_TIMEOUT = 4;  // a bounded wait on an asynchronous copy gave up
 
 // c8_h in raster order (cuimg/neighb2d_data.h:80-85), (row, col).
 __constant__ int8_t c_c8[8][2] = {{-1, 1}, {0, 1}, {1, 1}, {-1, 0}, {1, 0}, {-1, -1}, {0, -1}, {1, -1}};

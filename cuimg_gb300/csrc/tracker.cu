@@ -109,6 +109,10 @@ struct Group {
   int match_variant = 0;  // GBT_TUNE_MATCHER
   int mt_shape = 3;       // GBT_TUNE_MATCH_TILE: tiled matcher threads and particle assignment
   int fm_grid = 0;        // k_filter_merge CTAs: the ones all SMs hold at once
+  // TMA descriptors of every unit's s1 and s2 for the tiled matcher, parity 0
+  // then 1 (null when the driver cannot encode them: the matcher then stages
+  // its tiles with cp.async)
+  CUtensorMap* d_tmaps = nullptr;
   bool fixed_fpitch = true;  // every unit's s1/s2 pitch is FIXED_FPITCH
   bool any_alt_detector = false;  // a stream uses the regular or the dense detector
   std::string err;
@@ -238,6 +242,47 @@ static int upload_units(Group* ctx) {
     for (size_t i = 0; i < n; i++) v[i] = unit_view(ctx, i, par);
     CK(cudaMemcpy(ctx->d_units_v[par], v.data(), n * sizeof(Unit), cudaMemcpyHostToDevice));
   }
+  return GBT_OK;
+}
+
+// cuTensorMapEncodeTiled through the runtime's driver entry point (the
+// library does not link the driver API).
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+// 2-D uint8 maps over the bordered s1 / s2 (FIXED_FPITCH bytes by H + 2 RB
+// rows, row stride FIXED_FPITCH) with the matcher's staged box (MT_SC bytes
+// by MT_SR rows).  Leaves d_tmaps null when the entry point or an encoding is
+// unavailable.
+static int encode_tile_maps(Group* ctx) {
+  void* fn = nullptr;
+  cudaDriverEntryPointQueryResult q;
+  if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+      q != cudaDriverEntryPointSuccess || !fn) {
+    cudaGetLastError();
+    return GBT_OK;
+  }
+  const EncodeTiledFn encode = (EncodeTiledFn)fn;
+  const size_t nunits = ctx->units.size();
+  std::vector<CUtensorMap> maps(2 * nunits * 2);
+  for (int par = 0; par < 2; par++)
+    for (size_t ui = 0; ui < nunits; ui++) {
+      const Unit v = unit_view(ctx, ui, par);
+      const cuuint64_t dims[2] = {(cuuint64_t)FIXED_FPITCH, (cuuint64_t)(v.H + 2 * RB)};
+      const cuuint64_t strides[1] = {(cuuint64_t)FIXED_FPITCH};
+      const cuuint32_t box[2] = {(cuuint32_t)MT_SC, (cuuint32_t)MT_SR};
+      const cuuint32_t estr[2] = {1, 1};
+      uint8_t* img[2] = {v.s1, v.s2};
+      for (int k = 0; k < 2; k++)
+        if (encode(&maps[(par * nunits + ui) * 2 + k], CU_TENSOR_MAP_DATA_TYPE_UINT8, 2, img[k], dims, strides, box,
+                   estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+          return GBT_OK;
+    }
+  int r;
+  if ((r = dalloc_t(ctx, &ctx->d_tmaps, maps.size(), false))) return r;
+  CK(cudaMemcpy(ctx->d_tmaps, maps.data(), maps.size() * sizeof(CUtensorMap), cudaMemcpyHostToDevice));
   return GBT_OK;
 }
 
@@ -375,6 +420,7 @@ static int build(Group* ctx, const gbt_config* cfgs, int nstreams) {
   if ((r = dalloc_t(ctx, &ctx->d_units_v[1], nunits, false))) return r;
   ctx->d_units = ctx->d_units_v[0];
   if ((r = upload_units(ctx))) return r;
+  if (ctx->fixed_fpitch && (r = encode_tile_maps(ctx))) return r;
   if ((r = dalloc_t(ctx, &ctx->d_state, nunits))) return r;
   if ((r = dalloc_t(ctx, &ctx->d_frame, 1))) return r;
   if ((r = dalloc_t(ctx, &ctx->d_counts, nunits))) return r;
@@ -592,14 +638,16 @@ static int enqueue_back(Group* ctx, bool any_det, bool any_filt, int par, int& n
     { PROF("k_mt_scan"); k_mt_scan<<<1, 1024, 0, st>>>(ctx->d_mt_cnt, ctx->mt_tiles, ctx->d_mt_off); }
     { PROF("k_mt_scatter"); k_mt_bin<1><<<pgrid, CHUNK, 0, st>>>(du, ctx->d_state, ctx->d_pre, nunits, nullptr, ctx->d_mt_key, ctx->d_mt_off, ctx->d_mt_list); }
     PROF("k_match_tiled");
+    const CUtensorMap* tm = ctx->d_tmaps ? ctx->d_tmaps + (size_t)par * nunits * 2 : nullptr;
+    int* err = &ctx->d_frame->err;
     if (ctx->mt_shape == 1)
-      k_match_tiled<128, true, 8><<<ctx->mt_tiles, 128, 0, st>>>(du, ctx->d_state, ctx->d_frame, ctx->d_mt_prefix, nunits, ctx->d_mt_off, ctx->d_mt_list);
+      k_match_tiled<128, true, 8><<<ctx->mt_tiles, 128, 0, st>>>(du, ctx->d_state, ctx->d_frame, ctx->d_mt_prefix, nunits, ctx->d_mt_off, ctx->d_mt_list, tm, err);
     else if (ctx->mt_shape == 2)
-      k_match_tiled<64, true, 10><<<ctx->mt_tiles, 64, 0, st>>>(du, ctx->d_state, ctx->d_frame, ctx->d_mt_prefix, nunits, ctx->d_mt_off, ctx->d_mt_list);
+      k_match_tiled<64, true, 10><<<ctx->mt_tiles, 64, 0, st>>>(du, ctx->d_state, ctx->d_frame, ctx->d_mt_prefix, nunits, ctx->d_mt_off, ctx->d_mt_list, tm, err);
     else if (ctx->mt_shape == 3)
-      k_match_tiled<256, true, 4><<<ctx->mt_tiles, 256, 0, st>>>(du, ctx->d_state, ctx->d_frame, ctx->d_mt_prefix, nunits, ctx->d_mt_off, ctx->d_mt_list);
+      k_match_tiled<256, true, 4><<<ctx->mt_tiles, 256, 0, st>>>(du, ctx->d_state, ctx->d_frame, ctx->d_mt_prefix, nunits, ctx->d_mt_off, ctx->d_mt_list, tm, err);
     else
-      k_match_tiled<MT_THREADS, false, 4><<<ctx->mt_tiles, MT_THREADS, 0, st>>>(du, ctx->d_state, ctx->d_frame, ctx->d_mt_prefix, nunits, ctx->d_mt_off, ctx->d_mt_list);
+      k_match_tiled<MT_THREADS, false, 4><<<ctx->mt_tiles, MT_THREADS, 0, st>>>(du, ctx->d_state, ctx->d_frame, ctx->d_mt_prefix, nunits, ctx->d_mt_off, ctx->d_mt_list, tm, err);
     n += 4;
   } else if (ctx->match_variant == 1) {
     PROF("k_match_warp");
@@ -908,6 +956,7 @@ static int grp_sync(Group* ctx) {
   Frame f;
   CK(cudaMemcpy(&f, ctx->d_frame, sizeof f, cudaMemcpyDeviceToHost));
   if (f.err & ERR_CAPACITY) return set_err(ctx, GBT_E_CAPACITY, "particle capacity exceeded");
+  if (f.err & ERR_TIMEOUT) return set_err(ctx, GBT_E_TIMEOUT, "a bounded wait on an asynchronous copy gave up");
   return GBT_OK;
 }
 

@@ -626,6 +626,51 @@ __device__ __forceinline__ void cp_async16(void* sdst, const void* gsrc) {
 // Stages rows R0s .. R0s + MT_SR - 1 and columns C0s .. C0s + MT_SC - 1 of s1
 // and s2, skipping chunks outside the bordered images (never sampled: the taps
 // stay within 6 pixels of the domain, inside the zero border).
+// The same tile by two TMA copies (one per image) that complete on an
+// mbarrier.  The staged region starts at byte column C0s + CB of the bordered
+// rows, a multiple of 16 (C0s = 128 k - 32, CB = 16); rows above or below the
+// bordered image read zeros.  Thread 0 issues; mt_tma_wait waits.
+__device__ __forceinline__ void mt_tma_issue(const CUtensorMap* m1, const CUtensorMap* m2, int R0s, int C0s,
+                                             uint8_t* ts1, uint8_t* ts2, unsigned long long* mbar) {
+  const unsigned bar = (unsigned)__cvta_generic_to_shared(mbar);
+  if (threadIdx.x == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(bar) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const int x = C0s + CB, y = R0s + RB;
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(bar), "r"(2 * MT_SR * MT_SC)
+                 : "memory");
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];\n" ::"r"(
+            (unsigned)__cvta_generic_to_shared(ts1)),
+        "l"(m1), "r"(x), "r"(y), "r"(bar)
+        : "memory");
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];\n" ::"r"(
+            (unsigned)__cvta_generic_to_shared(ts2)),
+        "l"(m2), "r"(x), "r"(y), "r"(bar)
+        : "memory");
+  }
+}
+
+// Waits for the tile (phase 0 of the mbarrier), giving up after a bounded
+// number of polls; false when it gave up.
+__device__ __forceinline__ bool mt_tma_wait(unsigned long long* mbar) {
+  const unsigned bar = (unsigned)__cvta_generic_to_shared(mbar);
+  for (int it = 0; it < (1 << 22); it++) {
+    unsigned done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(bar)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+
 __device__ __forceinline__ void mt_stage_issue(const Unit& u, int R0s, int C0s, uint8_t* ts1, uint8_t* ts2) {
   constexpr int CPR = MT_SC / 16;
   for (int v = threadIdx.x; v < MT_SR * CPR; v += blockDim.x) {
@@ -640,6 +685,8 @@ __device__ __forceinline__ void mt_stage_issue(const Unit& u, int R0s, int C0s, 
   asm volatile("cp.async.commit_group;\n" ::: "memory");
 }
 
+// The tile arrives by TMA when the context encoded tensor maps (tmaps: s1
+// and s2 of every unit, for the frame's parity), by cp.async otherwise.
 // THREADS per CTA; with DYN the threads take the tile's particles one at a
 // time from a shared counter (a thread that finishes a short descent takes the
 // next particle) instead of every THREADS-th one.
@@ -649,9 +696,12 @@ __global__ void __launch_bounds__(THREADS, MINB) k_match_tiled(const Unit* __res
                                                                const Frame* __restrict__ fr,
                                                                const int* __restrict__ tile_prefix, int nunits,
                                                                const int* __restrict__ off,
-                                                               const int* __restrict__ list) {
-  __shared__ __align__(16) uint8_t ts1[MT_SR * MT_SC];
-  __shared__ __align__(16) uint8_t ts2[MT_SR * MT_SC];
+                                                               const int* __restrict__ list,
+                                                               const CUtensorMap* __restrict__ tmaps,
+                                                               int* __restrict__ err) {
+  __shared__ __align__(128) uint8_t ts1[MT_SR * MT_SC];
+  __shared__ __align__(128) uint8_t ts2[MT_SR * MT_SC];
+  __shared__ __align__(8) unsigned long long mbar;
   __shared__ int next;
   const int t = blockIdx.x;
   const int n0 = off[t], n1 = off[t + 1];
@@ -661,7 +711,10 @@ __global__ void __launch_bounds__(THREADS, MINB) k_match_tiled(const Unit* __res
   const int local = t - tile_prefix[ui];
   const int R0s = (local / u.MTC) * MT_R - MT_MR, C0s = (local % u.MTC) * MT_C - MT_MC;
   if (DYN && threadIdx.x == 0) next = n0 + THREADS;
-  mt_stage_issue(u, R0s, C0s, ts1, ts2);
+  if (tmaps)
+    mt_tma_issue(tmaps + 2 * ui, tmaps + 2 * ui + 1, R0s, C0s, ts1, ts2, &mbar);
+  else
+    mt_stage_issue(u, R0s, C0s, ts1, ts2);
   // The thread's first particle is read while the tile arrives.
   const int f = fr->f;
   const int b = st[ui].cur;
@@ -677,7 +730,14 @@ __global__ void __launch_bounds__(THREADS, MINB) k_match_tiled(const Unit* __res
     spd = u.spd[b][i];
     feat = u.feat[b][i];
   }
-  asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+  if (tmaps) {
+    if (!mt_tma_wait(&mbar)) {
+      if (threadIdx.x == 0) atomicOr(err, ERR_TIMEOUT);
+      return;
+    }
+  } else {
+    asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+  }
   __syncthreads();
   FeatFP<MT_SC> F;
   F.s1 = ts1 - (R0s * MT_SC + C0s);  // F.s1 + (r * MT_SC + c) is staged pixel (r, c)
