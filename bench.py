@@ -43,7 +43,7 @@ PER_PARTICLE_BYTES = 84  # state read/write, template read/write, sparse index
 # 4-stream launches (profiles/k_match_tiled_1080p_x4.md, profiles/k_match_1080p_x4.md),
 # and the busiest unit of the tiled matcher there (l1tex__data_pipe_lsu_wavefronts).
 DRAM_BYTES_PER_STREAM = {"k_match_tiled": 20.0e6, "k_match": 19.2e6}
-LIMITER = {"k_match_tiled": ("L1 / shared-memory data pipe (byte gathers at the ring offsets)", 0.69)}
+LIMITER = {"k_match_tiled": ("L1 / shared-memory data pipe (byte gathers at the ring offsets)", 0.74)}
 
 
 def level_pixels():
