@@ -25,6 +25,29 @@ KNOBS = {
 DEFAULT_CACHE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "_build", "autotune.json")
 
 
+def _load_cache(cache_path):
+    if os.path.exists(cache_path):
+        try:
+            with open(cache_path) as f:
+                return json.load(f)
+        except (OSError, ValueError):
+            pass
+    return {}
+
+
+def _store(cache_path, key, value):
+    """Adds one entry to the cache file, written to a temporary file first and
+    renamed over the old one, so that processes tuning at the same time (one per
+    GPU) never leave a partial file."""
+    os.makedirs(os.path.dirname(cache_path), exist_ok=True)
+    cache = _load_cache(cache_path)
+    cache[key] = value
+    tmp = "%s.%d.tmp" % (cache_path, os.getpid())
+    with open(tmp, "w") as f:
+        json.dump(cache, f, indent=1, sort_keys=True)
+    os.replace(tmp, cache_path)
+
+
 def _gpu_name(device):
     try:
         import torch
@@ -57,13 +80,7 @@ def tune(configs, frames, warmup=3, timed=8, device=0, cache_path=DEFAULT_CACHE,
     """frames[t][s]: frame t of stream s (numpy uint8).  Returns {knob: value}."""
     from .tracker import BatchTracker
     key = signature(configs, device)
-    cache = {}
-    if os.path.exists(cache_path):
-        try:
-            with open(cache_path) as f:
-                cache = json.load(f)
-        except (OSError, ValueError):
-            cache = {}
+    cache = _load_cache(cache_path)
     if key in cache and not force:
         return {int(k): v for k, v in cache[key].items()}
     lib = cuda_lib()
@@ -87,10 +104,7 @@ def tune(configs, frames, warmup=3, timed=8, device=0, cache_path=DEFAULT_CACHE,
             if best is None or ms < best[0]:
                 best = (ms, value)
         choice[knob] = best[1]
-    cache[key] = {str(k): v for k, v in choice.items()}
-    os.makedirs(os.path.dirname(cache_path), exist_ok=True)
-    with open(cache_path, "w") as f:
-        json.dump(cache, f, indent=1, sort_keys=True)
+    _store(cache_path, key, {str(k): v for k, v in choice.items()})
     return choice
 
 
@@ -114,14 +128,7 @@ def tune_lk(prev, cur, points, nlevels, prm, reps=3, cache_path=DEFAULT_CACHE, f
     dev = prev.device.index or 0
     key = "lk|%s|%s|%s|%d|%d|%d|%d|%d" % (_gpu_name(dev), "x".join(map(str, prev.shape)), str(prev.dtype),
                                          points.shape[-2], nlevels, prm.window, prm.npix, prm.max_iter)
-    cache = {}
-    if os.path.exists(cache_path):
-        try:
-            with open(cache_path) as f:
-                cache = json.load(f)
-        except (OSError, ValueError):
-            cache = {}
-    best = cache.get(key) if not force else None
+    best = _load_cache(cache_path).get(key) if not force else None
     if best is None:
         times = {}
         for w in LK_WARPS:
@@ -135,8 +142,5 @@ def tune_lk(prev, cur, points, nlevels, prm, reps=3, cache_path=DEFAULT_CACHE, f
             e1.synchronize()
             times[w] = e0.elapsed_time(e1)
         best = min(times, key=times.get)
-        cache[key] = best
-        os.makedirs(os.path.dirname(cache_path), exist_ok=True)
-        with open(cache_path, "w") as f:
-            json.dump(cache, f, indent=1, sort_keys=True)
+        _store(cache_path, key, best)
     return lk.params(prm.window, prm.npix, prm.max_iter, prm.eps, prm.max_err, int(best))
