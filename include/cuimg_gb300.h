@@ -127,8 +127,10 @@ int gbt_run_resident(gbt_ctx* ctx);
  * context stream (gbt_stream) or synchronously. */
 int gbt_input_slot(gbt_ctx* ctx, int32_t stream, uint8_t** dptr, int64_t* pitch);
 
-/* Capture the per-frame launch sequence into CUDA graphs (one per frame
- * kind) and replay them from then on (1), or launch stage by stage (0). */
+/* Capture the per-frame launch sequences into CUDA graphs and replay them
+ * from then on (1), or launch stage by stage (0).  Each stream group keeps a
+ * front-end graph per frame parity and a back-end graph per frame kind
+ * (detector and filter frames or not) and parity. */
 int gbt_use_graphs(gbt_ctx* ctx, int32_t enable);
 
 /* Waits for all queued work; returns GBT_E_CAPACITY/GBT_E_TIMEOUT if a
