@@ -310,8 +310,16 @@ static int build(Group* ctx, const gbt_config* cfgs, int nstreams) {
     CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_filter_merge, FM_THREADS, 0));
     ctx->fm_grid = ctx->nsm * std::max(1, per_sm);
   }
-  CK(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
-  CK(cudaStreamCreateWithFlags(&ctx->pre, cudaStreamNonBlocking));
+  {
+    // The back end carries the frame-to-frame dependency, so its blocks are
+    // dispatched first; the front end (next frame's pyramid and blurs) fills
+    // the SMs the back end leaves idle.  Graph launches take their stream's
+    // priority.
+    int least = 0, greatest = 0;
+    CK(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+    CK(cudaStreamCreateWithPriority(&ctx->stream, cudaStreamNonBlocking, greatest));
+    CK(cudaStreamCreateWithPriority(&ctx->pre, cudaStreamNonBlocking, least));
+  }
   for (cudaEvent_t* e : {&ctx->ev_front, &ctx->ev_back[0], &ctx->ev_back[1]})
     CK(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
   // Units: streams in order, scales 0..L-1 of each stream contiguous.
