@@ -108,6 +108,7 @@ struct Group {
   long long kernels_total = 0;  // kernels launched by this context, graph nodes included
   int match_variant = 0;  // GBT_TUNE_MATCHER
   int mt_shape = 3;       // GBT_TUNE_MATCH_TILE: tiled matcher threads and particle assignment
+  int withhold_tiles = 0; // test hook: the tiled matcher's tile copies are not issued
   int fm_grid = 0;        // k_filter_merge CTAs: the ones all SMs hold at once
   // TMA descriptors of every unit's s1 and s2 for the tiled matcher, parity 0
   // then 1 (null when the driver cannot encode them: the matcher then stages
@@ -649,13 +650,13 @@ static int enqueue_back(Group* ctx, bool any_det, bool any_filt, int par, int& n
     const CUtensorMap* tm = ctx->d_tmaps ? ctx->d_tmaps + (size_t)par * nunits * 2 : nullptr;
     int* err = &ctx->d_frame->err;
     if (ctx->mt_shape == 1)
-      k_match_tiled<128, true, 8><<<ctx->mt_tiles, 128, 0, st>>>(du, ctx->d_state, ctx->d_frame, ctx->d_mt_prefix, nunits, ctx->d_mt_off, ctx->d_mt_list, tm, err);
+      k_match_tiled<128, true, 8><<<ctx->mt_tiles, 128, 0, st>>>(du, ctx->d_state, ctx->d_frame, ctx->d_mt_prefix, nunits, ctx->d_mt_off, ctx->d_mt_list, tm, err, ctx->withhold_tiles);
     else if (ctx->mt_shape == 2)
-      k_match_tiled<64, true, 10><<<ctx->mt_tiles, 64, 0, st>>>(du, ctx->d_state, ctx->d_frame, ctx->d_mt_prefix, nunits, ctx->d_mt_off, ctx->d_mt_list, tm, err);
+      k_match_tiled<64, true, 10><<<ctx->mt_tiles, 64, 0, st>>>(du, ctx->d_state, ctx->d_frame, ctx->d_mt_prefix, nunits, ctx->d_mt_off, ctx->d_mt_list, tm, err, ctx->withhold_tiles);
     else if (ctx->mt_shape == 3)
-      k_match_tiled<256, true, 4><<<ctx->mt_tiles, 256, 0, st>>>(du, ctx->d_state, ctx->d_frame, ctx->d_mt_prefix, nunits, ctx->d_mt_off, ctx->d_mt_list, tm, err);
+      k_match_tiled<256, true, 4><<<ctx->mt_tiles, 256, 0, st>>>(du, ctx->d_state, ctx->d_frame, ctx->d_mt_prefix, nunits, ctx->d_mt_off, ctx->d_mt_list, tm, err, ctx->withhold_tiles);
     else
-      k_match_tiled<MT_THREADS, false, 4><<<ctx->mt_tiles, MT_THREADS, 0, st>>>(du, ctx->d_state, ctx->d_frame, ctx->d_mt_prefix, nunits, ctx->d_mt_off, ctx->d_mt_list, tm, err);
+      k_match_tiled<MT_THREADS, false, 4><<<ctx->mt_tiles, MT_THREADS, 0, st>>>(du, ctx->d_state, ctx->d_frame, ctx->d_mt_prefix, nunits, ctx->d_mt_off, ctx->d_mt_list, tm, err, ctx->withhold_tiles);
     n += 4;
   } else if (ctx->match_variant == 1) {
     PROF("k_match_warp");
@@ -859,6 +860,15 @@ static int grp_trajectories_enable(Group* ctx, int32_t history) {
   if (r2) return r2;
   drop_graphs(ctx);
   ctx->traj_T = history;
+  return GBT_OK;
+}
+
+static int grp_test_withhold_tile_copies(Group* ctx, int32_t enable) {
+  if (!ctx) return GBT_E_INVALID;
+  if (!ctx->d_tmaps || ctx->match_variant != 0 || !ctx->fixed_fpitch)
+    return set_err(ctx, GBT_E_INVALID, "the tiled matcher does not stage its tiles by TMA in this context");
+  if (ctx->withhold_tiles != (enable != 0)) drop_graphs(ctx);
+  ctx->withhold_tiles = enable != 0;
   return GBT_OK;
 }
 
@@ -1582,6 +1592,15 @@ extern "C" int gbt_trajectories_enable(gbt_ctx* c, int32_t history) {
 extern "C" int gbt_use_graphs(gbt_ctx* c, int32_t enable) {
   if (!c) return GBT_E_INVALID;
   for (Group* g : c->g) grp_use_graphs(g, enable);
+  return GBT_OK;
+}
+
+extern "C" int gbt_test_withhold_tile_copies(gbt_ctx* c, int32_t enable) {
+  if (!c) return GBT_E_INVALID;
+  for (Group* g : c->g) {
+    int r = grp_test_withhold_tile_copies(g, enable);
+    if (r) return adopt(c, g, r);
+  }
   return GBT_OK;
 }
 

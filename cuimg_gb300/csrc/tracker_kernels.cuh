@@ -631,7 +631,7 @@ __device__ __forceinline__ void cp_async16(void* sdst, const void* gsrc) {
 // rows, a multiple of 16 (C0s = 128 k - 32, CB = 16); rows above or below the
 // bordered image read zeros.  Thread 0 issues; mt_tma_wait waits.
 __device__ __forceinline__ void mt_tma_issue(const CUtensorMap* m1, const CUtensorMap* m2, int R0s, int C0s,
-                                             uint8_t* ts1, uint8_t* ts2, unsigned long long* mbar) {
+                                             uint8_t* ts1, uint8_t* ts2, unsigned long long* mbar, bool copies) {
   const unsigned bar = (unsigned)__cvta_generic_to_shared(mbar);
   if (threadIdx.x == 0) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(bar) : "memory");
@@ -642,6 +642,7 @@ __device__ __forceinline__ void mt_tma_issue(const CUtensorMap* m1, const CUtens
     const int x = C0s + CB, y = R0s + RB;
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(bar), "r"(2 * MT_SR * MT_SC)
                  : "memory");
+    if (!copies) return;  // test hook: the barrier is armed but nothing will complete it
     asm volatile(
         "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];\n" ::"r"(
             (unsigned)__cvta_generic_to_shared(ts1)),
@@ -655,10 +656,18 @@ __device__ __forceinline__ void mt_tma_issue(const CUtensorMap* m1, const CUtens
   }
 }
 
-// Waits for the tile (phase 0 of the mbarrier), giving up after a bounded
-// number of polls; false when it gave up.
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// Waits for the tile (phase 0 of the mbarrier), giving up after MT_WAIT_NS of
+// the global timer or 2^22 polls, whichever comes first; false when it gave up.
+constexpr unsigned long long MT_WAIT_NS = 500000000ull;
 __device__ __forceinline__ bool mt_tma_wait(unsigned long long* mbar) {
   const unsigned bar = (unsigned)__cvta_generic_to_shared(mbar);
+  const unsigned long long t0 = global_ns();
   for (int it = 0; it < (1 << 22); it++) {
     unsigned done;
     asm volatile(
@@ -667,6 +676,7 @@ __device__ __forceinline__ bool mt_tma_wait(unsigned long long* mbar) {
         : "r"(bar)
         : "memory");
     if (done) return true;
+    if (global_ns() - t0 > MT_WAIT_NS) break;
   }
   return false;
 }
@@ -689,7 +699,9 @@ __device__ __forceinline__ void mt_stage_issue(const Unit& u, int R0s, int C0s, 
 // and s2 of every unit, for the frame's parity), by cp.async otherwise.
 // THREADS per CTA; with DYN the threads take the tile's particles one at a
 // time from a shared counter (a thread that finishes a short descent takes the
-// next particle) instead of every THREADS-th one.
+// next particle) instead of every THREADS-th one.  A tile whose wait gives up
+// sets ERR_TIMEOUT in *err and leaves its particles unmatched; `withhold`
+// (a test hook) arms the barrier without issuing the copies, so that it does.
 template <int THREADS, bool DYN, int MINB>
 __global__ void __launch_bounds__(THREADS, MINB) k_match_tiled(const Unit* __restrict__ units,
                                                                const UState* __restrict__ st,
@@ -698,7 +710,7 @@ __global__ void __launch_bounds__(THREADS, MINB) k_match_tiled(const Unit* __res
                                                                const int* __restrict__ off,
                                                                const int* __restrict__ list,
                                                                const CUtensorMap* __restrict__ tmaps,
-                                                               int* __restrict__ err) {
+                                                               int* __restrict__ err, int withhold) {
   __shared__ __align__(128) uint8_t ts1[MT_SR * MT_SC];
   __shared__ __align__(128) uint8_t ts2[MT_SR * MT_SC];
   __shared__ __align__(8) unsigned long long mbar;
@@ -712,7 +724,7 @@ __global__ void __launch_bounds__(THREADS, MINB) k_match_tiled(const Unit* __res
   const int R0s = (local / u.MTC) * MT_R - MT_MR, C0s = (local % u.MTC) * MT_C - MT_MC;
   if (DYN && threadIdx.x == 0) next = n0 + THREADS;
   if (tmaps)
-    mt_tma_issue(tmaps + 2 * ui, tmaps + 2 * ui + 1, R0s, C0s, ts1, ts2, &mbar);
+    mt_tma_issue(tmaps + 2 * ui, tmaps + 2 * ui + 1, R0s, C0s, ts1, ts2, &mbar, !withhold);
   else
     mt_stage_issue(u, R0s, C0s, ts1, ts2);
   // The thread's first particle is read while the tile arrives.

@@ -134,8 +134,18 @@ int gbt_input_slot(gbt_ctx* ctx, int32_t stream, uint8_t** dptr, int64_t* pitch)
 int gbt_use_graphs(gbt_ctx* ctx, int32_t enable);
 
 /* Waits for all queued work; returns GBT_E_CAPACITY/GBT_E_TIMEOUT if a
- * device-side check failed since the last call. */
+ * device-side check has failed in this context (the flags stay set: the
+ * particle state is no longer the reference's from then on). */
 int gbt_sync(gbt_ctx* ctx);
+
+/* Test hook for the bounded device-side waits (no reference counterpart).
+ * With `enable` set, the tiled matcher arms each tile's barrier but issues no
+ * copy, so every tile's wait gives up (after 0.5 s of the GPU's global timer),
+ * leaves the tile's particles unmatched and flags the context: the next
+ * gbt_sync returns GBT_E_TIMEOUT.  Nothing faults; the device and other
+ * contexts stay usable.  GBT_E_INVALID when the context does not stage tiles
+ * by TMA (another matcher variant, or no tensor maps). */
+int gbt_test_withhold_tile_copies(gbt_ctx* ctx, int32_t enable);
 
 /* The CUDA stream (cudaStream_t) that follows the context's work: after every
  * call that queues work it waits for all of that work, so an event recorded

@@ -274,6 +274,39 @@ def test_flat_and_empty_frames():
     tr.close()
 
 
+def test_bounded_tile_wait_reports_timeout_and_the_device_stays_usable():
+    # The tiled matcher waits for its TMA-staged tile on an mbarrier with a
+    # time limit.  With the copies withheld nothing completes the barrier:
+    # every tile's wait gives up, the next gbt_sync reports GBT_E_TIMEOUT, and
+    # no fault follows -- a fresh context on the same device then tracks
+    # bit-exactly.
+    import time
+
+    from cuimg_gb300 import GbtError, synth
+    from cuimg_gb300._native import cuda_lib
+    lib = cuda_lib()
+    frames = synth.frames(5, 240, 320, 3)
+    tr = _gpu_tracker(240, 320, 2, detf=10, graphs=True)
+    for t in range(2):
+        tr.run(frames[t])
+    tr.sync()
+    assert tr.nparticles() > 0
+    assert lib.gbt_test_withhold_tile_copies(tr._ensure(), 1) == 0
+    t0 = time.perf_counter()
+    with pytest.raises(GbtError) as e:
+        tr.run(frames[2])
+        tr.sync()
+    assert e.value.code == 5
+    assert time.perf_counter() - t0 < 30.0
+    tr.close()
+    # Another matcher variant has no tile copies to withhold.
+    tr = _gpu_tracker(64, 96, 1)
+    tr.set_tuning(0, 2)
+    assert lib.gbt_test_withhold_tile_copies(tr._ensure(), 1) == 1
+    tr.close()
+    assert _compare_run(240, 320, 2, 4, 5) > 0
+
+
 def test_invalid_geometry_rejected():
     from cuimg_gb300 import GbtError, Tracker
     tr = Tracker((97, 131), 3)
