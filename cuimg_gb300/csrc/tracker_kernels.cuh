@@ -108,76 +108,103 @@ __global__ void __launch_bounds__(256) k_pyramid(const Unit* __restrict__ units,
 // s(r,c) = (2 t[r] + t[r-1] + t[r+1]) / 4 for r in [1, H-2]; every other
 // pixel (the ring and the border) is zero.
 //
-// One warp walks down a strip of BL_SR rows, 128 columns wide: every lane owns
+// One warp walks down a strip of SR rows, 128 columns wide: every lane owns
 // four columns (one 32-bit word per row), takes its horizontal neighbours from
 // the adjacent lanes by shuffle, and keeps the last three rows of both row
 // passes in registers, so each level pixel is read once and s1 / s2 are each
 // written once.  Lanes 0 and 31 only supply the horizontal halo; strips overlap
-// by 8 columns.  The arithmetic is SIMD within a register: a word's even and
-// odd bytes sit in the two 16-bit halves of two words, where the sums (at
-// most 4 x 255) cannot carry into the neighbouring half, so every operation
-// filters two pixels.
+// by 8 columns.  The arithmetic filters a word's four pixels at once:
+// floor((a + 2b + c) / 4) == floor((floor((a + c) / 2) + b) / 2) for all
+// integers a, b, c >= 0 (with a + c = 2k + e, e in {0, 1}, both sides are
+// floor((k + b) / 2): the extra e / 4 never reaches the next integer), and the
+// bytewise floor average (a & b) + ((a ^ b) >> 1 & 0x7F7F7F7F) cannot carry
+// from one byte into the next.
 constexpr int BL_SR = 64;                 // default rows per strip (tunable: 16, 32, 64)
 constexpr int BL_OC = 120;                // output columns per warp (lanes 1..30)
 constexpr int BL_WARPS = 8;
-constexpr uint32_t BL_LO = 0x00FF00FFu;   // the two 16-bit halves' low bytes
 
-// Two 16-bit lanes per word: e holds pixels 0 and 2 of a lane's four, o pixels 1 and 3.
-struct Pair {
-  uint32_t e, o;
-};
+// Per-byte floor((a + b) / 2).
+__device__ __forceinline__ uint32_t havg4(uint32_t a, uint32_t b) {
+  return (a & b) + (((a ^ b) >> 1) & 0x7F7F7F7Fu);
+}
 
-// Row pass (2 x[c] + x[c-1] + x[c+1]) / 4 of a lane's word w; the left
-// neighbour of pixel 0 is the top byte of wl, the right neighbour of pixel 3
-// the low byte of wr.  me / mo zero the pixels outside [1, W-2] (or the row).
-__device__ __forceinline__ Pair row_pass2(uint32_t E, uint32_t O, uint32_t wl, uint32_t wr, uint32_t me,
-                                          uint32_t mo) {
-  const uint32_t L = (O << 16) | (wl >> 24);           // left neighbours of pixels 0, 2
-  const uint32_t R = (E >> 16) | ((wr & 0xFFu) << 16); // right neighbours of pixels 1, 3
-  Pair t;
-  t.e = (((E << 1) + O + L) >> 2) & me;
-  t.o = (((O << 1) + E + R) >> 2) & mo;
-  return t;
+// Row pass (2 x[c] + x[c-1] + x[c+1]) / 4 of a lane's word w; wl / wr are the
+// words of the lanes to its left and right.  m zeroes the pixels outside
+// [1, W-2] (or the whole row).
+__device__ __forceinline__ uint32_t row_pass4(uint32_t w, uint32_t wl, uint32_t wr, uint32_t m) {
+  const uint32_t L = __funnelshift_l(wl, w, 8);  // byte j: pixel j - 1
+  const uint32_t R = __funnelshift_r(w, wr, 8);  // byte j: pixel j + 1
+  return havg4(havg4(L, R), w) & m;
 }
 
 // Column pass (2 t[r] + t[r-1] + t[r+1]) / 4; m zeroes a row outside [1, H-2].
-__device__ __forceinline__ Pair col_pass2(const Pair& up, const Pair& mid, const Pair& dn, uint32_t m) {
-  Pair s;
-  s.e = (((mid.e << 1) + up.e + dn.e) >> 2) & m;
-  s.o = (((mid.o << 1) + up.o + dn.o) >> 2) & m;
-  return s;
+__device__ __forceinline__ uint32_t col_pass4(uint32_t up, uint32_t mid, uint32_t dn, uint32_t m) {
+  return havg4(havg4(up, dn), mid) & m;
 }
 
-// One row step: level row r enters (word w); s1 row r-1 and s2 row r-2 leave.
-// a1/b1/c1 are the row-pass values of rows r-2, r-1 and (written here) r;
-// a2/b2/c2 those of s1 rows r-3, r-2 and (written here) r-1.
-__device__ __forceinline__ void blur_step(const Unit& U, uint32_t w, int r, int r0, int r1, int c0, int H,
-                                          bool out_lane, bool full_word, uint32_t me, uint32_t mo, const Pair& a1,
-                                          const Pair& b1, Pair& c1, const Pair& a2, const Pair& b2, Pair& c2) {
+// A lane's word of s1 or s2 (pixels c0 .. c0 + 3, clipped to the row).
+__device__ __forceinline__ void blur_store(uint8_t* p, uint32_t v, bool full_word, int c0, int W) {
+  if (full_word) *(uint32_t*)p = v;
+  else
+    for (int j = 0; j < 4 && c0 + j < W; j++) p[j] = (uint8_t)(v >> (8 * j));
+}
+
+// One row step: level row r enters (word w); s1 row r-1 and s2 row r-2 leave,
+// stored at d1 / d2 when they belong to the strip [r0, r1).  a1/b1/c1 are the
+// row-pass values of rows r-2, r-1 and (written here) r; a2/b2/c2 those of s1
+// rows r-3, r-2 and (written here) r-1.  EDGE: the strip reaches the image's
+// first or last two rows, so rows outside the image or its [1, H-2] interior
+// are zeroed; inside, every row that reaches a stored pixel is interior.
+template <bool EDGE>
+__device__ __forceinline__ void blur_step(uint32_t w, int r, int r0, int r1, int H, int W, int c0, bool out_lane,
+                                          bool full_word, uint32_t mcol, uint32_t a1, uint32_t b1, uint32_t& c1,
+                                          uint32_t a2, uint32_t b2, uint32_t& c2, uint8_t* d1, uint8_t* d2) {
   const uint32_t wl = __shfl_up_sync(0xffffffffu, w, 1), wr = __shfl_down_sync(0xffffffffu, w, 1);
-  const bool row_ok = r >= 0 && r < H;
-  c1 = row_pass2(w & BL_LO, (w >> 8) & BL_LO, wl, wr, row_ok ? me : 0u, row_ok ? mo : 0u);
-  const int rs1 = r - 1;
-  const Pair s1 = col_pass2(a1, b1, c1, (rs1 >= 1 && rs1 <= H - 2) ? BL_LO : 0u);
-  const uint32_t s1w = s1.e | (s1.o << 8);
-  const uint32_t s1l = __shfl_up_sync(0xffffffffu, s1w, 1), s1r = __shfl_down_sync(0xffffffffu, s1w, 1);
-  const bool row1_ok = rs1 >= 0 && rs1 < H;
-  c2 = row_pass2(s1.e, s1.o, s1l, s1r, row1_ok ? me : 0u, row1_ok ? mo : 0u);
-  const int rs2 = r - 2;
-  const Pair s2 = col_pass2(a2, b2, c2, (rs2 >= 1 && rs2 <= H - 2) ? BL_LO : 0u);
+  const int rs1 = r - 1, rs2 = r - 2;
+  c1 = row_pass4(w, wl, wr, (!EDGE || (r >= 0 && r < H)) ? mcol : 0u);
+  const uint32_t s1 = col_pass4(a1, b1, c1, (!EDGE || (rs1 >= 1 && rs1 <= H - 2)) ? ~0u : 0u);
+  const uint32_t s1l = __shfl_up_sync(0xffffffffu, s1, 1), s1r = __shfl_down_sync(0xffffffffu, s1, 1);
+  c2 = row_pass4(s1, s1l, s1r, (!EDGE || (rs1 >= 0 && rs1 < H)) ? mcol : 0u);
+  const uint32_t s2 = col_pass4(a2, b2, c2, (!EDGE || (rs2 >= 1 && rs2 <= H - 2)) ? ~0u : 0u);
   if (out_lane) {
-    if (rs1 >= r0 && rs1 < r1) {
-      uint8_t* p1 = (uint8_t*)fptr(U.s1, U.fpitch, rs1, c0);
-      if (full_word) *(uint32_t*)p1 = s1w;
-      else
-        for (int j = 0; j < 4 && c0 + j < U.W; j++) p1[j] = (uint8_t)(s1w >> (8 * j));
+    if (rs1 >= r0 && rs1 < r1) blur_store(d1, s1, full_word, c0, W);
+    if (rs2 >= r0 && rs2 < r1) blur_store(d2, s2, full_word, c0, W);
+  }
+}
+
+// Rows r0 - 2 .. r1 + 1 enter, six per batch: two rounds of three steps in
+// which the register windows rotate by renaming; the output row pointers move
+// down one row per step.
+template <bool EDGE>
+__device__ __forceinline__ void blur_strip(const uint8_t* img, int ipitch, uint8_t* s1, uint8_t* s2, int fpitch,
+                                           int H, int W, int r0, int r1, int c0, bool word_ok, bool out_lane,
+                                           bool full_word, uint32_t mcol) {
+  uint32_t t1a = 0, t1b = 0, t1c = 0, t2a = 0, t2b = 0, t2c = 0;
+  // The first step (r = r0 - 2) leaves s1 row r0 - 3 and s2 row r0 - 4.
+  uint8_t* d1 = s1 + (ptrdiff_t)(r0 - 3 + RB) * fpitch + (c0 + CB);
+  uint8_t* d2 = s2 + (ptrdiff_t)(r0 - 4 + RB) * fpitch + (c0 + CB);
+  for (int rb = r0 - 2; rb <= r1 + 1; rb += 6) {
+    uint32_t w6[6];
+#pragma unroll
+    for (int k = 0; k < 6; k++) {
+      const int r = rb + k;
+      const bool ok = word_ok && r < H && (!EDGE || r >= 0);
+      w6[k] = ok ? *(const uint32_t*)(img + (ptrdiff_t)r * ipitch + c0) : 0u;
     }
-    if (rs2 >= r0 && rs2 < r1) {
-      const uint32_t s2w = s2.e | (s2.o << 8);
-      uint8_t* p2 = (uint8_t*)fptr(U.s2, U.fpitch, rs2, c0);
-      if (full_word) *(uint32_t*)p2 = s2w;
-      else
-        for (int j = 0; j < 4 && c0 + j < U.W; j++) p2[j] = (uint8_t)(s2w >> (8 * j));
+#pragma unroll
+    for (int h = 0; h < 2; h++) {
+      const int r = rb + 3 * h;
+      blur_step<EDGE>(w6[3 * h], r, r0, r1, H, W, c0, out_lane, full_word, mcol, t1b, t1c, t1a, t2b, t2c, t2a, d1, d2);
+      d1 += fpitch;
+      d2 += fpitch;
+      blur_step<EDGE>(w6[3 * h + 1], r + 1, r0, r1, H, W, c0, out_lane, full_word, mcol, t1c, t1a, t1b, t2c, t2a, t2b,
+                      d1, d2);
+      d1 += fpitch;
+      d2 += fpitch;
+      blur_step<EDGE>(w6[3 * h + 2], r + 2, r0, r1, H, W, c0, out_lane, full_word, mcol, t1a, t1b, t1c, t2a, t2b, t2c,
+                      d1, d2);
+      d1 += fpitch;
+      d2 += fpitch;
     }
   }
 }
@@ -198,35 +225,18 @@ __global__ void __launch_bounds__(32 * BL_WARPS) k_blur(const Unit* __restrict__
   const int r0 = rs * SR, r1 = min(r0 + SR, H);
   const bool out_lane = lane >= 1 && lane <= 30 && c0 < W;
   const bool full_word = c0 + 4 <= W;
-  // Row-pass column masks: pixel c0 + j is filtered iff 1 <= c0 + j <= W - 2.
-  uint32_t me = 0, mo = 0;
+  // Row-pass column mask: pixel c0 + j is filtered iff 1 <= c0 + j <= W - 2.
+  uint32_t mcol = 0;
 #pragma unroll
   for (int j = 0; j < 4; j++) {
     const int c = c0 + j;
-    if (c >= 1 && c <= W - 2) {
-      if (j & 1) mo |= 0xFFu << (16 * (j >> 1));
-      else me |= 0xFFu << (16 * (j >> 1));
-    }
+    if (c >= 1 && c <= W - 2) mcol |= 0xFFu << (8 * j);
   }
   const bool word_ok = c0 >= 0 && c0 < U.ipitch;
-  Pair p1a{0, 0}, p1b{0, 0}, p1c{0, 0}, p2a{0, 0}, p2b{0, 0}, p2c{0, 0};
-  // Rows r0 - 2 .. r1 + 1 enter, six per batch: two rounds of three steps in
-  // which the register windows rotate by renaming.
-  for (int rb = r0 - 2; rb <= r1 + 1; rb += 6) {
-    uint32_t w6[6];
-#pragma unroll
-    for (int k = 0; k < 6; k++) {
-      const int r = rb + k;
-      w6[k] = (r >= 0 && r < H && word_ok) ? *(const uint32_t*)(U.img + (size_t)r * U.ipitch + c0) : 0u;
-    }
-#pragma unroll
-    for (int h = 0; h < 2; h++) {
-      const int r = rb + 3 * h;
-      blur_step(U, w6[3 * h], r, r0, r1, c0, H, out_lane, full_word, me, mo, p1b, p1c, p1a, p2b, p2c, p2a);
-      blur_step(U, w6[3 * h + 1], r + 1, r0, r1, c0, H, out_lane, full_word, me, mo, p1c, p1a, p1b, p2c, p2a, p2b);
-      blur_step(U, w6[3 * h + 2], r + 2, r0, r1, c0, H, out_lane, full_word, me, mo, p1a, p1b, p1c, p2a, p2b, p2c);
-    }
-  }
+  if (r0 >= 2 && r1 <= H - 2)  // warp-uniform
+    blur_strip<false>(U.img, U.ipitch, U.s1, U.s2, U.fpitch, H, W, r0, r1, c0, word_ok, out_lane, full_word, mcol);
+  else
+    blur_strip<true>(U.img, U.ipitch, U.s1, U.s2, U.fpitch, H, W, r0, r1, c0, word_ok, out_lane, full_word, mcol);
 }
 
 // ---------------------------------------------------------------------------

@@ -5,6 +5,7 @@
     python -m cuimg_gb300.profile_cases adjoint    # LK residual forward (tape) + backward, same batch
     python -m cuimg_gb300.profile_cases tracker    # 4 streams of 1920x1080, 6 frames
     python -m cuimg_gb300.profile_cases tracker_det  # the same with the detector every third frame
+    python -m cuimg_gb300.profile_cases tracker16  # 16 streams of 1920x1080 in one group, 4 frames
 
 Each case runs its kernels a few times on inputs larger than L2 but a few GB
 at most on the device, so a capture of one or two launches ends quickly.
@@ -93,7 +94,21 @@ def tracker_det(frames=8):
     bt.close()
 
 
-CASES = {"gaussian": gaussian, "lk": lk_case, "adjoint": adjoint, "tracker": tracker, "tracker_det": tracker_det}
+def tracker16(frames=4):
+    """16 streams of 1920x1080 in one stream group, blur strips of 32 rows."""
+    from . import BatchTracker, synth
+    cfg = [dict(rows=1080, cols=1920, nscales=4, detector_threshold=20, detector_frequency=10)] * 16
+    vids = [synth.frames(1000 + i, 1080, 1920, frames) for i in range(16)]
+    bt = BatchTracker(cfg, graphs=False, groups=1)
+    bt.set_tuning(1, 32)
+    for t in range(frames):
+        bt.run([v[t] for v in vids])
+    bt.sync()
+    bt.close()
+
+
+CASES = {"gaussian": gaussian, "lk": lk_case, "adjoint": adjoint, "tracker": tracker, "tracker_det": tracker_det,
+         "tracker16": tracker16}
 
 if __name__ == "__main__":
     for name in sys.argv[1:] or list(CASES):
