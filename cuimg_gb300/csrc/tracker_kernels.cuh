@@ -38,6 +38,18 @@ __device__ __forceinline__ int block_prefix(bool pred, int* warp_tot, int& total
 // memory, so each frame is read from HBM once.
 constexpr int PYR_TR = 32, PYR_TC = 128;
 
+// Four outputs (a + b + c + d) / 4 from 8 pixels of two rows (a, b: the upper
+// and lower rows' bytes).  The even and odd bytes of each 32-bit half go to
+// 16-bit lanes, where a sum of four bytes (at most 1020) cannot carry into the
+// next lane.
+__device__ __forceinline__ uint32_t pyr_mean2(uint32_t x, uint32_t y) {
+  constexpr uint32_t LO = 0x00FF00FFu;
+  return (((x & LO) + ((x >> 8) & LO) + (y & LO) + ((y >> 8) & LO)) >> 2) & LO;  // outputs in bytes 0 and 2
+}
+__device__ __forceinline__ uint32_t pyr_mean4(uint2 a, uint2 b) {
+  return __byte_perm(pyr_mean2(a.x, b.x), pyr_mean2(a.y, b.y), 0x6420);
+}
+
 __global__ void __launch_bounds__(256) k_pyramid(const Unit* __restrict__ units,
                                                  const int* __restrict__ stream_unit0,
                                                  const int* __restrict__ tile_prefix, int nstreams, int base,
@@ -84,17 +96,23 @@ __global__ void __launch_bounds__(256) k_pyramid(const Unit* __restrict__ units,
   int src = 0;
   for (int l = 1; l <= nlev; l++) {
     const Unit& O = units[u0 + base + l];
-    const int tr = PYR_TR >> l, tc = PYR_TC >> l;
-    const int r0 = R0 >> l, c0 = C0 >> l;
+    const int tr = PYR_TR >> l, tw4 = (PYR_TC >> l) / 4;  // output rows, 4-pixel words per row
+    const int r0 = R0 >> l, c0 = C0 >> l;                 // c0 is a multiple of 4 (l <= 5)
     const uint8_t* S = sm[src];
     uint8_t* D = sm[src ^ 1];
-    for (int v = threadIdx.x; v < tr * tc; v += blockDim.x) {
-      int r = v / tc, c = v % tc;
-      int a = S[(2 * r) * PYR_TC + 2 * c] + S[(2 * r) * PYR_TC + 2 * c + 1] + S[(2 * r + 1) * PYR_TC + 2 * c] +
-              S[(2 * r + 1) * PYR_TC + 2 * c + 1];
-      uint8_t o = (uint8_t)(a >> 2);
-      D[r * PYR_TC + c] = o;
-      if (r0 + r < O.H && c0 + c < O.W) O.img[(size_t)(r0 + r) * O.ipitch + c0 + c] = o;
+    for (int v = threadIdx.x; v < tr * tw4; v += blockDim.x) {
+      const int r = v / tw4, c = 4 * (v % tw4);
+      const uint2 a = *(const uint2*)&S[(2 * r) * PYR_TC + 2 * c];
+      const uint2 b = *(const uint2*)&S[(2 * r + 1) * PYR_TC + 2 * c];
+      const uint32_t o = pyr_mean4(a, b);
+      *(uint32_t*)&D[r * PYR_TC + c] = o;
+      const int gr = r0 + r, gc = c0 + c;
+      if (gr < O.H) {
+        uint8_t* g = O.img + (size_t)gr * O.ipitch + gc;
+        if (gc + 4 <= O.W) *(uint32_t*)g = o;
+        else
+          for (int j = 0; j < 4 && gc + j < O.W; j++) g[j] = (uint8_t)(o >> (8 * j));
+      }
     }
     __syncthreads();
     src ^= 1;
