@@ -3,11 +3,11 @@
 The tracker's results do not depend on its tuning knobs (GBT_TUNE_* in
 include/cuimg_gb300.h); only speed does, and the best setting depends on the
 GPU and on the streams' resolutions.  ``tune`` times every setting of each
-knob on the caller's own workload -- a throwaway context per setting, a few
-warm-up frames, then per-kernel CUDA-event time of the knob's kernel over the
-timed frames -- keeps the fastest, and caches the choice in a JSON file keyed
-by GPU name and stream geometry.  ``apply`` puts the cached choice on a
-tracker.
+knob on the caller's own workload -- a throwaway one-group context per
+setting, a few warm-up frames, then per-kernel CUDA-event time of the knob's
+kernel over the timed frames -- keeps the fastest, and caches the choice in a
+JSON file keyed by GPU name and stream geometry.  ``apply`` puts the cached
+choice on a tracker.
 """
 import ctypes
 import json
@@ -88,7 +88,13 @@ def tune(configs, frames, warmup=3, timed=8, device=0, cache_path=DEFAULT_CACHE,
     for knob, (name, settings, kernels) in KNOBS.items():
         best = None
         for value in settings:
-            bt = BatchTracker(configs, device=device, graphs=False)
+            # One stream group: each launch then covers every stream, so a
+            # setting is charged the work it does for the whole frame.  (Split
+            # into groups, per-kernel timing would time small launches one
+            # after another, which favours the setting with the most CTAs --
+            # e.g. 16-row blur strips -- over the one that costs least when the
+            # groups run together.)
+            bt = BatchTracker(configs, device=device, graphs=False, groups=1)
             bt._ensure()
             for k2, v2 in choice.items():
                 bt.set_tuning(k2, v2)
