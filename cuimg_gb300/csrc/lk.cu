@@ -28,8 +28,6 @@ namespace gbt_lk {
 
 constexpr int MAXW = 15;             // largest window
 constexpr int MAXPIX = MAXW * MAXW;  // 225
-constexpr int PPL = (MAXPIX + 31) / 32;
-constexpr int WARPS = 8;
 
 struct Level {
   int H, W;

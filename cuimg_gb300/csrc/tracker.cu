@@ -1857,8 +1857,8 @@ extern "C" int gbt_profile_read(gbt_ctx* c, int32_t i, char* name, size_t len, d
   std::vector<int> cnt;
   char nb[128];
   for (Group* g : c->g) {
-    double t;
-    int32_t n;
+    double t = 0;
+    int32_t n = 0;
     const int m = grp_profile_read(g, -1, nullptr, 0, nullptr, nullptr);
     for (int k = 0; k < m; k++) {
       grp_profile_read(g, k, nb, sizeof nb, &t, &n);

@@ -46,12 +46,14 @@ def test_gpu_matches_reference_golden(case):
     tr.close()
 
 
-def _compare_run(rows, cols, L, n, seed, detf=10, filtf=1, graphs=False, matcher=None):
+def _compare_run(rows, cols, L, n, seed, detf=10, filtf=1, graphs=False, matcher=None, blur_rows=None):
     from cuimg_gb300 import synth
     frames = synth.frames(seed, rows, cols, n)
     tr = _gpu_tracker(rows, cols, L, 20, detf, filtf, graphs)
     if matcher is not None:
         tr.set_tuning(0, matcher)
+    if blur_rows is not None:
+        tr.set_tuning(1, blur_rows)
     o = tracker_oracle(rows, cols, L, 20, detf, filtf)
     for t in range(n):
         tr.run(frames[t])
@@ -118,6 +120,13 @@ def test_gpu_matches_oracle_1080p():
 @pytest.mark.parametrize("matcher", [0, 1, 2, 3])
 def test_matcher_variants_match_oracle(matcher):
     _compare_run(480, 640, 3, 14, 6, detf=5, matcher=matcher)
+
+
+@pytest.mark.parametrize("blur_rows", [16, 32, 64])
+def test_blur_strip_heights_match_oracle(blur_rows):
+    # Strips of 16 / 32 / 64 rows: interior strips (no row checks) and the
+    # strips at each level's first and last rows, on four uneven levels.
+    assert _compare_run(203, 317, 4, 6, 9, detf=3, blur_rows=blur_rows) > 0
 
 
 def test_graph_replay_matches_oracle():
