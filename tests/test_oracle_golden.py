@@ -78,6 +78,34 @@ def test_oracle_matches_reference_live(rows, cols, L, detf, n, seed):
     o.destroy()
 
 
+@pytest.mark.skipif(not reference_available(), reason="reference not built here (oracle/_ref)")
+def test_oracle_matches_reference_live_random_geometries():
+    # Seeded random geometries, scale counts, thresholds and detector periods
+    # (GBT_REF_SWEEP cases, default 40; larger sweeps: GBT_REF_SWEEP=300),
+    # every stage of every frame compared.
+    from cuimg_gb300 import synth
+    rng = np.random.default_rng(20261203)
+    lib = oracle()
+    done, total = 0, int(os.environ.get("GBT_REF_SWEEP", "40"))
+    while done < total:
+        rows, cols, L = int(rng.integers(40, 400)), int(rng.integers(40, 600)), int(rng.integers(1, 5))
+        detf, n, seed = int(rng.choice([1, 2, 3, 5, 10])), int(rng.integers(4, 12)), int(rng.integers(0, 1000))
+        th = int(rng.choice([10, 20, 30]))
+        if not lib.oracle_sizes_ok(rows, cols, L):
+            continue
+        frames = synth.frames(seed, rows, cols, n)
+        ref = tracker_reference(rows, cols, L, th, detf, 1)
+        o = tracker_oracle(rows, cols, L, th, detf, 1)
+        for t in range(n):
+            ref.run(frames[t])
+            o.run(frames[t])
+            bad = diff_snapshots(snapshot(ref, L), snapshot(o, L), detector_frame=(t % detf == 0))
+            assert not bad, "%dx%d L%d det/%d th%d seed %d frame %d: %s" % (rows, cols, L, detf, th, seed, t, bad)
+        ref.destroy()
+        o.destroy()
+        done += 1
+
+
 def _alt_check(get, g, L, n, tag):
     for t in range(n):
         for s in range(L):
