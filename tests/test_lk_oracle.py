@@ -1,8 +1,9 @@
 """Pins the LK oracle against the reference's own pyramidal LK tracker
 (golden fixture from pyrlk_cpu<fast_detector<cpu>, iterative_lk_match_5x5>)."""
 import numpy as np
+import pytest
 
-from oracle_lib import box_pyramid_u8, load_golden, lk_track
+from oracle_lib import box_pyramid_u8, load_golden, lk_track, reference_available
 
 
 def test_lk_oracle_matches_reference_golden():
@@ -41,3 +42,59 @@ def test_lk_oracle_recovers_known_translation():
     out, st, _ = lk_track(prev, cur, pts, 2, pyr=1, window=11, npix=121, max_iter=30, eps=0.01)
     assert st.all()
     np.testing.assert_allclose(out - pts, [[-2.0, 3.0]] * 3, atol=0.05)
+
+
+def _reference_lk(rows, cols, L, frames):
+    """The reference's pyrlk_cpu tracker (compiled from its sources into
+    oracle/_ref) on a frame pair: births on frame 0, one LK step."""
+    import ctypes
+
+    from oracle_lib import REF
+    lib = ctypes.CDLL(REF)
+    lib.reflk_create.restype = ctypes.c_void_p
+    lib.reflk_create.argtypes = [ctypes.c_int] * 4
+    lib.reflk_run.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
+    lib.reflk_nparticles.argtypes = [ctypes.c_void_p, ctypes.c_int]
+    lib.reflk_get.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]
+    lib.reflk_destroy.argtypes = [ctypes.c_void_p]
+    h = lib.reflk_create(rows, cols, L, 20)
+    out = {}
+
+    def grab(tag):
+        for s in range(L):
+            n = lib.reflk_nparticles(h, s)
+            pos = np.zeros((n, 2), np.float32)
+            age = np.zeros(n, np.uint16)
+            lib.reflk_get(h, s, pos.ctypes.data, age.ctypes.data)
+            out[tag, s] = (pos, age)
+
+    lib.reflk_run(h, np.ascontiguousarray(frames[0]).ctypes.data)
+    grab("born")
+    lib.reflk_run(h, np.ascontiguousarray(frames[1]).ctypes.data)
+    grab("tracked")
+    lib.reflk_destroy(h)
+    return out
+
+
+@pytest.mark.skipif(not reference_available(), reason="reference not built here (oracle/_ref)")
+@pytest.mark.parametrize("rows,cols,L,seed", [(180, 260, 2, 3), (257, 391, 3, 8), (320, 480, 3, 40), (211, 603, 2, 77)])
+def test_lk_oracle_matches_reference_live(rows, cols, L, seed):
+    from cuimg_gb300 import synth
+    frames = synth.frames(seed, rows, cols, 2)
+    ref = _reference_lk(rows, cols, L, frames)
+    p0 = [frames[0]] + box_pyramid_u8(frames[0], L)
+    p1 = [frames[1]] + box_pyramid_u8(frames[1], L)
+    for s in range(L):
+        pts = ref["born", s][0]
+        ref_pos, ref_age = ref["tracked", s]
+        out, st, _ = lk_track(p0[s], p1[s], pts, L - s, pyr=0)
+        H, W = p0[s].shape
+        m = 12 * 2 ** (L - 1 - s)
+        inner = (pts[:, 0] >= m) & (pts[:, 1] >= m) & (pts[:, 0] < H - m) & (pts[:, 1] < W - m)
+        if inner.sum() < 20:
+            continue
+        np.testing.assert_array_equal(st[inner] > 0, ref_age[inner] > 0)
+        both = inner & (st > 0)
+        d = np.abs(out[both] - ref_pos[both]).max(axis=1)
+        assert (d < 0.01).mean() >= 0.97, (s, (d < 0.01).mean())
+        assert np.median(d) < 1e-4
