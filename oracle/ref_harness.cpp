@@ -1,4 +1,4 @@
-// Reference harness -- TEST INFRASTRUCTURE ONLY (the checker, never shipped).
+// Reference harness -- TEST INFRASTRUCTURE ONLY (never shipped).
 //
 // Compiles matt-42/cuimg's own CPU tracker
 // `tracker<tracking_strategies::bc2s_fast_gradient_cpu>`
