@@ -550,10 +550,12 @@ static void frame_kind(Group* ctx, bool& any_det, bool& any_filt) {
   }
 }
 
+// An event from the profiling pool, or null when none could be created (the
+// launch is then not timed).
 static cudaEvent_t next_event(Group* ctx) {
   if (ctx->event_next == ctx->event_pool.size()) {
-    cudaEvent_t e;
-    cudaEventCreate(&e);
+    cudaEvent_t e = nullptr;
+    if (cudaEventCreate(&e) != cudaSuccess) return nullptr;
     ctx->event_pool.push_back(e);
   }
   return ctx->event_pool[ctx->event_next++];
@@ -575,13 +577,15 @@ struct ProfScope {
   cudaEvent_t a = nullptr;
   ProfScope(Group* c, const char* name) : ctx(c) {
     if (!ctx->profiling) return;
-    slot = prof_slot(ctx, name);
     a = next_event(ctx);
+    if (!a) return;
+    slot = prof_slot(ctx, name);
     cudaEventRecord(a, ctx->stream);
   }
   ~ProfScope() {
     if (slot < 0) return;
     cudaEvent_t b = next_event(ctx);
+    if (!b) return;
     cudaEventRecord(b, ctx->stream);
     ctx->pending.push_back({slot, {a, b}});
   }
