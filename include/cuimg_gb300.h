@@ -153,9 +153,9 @@ int gbt_test_withhold_tile_copies(gbt_ctx* ctx, int32_t enable);
  * the caller writes on it is waited for.  (Each stream group works on its own
  * internal streams; a frame's input copy, pyramid and blurs overlap the
  * previous frame's matching and filtering.  The matching and filtering
- * streams have the device's greatest priority, the input, pyramid and blur
- * streams its least, so a caller's own work at the default priority goes
- * between the two.) */
+ * streams have the device's greatest priority and the input, pyramid and
+ * blur streams its least (the default priority), so a caller's own work at
+ * the default priority shares the GPU with the latter.) */
 int gbt_stream(gbt_ctx* ctx, void** cuda_stream);
 
 /* Particle set of (stream, scale): dense slot count (tombstones included,
