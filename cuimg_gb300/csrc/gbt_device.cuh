@@ -116,6 +116,10 @@ struct Frame {
 constexpr int ERR_CAPACITY = 1;
 constexpr int ERR_MERGE_OVERFLOW = 2;
 constexpr int ERR_TIMEOUT = 4;  // a bounded wait on an asynchronous copy gave up
+// ... and the copies were still in flight after a second bounded wait, when
+// the CTA had to return: they may complete into shared memory that another
+// CTA owns by then, so the context's results are no longer trustworthy.
+constexpr int ERR_COPY_INFLIGHT = 8;
 
 // c8_h in raster order (cuimg/neighb2d_data.h:80-85), (row, col).
 __constant__ int8_t c_c8[8][2] = {{-1, 1}, {0, 1}, {1, 1}, {-1, 0}, {1, 0}, {-1, -1}, {0, -1}, {1, -1}};

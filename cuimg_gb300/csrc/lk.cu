@@ -7,8 +7,9 @@
 // points.  Window size, mask size and iteration count are parameters (the
 // reference hard-codes 11, 25 and 30).  Undefined reference cases are defined
 // as in the oracle: clamp-to-edge sampling, identity flow when an upper match
-// leaves its level, ties in the strongest-gradient selection broken by the
-// lower window index.
+// leaves its level.  Equal gradient norms at the edge of the strongest-gradient
+// selection are resolved as the reference's std::nth_element (GNU libstdc++)
+// resolves them.
 //
 // Layout: per pair and level, the previous and current levels (fp32, dense
 // rows) and the Sobel/8 gradient of the previous level (float2), all in one
@@ -16,6 +17,7 @@
 // are spread over the lanes, the masked pixels are compacted by rank, and the
 // 2x2 normal matrix and right-hand side are warp reductions whose lane-0
 // result is broadcast, so every lane takes identical decisions.
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -23,6 +25,7 @@
 #include <vector>
 
 #include "cuimg_gb300.h"
+#include "nth_select.cuh"
 
 namespace gbt_lk {
 
@@ -84,9 +87,14 @@ __device__ __forceinline__ float warp_sum(float v) {
   return __shfl_sync(0xffffffffu, v, 0);
 }
 
-struct WarpSmem {
-  float as[MAXPIX];
-  float mgr[MAXPIX], mgc[MAXPIX], mas[MAXPIX];  // masked pixels by rank
+struct __align__(8) WarpSmem {
+  union {
+    struct {
+      float r[MAXPIX], c[MAXPIX];  // gradients of the masked pixels by rank
+    } mg;
+    unsigned long long ord[MAXPIX];  // (norm bits << 32 | window index) while selecting
+  };
+  float as[MAXPIX], mas[MAXPIX];
   short mr[MAXPIX], mc[MAXPIX];
 };
 
@@ -119,10 +127,11 @@ __device__ bool lk_match(const Level& lv, const Params& P, WarpSmem& S, float py
       nb[k] = __float_as_uint(__fsqrt_rn(__fadd_rn(__fmul_rn(g.x, g.x), __fmul_rn(g.y, g.y))));
     }
   }
-  // The N strongest gradients (ties: lower window index), the reference's
-  // nth_element selection (pyrlk_tracker.hpp:212-228): a bitwise search for
-  // the N-th largest norm t, then every norm above t and the first
-  // N - #(above t) norms equal to t in window order.
+  // The N strongest gradients, the reference's nth_element selection
+  // (pyrlk_tracker.hpp:207-228): a bitwise search for the N-th largest norm t;
+  // every norm above t is selected.  When the norms equal to t all fit
+  // (#above + #equal == N) they are selected too; otherwise which of them the
+  // reference keeps depends on nth_element's steps, replayed by one lane.
   bool sel[PPL];
   if (N >= n) {
 #pragma unroll
@@ -136,17 +145,29 @@ __device__ bool lk_match(const Level& lv, const Params& P, WarpSmem& S, float py
       for (int k = 0; k < PPL; k++) cnt += __popc(__ballot_sync(0xffffffffu, valid[k] && nb[k] >= cand));
       if (cnt >= N) t = cand;
     }
-    int above = 0;
+    int atleast = 0;
 #pragma unroll
-    for (int k = 0; k < PPL; k++) above += __popc(__ballot_sync(0xffffffffu, valid[k] && nb[k] > t));
-    const unsigned lt = (1u << lane) - 1u;
-    int eq_before = 0;
+    for (int k = 0; k < PPL; k++) atleast += __popc(__ballot_sync(0xffffffffu, valid[k] && nb[k] >= t));
+    if (atleast == N) {
 #pragma unroll
-    for (int k = 0; k < PPL; k++) {
-      const bool eq = valid[k] && nb[k] == t;
-      const unsigned be = __ballot_sync(0xffffffffu, eq);
-      sel[k] = (valid[k] && nb[k] > t) || (eq && eq_before + __popc(be & lt) < N - above);
-      eq_before += __popc(be);
+      for (int k = 0; k < PPL; k++) sel[k] = valid[k] && nb[k] >= t;
+    } else {
+#pragma unroll
+      for (int k = 0; k < PPL; k++) {
+        const int i = lane + 32 * k;
+        if (valid[k]) {
+          S.ord[i] = ((unsigned long long)nb[k] << 32) | (unsigned)i;
+          S.mr[i] = 0;
+        }
+      }
+      __syncwarp();
+      if (lane == 0) gbt_sel::nth_select(S.ord, n, N);
+      __syncwarp();
+      for (int j = lane; j < N; j += 32) S.mr[(int)(S.ord[j] & 0xffffffffu)] = 1;
+      __syncwarp();
+#pragma unroll
+      for (int k = 0; k < PPL; k++) sel[k] = valid[k] && S.mr[lane + 32 * k] != 0;
+      __syncwarp();
     }
   }
   // Selected pixels, compacted in window order.
@@ -158,8 +179,8 @@ __device__ bool lk_match(const Level& lv, const Params& P, WarpSmem& S, float py
       const unsigned bs = __ballot_sync(0xffffffffu, sel[k]);
       if (sel[k]) {
         const int m = base + __popc(bs & lt), i = lane + 32 * k;
-        S.mgr[m] = gr[k];
-        S.mgc[m] = gc[k];
+        S.mg.r[m] = gr[k];
+        S.mg.c[m] = gc[k];
         S.mas[m] = S.as[i];
         S.mr[m] = (short)(i / ws - hws);
         S.mc[m] = (short)(i % ws - hws);
@@ -171,7 +192,7 @@ __device__ bool lk_match(const Level& lv, const Params& P, WarpSmem& S, float py
   // Normal matrix over the masked pixels.
   float g00 = 0.f, g01 = 0.f, g11 = 0.f;
   for (int m = lane; m < N; m += 32) {
-    float a = S.mgr[m], b = S.mgc[m];
+    float a = S.mg.r[m], b = S.mg.c[m];
     g00 += a * a;
     g01 += a * b;
     g11 += b * b;
@@ -192,8 +213,8 @@ __device__ bool lk_match(const Level& lv, const Params& P, WarpSmem& S, float py
       float b0 = 0.f, b1 = 0.f;
       for (int m = lane; m < N; m += 32) {
         float dt = S.mas[m] - li(lv.cur, lv.H, lv.W, vy + (float)S.mr[m], vx + (float)S.mc[m]);
-        b0 += S.mgr[m] * dt;
-        b1 += S.mgc[m] * dt;
+        b0 += S.mg.r[m] * dt;
+        b1 += S.mg.c[m] * dt;
       }
       b0 = warp_sum(b0);
       b1 = warp_sum(b1);
@@ -528,8 +549,10 @@ extern "C" int gbt_lk_track_batch(const void* prev, const void* cur, int64_t pit
 // frames, points and outputs.
 //
 // Set-up: the first call on a device, with that device current, looks up the
-// array's device address once (cudaGetSymbolAddress) and caches it; make that
-// first call before capturing any stream into a CUDA graph.  Every call shares
+// array's device address once (cudaGetSymbolAddress) and caches it for that
+// device's context; a context re-created after cudaDeviceReset gets its own
+// lookup on its first call.  Make those first calls before capturing any
+// stream into a CUDA graph.  Every call shares
 // the one arena and overwrites it completely (levels, gradients, level table),
 // so nothing needs clearing between calls -- but calls whose GPU work overlaps
 // (different streams or host threads without ordering) race on it.
@@ -564,8 +587,39 @@ __global__ void k_fill_table(Level* table, int npairs, int nlevels, const float*
 
 }  // namespace gbt_lk
 
+// The array's address is valid for one CUDA context: a device whose context
+// is destroyed and re-created (cudaDeviceReset) loads the library's device
+// image again, so the cache is keyed on the context's unique id, read through
+// the runtime's driver entry points (the library does not link the driver
+// API).  0 when no context is current or the entry points are unavailable.
+typedef CUresult (*CtxGetCurrentFn)(CUcontext*);
+typedef CUresult (*CtxGetIdFn)(CUcontext, unsigned long long*);
+
+static unsigned long long current_context_id() {
+  static CtxGetCurrentFn get_current = nullptr;
+  static CtxGetIdFn get_id = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_current = (CtxGetCurrentFn)f;
+    f = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_id = (CtxGetIdFn)f;
+    cudaGetLastError();
+  });
+  CUcontext c = nullptr;
+  unsigned long long id = 0;
+  if (!get_current || !get_id || get_current(&c) != CUDA_SUCCESS || !c || get_id(c, &id) != CUDA_SUCCESS) return 0;
+  return id;
+}
+
 static std::mutex g_noalloc_mu;
 static void* g_noalloc_ptr[NOALLOC_MAX_DEVICES];
+static unsigned long long g_noalloc_ctx[NOALLOC_MAX_DEVICES];
 
 extern "C" int64_t gbt_lk_noalloc_max_bytes(void) { return NOALLOC_SCRATCH_BYTES; }
 
@@ -589,10 +643,15 @@ extern "C" int gbt_lk_track_batch_noalloc(const void* prev, const void* cur, int
   void* arena = nullptr;
   {
     std::lock_guard<std::mutex> lk(g_noalloc_mu);
-    if (!g_noalloc_ptr[dev]) {
+    const unsigned long long ctx_id = current_context_id();
+    if (!g_noalloc_ptr[dev] || ctx_id == 0 || ctx_id != g_noalloc_ctx[dev]) {
       void* p = nullptr;
-      if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) return GBT_E_CUDA;
+      if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) {
+        g_noalloc_ptr[dev] = nullptr;
+        return GBT_E_CUDA;
+      }
       g_noalloc_ptr[dev] = p;
+      g_noalloc_ctx[dev] = current_context_id();  // the lookup made the context current if none was
     }
     arena = g_noalloc_ptr[dev];
   }

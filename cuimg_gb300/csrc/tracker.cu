@@ -978,6 +978,10 @@ static int grp_sync(Group* ctx) {
   Frame f;
   CK(cudaMemcpy(&f, ctx->d_frame, sizeof f, cudaMemcpyDeviceToHost));
   if (f.err & ERR_CAPACITY) return set_err(ctx, GBT_E_CAPACITY, "particle capacity exceeded");
+  if (f.err & ERR_COPY_INFLIGHT)
+    return set_err(ctx, GBT_E_TIMEOUT,
+                   "a bounded wait on an asynchronous copy gave up with the copy still in flight; "
+                   "destroy this context");
   if (f.err & ERR_TIMEOUT) return set_err(ctx, GBT_E_TIMEOUT, "a bounded wait on an asynchronous copy gave up");
   return GBT_OK;
 }

@@ -690,23 +690,56 @@ __device__ __forceinline__ unsigned long long global_ns() {
   return t;
 }
 
-// Waits for the tile (phase 0 of the mbarrier), giving up after MT_WAIT_NS of
-// the global timer or 2^22 polls, whichever comes first; false when it gave up.
+// Waits for the tile (phase 0 of the mbarrier); false when it gave up.  The
+// budget is MT_WAIT_NS of the GPU's global timer counted only while this CTA
+// is resident: the gap between two consecutive polls counts at most
+// MT_POLL_GAP_NS, so time the context spends switched out (time-slicing with
+// other contexts) does not use the budget up; each poll asks to be suspended
+// no longer than MT_SUSPEND_HINT_NS, well inside that cap.  2^24 polls at
+// most, whatever the timer says.  Called by one thread.
 constexpr unsigned long long MT_WAIT_NS = 500000000ull;
+constexpr unsigned long long MT_POLL_GAP_NS = 100000ull;
+constexpr unsigned MT_SUSPEND_HINT_NS = 10000u;  // each poll suspends the thread for at most about this long
 __device__ __forceinline__ bool mt_tma_wait(unsigned long long* mbar) {
   const unsigned bar = (unsigned)__cvta_generic_to_shared(mbar);
-  const unsigned long long t0 = global_ns();
-  for (int it = 0; it < (1 << 22); it++) {
+  unsigned long long prev = global_ns(), counted = 0;
+  for (int it = 0; it < (1 << 24); it++) {
     unsigned done;
     asm volatile(
-        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0;\n selp.u32 %0, 1, 0, p;\n}\n"
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0, %2;\n selp.u32 %0, 1, 0, p;\n}\n"
         : "=r"(done)
-        : "r"(bar)
+        : "r"(bar), "r"(MT_SUSPEND_HINT_NS)
         : "memory");
     if (done) return true;
-    if (global_ns() - t0 > MT_WAIT_NS) break;
+    const unsigned long long now = global_ns(), gap = now - prev;
+    prev = now;
+    counted += gap < MT_POLL_GAP_NS ? gap : MT_POLL_GAP_NS;
+    if (counted > MT_WAIT_NS) break;
   }
   return false;
+}
+
+// Thread 0 waits for the tile and every thread of the CTA learns the outcome
+// (one branch for the whole CTA).  When the wait gives up after real copies
+// were issued, thread 0 waits once more with the same budget for them to
+// land, since a CTA cannot return with bulk copies still writing into its
+// shared memory without risking the next CTA's; if they still have not
+// landed, it flags ERR_COPY_INFLIGHT (the context is unrecoverable: the copies
+// may complete into another CTA's tile).  Returns false on a timeout, after
+// flagging ERR_TIMEOUT.
+__device__ __forceinline__ bool mt_tma_wait_cta(unsigned long long* mbar, bool copies_issued, int* err,
+                                                int* verdict) {
+  if (threadIdx.x == 0) {
+    int ok = mt_tma_wait(mbar) ? 1 : 0;
+    if (!ok) {
+      int flags = ERR_TIMEOUT;
+      if (copies_issued && !mt_tma_wait(mbar)) flags |= ERR_COPY_INFLIGHT;
+      atomicOr(err, flags);
+    }
+    *verdict = ok;
+  }
+  __syncthreads();
+  return *verdict != 0;
 }
 
 __device__ __forceinline__ void mt_stage_issue(const Unit& u, int R0s, int C0s, uint8_t* ts1, uint8_t* ts2) {
@@ -728,8 +761,9 @@ __device__ __forceinline__ void mt_stage_issue(const Unit& u, int R0s, int C0s, 
 // THREADS per CTA; with DYN the threads take the tile's particles one at a
 // time from a shared counter (a thread that finishes a short descent takes the
 // next particle) instead of every THREADS-th one.  A tile whose wait gives up
-// sets ERR_TIMEOUT in *err and leaves its particles unmatched; `withhold`
-// (a test hook) arms the barrier without issuing the copies, so that it does.
+// sets ERR_TIMEOUT in *err and leaves its particles unmatched (and
+// ERR_COPY_INFLIGHT if its copies never landed); `withhold` (a test hook) arms
+// the barrier without issuing the copies, so that the wait gives up.
 template <int THREADS, bool DYN, int MINB>
 __global__ void __launch_bounds__(THREADS, MINB) k_match_tiled(const Unit* __restrict__ units,
                                                                const UState* __restrict__ st,
@@ -743,6 +777,7 @@ __global__ void __launch_bounds__(THREADS, MINB) k_match_tiled(const Unit* __res
   __shared__ __align__(128) uint8_t ts2[MT_SR * MT_SC];
   __shared__ __align__(8) unsigned long long mbar;
   __shared__ int next;
+  __shared__ int tile_ok;
   const int t = blockIdx.x;
   const int n0 = off[t], n1 = off[t + 1];
   if (n0 == n1) return;
@@ -771,14 +806,11 @@ __global__ void __launch_bounds__(THREADS, MINB) k_match_tiled(const Unit* __res
     feat = u.feat[b][i];
   }
   if (tmaps) {
-    if (!mt_tma_wait(&mbar)) {
-      if (threadIdx.x == 0) atomicOr(err, ERR_TIMEOUT);
-      return;
-    }
+    if (!mt_tma_wait_cta(&mbar, !withhold, err, &tile_ok)) return;  // the whole CTA returns together
   } else {
     asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+    __syncthreads();
   }
-  __syncthreads();
   FeatFP<MT_SC> F;
   F.s1 = ts1 - (R0s * MT_SC + C0s);  // F.s1 + (r * MT_SC + c) is staged pixel (r, c)
   F.s2 = ts2 - (R0s * MT_SC + C0s);

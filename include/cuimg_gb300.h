@@ -140,9 +140,13 @@ int gbt_sync(gbt_ctx* ctx);
 
 /* Test hook for the bounded device-side waits (no reference counterpart).
  * With `enable` set, the tiled matcher arms each tile's barrier but issues no
- * copy, so every tile's wait gives up (after 0.5 s of the GPU's global timer),
- * leaves the tile's particles unmatched and flags the context: the next
- * gbt_sync returns GBT_E_TIMEOUT.  Nothing faults; the device and other
+ * copy, so every tile's wait gives up (after 0.5 s of the GPU's global timer,
+ * counted while the CTA is resident), leaves the tile's particles unmatched and
+ * flags the context: the next gbt_sync returns GBT_E_TIMEOUT.  (Outside the
+ * hook, a tile whose copies were issued and still had not landed after a
+ * second 0.5 s wait also reports "copy still in flight" in gbt_last_error:
+ * destroy that context, since the copies may land in another tile's shared
+ * memory.)  Nothing faults; the device and other
  * contexts stay usable.  GBT_E_INVALID when the context does not stage tiles
  * by TMA (another matcher variant, or no tensor maps). */
 int gbt_test_withhold_tile_copies(gbt_ctx* ctx, int32_t enable);
@@ -373,8 +377,10 @@ int gbt_lkd_backward_tape(const float* I0, const float* I1, int64_t pitch, int64
  * array of gbt_lk_noalloc_max_bytes() bytes (48 MiB) that every GPU loading
  * this library holds until exit.  Requests needing more scratch than that
  * (gbt_lk_scratch_bytes) return GBT_E_TOO_LARGE.  The first call on a device
- * looks up the array's address, so make it before any stream capture.  All
- * calls share the array: calls whose GPU work overlaps race. */
+ * (and the first after its context is re-created by cudaDeviceReset) looks up
+ * the array's address, so make it before any stream capture.  All calls share
+ * the array and overwrite what it holds: calls queued one after another on one
+ * stream are ordered and safe; calls whose GPU work overlaps race. */
 int64_t gbt_lk_noalloc_max_bytes(void);
 int gbt_lk_track_batch_noalloc(const void* prev, const void* cur, int64_t pitch, int64_t img_bytes, int32_t rows,
                                int32_t cols, int32_t is_u8, int32_t nlevels, const gbt_lk_params* params,

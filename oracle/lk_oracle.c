@@ -15,7 +15,10 @@
  *   - get_flow_at returns the identity when the match leaves the level
  *     (the reference falls off the end of the function, :1048-1058);
  *   - ties in the strongest-gradient selection (std::nth_element, :212-228)
- *     are broken by the lower window index.
+ *     are left to the library by the C++ standard; this restatement follows
+ *     the selection algorithm of GNU libstdc++ (the library the reference's
+ *     CPU build links with g++), so equal norms land on the same side of the
+ *     N-th position as in the reference (nth_select below).
  * Pyramids: pyr 0 = the tracker's 2x2 floor-mean pyramid of uint8 levels with
  * the template truncated to uint8 (the reference's gl8u path); pyr 1 = the
  * sigma-1 Gaussian fp32 pyramid with an fp32 template.
@@ -54,6 +57,133 @@ static float li(const float* img, int H, int W, float y, float x) {
   return (1 - a0) * (1 - a1) * v00 + a0 * (1 - a1) * v10 + (1 - a0) * a1 * v01 + a0 * a1 * v11;
 }
 
+/* ---------------------------------------------------------------------------
+ * nth_select: std::nth_element(idx, idx + nth, idx + n, comp) with
+ * comp(a, b) = key[a] > key[b], restated from the introselect algorithm
+ * (Musser 1997) as GNU libstdc++ implements it: while more than 3 elements
+ * remain, pick the median of (second, middle, last) elements, move it to the
+ * front, partition the rest around it with two inward scans that stop on
+ * elements not strictly on their side (so equal elements are swapped), and
+ * keep the side holding nth; after 2 * floor(log2 n) partitions fall back to a
+ * heap selection; finish the last <= 3 elements with an insertion sort.  Only
+ * the order of elements that compare equal depends on these steps, and the
+ * mask the reference takes (the first N positions) depends on it exactly when
+ * equal norms straddle position N.  Counts how often each path ran.
+ */
+long long oracle_nth_heap_paths = 0;
+/* Mask selections, and those where equal norms straddle position N (the
+ * case in which the order among equal norms changes the mask). */
+long long oracle_lk_selections = 0, oracle_lk_straddles = 0;
+
+static int cmp_gt(const float* key, int a, int b) { return key[a] > key[b]; }
+
+/* Moves `val` up from `hole` towards `top` while its parent compares lower. */
+static void heap_up(int* h, int hole, int top, int val, const float* key) {
+  int parent = (hole - 1) / 2;
+  while (hole > top && cmp_gt(key, h[parent], val)) {
+    h[hole] = h[parent];
+    hole = parent;
+    parent = (hole - 1) / 2;
+  }
+  h[hole] = val;
+}
+
+/* Sinks the hole at `hole` to a leaf along the preferred children, then
+ * places `val` by moving it back up. */
+static void heap_down(int* h, int hole, int len, int val, const float* key) {
+  const int top = hole;
+  int child = hole;
+  while (child < (len - 1) / 2) {
+    child = 2 * (child + 1);
+    if (cmp_gt(key, h[child], h[child - 1])) child--;
+    h[hole] = h[child];
+    hole = child;
+  }
+  if ((len & 1) == 0 && child == (len - 2) / 2) {
+    child = 2 * (child + 1);
+    h[hole] = h[child - 1];
+    hole = child - 1;
+  }
+  heap_up(h, hole, top, val, key);
+}
+
+static void heap_select(int* a, int middle, int len, const float* key) {
+  if (middle > 1)
+    for (int parent = (middle - 2) / 2;; parent--) {
+      heap_down(a, parent, middle, a[parent], key);
+      if (parent == 0) break;
+    }
+  for (int i = middle; i < len; i++)
+    if (cmp_gt(key, a[i], a[0])) {
+      int v = a[i];
+      a[i] = a[0];
+      heap_down(a, 0, middle, v, key);
+    }
+}
+
+static void swap_int(int* a, int* b) {
+  int t = *a;
+  *a = *b;
+  *b = t;
+}
+
+static void nth_select(int* a, int n, int nth, const float* key) {
+  if (n == 0 || nth == n) return;
+  int first = 0, last = n, depth = 0;
+  for (int m = n; m > 1; m >>= 1) depth++;
+  depth *= 2;
+  while (last - first > 3) {
+    if (depth == 0) {
+      oracle_nth_heap_paths++;
+      heap_select(a + first, nth + 1 - first, last - first, key);
+      swap_int(&a[first], &a[nth]);
+      return;
+    }
+    depth--;
+    /* median of a[first+1], a[mid], a[last-1] to a[first] */
+    int x = first + 1, y = first + (last - first) / 2, z = last - 1, m;
+    if (cmp_gt(key, a[x], a[y]))
+      m = cmp_gt(key, a[y], a[z]) ? y : (cmp_gt(key, a[x], a[z]) ? z : x);
+    else
+      m = cmp_gt(key, a[x], a[z]) ? x : (cmp_gt(key, a[y], a[z]) ? z : y);
+    swap_int(&a[first], &a[m]);
+    /* partition [first+1, last) around the pivot a[first] */
+    const int piv = a[first];
+    int lo = first + 1, hi = last;
+    for (;;) {
+      while (cmp_gt(key, a[lo], piv)) lo++;
+      hi--;
+      while (cmp_gt(key, piv, a[hi])) hi--;
+      if (!(lo < hi)) break;
+      swap_int(&a[lo], &a[hi]);
+      lo++;
+    }
+    if (lo <= nth)
+      first = lo;
+    else
+      last = lo;
+  }
+  /* insertion sort of [first, last) */
+  for (int i = first + 1; i < last; i++) {
+    int v = a[i];
+    if (cmp_gt(key, v, a[first])) {
+      for (int j = i; j > first; j--) a[j] = a[j - 1];
+      a[first] = v;
+    } else {
+      int j = i;
+      while (cmp_gt(key, v, a[j - 1])) {
+        a[j] = a[j - 1];
+        j--;
+      }
+      a[j] = v;
+    }
+  }
+}
+
+/* Exported for the tests: runs nth_select on idx[0..n) (initially any
+ * permutation) with `key`. */
+void oracle_nth_select(int* idx, int n, int nth, const float* key) { nth_select(idx, n, nth, key); }
+
 static int box_has(int H, int W, int b, float y, float x) { /* (domain - border(b)).has(i_int2(p)) */
   int r = (int)y, c = (int)x;
   return r >= b && r <= H - b - 1 && c >= b && c <= W - b - 1;
@@ -81,14 +211,22 @@ static int lk_match(const lk_ctx* k, const lk_level* l, const float p[2], const 
       as[i] = k->u8 ? (float)(unsigned char)a : a;
       nrm[i] = sqrtf(gsr[i] * gsr[i] + gsc[i] * gsc[i]);
     }
-  /* The npix strongest gradients (ties: lower index first). */
+  /* The npix strongest gradients: the first N window indexes after
+   * nth_element (:207-228). */
   int N = k->npix < n ? k->npix : n;
-  for (int i = 0; i < n; i++) {
-    int rank = 0;
-    for (int j = 0; j < n; j++)
-      if (nrm[j] > nrm[i] || (nrm[j] == nrm[i] && j < i)) rank++;
-    mask[i] = rank < N;
+  int* idx = (int*)malloc(sizeof(int) * n);
+  for (int i = 0; i < n; i++) idx[i] = i;
+  nth_select(idx, n, N, nrm);
+  for (int i = 0; i < N; i++) mask[idx[i]] = 1;
+  if (N > 0 && N < n) {
+    float t = nrm[idx[0]];
+    for (int i = 1; i < N; i++) t = nrm[idx[i]] < t ? nrm[idx[i]] : t;
+    int straddle = 0;
+    for (int i = N; i < n; i++) straddle |= nrm[idx[i]] == t;
+    oracle_lk_selections++;
+    oracle_lk_straddles += straddle;
   }
+  free(idx);
   float G00 = 0, G01 = 0, G11 = 0;
   for (int i = 0; i < n; i++)
     if (mask[i]) {

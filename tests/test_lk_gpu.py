@@ -87,7 +87,7 @@ def test_lk_matches_reference_golden():
         np.testing.assert_array_equal(st[inner] > 0, ref_age[inner] > 0)
         both = inner & (st > 0)
         d = np.abs(out[both] - ref_pos[both]).max(axis=1)
-        assert (d < TOL_PX).mean() >= 0.97  # std::nth_element tie order, as for the oracle
+        assert (d < TOL_PX).mean() >= MIN_AGREE, (s, (d < TOL_PX).mean())
 
 
 def test_lk_edge_points_and_empty():

@@ -22,13 +22,10 @@ def test_lk_oracle_matches_reference_golden():
         assert inner.sum() > 50
         np.testing.assert_array_equal(st[inner] > 0, ref_age[inner] > 0)
         both = inner & (st > 0)
-        d = np.abs(out[both] - ref_pos[both]).max(axis=1)
-        # Residual differences come from std::nth_element's unspecified order
-        # among equal gradient norms (frequent at integer positions, where the
-        # window samples the Sobel grid exactly); the oracle takes the lower
-        # window index.
-        assert (d < 0.01).mean() >= 0.97, (s, (d < 0.01).mean())
-        assert np.median(d) < 1e-4
+        # The restatement computes in the reference's order and selects the
+        # mask with the reference's std::nth_element order among equal norms,
+        # so the tracked positions are identical, not just within 0.01 px.
+        np.testing.assert_array_equal(out[both], ref_pos[both], err_msg="scale %d" % s)
 
 
 def test_lk_oracle_recovers_known_translation():
@@ -95,6 +92,4 @@ def test_lk_oracle_matches_reference_live(rows, cols, L, seed):
             continue
         np.testing.assert_array_equal(st[inner] > 0, ref_age[inner] > 0)
         both = inner & (st > 0)
-        d = np.abs(out[both] - ref_pos[both]).max(axis=1)
-        assert (d < 0.01).mean() >= 0.97, (s, (d < 0.01).mean())
-        assert np.median(d) < 1e-4
+        np.testing.assert_array_equal(out[both], ref_pos[both], err_msg="scale %d" % s)

@@ -3,9 +3,12 @@
 gbt_lk_track_batch_noalloc serves callers that cannot allocate device memory
 (an application owning the device heap or budget, a plugin forbidden to call
 cudaMalloc): it runs the same tracker out of a fixed static device arena.
-Two calls in a row, on different inputs, must each reproduce
-gbt_lk_track_batch's output within the LK tolerance of the other GPU tests;
-oversized requests must be refused.  This file is collected last on purpose.
+Both entry points launch the same kernels on the same inputs, so their
+outputs must be bitwise equal -- for two calls in a row on different inputs,
+and for two calls queued back to back on one stream with a single wait at the
+end (the arena is shared; stream order must keep the second call from
+overwriting it under the first).  Oversized requests must be refused.  This
+file is collected last on purpose.
 """
 import ctypes
 
@@ -14,7 +17,6 @@ import pytest
 
 pytestmark = pytest.mark.gpu
 
-TOL_PX = 0.01
 GBT_E_TOO_LARGE = 6
 
 
@@ -30,7 +32,9 @@ def _lib():
     return lib, lk
 
 
-def _run(fn, prev, cur, pts, L, prm, is_u8):
+def _queue(fn, prev, cur, pts, L, prm, is_u8):
+    """Queues one call on the current stream; returns (code, out, status, err)
+    as device tensors (not yet waited for)."""
     import torch
     npairs, H, W = prev.shape
     n = pts.shape[1]
@@ -39,7 +43,14 @@ def _run(fn, prev, cur, pts, L, prm, is_u8):
     st = torch.full((npairs, n), -7, dtype=torch.int32, device="cuda")
     err = torch.full((npairs, n), -7.0, device="cuda")
     code = fn(prev.data_ptr(), cur.data_ptr(), W * es, H * W * es, H, W, int(is_u8), L, ctypes.byref(prm), npairs,
-              pts.data_ptr(), n, out.data_ptr(), st.data_ptr(), err.data_ptr(), None)
+              pts.data_ptr(), n, out.data_ptr(), st.data_ptr(), err.data_ptr(),
+              ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
+    return code, out, st, err
+
+
+def _run(fn, *args):
+    import torch
+    code, out, st, err = _queue(fn, *args)
     torch.cuda.synchronize()
     return code, out.cpu().numpy(), st.cpu().numpy(), err.cpu().numpy()
 
@@ -54,9 +65,16 @@ def _inputs(seed, npairs, H, W, n, is_u8):
         prevs.append(s.frame(1) if is_u8 else s.frame_f32(1))
         curs.append(s.frame(2) if is_u8 else s.frame_f32(2))
     pts = np.stack([np.stack([rng.uniform(20, H - 20, n), rng.uniform(20, W - 20, n)], 1) for _ in range(npairs)])
+    # half the points on integer pixels, where equal gradient norms are common
+    pts[:, : n // 2] = np.floor(pts[:, : n // 2])
     dt = torch.uint8 if is_u8 else torch.float32
     return (torch.from_numpy(np.stack(prevs)).to("cuda", dt), torch.from_numpy(np.stack(curs)).to("cuda", dt),
             torch.from_numpy(pts.astype(np.float32)).cuda())
+
+
+def _assert_same(a, b):
+    for x, y in zip(a[1:], b[1:]):
+        np.testing.assert_array_equal(x, y)
 
 
 @pytest.mark.parametrize("is_u8,L,window", [(True, 3, 11), (False, 4, 9)])
@@ -66,14 +84,27 @@ def test_noalloc_matches_allocating_entry_point_twice(is_u8, L, window):
     prm = lk.params(window=window)
     for call, seed in enumerate((3, 4)):  # two calls in a row, different inputs
         prev, cur, pts = _inputs(seed, 2, 240, 320, 300, is_u8)
-        c0, o0, s0, e0 = _run(lib.gbt_lk_track_batch, prev, cur, pts, L, prm, is_u8)
-        c1, o1, s1, e1 = _run(lib.gbt_lk_track_batch_noalloc, prev, cur, pts, L, prm, is_u8)
-        assert c0 == 0 and c1 == 0, (call, c0, c1)
-        np.testing.assert_array_equal(s1, s0)
-        both = s0 > 0
-        assert both.sum() > 100
-        assert np.abs(o1 - o0)[both].max() < TOL_PX
-        np.testing.assert_allclose(e1[both], e0[both], rtol=1e-5)
+        r0 = _run(lib.gbt_lk_track_batch, prev, cur, pts, L, prm, is_u8)
+        r1 = _run(lib.gbt_lk_track_batch_noalloc, prev, cur, pts, L, prm, is_u8)
+        assert r0[0] == 0 and r1[0] == 0, (call, r0[0], r1[0])
+        assert (r0[2] > 0).sum() > 100
+        _assert_same(r1, r0)
+
+
+def test_noalloc_calls_queued_back_to_back_on_one_stream():
+    torch = pytest.importorskip("torch")
+    lib, lk = _lib()
+    prm = lk.params()
+    a = _inputs(6, 2, 240, 320, 400, True)
+    b = _inputs(7, 3, 200, 288, 500, True)  # another geometry: the arena's layout changes between the calls
+    ref_a = _run(lib.gbt_lk_track_batch, *a, 3, prm, True)
+    ref_b = _run(lib.gbt_lk_track_batch, *b, 3, prm, True)
+    qa = _queue(lib.gbt_lk_track_batch_noalloc, *a, 3, prm, True)
+    qb = _queue(lib.gbt_lk_track_batch_noalloc, *b, 3, prm, True)
+    torch.cuda.synchronize()
+    assert qa[0] == 0 and qb[0] == 0
+    _assert_same([0] + [t.cpu().numpy() for t in qa[1:]], ref_a)
+    _assert_same([0] + [t.cpu().numpy() for t in qb[1:]], ref_b)
 
 
 def test_noalloc_rejects_requests_beyond_its_arena():
