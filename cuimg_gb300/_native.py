@@ -101,9 +101,8 @@ def _declare(lib):
     lib.gbt_get_tuning.argtypes = [P, I32, I32P]
     lib.gbt_profile_enable.argtypes = [P, I32]
     lib.gbt_profile_read.argtypes = [P, I32, ctypes.c_char_p, ctypes.c_size_t, ctypes.POINTER(ctypes.c_double), I32P]
-    for name in ("gbt_set_param",):
-        if hasattr(lib, name):
-            getattr(lib, name).argtypes = [P, I32, I32, I32, I32]
+    lib.gbt_set_param.argtypes = [P, I32, I32, I32, I32]
+    lib.gbt_get_param.argtypes = [P, I32, I32, I32, I32P]
     if hasattr(lib, "gbt_gaussian_taps"):
         lib.gbt_gaussian_taps.argtypes = [ctypes.c_float, P, I32P]
         lib.gbt_gaussian_f32.argtypes = [P, ctypes.c_int64, P, ctypes.c_int64, I32, I32, ctypes.c_float, P]

@@ -541,13 +541,75 @@ static int grp_input_slot(Group* ctx, int32_t stream, uint8_t** dptr, int64_t* p
   return GBT_OK;
 }
 
-// Frame kind of the frame about to run.
+// Frame kind of the frame about to run (per unit: gbt_set_param may give the
+// scales of a stream different frequencies, as the reference's per-scale
+// setters can).
 static void frame_kind(Group* ctx, bool& any_det, bool& any_filt) {
   any_det = any_filt = false;
-  for (auto& s : ctx->streams) {
-    if (ctx->host_frame % s.cfg.detector_frequency == 0) any_det = true;
-    if (ctx->host_frame % s.cfg.filtering_frequency == 0) any_filt = true;
+  for (const Unit& u : ctx->units) {
+    if (ctx->host_frame % u.det_freq == 0) any_det = true;
+    if (ctx->host_frame % u.filt_freq == 0) any_filt = true;
   }
+}
+
+// The unit field a gbt_set_param key addresses, with its accepted range.
+static int* param_field(Unit& u, int key, int& lo, int& hi) {
+  lo = 0;
+  hi = 1 << 30;
+  switch (key) {
+    case GBT_PARAM_DETECTOR_THRESHOLD: return &u.threshold;
+    case GBT_PARAM_DETECTOR_N: lo = 1; hi = 16; return &u.nfast;
+    case GBT_PARAM_DETECTOR_FREQUENCY: lo = 1; return &u.det_freq;
+    case GBT_PARAM_FILTERING_FREQUENCY: lo = 1; return &u.filt_freq;
+    case GBT_PARAM_K: return &u.k;
+    case GBT_PARAM_WITH_MERGE: hi = 1; return &u.with_merge;
+    case GBT_PARAM_DETECTOR_GRAD_TH: return &u.det_grad_th;
+    default: return nullptr;
+  }
+}
+
+static int* config_field(gbt_config& c, int key) {
+  switch (key) {
+    case GBT_PARAM_DETECTOR_THRESHOLD: return &c.detector_threshold;
+    case GBT_PARAM_DETECTOR_N: return &c.detector_n;
+    case GBT_PARAM_DETECTOR_FREQUENCY: return &c.detector_frequency;
+    case GBT_PARAM_FILTERING_FREQUENCY: return &c.filtering_frequency;
+    case GBT_PARAM_K: return &c.k;
+    case GBT_PARAM_WITH_MERGE: return &c.with_merge;
+    case GBT_PARAM_DETECTOR_GRAD_TH: return &c.detector_grad_th;
+    default: return nullptr;
+  }
+}
+
+// Waits for the group's queued work, changes the parameter of the stream's
+// scale (every scale when scale is -1, which also updates the stream's
+// configuration) and re-uploads the unit tables; frames run from then on use
+// the new value.
+static int grp_set_param(Group* ctx, int32_t stream, int32_t scale, int32_t key, int32_t value) {
+  if (!ctx || stream < 0 || stream >= (int)ctx->streams.size()) return GBT_E_INVALID;
+  StreamInfo& si = ctx->streams[stream];
+  if (scale < -1 || scale >= si.cfg.nscales) return GBT_E_INVALID;
+  int lo, hi;
+  if (!param_field(ctx->units[si.unit0], key, lo, hi)) return set_err(ctx, GBT_E_INVALID, "unknown parameter %d", key);
+  if (value < lo || value > hi) return set_err(ctx, GBT_E_INVALID, "parameter %d out of range: %d", key, value);
+  CK(cudaSetDevice(ctx->device));
+  int r = sync_all(ctx);
+  if (r) return r;
+  const int l0 = scale < 0 ? 0 : scale, l1 = scale < 0 ? si.cfg.nscales : scale + 1;
+  for (int l = l0; l < l1; l++) *param_field(ctx->units[si.unit0 + l], key, lo, hi) = value;
+  if (scale < 0) *config_field(si.cfg, key) = value;
+  return upload_units(ctx);
+}
+
+static int grp_get_param(Group* ctx, int32_t stream, int32_t scale, int32_t key, int32_t* value) {
+  if (!ctx || !value || stream < 0 || stream >= (int)ctx->streams.size()) return GBT_E_INVALID;
+  const StreamInfo& si = ctx->streams[stream];
+  if (scale < 0 || scale >= si.cfg.nscales) return GBT_E_INVALID;
+  int lo, hi;
+  const int* f = param_field(ctx->units[si.unit0 + scale], key, lo, hi);
+  if (!f) return GBT_E_INVALID;
+  *value = *f;
+  return GBT_OK;
 }
 
 // An event from the profiling pool, or null when none could be created (the
@@ -1691,6 +1753,14 @@ extern "C" int gbt_kernels_per_frame(gbt_ctx* c, int32_t* n) {
   Group* g = c->g[c->grp[stream]];                       \
   const int32_t ls = c->local[stream];                   \
   return adopt(c, g, call_with_local)
+
+extern "C" int gbt_set_param(gbt_ctx* c, int32_t stream, int32_t scale, int32_t key, int32_t value) {
+  DISPATCH(grp_set_param(g, ls, scale, key, value));
+}
+
+extern "C" int gbt_get_param(gbt_ctx* c, int32_t stream, int32_t scale, int32_t key, int32_t* value) {
+  DISPATCH(grp_get_param(g, ls, scale, key, value));
+}
 
 extern "C" int gbt_nparticles(gbt_ctx* c, int32_t stream, int32_t scale, int32_t* n) {
   DISPATCH(grp_nparticles(g, ls, scale, n));

@@ -8,9 +8,11 @@
     ps.dense_particles(), ps.features(), ps.matches(), ps.sync_attributes(v, new)
 
 (cuimg/tracking2/tracker.h:10-47, tracking_strategies.h:28-107,
-particle_container.h:62-183.)  Settings are fixed when the first frame runs.
-``BatchTracker`` advances many independent streams of any resolution with one
-launch per stage.
+particle_container.h:62-183.)  Setters work at any time, per scale as in the
+reference: the frequencies and k set on scale s apply to s and every coarser
+scale (tracking_strategies.hpp:56-82), with_merge and the detector's n and
+threshold to scale s only.  ``BatchTracker`` advances many independent streams
+of any resolution with one launch per stage.
 """
 import ctypes
 
@@ -27,6 +29,12 @@ def sizes_ok(rows, cols, nscales):
     return bool(cuda_lib().gbt_sizes_ok(rows, cols, nscales))
 
 
+# gbt_set_param keys, and whether a setter on scale s also sets the coarser
+# scales (as generic_strategy's setters forward to upper_).
+PARAMS = dict(detector_threshold=(0, False), detector_n=(1, False), detector_frequency=(2, True),
+              filtering_frequency=(3, True), k=(4, True), with_merge=(5, False), detector_grad_th=(6, False))
+
+
 class _Detector:
     def __init__(self, owner):
         self._o = owner
@@ -36,6 +44,8 @@ class _Detector:
         return self
 
     def set_fast_threshold(self, th):
+        if float(th) != int(th) or th < 0:
+            raise ValueError("the FAST threshold must be a whole number >= 0")
         self._o._set("detector_threshold", int(th))
         return self
 
@@ -139,7 +149,7 @@ class _ScaleSetter:
         self.t, self.s, self.l = t, s, l
 
     def _set(self, key, value):
-        self.t._set_param(self.s, self.l, key, value)
+        self.t._set_param(self.s, 0 if self.l is None else self.l, key, value)
 
     def _stage(self, name):
         return self.t.stage(self.s, self.l, name)
@@ -163,15 +173,33 @@ class BatchTracker:
         self._graphs = graphs
         self._groups = groups
         self._ctx = None
+        self._pending = []  # per-scale settings made before the context exists
         self.nstreams = len(self._cfgs)
 
-    # -- settings (applied before the first frame) --
+    # -- settings (the reference's setters, at any time) --
     def _set_param(self, stream, scale, key, value):
-        if self._ctx is not None:
-            raise RuntimeError("tracker settings are fixed once the first frame has run")
+        """Sets `key` on `scale` (and the coarser scales for the frequencies
+        and k) of `stream` (every stream when None), through gbt_set_param
+        once the context runs."""
+        pid, upward = PARAMS[key]
         streams = range(self.nstreams) if stream is None else [stream]
         for s in streams:
-            setattr(self._cfgs[s], key, value)
+            L = self._cfgs[s].nscales
+            scales = range(scale, L) if upward else [scale]
+            if self._ctx is None:
+                if len(scales) == L:  # every scale: the stream's configuration, replacing earlier per-scale values
+                    setattr(self._cfgs[s], key, value)
+                    self._pending = [e for e in self._pending if not (e[0] == s and e[2] == pid)]
+                else:
+                    self._pending.append((s, list(scales), pid, value))
+            else:
+                for l in scales:
+                    check(self._lib.gbt_set_param(self._ctx, s, l, pid, value), self._ctx)
+
+    def get_param(self, key, stream=0, scale=0):
+        v = ctypes.c_int32()
+        check(self._lib.gbt_get_param(self._ensure(), stream, scale, PARAMS[key][0], ctypes.byref(v)), self._ctx)
+        return v.value
 
     def _ensure(self):
         if self._ctx is None:
@@ -182,6 +210,10 @@ class BatchTracker:
                 raise GbtError(code, "gbt_create failed (sizes ok: %s)" % [
                     sizes_ok(c.rows, c.cols, c.nscales) for c in self._cfgs])
             self._ctx = ctx
+            for s, scales, pid, value in self._pending:
+                for l in scales:
+                    check(self._lib.gbt_set_param(ctx, s, l, pid, value), ctx)
+            self._pending = []
             if self._graphs:
                 check(self._lib.gbt_use_graphs(self._ctx, 1), self._ctx)
         return self._ctx

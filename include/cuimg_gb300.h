@@ -162,6 +162,29 @@ int gbt_test_withhold_tile_copies(gbt_ctx* ctx, int32_t enable);
  * the default priority shares the GPU with the latter.) */
 int gbt_stream(gbt_ctx* ctx, void** cuda_stream);
 
+/* Runtime setters, callable between frames at any time, as the reference's
+ * strategy and detector setters are: generic_strategy::set_detector_frequency,
+ * set_filtering_frequency, set_k, set_with_merge
+ * (cuimg/tracking2/tracking_strategies.hpp:56-91), fast_detector::set_n and
+ * set_fast_threshold (cuimg/tracking2/fast_detector.hpp:170-193) and
+ * regular_detector::set_grad_th (cuimg/tracking2/regular_detector.hpp:25-40).
+ * `scale` selects one scale of the stream (the reference's
+ * tracker.scale(s).strategy()...) or, with -1, every scale and the stream's
+ * configuration.  gbt_set_param waits for the context's queued work; the
+ * frames queued after it use the new value.  Ranges as gbt_create: threshold,
+ * k and grad_th >= 0, n in 1..16, frequencies >= 1, with_merge 0 or 1.
+ * Values set for one scale only are not part of a checkpoint's configuration
+ * check: set them again on the context a checkpoint is loaded into. */
+#define GBT_PARAM_DETECTOR_THRESHOLD 0
+#define GBT_PARAM_DETECTOR_N 1
+#define GBT_PARAM_DETECTOR_FREQUENCY 2
+#define GBT_PARAM_FILTERING_FREQUENCY 3
+#define GBT_PARAM_K 4
+#define GBT_PARAM_WITH_MERGE 5
+#define GBT_PARAM_DETECTOR_GRAD_TH 6
+int gbt_set_param(gbt_ctx* ctx, int32_t stream, int32_t scale, int32_t key, int32_t value);
+int gbt_get_param(gbt_ctx* ctx, int32_t stream, int32_t scale, int32_t key, int32_t* value);
+
 /* Particle set of (stream, scale): dense slot count (tombstones included,
  * as particle_container::size(), particle_container.h:137). */
 int gbt_nparticles(gbt_ctx* ctx, int32_t stream, int32_t scale, int32_t* n);

@@ -103,6 +103,26 @@ void ref_destroy(void* h) {
   delete c;
 }
 
+// The reference's own setter of scale `scale`, called between frames: 0
+// detector().set_fast_threshold, 1 detector().set_n, 2 set_detector_frequency,
+// 3 set_filtering_frequency, 4 set_k (these three also set every coarser
+// scale, tracking_strategies.hpp:56-82), 5 set_with_merge.
+int ref_set_param(void* h, int scale, int key, int value) {
+  ref_ctx* c = (ref_ctx*)h;
+  if (scale < 0 || scale >= c->nscales) return -1;
+  S& st = c->tr->scale(scale).strategy();
+  switch (key) {
+    case 0: st.detector().set_fast_threshold(value); break;
+    case 1: st.detector().set_n(value); break;
+    case 2: st.set_detector_frequency(value); break;
+    case 3: st.set_filtering_frequency(value); break;
+    case 4: st.set_k(value); break;
+    case 5: st.set_with_merge(value != 0); break;
+    default: return -1;
+  }
+  return 0;
+}
+
 void ref_run(void* h, const uint8_t* frame) {
   ref_ctx* c = (ref_ctx*)h;
   host_image2d<gl8u> in(c->dom);

@@ -66,13 +66,15 @@ typedef struct {
   int compact_has_run;
   uint8_t* moved;   /* per particle, scratch */
   int frame_cpt;
+  /* This scale's strategy and detector settings (the reference keeps them per
+   * scale: generic_strategy and its detector, tracking_strategies.h:99-106). */
+  int threshold, det_freq, filt_freq, k, with_merge, n_fast, grad_th;
 } olevel;
 
 typedef struct {
   int L;
   olevel* lv;
-  int threshold, det_freq, filt_freq, k, with_merge, n_fast;
-  int detector, step, grad_th; /* 0 FAST, 1 regular, 2 dense */
+  int detector, step; /* 0 FAST, 1 regular, 2 dense */
 } otracker;
 
 #define AT(img, pitch, b, r, c) ((img)[(size_t)((r) + (b)) * (pitch) + ((c) + (b))])
@@ -321,7 +323,7 @@ static void match_particles(otracker* t, int s) {
       unsigned n_diff = 0, cpt = 0;
       for (int j = 8; j < 16; j++) {
         cpt++;
-        if (abs((int)f[j] - (int)mf[j]) > t->k) n_diff++;
+        if (abs((int)f[j] - (int)mf[j]) > l->k) n_diff++;
       }
       accept = n_diff < cpt / 2;
     }
@@ -513,7 +515,7 @@ static int alt_births(otracker* t, olevel* l) {
           for (int i = 0; i < 8; i++) res += abs((int)AT(l->in, l->pin, 6, r + 2 * C8[i][0], c + 2 * C8[i][1]) - vp);
           rc = res / 8;
         }
-        if (rc < t->grad_th) continue;
+        if (rc < l->grad_th) continue;
       }
       if (add_particle(l, r, c)) return -1;
     }
@@ -542,7 +544,7 @@ static int detect_and_compact(otracker* t, int s) {
   for (int r = 0; r < H; r++)
     for (int c = 0; c < W; c++)
       if (AT(l->mask, l->pmask, 4, r, c) != 0)
-        AT(l->sal, l->psal, 1, r, c) = fast_saliency(l, r, c, t->n_fast, t->threshold);
+        AT(l->sal, l->psal, 1, r, c) = fast_saliency(l, r, c, l->n_fast, l->threshold);
 
   memset(l->newpts, 0, (size_t)H * W);
   int TH = H / 3, TW = W / 3;
@@ -570,7 +572,7 @@ static int detect_and_compact(otracker* t, int s) {
               mc = pc + c;
             }
           }
-      if (vmax < (float)t->threshold) continue;
+      if (vmax < (float)l->threshold) continue;
       l->newpts[(size_t)mr * W + mc] = 1;
     }
   /* Births in raster order over domain - border(3). */
@@ -647,11 +649,11 @@ static int strategy_update(otracker* t, int s) {
   compute_contrast(l);
   update_feature(l);
   match_particles(t, s);
-  if (!(l->frame_cpt % t->det_freq))
+  if (!(l->frame_cpt % l->det_freq))
     if (detect_and_compact(t, s)) return -1;
-  if (!(l->frame_cpt % t->filt_freq)) {
+  if (!(l->frame_cpt % l->filt_freq)) {
     filter_particles(l);
-    if (t->with_merge) merge_particles(l);
+    if (l->with_merge) merge_particles(l);
   }
   l->frame_cpt++;
   return 0;
@@ -684,16 +686,18 @@ void* oracle_create(int rows, int cols, int nscales, int threshold, int det_freq
   otracker* t = (otracker*)calloc(1, sizeof(otracker));
   if (!t) return NULL;
   t->L = nscales;
-  t->threshold = threshold;
-  t->det_freq = det_freq;
-  t->filt_freq = filt_freq;
-  t->k = 300;
-  t->with_merge = 1;
-  t->n_fast = 9;
   t->lv = (olevel*)calloc(nscales, sizeof(olevel));
   int H = rows, W = cols;
   for (int s = 0; s < nscales; s++) {
-    if (level_alloc(&t->lv[s], H, W)) return NULL;
+    olevel* l = &t->lv[s];
+    if (level_alloc(l, H, W)) return NULL;
+    l->threshold = threshold;
+    l->det_freq = det_freq;
+    l->filt_freq = filt_freq;
+    l->k = 300;
+    l->with_merge = 1;
+    l->n_fast = 9;
+    l->grad_th = 1;
     H /= 2;
     W /= 2;
   }
@@ -708,14 +712,37 @@ void oracle_destroy(void* h) {
   free(t);
 }
 
-void oracle_set_k(void* h, int k) { ((otracker*)h)->k = k; }
-void oracle_set_with_merge(void* h, int m) { ((otracker*)h)->with_merge = m; }
-void oracle_set_n(void* h, int n) { ((otracker*)h)->n_fast = n; }
+/* One setting of scale `s` (every scale when s < 0), the keys of
+ * gbt_set_param: 0 threshold, 1 n, 2 detector frequency, 3 filtering
+ * frequency, 4 k, 5 with_merge, 6 grad_th.  Callable between frames, as the
+ * reference's setters are. */
+int oracle_set_param(void* h, int s, int key, int value) {
+  otracker* t = (otracker*)h;
+  int s0 = s < 0 ? 0 : s, s1 = s < 0 ? t->L : s + 1;
+  if (s >= t->L) return -1;
+  for (int i = s0; i < s1; i++) {
+    olevel* l = &t->lv[i];
+    switch (key) {
+      case 0: l->threshold = value; break;
+      case 1: l->n_fast = value; break;
+      case 2: l->det_freq = value; break;
+      case 3: l->filt_freq = value; break;
+      case 4: l->k = value; break;
+      case 5: l->with_merge = value; break;
+      case 6: l->grad_th = value; break;
+      default: return -1;
+    }
+  }
+  return 0;
+}
+void oracle_set_k(void* h, int k) { oracle_set_param(h, -1, 4, k); }
+void oracle_set_with_merge(void* h, int m) { oracle_set_param(h, -1, 5, m); }
+void oracle_set_n(void* h, int n) { oracle_set_param(h, -1, 1, n); }
 void oracle_set_detector(void* h, int kind, int step, int grad_th) {
   otracker* t = (otracker*)h;
   t->detector = kind;
   t->step = step;
-  t->grad_th = grad_th;
+  oracle_set_param(h, -1, 6, grad_th);
 }
 
 int oracle_run(void* h, const uint8_t* frame) {

@@ -49,6 +49,14 @@ class StageLib:
         self.L = nscales
         return self
 
+    def set_param(self, scale, key, value):
+        """The library's setter of one scale between frames (keys of
+        gbt_set_param; see oracle_set_param / ref_set_param)."""
+        f = self._f("set_param")
+        f.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int]
+        if f(self.h, scale, key, value) != 0:
+            raise RuntimeError("set_param failed")
+
     def destroy(self):
         if self.h:
             self._f("destroy")(self.h)
@@ -177,3 +185,46 @@ def diff_snapshots(a, b, detector_frame, keys=None, fast_detector=True):
             elif x["compact"] and not np.array_equal(x["matches"], y["matches"]):
                 bad.append("scale %d: matches" % s)
     return bad
+
+
+# Setter calls made between frames, as the reference's own setters of one
+# scale: (before frame, scale, key, value), keys of gbt_set_param (0 FAST
+# threshold, 1 arc length n, 2 detector frequency, 3 filtering frequency,
+# 4 k, 5 with_merge).  The frequency and k setters also set every coarser
+# scale (tracking_strategies.hpp:56-82); the others set their scale only.
+SETTER_SCHEDULE = [
+    (2, 0, 2, 3),    # detector every 3 frames, all scales
+    (4, 1, 0, 35),   # per-scale thresholds
+    (4, 2, 0, 12),
+    (6, 1, 5, 0),    # no merge on scale 1
+    (8, 1, 2, 2),    # detector every 2 frames on scales 1 and up
+    (9, 0, 4, 60),   # k = 60 everywhere: many more matches rejected
+    (11, 2, 3, 2),   # filter every 2 frames on scale 2
+    (12, 0, 1, 12),  # arc length 12 on scale 0
+    (14, 0, 4, 300),
+]
+UPWARD_KEYS = (2, 3, 4)
+
+
+def scales_set_by(L, scale, key):
+    """Scales one reference setter call changes."""
+    return list(range(scale, L)) if key in UPWARD_KEYS else [scale]
+
+
+class SettingsTrack:
+    """The per-scale settings a SETTER_SCHEDULE has produced so far."""
+
+    def __init__(self, L, det_freq, filt_freq):
+        self.det = [det_freq] * L
+        self.filt = [filt_freq] * L
+
+    def apply(self, L, scale, key, value):
+        for s in scales_set_by(L, scale, key):
+            if key == 2:
+                self.det[s] = value
+            elif key == 3:
+                self.filt[s] = value
+
+    def all_detect(self, frame):
+        return all(frame % d == 0 for d in self.det)
+

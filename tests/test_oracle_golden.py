@@ -79,6 +79,35 @@ def test_oracle_matches_reference_live(rows, cols, L, detf, n, seed):
 
 
 @pytest.mark.skipif(not reference_available(), reason="reference not built here (oracle/_ref)")
+@pytest.mark.parametrize("rows,cols,L,seed", [(240, 320, 3, 12), (480, 640, 3, 1)])
+def test_oracle_runtime_setters_match_reference_live(rows, cols, L, seed):
+    # The reference's setters called between frames (per-scale thresholds,
+    # frequencies, k, merge, arc length; SETTER_SCHEDULE) and the oracle's
+    # oracle_set_param on the scales each call sets: every stage of every
+    # frame equal.
+    from cuimg_gb300 import synth
+    from stage_api import SETTER_SCHEDULE, SettingsTrack, scales_set_by
+    n = 18
+    frames = synth.frames(seed, rows, cols, n)
+    ref = tracker_reference(rows, cols, L, 20, 10, 1)
+    o = tracker_oracle(rows, cols, L, 20, 10, 1)
+    track = SettingsTrack(L, 10, 1)
+    for t in range(n):
+        for (ft, scale, key, value) in SETTER_SCHEDULE:
+            if ft == t and scale < L:
+                ref.set_param(scale, key, value)
+                for s in scales_set_by(L, scale, key):
+                    o.set_param(s, key, value)
+                track.apply(L, scale, key, value)
+        ref.run(frames[t])
+        o.run(frames[t])
+        bad = diff_snapshots(snapshot(ref, L), snapshot(o, L), detector_frame=track.all_detect(t))
+        assert not bad, "frame %d: %s" % (t, bad)
+    ref.destroy()
+    o.destroy()
+
+
+@pytest.mark.skipif(not reference_available(), reason="reference not built here (oracle/_ref)")
 def test_oracle_matches_reference_live_random_geometries():
     # Seeded random geometries, scale counts, thresholds and detector periods
     # (GBT_REF_SWEEP cases, default 40; larger sweeps: GBT_REF_SWEEP=300),

@@ -321,3 +321,74 @@ def test_invalid_geometry_rejected():
     tr = Tracker((97, 131), 3)
     with pytest.raises(GbtError):
         tr.run(np.zeros((97, 131), np.uint8))
+
+
+def _apply_setter(strategy, key, value):
+    """One of the reference's setters on a scale's strategy() (keys of
+    gbt_set_param)."""
+    if key == 0:
+        strategy.detector().set_fast_threshold(value)
+    elif key == 1:
+        strategy.detector().set_n(value)
+    elif key == 2:
+        strategy.set_detector_frequency(value)
+    elif key == 3:
+        strategy.set_filtering_frequency(value)
+    elif key == 4:
+        strategy.set_k(value)
+    else:
+        strategy.set_with_merge(bool(value))
+
+
+@pytest.mark.parametrize("graphs", [False, True])
+def test_runtime_setters_match_oracle(graphs):
+    # Settings changed between frames through the reference-style setters
+    # (gbt_set_param): per-scale thresholds and arc length, frequencies and k
+    # forwarded to the coarser scales, merge off on one scale; every stage of
+    # every frame bit-exact with the oracle given the same calls, with and
+    # without graph replay.
+    from cuimg_gb300 import synth
+    from stage_api import SETTER_SCHEDULE, SettingsTrack, scales_set_by
+    rows, cols, L, n = 240, 320, 3, 18
+    frames = synth.frames(12, rows, cols, n)
+    tr = _gpu_tracker(rows, cols, L, 20, 10, 1, graphs)
+    o = tracker_oracle(rows, cols, L, 20, 10, 1)
+    track = SettingsTrack(L, 10, 1)
+    for t in range(n):
+        for (ft, scale, key, value) in SETTER_SCHEDULE:
+            if ft == t:
+                _apply_setter(tr.scale(scale).strategy(), key, value)
+                for s in scales_set_by(L, scale, key):
+                    o.set_param(s, key, value)
+                track.apply(L, scale, key, value)
+        tr.run(frames[t])
+        o.run(frames[t])
+        bad = diff_snapshots(snapshot(o, L), tr.snapshot(), detector_frame=track.all_detect(t))
+        assert not bad, "frame %d: %s" % (t, bad)
+    assert tr.get_param("detector_threshold", 0, 1) == 35
+    assert tr.get_param("detector_frequency", 0, 2) == 2 and tr.get_param("detector_frequency", 0, 0) == 3
+    tr.close()
+    o.destroy()
+
+
+def test_runtime_setter_on_one_stream_of_a_batch():
+    # A setter on one stream of a batch changes that stream only.
+    from cuimg_gb300 import BatchTracker, synth
+    rows, cols, L, n = 240, 320, 3, 12
+    vids = [synth.frames(30 + i, rows, cols, n) for i in range(2)]
+    bt = BatchTracker([dict(rows=rows, cols=cols, nscales=L, detector_threshold=20, detector_frequency=10)] * 2,
+                      graphs=True, groups=1)
+    os_ = [tracker_oracle(rows, cols, L, 20, 10, 1) for _ in range(2)]
+    for t in range(n):
+        if t == 3:
+            bt._set_param(1, 0, "detector_frequency", 2)
+            for s in range(L):
+                os_[1].set_param(s, 2, 2)
+        bt.run([v[t] for v in vids])
+        for i in range(2):
+            os_[i].run(vids[i][t])
+            bad = diff_snapshots(snapshot(os_[i], L), bt.snapshot(i), detector_frame=False)
+            assert not bad, "stream %d frame %d: %s" % (i, t, bad)
+    bt.close()
+    for o in os_:
+        o.destroy()
