@@ -2,8 +2,12 @@
 
 Workload (one "step" = one frame of every stream): B independent 1920x1080
 uint8 gray video streams from the seeded generator, 4 scales, FAST threshold
-20, detector every 10 frames, filtering every frame (~100k live particles per
-stream), advanced by one launch per stage replayed as a CUDA graph.
+20, detector every 10 frames, filtering every frame, advanced by one launch
+per stage replayed as a CUDA graph.  Every stream first runs PREROLL frames
+untimed (the 120 frames of the 1080p configuration), so the timed frames see
+the steady-state particle population, not the ramp-up after the first
+detection.  Where a clip is replayed longer than it was generated, frames are
+played back and forth (palindromic order), so the motion stays coherent.
 
 Prints one JSON line:
   value      tracked frames/s over all streams (batched), frames resident in HBM
@@ -15,6 +19,8 @@ Prints one JSON line:
   cpu_baseline  the oracle port (C restatement of the reference CPU tracker)
              on the host cores, bounded sample
 `--impl reference` times that CPU implementation alone on the same workload.
+`--profile-case NAME` runs one small case of a kernel family for profiler
+captures (no timing, no JSON).
 """
 import argparse
 import concurrent.futures as cf
@@ -32,27 +38,37 @@ sys.path.insert(0, ROOT)
 
 ROWS, COLS, NSCALES = 1080, 1920, 4
 DET_FREQ, FILT_FREQ, THRESHOLD = 10, 1, 20
+PREROLL = 120  # frames run before any timed region
 METRIC = "tracked_frames_per_s_1080p"
 UNIT = "frames/s"
 PER_PARTICLE_BYTES = 84  # state read/write, template read/write, sparse index
-# DRAM bytes (read + write) of one matcher launch per 1080p stream, from the
-# ncu captures summarised in profiles/k_match_tiled_1080p_x4.md (4 streams,
-# 75.0 MB per launch) and profiles/k_match_1080p_x4.md (76.8 MB); a launch's
-# traffic grows with the streams it covers.
-# DRAM read + write per launch per 1080p stream (4 scales) from ncu captures of
-# 4-stream launches (profiles/k_match_tiled_1080p_x4.md, profiles/k_match_1080p_x4.md),
-# and the busiest unit of the tiled matcher there (l1tex__data_pipe_lsu_wavefronts).
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one launch per
+# 1080p stream (4 scales), measured by ncu on one launch over four 1080p
+# streams (k_match_tiled: 80.0 MB, k_match: 76.8 MB, at about 54k live
+# particles per stream); a launch's traffic grows with the streams it covers.
 DRAM_BYTES_PER_STREAM = {"k_match_tiled": 20.0e6, "k_match": 19.2e6}
+# The unit that limits the tiled matcher and its utilisation in the same ncu
+# capture (l1tex__data_pipe_lsu_wavefronts: shared-memory byte gathers).
 LIMITER = {"k_match_tiled": ("L1 / shared-memory data pipe (byte gathers at the ring offsets)", 0.74)}
 
 
-def level_pixels():
-    return [(ROWS >> l) * (COLS >> l) for l in range(NSCALES)]
+def pal(t, n):
+    """Frame index of step t when a clip of n frames is played back and forth
+    (0, 1, .., n-1, n-2, .., 1, 0, 1, ..)."""
+    if n <= 1:
+        return 0
+    p = 2 * n - 2
+    t %= p
+    return t if t < n else p - t
 
 
-def frame_bytes_model(live_particles):
+def level_pixels(rows=ROWS, cols=COLS, nscales=NSCALES):
+    return [(rows >> l) * (cols >> l) for l in range(nscales)]
+
+
+def frame_bytes_model(live_particles, rows=ROWS, cols=COLS, nscales=NSCALES):
     """Algorithmic HBM bytes of one tracked frame (one stream)."""
-    P = level_pixels()
+    P = level_pixels(rows, cols, nscales)
     Pt = sum(P)
     return P[0] + sum(P[1:]) + 2 * Pt + Pt + 2 * Pt + Pt / 8 + PER_PARTICLE_BYTES * live_particles
 
@@ -70,14 +86,30 @@ def kernel_bytes_model(name, live_particles, nstreams):
     return None if per is None else per * nstreams
 
 
-def gen_streams(nstreams, nframes, seed0=1000):
+def gen_clips(specs, workers=None):
+    """specs: (seed, rows, cols, nframes) per clip.  Every clip's generator is
+    made once and its frames are generated in threads (frame generation only
+    reads the generator's texture, and its C calls release the interpreter
+    lock)."""
+    import numpy as np
+
     from cuimg_gb300 import synth
+    outs = [np.empty((n, r, c), np.uint8) for (_, r, c, n) in specs]
+    with cf.ThreadPoolExecutor(max_workers=workers or min(32, os.cpu_count() or 4)) as ex:
+        streams = list(ex.map(lambda sp: synth.Stream(sp[0], sp[1], sp[2]), specs))
 
-    def one(i):
-        return synth.frames(seed0 + i, ROWS, COLS, nframes)
+        def one(job):
+            k, t = job
+            outs[k][t] = streams[k].frame(t)
 
-    with cf.ThreadPoolExecutor(max_workers=min(16, os.cpu_count() or 4)) as ex:
-        return list(ex.map(one, range(nstreams)))
+        list(ex.map(one, [(k, t) for k, sp in enumerate(specs) for t in range(sp[3])]))
+    for s in streams:
+        s.close()
+    return outs
+
+
+def gen_streams(nstreams, nframes, seed0=1000):
+    return gen_clips([(seed0 + i, ROWS, COLS, nframes) for i in range(nstreams)])
 
 
 class ClockSampler:
@@ -134,34 +166,37 @@ def cpu_model():
     return platform.machine()
 
 
-def _cpu_stream_worker(i, nframes, warmup, barrier, out):
+def _cpu_stream_worker(i, preroll, nframes, barrier, out):
     """One stream of the CPU tracker (oracle port, one thread) in its own
-    process: frames of stream i, `warmup` untimed, the rest timed between
-    barriers shared by all streams."""
+    process: `preroll` frames untimed, then `nframes` timed between barriers
+    shared by all streams; reports the live particles (age > 0) afterwards."""
     os.environ["OMP_NUM_THREADS"] = "1"
     sys.path.insert(0, ROOT)
     sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import numpy as np
+
     from cuimg_gb300 import synth
     from oracle_lib import tracker_oracle
-    frames = synth.frames(1000 + i, ROWS, COLS, nframes)
+    frames = synth.frames(1000 + i, ROWS, COLS, preroll + nframes)
     o = tracker_oracle(ROWS, COLS, NSCALES, THRESHOLD, DET_FREQ, FILT_FREQ)
-    for t in range(warmup):
+    for t in range(preroll):
         o.run(frames[t])
     barrier.wait()
     t0 = time.perf_counter()
-    for t in range(warmup, nframes):
+    for t in range(preroll, preroll + nframes):
         o.run(frames[t])
     dt = time.perf_counter() - t0
     barrier.wait()
-    out.put((i, dt, sum(o.nparticles(s) for s in range(NSCALES))))
+    live = sum(int((o.particles(s)["age"] > 0).sum()) for s in range(NSCALES))
+    out.put((i, dt, live))
     o.destroy()
 
 
-def run_cpu_streams(nstreams, steps, warmup):
+def run_cpu_streams(nstreams, steps, preroll):
     """The CPU tracker on `nstreams` 1080p streams at once, one process and
     one core per stream (the streams are independent, as on the GPU); returns
     frames/s over all streams, the wall time of the timed frames, the cores
-    used and the mean live particles per stream."""
+    used and the mean live particles (age > 0) per stream."""
     import multiprocessing as mp
 
     import numpy as np
@@ -170,8 +205,7 @@ def run_cpu_streams(nstreams, steps, warmup):
     ctx = mp.get_context("spawn")
     barrier = ctx.Barrier(workers)
     out = ctx.Queue()
-    procs = [ctx.Process(target=_cpu_stream_worker, args=(i, warmup + steps, warmup, barrier, out))
-             for i in range(workers)]
+    procs = [ctx.Process(target=_cpu_stream_worker, args=(i, preroll, steps, barrier, out)) for i in range(workers)]
     for pr in procs:
         pr.start()
     res = [out.get() for _ in procs]
@@ -194,22 +228,25 @@ def dist_setup():
     return world, rank, local, pg
 
 
+def workload_name(nstreams):
+    return ("%d streams x 1920x1080 gray, 4 scales, FAST th 20, detector every 10 frames, filter every frame; "
+            "%d frames of every stream before timing; one frame of every stream per step" % (nstreams, PREROLL))
+
+
 def bench_reference(args):
     world, rank, local, pg = dist_setup()
     if rank != 0:
         return
-    fps, wall, cores, n = run_cpu_streams(args.streams, args.steps, args.warmup)
+    fps, wall, cores, n = run_cpu_streams(args.streams, args.steps, PREROLL + args.warmup)
     line = {
         "impl": "reference", "metric": METRIC, "value": round(fps, 3), "unit": UNIT, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1000 * wall / args.steps, 3),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8", "data": "synthetic",
-        "config": {"workload": "%d streams x 1920x1080 gray, 4 scales, FAST th 20, detector every 10 frames, "
-                               "filter every frame; one frame of every stream per step" % cores,
-                   "streams": cores, "live_particles_per_stream": round(n)},
+        "config": {"workload": workload_name(cores), "streams": cores, "live_particles_per_stream": round(n)},
         "cpu_baseline": {"value": round(fps, 3), "unit": UNIT, "cores": cores, "kind": "port",
                          "per_core": round(fps / cores, 3), "cpu": cpu_model(),
-                         "sample": "%d timed frames of each of %d streams after %d warm-up frames, one process and "
-                                   "core per stream" % (args.steps, cores, args.warmup)},
+                         "sample": "%d timed frames of each of %d streams after %d untimed frames, one process and "
+                                   "core per stream" % (args.steps, cores, PREROLL + args.warmup)},
         "e2e": {"value": round(fps, 3), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -227,7 +264,8 @@ def bench_ours(args):
     dev = torch.device("cuda", local)
     lib = cuda_lib()
     B = args.streams
-    nfr = args.warmup + args.steps
+    W0 = PREROLL + args.warmup  # untimed frames before every timed region
+    nfr = W0 + args.steps
     frames = gen_streams(B, nfr, seed0=1000 + rank * B)
     cfg = [dict(rows=ROWS, cols=COLS, nscales=NSCALES, detector_threshold=THRESHOLD, detector_frequency=DET_FREQ,
                 filtering_frequency=FILT_FREQ) for _ in range(B)]
@@ -236,8 +274,9 @@ def bench_ours(args):
     if args.matcher >= 0:
         tuning = {0: args.matcher}
     else:
-        tuning = autotune.tune(cfg, [[frames[s][t] for s in range(B)] for t in range(min(nfr, 11))], warmup=3, timed=8,
-                               device=local)
+        # Tuned at steady state: every setting runs the pre-roll, then is timed.
+        tuning = autotune.tune(cfg, [[frames[s][pal(t, nfr)] for s in range(B)] for t in range(PREROLL + 8)],
+                               warmup=PREROLL, timed=8, device=local)
 
     def make(nstreams, graphs=True, groups=0):
         bt = BatchTracker(cfg[:nstreams], device=local, graphs=graphs, groups=groups)
@@ -251,19 +290,24 @@ def bench_ours(args):
     launches = [0]  # kernels launched inside the last timed region
     step_stats = [None]  # per-step milliseconds of the last timed region
 
-    def timed_resident(bt, nstreams, steps, warmup, offset=0, sustain_s=0.0):
+    def resident_step(bt, nstreams, t, ptrs, pitches):
+        for s in range(nstreams):
+            ptrs[s] = dev_frames[s][pal(t, nfr)].data_ptr()
+        check(lib.gbt_run(bt._ctx, ptrs, pitches, 1), bt._ctx)
+
+    def preroll(bt, nstreams, n):
+        ptrs = (ctypes.c_void_p * nstreams)()
+        pitches = (ctypes.c_int64 * nstreams)(*([COLS] * nstreams))
+        for t in range(n):
+            resident_step(bt, nstreams, t, ptrs, pitches)
+        bt.sync()
+
+    def timed_resident(bt, nstreams, steps, sustain_s=0.0):
+        """Frames 0 .. W0 - 1 untimed, then `steps` timed frames."""
         stream = torch.cuda.ExternalStream(bt.cuda_stream(), device=dev)
         ptrs = (ctypes.c_void_p * nstreams)()
         pitches = (ctypes.c_int64 * nstreams)(*([COLS] * nstreams))
-
-        def step(t):
-            for s in range(nstreams):
-                ptrs[s] = dev_frames[s][t % nfr].data_ptr()
-            check(lib.gbt_run(bt._ctx, ptrs, pitches, 1), bt._ctx)
-
-        for t in range(warmup):
-            step(offset + t)
-        bt.sync()
+        preroll(bt, nstreams, W0)
         if pg:
             pg.barrier()
         torch.cuda.synchronize()
@@ -271,7 +315,7 @@ def bench_ours(args):
         k0 = bt.kernel_launches()
         ev[0].record(stream)
         for t in range(steps):
-            step(offset + warmup + t)
+            resident_step(bt, nstreams, W0 + t, ptrs, pitches)
             ev[t + 1].record(stream)
         launches[0] = bt.kernel_launches() - k0
         ev[-1].synchronize()
@@ -282,10 +326,10 @@ def bench_ours(args):
                          "p90": round(per[min(len(per) - 1, (9 * len(per)) // 10)], 4)}
         # Keep the same step running so the clock sampler sees the GPU under
         # this load for longer than the (short) timed region; not timed.
-        t_end, t = time.perf_counter() + sustain_s, steps
+        t_end, t = time.perf_counter() + sustain_s, W0 + steps
         while time.perf_counter() < t_end:
             for _ in range(32):
-                step(offset + warmup + t)
+                resident_step(bt, nstreams, t, ptrs, pitches)
                 t += 1
             bt.sync()
         if pg:
@@ -294,10 +338,14 @@ def bench_ours(args):
             ms = float(tt.item())
         return ms
 
+    def live_per_stream(bt, nstreams):
+        return float(np.mean([sum(int((bt._particles(s, l)["age"] > 0).sum()) for l in range(NSCALES))
+                              for s in range(nstreams)]))
+
     # Batched, resident.
     bt = make(B)
     with ClockSampler(local) as clk:
-        ms = timed_resident(bt, B, args.steps, args.warmup, sustain_s=1.5)
+        ms = timed_resident(bt, B, args.steps, sustain_s=1.5)
     timed_launches = launches[0]
     batched_steps = step_stats[0]
     clocks = clk.summary()
@@ -309,28 +357,26 @@ def bench_ours(args):
     # The same with device-side trajectories (20 positions per particle).
     btt = make(B)
     btt.enable_trajectories(20)
-    ms_t = timed_resident(btt, B, args.steps, args.warmup)
+    ms_t = timed_resident(btt, B, args.steps)
     traj_fps = B * world * args.steps / (ms_t / 1000.0)
     btt.close()
 
     # Plain single stream, resident.
     bt1 = make(1)
-    ms1 = timed_resident(bt1, 1, args.steps, args.warmup)
+    ms1 = timed_resident(bt1, 1, args.steps)
     plain = args.steps / (ms1 / 1000.0)
     bt1.close()
 
-    # Per-kernel device time (eager, CUDA events on the context stream).
+    # Per-kernel device time (eager, CUDA events on the context stream), over
+    # the frames the timed region ran, after the same pre-roll.
     btp = make(B, graphs=False, groups=1)  # one launch per kernel over all streams, serialised
     nprof = max(args.steps, DET_FREQ)
-    for t in range(args.warmup):
-        btp.run([frames[s][t % nfr] for s in range(B)])
+    preroll(btp, B, W0)
     lib.gbt_profile_enable(btp._ctx, 1)
-    ptrs = (ctypes.c_void_p * B)()
+    preroll_ptrs = (ctypes.c_void_p * B)()
     pitches = (ctypes.c_int64 * B)(*([COLS] * B))
     for t in range(nprof):
-        for s in range(B):
-            ptrs[s] = dev_frames[s][(args.warmup + t) % nfr].data_ptr()
-        check(lib.gbt_run(btp._ctx, ptrs, pitches, 1), btp._ctx)
+        resident_step(btp, B, W0 + t, preroll_ptrs, pitches)
     btp.sync()
     prof = {}
     nameb = ctypes.create_string_buffer(64)
@@ -343,12 +389,7 @@ def bench_ours(args):
             break
         prof[nameb.value.decode()] = (tot.value, cnt.value)
         k += 1
-    # Live particles after the same frames the timed region ran.
-    live = []
-    for s in range(B):
-        p = [btp._particles(s, l) for l in range(NSCALES)]
-        live.append(sum(int((q["age"] > 0).sum()) for q in p))
-    live_mean = float(np.mean(live))
+    live_mean = live_per_stream(btp, B)  # live particles (age > 0) at the end of the profiled frames
     btp.close()
     total_ms = sum(v[0] for v in prof.values())
     shares = {n: round(v[0] / total_ms, 4) for n, v in sorted(prof.items(), key=lambda kv: -kv[1][0])}
@@ -368,18 +409,20 @@ def bench_ours(args):
     # per-unit particle counts out, H2D and D2H inside the timed region.
     # "e2e" reads step t's counts while step t + 1 runs (gbt_read_counts_async
     # into pinned memory, an event per step); "blocking" waits for each step's
-    # counts before queuing the next.  Host clock, max over ranks; the median
-    # of three timed blocks (the host shares its cores with other work).
+    # counts before queuing the next.  Each context first runs the pre-roll
+    # from resident frames; the timed steps continue the same clip in
+    # palindromic order.  Host clock, max over ranks; the median of three
+    # timed blocks (the host shares its cores with other work).
     nunits = B * NSCALES
     e2e_steps = max(args.steps, 100)
     E2E_REPEATS = 3
 
-    def timed_e2e(host_frames, pitch_bytes, location, pipelined):
+    def timed_e2e(host_frames, frame_index, pitch_bytes, location, pipelined):
         bt_ = make(B)
+        preroll(bt_, B, W0)
         stream = torch.cuda.ExternalStream(bt_.cuda_stream(), device=dev)
         ptrs_ = (ctypes.c_void_p * B)()
         pitch_ = (ctypes.c_int64 * B)(*([pitch_bytes] * B))
-        nh = host_frames[0].shape[0]
         outs = [torch.zeros(nunits, dtype=torch.int32).pin_memory() for _ in range(2)]
         evs = [torch.cuda.Event() for _ in range(2)]
         seen = [0]
@@ -390,7 +433,7 @@ def bench_ours(args):
 
         def run(t, k):
             for s_ in range(B):
-                ptrs_[s_] = host_frames[s_][t % nh].data_ptr()
+                ptrs_[s_] = host_frames[s_][frame_index(t)].data_ptr()
             check(lib.gbt_run(bt_._ctx, ptrs_, pitch_, location), bt_._ctx)
             if pipelined:
                 check(lib.gbt_read_counts_async(bt_._ctx, outs[k].data_ptr(), nunits), bt_._ctx)
@@ -407,52 +450,54 @@ def bench_ours(args):
             if pipelined:
                 consume((n - 1) & 1)
 
-        block(0, args.warmup)
         rates = []
         for rep_ in range(E2E_REPEATS):
             if pg:
                 pg.barrier()
             t0 = time.perf_counter()
-            block(args.warmup + rep_ * e2e_steps, e2e_steps)
+            block(rep_ * e2e_steps, e2e_steps)
             el = time.perf_counter() - t0
             if pg:
                 tt = torch.tensor([el], device=dev)
                 pg.all_reduce(tt, op=pg.ReduceOp.MAX)
                 el = float(tt.item())
             rates.append(B * world * e2e_steps / el)
+        live = live_per_stream(bt_, B)
         bt_.close()
-        return sorted(rates)[len(rates) // 2], rates
+        return sorted(rates)[len(rates) // 2], rates, live
 
     host = [torch.from_numpy(f).pin_memory() for f in frames]
-    e2e, e2e_all = timed_e2e(host, COLS, 0, True)
-    e2e_block, _ = timed_e2e(host, COLS, 0, False)
+    gray_index = lambda t: pal(W0 + t, nfr)  # noqa: E731  (continues the clip after the pre-roll)
+    e2e, e2e_all, e2e_live = timed_e2e(host, gray_index, COLS, 0, True)
+    e2e_block, _, _ = timed_e2e(host, gray_index, COLS, 0, False)
     del host
     # RGB frames: 3 bytes per pixel go to the device and the pyramid kernel
-    # makes them gray (channel 0, as the reference's sample).
-    nrgb = min(nfr, 8)
-    host_rgb = [torch.from_numpy(np.ascontiguousarray(np.repeat(frames[s][:nrgb, :, :, None], 3, axis=3))).pin_memory()
-                for s in range(B)]
-    e2e_rgb, _ = timed_e2e(host_rgb, COLS * 3, 2, True)
+    # makes them gray (channel 0, as the reference's sample).  The RGB clip is
+    # the (at most 40) frames that follow the pre-roll, played back and forth.
+    nrgb = max(1, min(40, nfr - W0))
+    host_rgb = [torch.from_numpy(np.ascontiguousarray(np.repeat(frames[s][W0:W0 + nrgb, :, :, None], 3,
+                                                                axis=3))).pin_memory() for s in range(B)]
+    e2e_rgb, _, _ = timed_e2e(host_rgb, lambda t: pal(t, nrgb), COLS * 3, 2, True)
     del host_rgb
 
     extras = {} if args.no_extras else measure_extras(args, dev, local, peak)
 
     cpu = None
     if rank == 0 and not args.no_cpu:
-        fps_cpu, wall_cpu, cores_cpu, _ = run_cpu_streams(B, args.cpu_frames, 2)
+        fps_cpu, wall_cpu, cores_cpu, live_cpu = run_cpu_streams(B, args.cpu_frames, PREROLL)
         cpu = {"value": round(fps_cpu, 3), "unit": UNIT, "cores": cores_cpu, "kind": "port",
                "per_core": round(fps_cpu / cores_cpu, 3), "cpu": cpu_model(),
-               "sample": "%d frames of each of %d 1080p streams (%.1f s wall), one process and core per stream"
-                         % (args.cpu_frames, cores_cpu, wall_cpu)}
+               "live_particles_per_stream": round(live_cpu),
+               "sample": "%d frames of each of %d 1080p streams after %d untimed frames (%.1f s wall), one process "
+                         "and core per stream" % (args.cpu_frames, cores_cpu, PREROLL, wall_cpu)}
 
     if rank == 0:
         line = {
             "metric": METRIC, "value": round(value, 2), "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 4), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "u8", "data": "synthetic",
-            "config": {"workload": "%d streams x 1920x1080 gray, 4 scales, FAST th 20, detector every 10 frames, "
-                                   "filter every frame, CUDA-graph replay" % B,
-                       "streams_per_gpu": B, "stream_groups": ngroups,
+            "config": {"workload": workload_name(B) + ", CUDA-graph replay",
+                       "streams_per_gpu": B, "stream_groups": ngroups, "preroll_frames": PREROLL,
                        "live_particles_per_stream": round(live_mean),
                        "l2": "working set per step > L2 (inputs larger than L2)",
                        "parallelism": "replicas only (independent streams per GPU)"},
@@ -477,12 +522,14 @@ def bench_ours(args):
             "clocks": clocks,
             "e2e_rgb": {"value": round(e2e_rgb, 2), "unit": UNIT, "h2d_bytes_per_step": B * ROWS * COLS * 3,
                         "d2h_bytes_per_step": nunits * 4, "steps": e2e_steps, "repeats": E2E_REPEATS,
-                        "note": "pinned RGB host frames, gray made on the GPU; results read one step behind"},
+                        "note": "pinned RGB host frames (the %d frames after the pre-roll, back and forth), gray "
+                                "made on the GPU; results read one step behind" % nrgb},
             "e2e": {"value": round(e2e, 2), "unit": UNIT, "h2d_bytes_per_step": B * ROWS * COLS,
                     "d2h_bytes_per_step": 4 * nunits, "steps": e2e_steps, "repeats": E2E_REPEATS,
-                    "all": [round(x, 1) for x in e2e_all],
-                    "note": "gbt_run from pinned host frames; each step's per-unit counts read with "
-                            "gbt_read_counts_async while the next step runs",
+                    "all": [round(x, 1) for x in e2e_all], "live_particles_per_stream": round(e2e_live),
+                    "note": "gbt_run from pinned host frames continuing the clip after the pre-roll (palindromic "
+                            "order); each step's per-unit counts read with gbt_read_counts_async while the next "
+                            "step runs",
                     "blocking": round(e2e_block, 2)},
             "cpu_baseline": cpu,
             "tuning": {autotune.KNOBS[int(k)][0]: v for k, v in tuning.items()},
@@ -509,7 +556,8 @@ def _events_ms(fn, reps, stream):
 
 def measure_extras(args, dev, local, peak):
     """The other measured rows: isolated Gaussian (8 B/px), pyramidal LK,
-    the LK/pyramid adjoint, and batched streams of uneven resolution."""
+    the LK/pyramid adjoint, batched streams of uneven resolution and the
+    large combined 4K workload."""
     import numpy as np
     import torch
 
@@ -575,102 +623,208 @@ def measure_extras(args, dev, local, peak):
                                      "pairs_per_s": round(P / ((msf + msb) / 1000), 1)}
     del tape
     del A, Bt, X, A8, B8, U0, x, y
-    # Batched uneven streams: 64 streams drawn from five resolutions.
+    torch.cuda.empty_cache()
+    out["batched_uneven_64"] = measure_uneven(dev, local)
+    out["combined_4k"] = measure_combined_4k(dev)
+    return out
+
+
+def measure_uneven(dev, local, nstreams=64, nf=60, timed=20):
+    """64 streams drawn from five resolutions, 60-frame clips: frames 0..39
+    untimed, 20 timed steps on frames 40..59 (one launch per stage over every
+    stream, graph replay, launch shapes autotuned on the same streams)."""
+    import numpy as np
+    import torch
+
+    from cuimg_gb300 import BatchTracker, autotune
+    from cuimg_gb300._native import check, cuda_lib
+    lib = cuda_lib()
     shapes = [(240, 320, 3), (480, 640, 3), (720, 1280, 4), (1080, 1920, 4), (2160, 3840, 5)]
     rs = np.random.default_rng(4)
-    picks = [shapes[i] for i in rs.integers(0, 5, 64)]
+    picks = [shapes[i] for i in rs.integers(0, 5, nstreams)]
     cfgs = [dict(rows=r, cols=c, nscales=L, detector_threshold=THRESHOLD, detector_frequency=DET_FREQ,
                  filtering_frequency=FILT_FREQ) for r, c, L in picks]
-    nf = 8
-
-    def gen(i):
-        r, c, L = picks[i]
-        return synth.frames(5000 + i, r, c, nf)
-
-    with cf.ThreadPoolExecutor(max_workers=min(16, os.cpu_count() or 4)) as ex:
-        vids = list(ex.map(gen, range(64)))
+    vids = gen_clips([(5000 + i, r, c, nf) for i, (r, c, L) in enumerate(picks)])
     dvid = [torch.from_numpy(v).to(dev) for v in vids]
-    tuning = autotune.tune(cfgs, [[vids[s][t] for s in range(64)] for t in range(nf)], warmup=2, timed=4,
-                           device=local)
+    pre = nf - timed
+    tuning = autotune.tune(cfgs, [[vids[s][t] for s in range(nstreams)] for t in range(pre + 6)], warmup=pre,
+                           timed=6, device=local)
     bt = BatchTracker(cfgs, device=local, graphs=True)
     bt._ensure()
     autotune.apply(bt, tuning)
-    ptrs = (ctypes.c_void_p * 64)()
-    pit = (ctypes.c_int64 * 64)(*[c for r, c, L in picks])
+    ptrs = (ctypes.c_void_p * nstreams)()
+    pit = (ctypes.c_int64 * nstreams)(*[c for r, c, L in picks])
     cst = torch.cuda.ExternalStream(bt.cuda_stream(), device=dev)
 
     def step(t):
-        for s in range(64):
-            ptrs[s] = dvid[s][t % nf].data_ptr()
+        for s in range(nstreams):
+            ptrs[s] = dvid[s][t].data_ptr()
         check(lib.gbt_run(bt._ctx, ptrs, pit, 1), bt._ctx)
 
-    for t in range(3):
+    for t in range(pre):
         step(t)
     bt.sync()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    steps = 5
-    e0.record(cst)
-    for t in range(steps):
-        step(3 + t)
-    e1.record(cst)
-    e1.synchronize()
-    ms = e0.elapsed_time(e1) / steps
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(timed + 1)]
+    ev[0].record(cst)
+    for t in range(timed):
+        step(pre + t)
+        ev[t + 1].record(cst)
+    ev[-1].synchronize()
+    ms = ev[0].elapsed_time(ev[-1]) / timed
     px = sum(r * c for r, c, L in picks)
+    live = sum(int((bt._particles(s, l)["age"] > 0).sum()) for s in range(nstreams) for l in range(picks[s][2]))
     bt.close()
-    del dvid
-    # Large combined workload: one 3840x2160 stream (5 scales) tracked frame by
-    # frame, with the LK residual and its adjoint through the Gaussian pyramid
-    # (fp32, 5 levels, 9x9, 10 steps) on every 10th frame pair, over the
-    # tracker's level-0 particles.
-    H4, W4, n4 = 2160, 3840, 21
-    v4 = synth.frames(7000, H4, W4, n4)
+    return {"streams": nstreams, "ms_per_step": round(ms, 3), "frames_per_s": round(nstreams / (ms / 1000), 1),
+            "mpix_per_s": round(px / (ms / 1000) / 1e6, 1), "live_particles": live,
+            "resolutions": {"%dx%d" % (c, r): sum(1 for p in picks if p[:2] == (r, c)) for r, c, L in shapes},
+            "tuning": {autotune.KNOBS[int(k)][0]: v for k, v in tuning.items()},
+            "note": "%d-frame clips: frames 0..%d untimed, %d timed steps (CUDA events)" % (nf, pre - 1, timed)}
+
+
+def measure_combined_4k(dev, nf=300, every=10):
+    """One 3840x2160 stream (5 scales) tracked for 300 frames, with the LK
+    residual and its adjoint through the Gaussian pyramid (fp32, 5 levels,
+    9x9, 10 steps; pyramids recomputed in the backward pass) on every 10th
+    frame pair, over the level-0 particles alive at that frame.  Tracker
+    frames and adjoint pairs timed with CUDA events."""
+    import numpy as np
+    import torch
+
+    from cuimg_gb300 import BatchTracker, lkd
+    from cuimg_gb300._native import check, cuda_lib
+    lib = cuda_lib()
+    H4, W4 = 2160, 3840
+    v4 = gen_clips([(7000, H4, W4, nf)])[0]
     d4 = torch.from_numpy(v4).to(dev)
+    del v4
     bt4 = BatchTracker([dict(rows=H4, cols=W4, nscales=5, detector_threshold=THRESHOLD,
-                             detector_frequency=DET_FREQ, filtering_frequency=FILT_FREQ)], device=local, graphs=True)
+                             detector_frequency=DET_FREQ, filtering_frequency=FILT_FREQ)], device=dev.index or 0,
+                       graphs=True)
     bt4._ensure()
+    cst = torch.cuda.ExternalStream(bt4.cuda_stream(), device=dev)
+    ts = torch.cuda.current_stream()
     p4 = (ctypes.c_void_p * 1)()
     pit4 = (ctypes.c_int64 * 1)(W4)
-
-    def track4(t):
+    t_trk, t_adj, npairs, npts = 0.0, 0.0, 0, []
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    for t in range(nf):
         p4[0] = d4[t].data_ptr()
+        e0.record(cst)
         check(lib.gbt_run(bt4._ctx, p4, pit4, 1), bt4._ctx)
-
-    for t in range(10):
-        track4(t)
-    bt4.sync()
-    parts = bt4._particles(0, 0)
-    pts4 = torch.from_numpy(parts["pos"][parts["age"] > 0].astype(np.float32)).to(dev)[None]
-    u4 = torch.zeros_like(pts4)
-    ones4 = torch.ones(pts4.shape[:2], device=dev)
-    torch.cuda.synchronize()
-    t_trk, t_adj = 0.0, 0.0
-    for t in range(10, n4):
-        t0 = time.perf_counter()
-        track4(t)
-        bt4.sync()
-        t_trk += time.perf_counter() - t0
-        if t % 10 == 0:
+        e1.record(cst)
+        e1.synchronize()
+        t_trk += e0.elapsed_time(e1)
+        if t > 0 and t % every == 0:
+            parts = bt4._particles(0, 0)  # the points: level-0 particles alive now (read outside the timing)
+            pts = torch.from_numpy(parts["pos"][parts["age"] > 0].astype(np.float32)).to(dev)[None]
+            u0 = torch.zeros_like(pts)
+            ones = torch.ones(pts.shape[:2], device=dev)
             a, b = d4[t - 1].float()[None], d4[t].float()[None]
             torch.cuda.synchronize()
-            t0 = time.perf_counter()
-            tp = lkd.forward(a, b, u4, pts4, 5, 9, 10, tape=True)[2]
-            lkd.backward(a, b, u4, pts4, ones4, 5, 9, 10, tape=tp)
-            torch.cuda.synchronize()
-            t_adj += time.perf_counter() - t0
-    nt = n4 - 10
+            e0.record(ts)
+            tp = lkd.forward(a, b, u0, pts, 5, 9, 10, tape=True)[2]
+            lkd.backward(a, b, u0, pts, ones, 5, 9, 10, tape=tp)
+            e1.record(ts)
+            e1.synchronize()
+            t_adj += e0.elapsed_time(e1)
+            npairs += 1
+            npts.append(int(pts.shape[1]))
+            del tp, a, b
+    live = sum(int((bt4._particles(0, l)["age"] > 0).sum()) for l in range(5))
     bt4.close()
-    out["combined_4k"] = {"frames": nt, "points": int(pts4.shape[1]), "tracker_ms_per_frame": round(1000 * t_trk / nt, 3),
-                          "adjoint_pairs": sum(1 for t in range(10, n4) if t % 10 == 0),
-                          "adjoint_ms_per_pair": round(1000 * t_adj / max(1, sum(1 for t in range(10, n4) if t % 10 == 0)), 2),
-                          "frames_per_s": round(nt / (t_trk + t_adj), 1),
-                          "note": "host clock around synchronised calls; frames 10..20"}
     del d4
-    out["batched_uneven_64"] = {"streams": 64, "ms_per_step": round(ms, 3), "frames_per_s": round(64 / (ms / 1000), 1),
-                                "mpix_per_s": round(px / (ms / 1000) / 1e6, 1),
-                                "resolutions": {"%dx%d" % (c, r): sum(1 for p in picks if p[:2] == (r, c))
-                                                for r, c, L in shapes},
-                                "note": "frames 3..7 of 8 per stream"}
-    return out
+    torch.cuda.empty_cache()
+    return {"frames": nf, "tracker_ms_per_frame": round(t_trk / nf, 4), "adjoint_pairs": npairs,
+            "adjoint_ms_per_pair": round(t_adj / max(1, npairs), 3), "points_per_pair_mean": round(float(np.mean(npts))),
+            "live_particles_final": live, "frames_per_s": round(nf / ((t_trk + t_adj) / 1000), 1),
+            "note": "CUDA events: each tracked frame on the context stream, each adjoint pair (forward with tape + "
+                    "backward) on the torch stream; particle read-back between them untimed"}
+
+
+# --- profiler capture cases -------------------------------------------------
+# Each runs its kernels a few times on inputs larger than L2 but a few GB at
+# most on the device, so a capture of one or two launches ends quickly.
+
+def _case_gaussian(reps=3):
+    """8 fp32 1920x1080 images, sigma 4."""
+    import torch
+
+    from cuimg_gb300 import synth
+    from cuimg_gb300._native import check, cuda_lib
+    lib = cuda_lib()
+    n = 8
+    x = torch.from_numpy(synth.Stream(7, ROWS, COLS).frame_f32(0)).cuda().repeat(n, 1, 1).contiguous()
+    y = torch.empty_like(x)
+    for _ in range(reps):
+        check(lib.gbt_gaussian_f32_batch(x.data_ptr(), COLS * 4, ROWS * COLS * 4, y.data_ptr(), COLS * 4,
+                                         ROWS * COLS * 4, ROWS, COLS, n, ctypes.c_float(4.0), None))
+    torch.cuda.synchronize()
+
+
+def _lk_batch(P=4, n=20000):
+    import numpy as np
+    import torch
+
+    from cuimg_gb300 import synth
+    H, W = 480, 640
+    rng = np.random.default_rng(0)
+    f0 = np.empty((P, H, W), np.float32)
+    f1 = np.empty((P, H, W), np.float32)
+    for p in range(P):
+        s = synth.Stream(300 + p, H, W)
+        f0[p], f1[p] = s.frame_f32(0), s.frame_f32(1)
+    pts = np.stack([rng.uniform(30, H - 30, (P, n)), rng.uniform(30, W - 30, (P, n))], -1).astype(np.float32)
+    u0 = rng.uniform(-2, 2, (P, n, 2)).astype(np.float32)
+    t = lambda a: torch.from_numpy(a).cuda()  # noqa: E731
+    return t(f0), t(f1), t(pts), t(u0)
+
+
+def _case_lk(reps=3):
+    """4 fp32 640x480 pairs, 5 levels, 9x9, 10 steps, 20k points each."""
+    import torch
+
+    from cuimg_gb300 import lk
+    A, B, X, _ = _lk_batch()
+    prm = lk.params(window=9, npix=81, max_iter=10)
+    for _ in range(reps):
+        lk.track(A, B, X, nlevels=5, prm=prm)
+    torch.cuda.synchronize()
+
+
+def _case_adjoint(reps=2):
+    """LK residual forward (tape) + backward on the same batch."""
+    import torch
+
+    from cuimg_gb300 import lkd
+    A, B, X, U = _lk_batch()
+    ones = torch.ones(X.shape[:2], device="cuda")
+    for _ in range(reps):
+        tape = lkd.forward(A, B, U, X, 5, 9, 10, tape=True)[2]
+        lkd.backward(A, B, U, X, ones, 5, 9, 10, tape=tape)
+    torch.cuda.synchronize()
+
+
+def _case_tracker(nstreams, frames, det_freq, blur_rows=None):
+    from cuimg_gb300 import BatchTracker
+    cfg = [dict(rows=ROWS, cols=COLS, nscales=NSCALES, detector_threshold=THRESHOLD, detector_frequency=det_freq)]
+    vids = gen_streams(nstreams, frames)
+    bt = BatchTracker(cfg * nstreams, graphs=False, groups=1)  # one launch per stage over every stream
+    if blur_rows:
+        bt.set_tuning(1, blur_rows)
+    for t in range(frames):
+        bt.run([v[t] for v in vids])
+    bt.sync()
+    bt.close()
+
+
+PROFILE_CASES = {
+    "gaussian": _case_gaussian,
+    "lk": _case_lk,
+    "adjoint": _case_adjoint,
+    "tracker": lambda: _case_tracker(4, 6, 10),        # 4 streams of 1920x1080, 6 frames
+    "tracker_det": lambda: _case_tracker(4, 8, 3),     # the same with the detector every third frame
+    "tracker16": lambda: _case_tracker(16, 4, 10, 32),  # 16 streams in one group, 32-row blur strips
+}
 
 
 def main():
@@ -683,8 +837,16 @@ def main():
     ap.add_argument("--cpu-frames", type=int, default=12)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--matcher", type=int, default=-1, help="matcher variant (default: autotuned)")
-    ap.add_argument("--no-extras", action="store_true", help="skip the Gaussian / LK / adjoint / uneven-batch lines")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="skip the Gaussian / LK / adjoint / uneven-batch / 4K lines")
+    ap.add_argument("--profile-case", nargs="+", choices=sorted(PROFILE_CASES),
+                    help="run these small cases for a profiler capture and exit")
     args = ap.parse_args()
+    if args.profile_case:
+        for name in args.profile_case:
+            PROFILE_CASES[name]()
+        print("ok")
+        return
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":
