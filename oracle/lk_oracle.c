@@ -24,6 +24,7 @@
  * sigma-1 Gaussian fp32 pyramid with an fp32 template.
  */
 #include <math.h>
+#include <stdint.h>
 #include <stdlib.h>
 #include <string.h>
 
@@ -429,4 +430,369 @@ int oracle_lk_track(const float* prev, const float* cur, int H, int W, int L, in
   }
   free(k.lv);
   return 0;
+}
+
+/* ===========================================================================
+ * The reference's pyramidal LK tracker strategy over frames:
+ * tracker<pyrlk_cpu<fast_detector<cpu>, iterative_lk_match_5x5>>
+ * (cuimg/tracking2/pyrlk_tracker.h:16-82, pyrlk_tracker.hpp:772-1063), which
+ * the reference never instantiates.  Per frame and scale, coarsest first
+ * (tracker.hpp:83-91), pyrlk_cpu::update (:833-875):
+ *   - prev_input_ = the previous frame's input_ (the first frame: the frame);
+ *     input_ = a fresh copy of the tracker's level (see below);
+ *   - frames > 0: match_particles (:902-971): the sparse index emptied, the
+ *     Sobel/8 gradient of prev_input_, then pyrlk_match_particles_kernel
+ *     (:677-769) over the slots in index order: the prediction through the
+ *     upper scale's get_flow_at (:1027-1063; the top scale uses the motion
+ *     prediction, predictions.h:61-74), the LK match, the acceptance and
+ *     kernel_particle_container::move (particle_container.hpp:422-466);
+ *   - detector frames: create_detector_mask (:878-887: every slot's position
+ *     and its 8 neighbours, dead slots included), the FAST saliency
+ *     (fast_detector.hpp:296-313), new_particles (:217-262) and compact
+ *     (particle_container.hpp:215-252);
+ *   - filtering frames: filter_bad_particles_kernel (tracking_strategies.hpp:
+ *     482-523), which never removes a particle here because the strategy's
+ *     multiscale_count_ image stays zero (it is only ever memset), then
+ *     merge_trajectories (merge_trajectories.h:10-35) in index order.
+ * input_ is `host_image2d(in.domain(), in.border())` filled by
+ * copy(in, input_), which for equal borders copies nrows * pitch bytes from
+ * the start of the allocation (cuimg/copy.h:30-40, host_image2d.hpp:76-110):
+ * the top border rows and the domain rows 0 .. H - 1 - b come over (b = 3,
+ * the FAST detector's border, pyrlk_tracker.hpp:822-827); rows H - b .. H - 1
+ * and the bottom border stay zero.  The LK and the detector read that image.
+ * Window samples outside the domain are clamped to the edge (undefined in the
+ * reference), as in the LK restatement above.
+ * ======================================================================== */
+uint8_t oracle_fast_saliency_at(const uint8_t* p00, int pitch, int r, int c, int n_, int th);
+
+#define PK_B 3 /* the tracker input's border: fast_detector::border_needed() */
+#define PK_MB 4 /* the detector mask's border */
+static const int PK_C8[8][2] = {{-1, 1}, {0, 1}, {1, 1}, {-1, 0}, {1, 0}, {-1, -1}, {0, -1}, {1, -1}};
+
+typedef struct {
+  int H, W, ipitch;      /* ipitch: input_'s row pitch ((W + 2b) rounded up to 4 bytes) */
+  uint8_t* lvl;          /* the tracker's level (H x W) */
+  uint8_t* inb;          /* input_: (H + 2b) rows of ipitch bytes */
+  float *cur, *prev, *gr, *gc; /* H x W */
+  uint8_t* mask;         /* (H + 2 PK_MB) x (W + 2 PK_MB) */
+  uint8_t* sal;          /* H x W */
+  uint8_t* newpts;       /* H x W */
+  uint32_t* sparse;      /* H x W, 0xFFFFFFFF = none */
+  int n, cap, nmatches, compact_has_run, frame_cpt;
+  float *pos, *speed;    /* 2 per slot */
+  uint16_t* age;
+  int32_t* matches;
+  int threshold, n_fast, det_freq, filt_freq, k, with_merge;
+} pk_level;
+
+typedef struct {
+  int L;
+  pk_level* lv;
+  lk_level* lkl; /* the LK's view of every scale (prev, cur, gradient) */
+  lk_ctx lk;
+} pk_tracker;
+
+static int pk_reserve(pk_level* l, int n) {
+  if (n <= l->cap) return 0;
+  int cap = l->cap ? l->cap : 1024;
+  while (cap < n) cap *= 2;
+  float* p = (float*)realloc(l->pos, sizeof(float) * 2 * cap);
+  float* sp = (float*)realloc(l->speed, sizeof(float) * 2 * cap);
+  uint16_t* a = (uint16_t*)realloc(l->age, sizeof(uint16_t) * cap);
+  int32_t* m = (int32_t*)realloc(l->matches, sizeof(int32_t) * cap);
+  if (!p || !sp || !a || !m) return -1;
+  l->pos = p;
+  l->speed = sp;
+  l->age = a;
+  l->matches = m;
+  l->cap = cap;
+  return 0;
+}
+
+void* oracle_pyrlk_create(int rows, int cols, int nscales, int threshold, int det_freq, int filt_freq) {
+  if (nscales < 1 || nscales > 9 || det_freq < 1 || filt_freq < 1) return NULL;
+  pk_tracker* t = (pk_tracker*)calloc(1, sizeof(pk_tracker));
+  t->L = nscales;
+  t->lv = (pk_level*)calloc(nscales, sizeof(pk_level));
+  t->lkl = (lk_level*)calloc(nscales, sizeof(lk_level));
+  int H = rows, W = cols;
+  for (int s = 0; s < nscales; s++) {
+    pk_level* l = &t->lv[s];
+    if (H < 16 || W < 16) return NULL;
+    l->H = H;
+    l->W = W;
+    l->ipitch = (W + 2 * PK_B + 3) / 4 * 4;
+    size_t np = (size_t)H * W;
+    l->lvl = (uint8_t*)calloc(np, 1);
+    l->inb = (uint8_t*)calloc((size_t)(H + 2 * PK_B) * l->ipitch, 1);
+    l->cur = (float*)calloc(np, 4);
+    l->prev = (float*)calloc(np, 4);
+    l->gr = (float*)calloc(np, 4);
+    l->gc = (float*)calloc(np, 4);
+    l->mask = (uint8_t*)calloc((size_t)(H + 2 * PK_MB) * (W + 2 * PK_MB), 1);
+    l->sal = (uint8_t*)calloc(np, 1);
+    l->newpts = (uint8_t*)calloc(np, 1);
+    l->sparse = (uint32_t*)malloc(np * 4);
+    memset(l->sparse, 0xFF, np * 4);
+    l->threshold = threshold;
+    l->n_fast = 9;
+    l->det_freq = det_freq;
+    l->filt_freq = filt_freq;
+    l->k = 300;
+    l->with_merge = 1;
+    t->lkl[s].H = H;
+    t->lkl[s].W = W;
+    t->lkl[s].prev = l->prev;
+    t->lkl[s].cur = l->cur;
+    t->lkl[s].gr = l->gr;
+    t->lkl[s].gc = l->gc;
+    H /= 2;
+    W /= 2;
+  }
+  lk_ctx k = {nscales, 11, 25, 30, 1, 0.1f, 300.f, t->lkl};
+  t->lk = k;
+  return t;
+}
+
+void oracle_pyrlk_destroy(void* h) {
+  pk_tracker* t = (pk_tracker*)h;
+  if (!t) return;
+  for (int s = 0; s < t->L; s++) {
+    pk_level* l = &t->lv[s];
+    free(l->lvl);
+    free(l->inb);
+    free(l->cur);
+    free(l->prev);
+    free(l->gr);
+    free(l->gc);
+    free(l->mask);
+    free(l->sal);
+    free(l->newpts);
+    free(l->sparse);
+    free(l->pos);
+    free(l->speed);
+    free(l->age);
+    free(l->matches);
+  }
+  free(t->lv);
+  free(t->lkl);
+  free(t);
+}
+
+/* Settings of scale s (every scale when s < 0), keys as oracle_set_param:
+ * 0 threshold, 1 n, 2 detector frequency, 3 filtering frequency, 4 k,
+ * 5 with_merge. */
+int oracle_pyrlk_set_param(void* h, int s, int key, int value) {
+  pk_tracker* t = (pk_tracker*)h;
+  if (s >= t->L) return -1;
+  for (int i = s < 0 ? 0 : s; i < (s < 0 ? t->L : s + 1); i++) {
+    pk_level* l = &t->lv[i];
+    switch (key) {
+      case 0: l->threshold = value; break;
+      case 1: l->n_fast = value; break;
+      case 2: l->det_freq = value; break;
+      case 3: l->filt_freq = value; break;
+      case 4: l->k = value; break;
+      case 5: l->with_merge = value; break;
+      default: return -1;
+    }
+  }
+  return 0;
+}
+
+#define PK_IN(l, r, c) ((l)->inb[(size_t)((r) + PK_B) * (l)->ipitch + ((c) + PK_B)])
+#define PK_MASK(l, r, c) ((l)->mask[(size_t)((r) + PK_MB) * ((l)->W + 2 * PK_MB) + ((c) + PK_MB)])
+
+/* input_ of a scale from the tracker's level (see the header above). */
+static void pk_make_input(pk_level* l) {
+  const int H = l->H, W = l->W, b = PK_B;
+  memset(l->inb, 0, (size_t)(H + 2 * b) * l->ipitch);
+  for (int r = -b; r < H - b; r++) /* the copied rows: bordered rows -b .. H - b - 1 */
+    for (int c = -b; c < W + b; c++) {
+      int rr = r < 0 ? 0 : r, cc = c < 0 ? 0 : (c > W - 1 ? W - 1 : c);
+      PK_IN(l, r, c) = l->lvl[(size_t)rr * W + cc];
+    }
+}
+
+static void pk_match(pk_tracker* t, int s) {
+  pk_level* l = &t->lv[s];
+  const int H = l->H, W = l->W;
+  memset(l->sparse, 0xFF, (size_t)H * W * 4);
+  l->compact_has_run = 0;
+  sobel8(l->prev, H, W, l->gr, l->gc);
+  lk_ctx k = t->lk;
+  k.kerr = (float)l->k;
+  for (int i = 0; i < l->n; i++) {
+    float p[2] = {l->pos[2 * i], l->pos[2 * i + 1]};
+    if (l->age[i] == 0 || !box_has(H, W, 3, p[0], p[1])) {
+      l->age[i] = 0;
+      continue;
+    }
+    float pred_tr[2] = {0.f, 0.f};
+    if (s + 1 < t->L) {
+      float q[2] = {p[0] / 2.f, p[1] / 2.f}, u[2];
+      flow_at(&k, s + 1, q, u);
+      pred_tr[0] = 2.f * u[0];
+      pred_tr[1] = 2.f * u[1];
+    } else if (l->age[i] != 1) {
+      pred_tr[0] = l->speed[2 * i];
+      pred_tr[1] = l->speed[2 * i + 1];
+    }
+    float pred[2] = {p[0] + pred_tr[0], p[1] + pred_tr[1]};
+    if (!box_has(H, W, 3, pred[0], pred[1])) {
+      l->age[i] = 0;
+      continue;
+    }
+    float tr[2], e;
+    lk_match(&k, &t->lkl[s], p, pred_tr, tr, &e);
+    float m0 = (float)(int)(p[0] + tr[0]), m1 = (float)(int)(p[1] + tr[1]);
+    float d0 = m0 - pred[0], d1 = m1 - pred[1];
+    if (box_has(H, W, 3, p[0] + tr[0], p[1] + tr[1]) && e < (float)l->k && sqrtf(d0 * d0 + d1 * d1) < 160.f) {
+      l->age[i]++;
+      l->speed[2 * i] = tr[0];
+      l->speed[2 * i + 1] = tr[1];
+      l->pos[2 * i] = p[0] + tr[0];
+      l->pos[2 * i + 1] = p[1] + tr[1];
+      l->sparse[(size_t)(int)l->pos[2 * i] * W + (int)l->pos[2 * i + 1]] = (uint32_t)i;
+    } else {
+      l->age[i] = 0;
+    }
+  }
+}
+
+static int pk_detect_and_compact(pk_level* l) {
+  const int H = l->H, W = l->W;
+  memset(l->mask, 255, (size_t)(H + 2 * PK_MB) * (W + 2 * PK_MB));
+  for (int i = 0; i < l->n; i++) { /* every slot, dead ones included */
+    int pr = (int)l->pos[2 * i], pc = (int)l->pos[2 * i + 1];
+    PK_MASK(l, pr, pc) = 0;
+    for (int k = 0; k < 8; k++) PK_MASK(l, pr + PK_C8[k][0], pc + PK_C8[k][1]) = 0;
+  }
+  memset(l->sal, 0, (size_t)H * W);
+  for (int r = 0; r < H; r++)
+    for (int c = 0; c < W; c++)
+      if (PK_MASK(l, r, c) != 0)
+        l->sal[(size_t)r * W + c] = oracle_fast_saliency_at(&PK_IN(l, 0, 0), l->ipitch, r, c, l->n_fast, l->threshold);
+  memset(l->newpts, 0, (size_t)H * W);
+  for (int tr = 0; tr < H / 3; tr++)
+    for (int tc = 0; tc < W / 3; tc++) {
+      int pr = tr * 3 + 1, pc = tc * 3 + 1, skip = 0;
+      for (int r = 0; r < 3 && !skip; r++)
+        for (int c = 0; c < 3; c++)
+          if (pr + r < H && pc + c < W && l->sparse[(size_t)(pr + r) * W + pc + c] != 0xFFFFFFFFu) {
+            skip = 1;
+            break;
+          }
+      if (skip) continue;
+      float vmax = l->sal[(size_t)pr * W + pc];
+      int mr = pr, mc = pc;
+      for (int r = 0; r < 3; r++)
+        for (int c = 0; c < 3; c++)
+          if (pr + r < H && pc + c < W) {
+            float v = l->sal[(size_t)(pr + r) * W + pc + c];
+            if (vmax < v) {
+              vmax = v;
+              mr = pr + r;
+              mc = pc + c;
+            }
+          }
+      if (vmax < (float)l->threshold) continue;
+      l->newpts[(size_t)mr * W + mc] = 1;
+    }
+  for (int r = 3; r <= H - 4; r++)
+    for (int c = 3; c <= W - 4; c++)
+      if (l->newpts[(size_t)r * W + c]) {
+        if (pk_reserve(l, l->n + 1)) return -1;
+        int i = l->n++;
+        l->age[i] = 1;
+        l->speed[2 * i] = l->speed[2 * i + 1] = 0.f;
+        l->pos[2 * i] = (float)r;
+        l->pos[2 * i + 1] = (float)c;
+        l->sparse[(size_t)r * W + c] = (uint32_t)i;
+      }
+  l->compact_has_run = 1;
+  l->nmatches = l->n;
+  int o = 0;
+  for (int i = 0; i < l->n; i++) {
+    l->matches[i] = -1;
+    if (l->age[i] == 0) continue;
+    l->age[o] = l->age[i];
+    l->speed[2 * o] = l->speed[2 * i];
+    l->speed[2 * o + 1] = l->speed[2 * i + 1];
+    l->pos[2 * o] = l->pos[2 * i];
+    l->pos[2 * o + 1] = l->pos[2 * i + 1];
+    l->sparse[(size_t)(int)l->pos[2 * o] * W + (int)l->pos[2 * o + 1]] = (uint32_t)o;
+    l->matches[i] = o;
+    o++;
+  }
+  l->n = o;
+  return 0;
+}
+
+static void pk_merge(pk_level* l) {
+  const int W = l->W;
+  for (int i = 0; i < l->n; i++) {
+    if (l->age[i] == 0) continue;
+    int pr = (int)l->pos[2 * i], pc = (int)l->pos[2 * i + 1];
+    for (int k = 0; k < 8; k++) {
+      uint32_t j = l->sparse[(size_t)(pr + PK_C8[k][0]) * W + (pc + PK_C8[k][1])];
+      if (j == 0xFFFFFFFFu) continue;
+      float dx = l->speed[2 * i] - l->speed[2 * j], dy = l->speed[2 * i + 1] - l->speed[2 * j + 1];
+      if ((int)l->age[j] > (int)l->age[i] + 2 && sqrtf(dx * dx + dy * dy) < 2.f) {
+        l->age[j] = 0;
+        break;
+      }
+    }
+  }
+}
+
+int oracle_pyrlk_run(void* h, const uint8_t* frame) {
+  pk_tracker* t = (pk_tracker*)h;
+  memcpy(t->lv[0].lvl, frame, (size_t)t->lv[0].H * t->lv[0].W);
+  for (int s = 1; s < t->L; s++) { /* tracker::subsample_input: 2x2 floor means of the level below */
+    pk_level *a = &t->lv[s - 1], *o = &t->lv[s];
+    for (int r = 0; r < o->H; r++)
+      for (int c = 0; c < o->W; c++) {
+        int v = a->lvl[(size_t)(2 * r) * a->W + 2 * c] + a->lvl[(size_t)(2 * r) * a->W + 2 * c + 1] +
+                a->lvl[(size_t)(2 * r + 1) * a->W + 2 * c] + a->lvl[(size_t)(2 * r + 1) * a->W + 2 * c + 1];
+        o->lvl[(size_t)r * o->W + c] = (uint8_t)(v / 4);
+      }
+  }
+  for (int s = t->L - 1; s >= 0; s--) {
+    pk_level* l = &t->lv[s];
+    const size_t np = (size_t)l->H * l->W;
+    if (l->frame_cpt > 0)
+      memcpy(l->prev, l->cur, np * 4); /* copy(input_, prev_input_) before input_ is replaced */
+    else
+      for (size_t i = 0; i < np; i++) l->prev[i] = (float)l->lvl[i];
+    pk_make_input(l);
+    for (int r = 0; r < l->H; r++)
+      for (int c = 0; c < l->W; c++) l->cur[(size_t)r * l->W + c] = (float)PK_IN(l, r, c);
+    if (l->frame_cpt > 0) pk_match(t, s);
+    if (!(l->frame_cpt % l->det_freq))
+      if (pk_detect_and_compact(l)) return -1;
+    if (!(l->frame_cpt % l->filt_freq) && l->with_merge) pk_merge(l);
+    l->frame_cpt++;
+  }
+  return 0;
+}
+
+int oracle_pyrlk_nparticles(void* h, int s) { return ((pk_tracker*)h)->lv[s].n; }
+
+/* Particle state of scale s: pos and speed (2 floats each), age; matches of
+ * the last compaction (*nmatches of them) and whether this frame compacted. */
+void oracle_pyrlk_get(void* h, int s, float* pos, float* speed, uint16_t* age, int32_t* matches, int* nmatches,
+                      int* compact_has_run) {
+  pk_level* l = &((pk_tracker*)h)->lv[s];
+  if (pos) memcpy(pos, l->pos, (size_t)l->n * 8);
+  if (speed) memcpy(speed, l->speed, (size_t)l->n * 8);
+  if (age) memcpy(age, l->age, (size_t)l->n * 2);
+  if (nmatches) *nmatches = l->nmatches;
+  if (matches) memcpy(matches, l->matches, (size_t)l->nmatches * 4);
+  if (compact_has_run) *compact_has_run = l->compact_has_run;
+}
+
+void oracle_pyrlk_get_sparse(void* h, int s, uint32_t* out) {
+  pk_level* l = &((pk_tracker*)h)->lv[s];
+  memcpy(out, l->sparse, (size_t)l->H * l->W * 4);
 }

@@ -317,6 +317,53 @@ void reflk_get(void* h, int scale, float* pos, uint16_t* age) {
   }
 }
 
+// The LK tracker as the sample would run it: detector every `det_freq`
+// frames, filtering (and merging, when `with_merge`) every `filt_freq`.
+void* reflk_create_full(int rows, int cols, int nscales, int threshold, int det_freq, int filt_freq, int with_merge) {
+  reflk_ctx* c = new reflk_ctx;
+  c->dom = obox2d(rows, cols);
+  c->tr = new LKT(c->dom, nscales);
+  c->tr->strategy().set_detector_frequency(det_freq);
+  c->tr->strategy().set_filtering_frequency(filt_freq);
+  for (int s = 0; s < nscales; s++) {
+    c->tr->scale(s).strategy().set_with_merge(with_merge != 0);
+    c->tr->scale(s).strategy().detector().set_n(9).set_fast_threshold(threshold);
+  }
+  return c;
+}
+
+// Full particle state of a scale: pos, speed (2 floats each), age, the last
+// compaction's matches and whether this frame compacted.
+void reflk_get_full(void* h, int scale, float* pos, float* speed, uint16_t* age, int32_t* matches, int* nmatches,
+                    int* compact_has_run) {
+  reflk_ctx* c = (reflk_ctx*)h;
+  auto& ps = c->tr->scale(scale).pset();
+  const auto& P = ps.dense_particles();
+  for (size_t i = 0; i < P.size(); i++) {
+    if (pos) {
+      pos[2 * i] = P[i].pos.x;
+      pos[2 * i + 1] = P[i].pos.y;
+    }
+    if (speed) {
+      speed[2 * i] = P[i].speed.x;
+      speed[2 * i + 1] = P[i].speed.y;
+    }
+    if (age) age[i] = P[i].age;
+  }
+  const auto& M = ps.matches();
+  *nmatches = (int)M.size();
+  if (matches)
+    for (size_t i = 0; i < M.size(); i++) matches[i] = (int32_t)M[i];
+  *compact_has_run = ps.compact_has_run();
+}
+
+void reflk_get_sparse(void* h, int scale, uint32_t* out) {
+  reflk_ctx* c = (reflk_ctx*)h;
+  const auto& sp = c->tr->scale(scale).pset().sparse_particles();
+  for (int r = 0; r < sp.nrows(); r++)
+    for (int cc = 0; cc < sp.ncols(); cc++) out[(size_t)r * sp.ncols() + cc] = sp(r, cc);
+}
+
 }  // extern "C"
 
 // ---------------------------------------------------------------------------

@@ -22,6 +22,7 @@
  * same for any thread count.
  */
 #include <math.h>
+#include <stddef.h>
 #include <stdint.h>
 #include <stdlib.h>
 #include <string.h>
@@ -406,13 +407,15 @@ static void match_particles(otracker* t, int s) {
   }
 }
 
-/* fast::compute_saliency (fast_detector.hpp:26-157). */
-static uint8_t fast_saliency(const olevel* l, int r, int c, int n_, int th) {
+/* fast::compute_saliency (fast_detector.hpp:26-157) at pixel (r, c) of an
+ * image whose pixel (0, 0) is at `p00`, rows `pitch` bytes apart, with at
+ * least 3 pixels of border on every side. */
+uint8_t oracle_fast_saliency_at(const uint8_t* p00, int pitch, int r, int c, int n_, int th) {
   unsigned max_n = 0, n = 0;
   int status = 2;
-  int vp = AT(l->in, l->pin, 6, r, c);
+  int vp = p00[(ptrdiff_t)r * pitch + c];
   unsigned sum_bright = 0, sum_dark = 0;
-#define RV(i) ((int)AT(l->in, l->pin, 6, r + RING[i][0], c + RING[i][1]))
+#define RV(i) ((int)p00[(ptrdiff_t)(r + RING[i][0]) * pitch + (c + RING[i][1])])
   if (n_ >= 9) {
     static const int to_test[6] = {0, 4, 8, 12, 0, 4};
     int equals = 0;
@@ -476,6 +479,10 @@ static uint8_t fast_saliency(const olevel* l, int r, int c, int n_, int th) {
   if (n > max_n) max_n = n;
   if (max_n < (unsigned)n_) return 0;
   return (uint8_t)(sum_bright > sum_dark ? sum_bright : sum_dark);
+}
+
+static uint8_t fast_saliency(const olevel* l, int r, int c, int n_, int th) {
+  return oracle_fast_saliency_at(&AT(l->in, l->pin, 6, 0, 0), l->pin, r, c, n_, th);
 }
 
 /* create_detector_mask (tracking_strategies.hpp:254-272), detector update

@@ -191,3 +191,99 @@ def lkd_grad_fd64(I0, I1, pts, u0, L, window, iters, wts, h=1e-3):
     lib.oracle_lkd_grad_fd(a.ctypes.data, b.ctypes.data, H, W, L, window, iters, p.ctypes.data, u.ctypes.data,
                            len(p), w.ctypes.data, h, g0.ctypes.data, g1.ctypes.data, gu.ctypes.data)
     return g0, g1, gu
+
+
+class PyrlkLib:
+    """The pyramidal LK tracker strategy (pyrlk_cpu<fast_detector<cpu>,
+    iterative_lk_match_5x5>) from the oracle (prefix oracle_pyrlk_) or the
+    reference built from its own sources (reflk_)."""
+
+    def __init__(self, which, rows, cols, nscales, threshold=20, det_freq=10, filt_freq=1, with_merge=1):
+        self.L = nscales
+        self.dims = [(rows >> s, cols >> s) for s in range(nscales)]
+        P, I = ctypes.c_void_p, ctypes.c_int
+        if which == "oracle":
+            lib = oracle()
+            lib.oracle_pyrlk_create.restype = P
+            lib.oracle_pyrlk_create.argtypes = [I] * 6
+            lib.oracle_pyrlk_run.argtypes = [P, P]
+            lib.oracle_pyrlk_nparticles.argtypes = [P, I]
+            lib.oracle_pyrlk_get.argtypes = [P, I] + [P] * 6
+            lib.oracle_pyrlk_get_sparse.argtypes = [P, I, P]
+            lib.oracle_pyrlk_destroy.argtypes = [P]
+            lib.oracle_pyrlk_set_param.argtypes = [P, I, I, I]
+            self.h = lib.oracle_pyrlk_create(rows, cols, nscales, threshold, det_freq, filt_freq)
+            if not with_merge:
+                lib.oracle_pyrlk_set_param(self.h, -1, 5, 0)
+            self._run, self._n, self._get = lib.oracle_pyrlk_run, lib.oracle_pyrlk_nparticles, lib.oracle_pyrlk_get
+            self._sparse, self._destroy = lib.oracle_pyrlk_get_sparse, lib.oracle_pyrlk_destroy
+            self.set_param = lambda s, key, value: lib.oracle_pyrlk_set_param(self.h, s, key, value)
+        else:
+            lib = ctypes.CDLL(REF)
+            lib.reflk_create_full.restype = P
+            lib.reflk_create_full.argtypes = [I] * 7
+            lib.reflk_run.argtypes = [P, P]
+            lib.reflk_nparticles.argtypes = [P, I]
+            lib.reflk_get_full.argtypes = [P, I] + [P] * 6
+            lib.reflk_get_sparse.argtypes = [P, I, P]
+            lib.reflk_destroy.argtypes = [P]
+            self.h = lib.reflk_create_full(rows, cols, nscales, threshold, det_freq, filt_freq, with_merge)
+            self._run, self._n, self._get = lib.reflk_run, lib.reflk_nparticles, lib.reflk_get_full
+            self._sparse, self._destroy = lib.reflk_get_sparse, lib.reflk_destroy
+
+    def run(self, frame):
+        f = np.ascontiguousarray(frame, np.uint8)
+        self._run(self.h, f.ctypes.data)
+
+    def particles(self, s):
+        n = self._n(self.h, s)
+        pos = np.zeros((n, 2), np.float32)
+        speed = np.zeros((n, 2), np.float32)
+        age = np.zeros(n, np.uint16)
+        nm, comp = ctypes.c_int(), ctypes.c_int()
+        self._get(self.h, s, None, None, None, None, ctypes.byref(nm), ctypes.byref(comp))
+        matches = np.zeros(max(nm.value, 1), np.int32)
+        self._get(self.h, s, pos.ctypes.data, speed.ctypes.data, age.ctypes.data, matches.ctypes.data,
+                  ctypes.byref(nm), ctypes.byref(comp))
+        return dict(pos=pos, speed=speed, age=age, matches=matches[: nm.value], compact=bool(comp.value))
+
+    def sparse(self, s):
+        H, W = self.dims[s]
+        out = np.zeros((H, W), np.uint32)
+        self._sparse(self.h, s, out.ctypes.data)
+        return out
+
+    def destroy(self):
+        if self.h:
+            self._destroy(self.h)
+            self.h = None
+
+
+def black_margin_frames(seed, rows, cols, n, margin):
+    """Seeded synthetic frames with a black margin of `margin` pixels on every
+    side: the LK windows of every particle then stay inside the image at every
+    scale (the reference reads outside its images otherwise)."""
+    from cuimg_gb300 import synth
+    f = synth.frames(seed, rows, cols, n)
+    f[:, :margin] = 0
+    f[:, rows - margin:] = 0
+    f[:, :, :margin] = 0
+    f[:, :, cols - margin:] = 0
+    return f
+
+
+def diff_pyrlk(a, b, L, with_sparse=True):
+    """Names of what differs between two PyrlkLib-like states (empty = equal)."""
+    bad = []
+    for s in range(L):
+        x, y = a.particles(s), b.particles(s)
+        for k in ("pos", "speed", "age"):
+            if x[k].shape != y[k].shape or not np.array_equal(x[k], y[k]):
+                bad.append("scale %d %s" % (s, k))
+        if x["compact"] != y["compact"]:
+            bad.append("scale %d compact" % s)
+        elif x["compact"] and not np.array_equal(x["matches"], y["matches"]):
+            bad.append("scale %d matches" % s)
+        if with_sparse and not np.array_equal(a.sparse(s), b.sparse(s)):
+            bad.append("scale %d sparse" % s)
+    return bad

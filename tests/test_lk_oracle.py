@@ -93,3 +93,32 @@ def test_lk_oracle_matches_reference_live(rows, cols, L, seed):
         np.testing.assert_array_equal(st[inner] > 0, ref_age[inner] > 0)
         both = inner & (st > 0)
         np.testing.assert_array_equal(out[both], ref_pos[both], err_msg="scale %d" % s)
+
+
+@pytest.mark.skipif(not reference_available(), reason="reference not built here (oracle/_ref)")
+@pytest.mark.parametrize("rows,cols,L,det,filt,merge,seed,n", [
+    (320, 480, 3, 3, 1, 1, 5, 16),
+    (256, 384, 2, 1, 1, 1, 6, 10),
+    (480, 640, 3, 10, 2, 1, 7, 22),
+    (300, 420, 3, 4, 1, 0, 8, 12),
+])
+def test_pyrlk_tracker_oracle_matches_reference_live(rows, cols, L, det, filt, merge, seed, n):
+    # The whole LK tracker strategy over frames (pyrlk_cpu: LK matching with
+    # the coarse-to-fine prediction, FAST births, compaction, merge) against
+    # the reference's own, on frames with a black margin wide enough that no
+    # window ever reads outside an image at any scale (which the reference
+    # leaves undefined): every particle's position, speed and age, the
+    # compaction map and the sparse index equal on every frame and scale.
+    from oracle_lib import PyrlkLib, black_margin_frames, diff_pyrlk
+    frames = black_margin_frames(seed, rows, cols, n, 16 << (L - 1))
+    o = PyrlkLib("oracle", rows, cols, L, 20, det, filt, merge)
+    r = PyrlkLib("ref", rows, cols, L, 20, det, filt, merge)
+    for t in range(n):
+        o.run(frames[t])
+        r.run(frames[t])
+        bad = diff_pyrlk(o, r, L)
+        assert not bad, "frame %d: %s" % (t, bad)
+    live = [int((o.particles(s)["age"] > 0).sum()) for s in range(L)]
+    assert live[0] > 500
+    o.destroy()
+    r.destroy()
