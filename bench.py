@@ -168,8 +168,10 @@ def cpu_model():
 
 def _cpu_stream_worker(i, preroll, nframes, barrier, out):
     """One stream of the CPU tracker (oracle port, one thread) in its own
-    process: `preroll` frames untimed, then `nframes` timed between barriers
-    shared by all streams; reports the live particles (age > 0) afterwards."""
+    process: `preroll` frames untimed, then `nframes` timed frames, started
+    together by a barrier shared by all streams.  Reports the time spent in
+    the timed frames' tracker calls and the live particles (age > 0, summed
+    over the scales) averaged over those frames, counted between the calls."""
     os.environ["OMP_NUM_THREADS"] = "1"
     sys.path.insert(0, ROOT)
     sys.path.insert(0, os.path.join(ROOT, "tests"))
@@ -182,21 +184,23 @@ def _cpu_stream_worker(i, preroll, nframes, barrier, out):
     for t in range(preroll):
         o.run(frames[t])
     barrier.wait()
-    t0 = time.perf_counter()
+    dt, live = 0.0, []
     for t in range(preroll, preroll + nframes):
+        t0 = time.perf_counter()
         o.run(frames[t])
-    dt = time.perf_counter() - t0
+        dt += time.perf_counter() - t0
+        live.append(sum(int((o.particles(s)["age"] > 0).sum()) for s in range(NSCALES)))
     barrier.wait()
-    live = sum(int((o.particles(s)["age"] > 0).sum()) for s in range(NSCALES))
-    out.put((i, dt, live))
+    out.put((i, dt, float(np.mean(live))))
     o.destroy()
 
 
 def run_cpu_streams(nstreams, steps, preroll):
     """The CPU tracker on `nstreams` 1080p streams at once, one process and
     one core per stream (the streams are independent, as on the GPU); returns
-    frames/s over all streams, the wall time of the timed frames, the cores
-    used and the mean live particles (age > 0) per stream."""
+    frames/s over all streams, the time of the timed frames (the slowest
+    stream's), the cores used and the live particles (age > 0) per stream,
+    averaged over the timed frames and the streams."""
     import multiprocessing as mp
 
     import numpy as np
@@ -375,8 +379,11 @@ def bench_ours(args):
     lib.gbt_profile_enable(btp._ctx, 1)
     preroll_ptrs = (ctypes.c_void_p * B)()
     pitches = (ctypes.c_int64 * B)(*([COLS] * B))
+    live_hist = []
     for t in range(nprof):
         resident_step(btp, B, W0 + t, preroll_ptrs, pitches)
+        btp.sync()
+        live_hist.append(live_per_stream(btp, B))  # between frames: the per-kernel events are unaffected
     btp.sync()
     prof = {}
     nameb = ctypes.create_string_buffer(64)
@@ -389,7 +396,10 @@ def bench_ours(args):
             break
         prof[nameb.value.decode()] = (tot.value, cnt.value)
         k += 1
-    live_mean = live_per_stream(btp, B)  # live particles (age > 0) at the end of the profiled frames
+    # Live particles (age > 0) per stream, averaged over the profiled frames --
+    # the timed region's frames (the count swings about 3x with the detector
+    # period, so a single frame's count depends on where it falls).
+    live_mean = float(np.mean(live_hist))
     btp.close()
     total_ms = sum(v[0] for v in prof.values())
     shares = {n: round(v[0] / total_ms, 4) for n, v in sorted(prof.items(), key=lambda kv: -kv[1][0])}
@@ -462,14 +472,13 @@ def bench_ours(args):
                 pg.all_reduce(tt, op=pg.ReduceOp.MAX)
                 el = float(tt.item())
             rates.append(B * world * e2e_steps / el)
-        live = live_per_stream(bt_, B)
         bt_.close()
-        return sorted(rates)[len(rates) // 2], rates, live
+        return sorted(rates)[len(rates) // 2], rates
 
     host = [torch.from_numpy(f).pin_memory() for f in frames]
     gray_index = lambda t: pal(W0 + t, nfr)  # noqa: E731  (continues the clip after the pre-roll)
-    e2e, e2e_all, e2e_live = timed_e2e(host, gray_index, COLS, 0, True)
-    e2e_block, _, _ = timed_e2e(host, gray_index, COLS, 0, False)
+    e2e, e2e_all = timed_e2e(host, gray_index, COLS, 0, True)
+    e2e_block, _ = timed_e2e(host, gray_index, COLS, 0, False)
     del host
     # RGB frames: 3 bytes per pixel go to the device and the pyramid kernel
     # makes them gray (channel 0, as the reference's sample).  The RGB clip is
@@ -477,7 +486,7 @@ def bench_ours(args):
     nrgb = max(1, min(40, nfr - W0))
     host_rgb = [torch.from_numpy(np.ascontiguousarray(np.repeat(frames[s][W0:W0 + nrgb, :, :, None], 3,
                                                                 axis=3))).pin_memory() for s in range(B)]
-    e2e_rgb, _, _ = timed_e2e(host_rgb, lambda t: pal(t, nrgb), COLS * 3, 2, True)
+    e2e_rgb, _ = timed_e2e(host_rgb, lambda t: pal(t, nrgb), COLS * 3, 2, True)
     del host_rgb
 
     extras = {} if args.no_extras else measure_extras(args, dev, local, peak)
@@ -499,6 +508,7 @@ def bench_ours(args):
             "config": {"workload": workload_name(B) + ", CUDA-graph replay",
                        "streams_per_gpu": B, "stream_groups": ngroups, "preroll_frames": PREROLL,
                        "live_particles_per_stream": round(live_mean),
+                       "live_particles_note": "age > 0, all scales, mean over the timed frames",
                        "l2": "working set per step > L2 (inputs larger than L2)",
                        "parallelism": "replicas only (independent streams per GPU)"},
             "plain": {"value": round(plain, 2), "unit": UNIT, "streams": 1, "ms_per_frame": round(ms1 / args.steps, 4),
@@ -526,7 +536,7 @@ def bench_ours(args):
                                 "made on the GPU; results read one step behind" % nrgb},
             "e2e": {"value": round(e2e, 2), "unit": UNIT, "h2d_bytes_per_step": B * ROWS * COLS,
                     "d2h_bytes_per_step": 4 * nunits, "steps": e2e_steps, "repeats": E2E_REPEATS,
-                    "all": [round(x, 1) for x in e2e_all], "live_particles_per_stream": round(e2e_live),
+                    "all": [round(x, 1) for x in e2e_all],
                     "note": "gbt_run from pinned host frames continuing the clip after the pre-roll (palindromic "
                             "order); each step's per-unit counts read with gbt_read_counts_async while the next "
                             "step runs",
@@ -834,7 +844,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--streams", type=int, default=16)
-    ap.add_argument("--cpu-frames", type=int, default=12)
+    ap.add_argument("--cpu-frames", type=int, default=DET_FREQ,
+                    help="timed frames per stream of the CPU baseline (default: one detector period)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--matcher", type=int, default=-1, help="matcher variant (default: autotuned)")
     ap.add_argument("--no-extras", action="store_true",

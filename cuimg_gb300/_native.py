@@ -59,7 +59,7 @@ def synth_lib():
 class gbt_config(ctypes.Structure):
     _fields_ = [(n, ctypes.c_int32) for n in (
         "rows", "cols", "nscales", "detector_threshold", "detector_n", "detector_frequency",
-        "filtering_frequency", "k", "with_merge", "detector", "detector_step", "detector_grad_th")]
+        "filtering_frequency", "k", "with_merge", "detector", "detector_step", "detector_grad_th", "matcher")]
 
 
 def _declare(lib):
@@ -83,6 +83,7 @@ def _declare(lib):
     lib.gbt_stream.argtypes = [P, ctypes.POINTER(P)]
     lib.gbt_nparticles.argtypes = [P, I32, I32, I32P]
     lib.gbt_get_particles.argtypes = [P, I32, I32, P, P, P, P, P, I32P, I32P]
+    lib.gbt_get_particles_f.argtypes = [P, I32, I32, P, P, P, P, I32P, I32P]
     lib.gbt_get_stage.argtypes = [P, I32, I32, I32, I32, P]
     lib.gbt_bins.argtypes = [P, I32, I32, I32P, I32P]
     lib.gbt_get_bins.argtypes = [P, I32, I32, P, P, P, P]

@@ -18,10 +18,10 @@ CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 INCLUDE = os.path.join(ROOT, "include")
 
-CUDA_SOURCES = ["tracker.cu", "gaussian.cu", "lk.cu", "lkd.cu"]
-# Per-file flags: the LK solver keeps separate multiply/add roundings, as the
+CUDA_SOURCES = ["tracker.cu", "gaussian.cu", "lk.cu", "lkd.cu", "pyrlk.cu"]
+# Per-file flags: the LK solvers keep separate multiply/add roundings, as the
 # reference's C++ evaluates them.
-EXTRA_FLAGS = {"lk.cu": ["--fmad=false"]}
+EXTRA_FLAGS = {"lk.cu": ["--fmad=false"], "pyrlk.cu": ["--fmad=false"]}
 NVCC_FLAGS = [
     "-gencode", "arch=compute_103a,code=sm_103a",
     "-O3", "-lineinfo", "-std=c++17",

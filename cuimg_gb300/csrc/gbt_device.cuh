@@ -136,6 +136,52 @@ __host__ __device__ constexpr int circle16_r(int i) {
 }
 __host__ __device__ constexpr int circle16_c(int i) { return circle16_r((i + 4) & 15); }
 
+// fast::compute_saliency (tracking2/fast_detector.hpp:28-157) without
+// branches, from the centre value vp and the 16 ring values (circle16 order).
+// A ring pixel is "strong" when it differs from the centre by more than th
+// (bright: above, dark: below); the reference scans the ring for the longest
+// run of strong pixels of one sign, wrapping around (:95-146), and scores
+// max(sum bright, sum dark) over all strong pixels (stored as gl8u).  Here the
+// runs are tested on 16-bit masks doubled to 32 bits (so a run may wrap): a
+// run of n_ exists iff the AND of the mask shifted by 0..n_-1 is non-zero.
+// The reference's pre-test on ring pixels 0, 4, 8, 12 only rejects pixels the
+// full test rejects too (a run of n_ >= 9 covers two cyclically adjacent ones
+// of them, n_ >= 12 three), so it is left out.  th >= 0.
+__device__ __forceinline__ int fast_score(const int (&ring)[16], int vp, int n_, int th) {
+  unsigned B = 0, D = 0;
+  int sb = 0, sd = 0;
+#pragma unroll
+  for (int i = 0; i < 16; i++) {
+    const int d = ring[i] - vp;
+    const bool br = d > th, dk = -d > th;
+    B |= (unsigned)br << i;
+    D |= (unsigned)dk << i;
+    sb += br ? d : 0;
+    sd += dk ? -d : 0;
+  }
+  if (n_ > 16) return 0;
+  const unsigned MB = B | (B << 16), MD = D | (D << 16);
+  unsigned xb, xd;
+  if (n_ == 9) {  // runs of 2, 4, 8, then 9
+    xb = MB & (MB >> 1);
+    xd = MD & (MD >> 1);
+    xb &= xb >> 2;
+    xd &= xd >> 2;
+    xb &= xb >> 4;
+    xd &= xd >> 4;
+    xb &= MB >> 8;
+    xd &= MD >> 8;
+  } else {
+    xb = MB;
+    xd = MD;
+    for (int k = 1; k < n_; k++) {
+      xb &= MB >> k;
+      xd &= MD >> k;
+    }
+  }
+  return (xb | xd) ? ((sb > sd ? sb : sd) & 255) : 0;
+}
+
 __device__ __forceinline__ int clampi(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }
 
 // Level image read with the reference's clamp-to-edge border semantics.

@@ -17,6 +17,7 @@
 #include <vector>
 
 #include "cuimg_gb300.h"
+#include "pyrlk.h"
 #include "tracker_kernels.cuh"
 
 using namespace gbt;
@@ -187,6 +188,7 @@ extern "C" void gbt_config_default(gbt_config* cfg, int32_t rows, int32_t cols, 
   cfg->detector = GBT_DETECTOR_FAST;
   cfg->detector_step = 1;   // regular_detector defaults (regular_detector.hpp:12-17)
   cfg->detector_grad_th = 1;
+  cfg->matcher = GBT_MATCHER_BC2S;
 }
 
 extern "C" int gbt_sizes_ok(int32_t rows, int32_t cols, int32_t nscales) {
@@ -1481,7 +1483,22 @@ struct gbt_ctx {
   cudaEvent_t ev_join = nullptr;
   bool profiling = false;                  // per-kernel timing: groups run one after another
   std::string err;
+  PkTracker* pk = nullptr;                 // the LK matcher's engine (gbt_config.matcher == GBT_MATCHER_LK)
 };
+
+// Entry points of an LK-matcher context: the engine's status, with its message.
+static int pk_adopt(gbt_ctx* c, int r) {
+  if (r) c->err = pk_error(c->pk);
+  return r;
+}
+static int pk_unsupported(gbt_ctx* c, const char* what) {
+  c->err = std::string(what) + " is not available with the LK matcher";
+  return GBT_E_INVALID;
+}
+#define LK_ONLY(call) \
+  if (c && c->pk) return pk_adopt(c, (call))
+#define LK_NOT(name) \
+  if (c && c->pk) return pk_unsupported(c, name)
 
 #define CKO(call)                                                                              \
   do {                                                                                         \
@@ -1545,11 +1562,44 @@ static void partition(const gbt_config* cfgs, int n, int G, std::vector<std::vec
   for (auto& m : members) std::sort(m.begin(), m.end());
 }
 
+static bool lk_config_ok(const gbt_config& c) {
+  if (c.nscales < 1 || c.nscales > 9 || c.detector_frequency < 1 || c.filtering_frequency < 1 || c.detector_n < 1 ||
+      c.detector_n > 16 || c.detector_threshold < 0 || c.k < 0 || c.detector != GBT_DETECTOR_FAST)
+    return false;
+  for (int l = 0; l < c.nscales; l++)
+    if ((c.rows >> l) < 16 || (c.cols >> l) < 16) return false;
+  return true;
+}
+
 extern "C" int gbt_create_ex(const gbt_config* cfgs, int32_t nstreams, int32_t device, int32_t groups,
                              gbt_ctx** out) {
   if (!out) return GBT_E_INVALID;
   *out = nullptr;
   if (!cfgs || nstreams < 1) return GBT_E_INVALID;
+  for (int s = 0; s < nstreams; s++)
+    if (cfgs[s].matcher != cfgs[0].matcher || (cfgs[s].matcher != GBT_MATCHER_BC2S && cfgs[s].matcher != GBT_MATCHER_LK))
+      return GBT_E_INVALID;
+  if (cfgs[0].matcher == GBT_MATCHER_LK) {
+    for (int s = 0; s < nstreams; s++)
+      if (!lk_config_ok(cfgs[s])) return GBT_E_INVALID;
+    gbt_ctx* c = new gbt_ctx;
+    c->device = device;
+    std::string err;
+    int r = pk_create(cfgs, nstreams, device, &c->pk, err);
+    if (r) {
+      fprintf(stderr, "gbt_create: %s\n", err.c_str());
+      delete c;
+      return r;
+    }
+    c->nunits = 0;
+    for (int s = 0; s < nstreams; s++) {
+      c->nscales.push_back(cfgs[s].nscales);
+      c->unit0.push_back(c->nunits);
+      c->nunits += cfgs[s].nscales;
+    }
+    *out = c;
+    return GBT_OK;
+  }
   int G = groups > 0 ? groups : 4;
   G = std::max(1, std::min(G, (int)nstreams));
   gbt_ctx* c = new gbt_ctx;
@@ -1603,12 +1653,21 @@ extern "C" int gbt_create(const gbt_config* cfgs, int32_t nstreams, int32_t devi
 }
 
 extern "C" int gbt_groups(gbt_ctx* c, int32_t* groups) {
+  if (c && c->pk && groups) {
+    *groups = 1;
+    return GBT_OK;
+  }
   if (!c || !groups) return GBT_E_INVALID;
   *groups = (int32_t)c->g.size();
   return GBT_OK;
 }
 
 extern "C" int gbt_destroy(gbt_ctx* c) {
+  if (c && c->pk) {
+    pk_destroy(c->pk);
+    delete c;
+    return GBT_OK;
+  }
   if (!c) return GBT_E_INVALID;
   cudaSetDevice(c->device);
   if (c->join) cudaStreamSynchronize(c->join);
@@ -1623,6 +1682,10 @@ extern "C" int gbt_last_error(gbt_ctx* c, char* buf, size_t len) {
 }
 
 extern "C" int gbt_stream(gbt_ctx* c, void** s) {
+  if (c && c->pk && s) {
+    *s = (void*)pk_stream(c->pk);
+    return GBT_OK;
+  }
   if (!c || !s) return GBT_E_INVALID;
   *s = (void*)c->join;
   return GBT_OK;
@@ -1631,12 +1694,14 @@ extern "C" int gbt_stream(gbt_ctx* c, void** s) {
 static bool stream_ok(const gbt_ctx* c, int32_t s) { return c && s >= 0 && s < (int32_t)c->grp.size(); }
 
 extern "C" int gbt_input_slot(gbt_ctx* c, int32_t stream, uint8_t** dptr, int64_t* pitch) {
+  LK_NOT("gbt_input_slot");
   if (!stream_ok(c, stream)) return GBT_E_INVALID;
   Group* g = c->g[c->grp[stream]];
   return adopt(c, g, grp_input_slot(g, c->local[stream], dptr, pitch));
 }
 
 extern "C" int gbt_set_tuning(gbt_ctx* c, int32_t knob, int32_t value) {
+  LK_NOT("gbt_set_tuning");
   if (!c) return GBT_E_INVALID;
   for (Group* g : c->g) {
     int r = grp_set_tuning(g, knob, value);
@@ -1646,11 +1711,13 @@ extern "C" int gbt_set_tuning(gbt_ctx* c, int32_t knob, int32_t value) {
 }
 
 extern "C" int gbt_get_tuning(gbt_ctx* c, int32_t knob, int32_t* value) {
+  LK_NOT("gbt_get_tuning");
   if (!c) return GBT_E_INVALID;
   return adopt(c, c->g[0], grp_get_tuning(c->g[0], knob, value));
 }
 
 extern "C" int gbt_trajectories_enable(gbt_ctx* c, int32_t history) {
+  LK_NOT("device-side trajectories");
   if (!c) return GBT_E_INVALID;
   for (Group* g : c->g) {
     int r = grp_trajectories_enable(g, history);
@@ -1660,12 +1727,14 @@ extern "C" int gbt_trajectories_enable(gbt_ctx* c, int32_t history) {
 }
 
 extern "C" int gbt_use_graphs(gbt_ctx* c, int32_t enable) {
+  LK_NOT("gbt_use_graphs");
   if (!c) return GBT_E_INVALID;
   for (Group* g : c->g) grp_use_graphs(g, enable);
   return GBT_OK;
 }
 
 extern "C" int gbt_test_withhold_tile_copies(gbt_ctx* c, int32_t enable) {
+  LK_NOT("gbt_test_withhold_tile_copies");
   if (!c) return GBT_E_INVALID;
   for (Group* g : c->g) {
     int r = grp_test_withhold_tile_copies(g, enable);
@@ -1675,6 +1744,7 @@ extern "C" int gbt_test_withhold_tile_copies(gbt_ctx* c, int32_t enable) {
 }
 
 extern "C" int gbt_set_rgb_to_gray(gbt_ctx* c, int32_t mode) {
+  LK_NOT("RGB input");
   if (!c) return GBT_E_INVALID;
   for (Group* g : c->g) {
     int r = grp_set_rgb_to_gray(g, mode);
@@ -1684,6 +1754,7 @@ extern "C" int gbt_set_rgb_to_gray(gbt_ctx* c, int32_t mode) {
 }
 
 extern "C" int gbt_run_resident(gbt_ctx* c) {
+  LK_NOT("gbt_run_resident");
   if (!c) return GBT_E_INVALID;
   CKO(cudaSetDevice(c->device));
   CKO(cudaEventRecord(c->ev_join, c->join));  // the caller's slot writes on gbt_stream
@@ -1696,6 +1767,7 @@ extern "C" int gbt_run_resident(gbt_ctx* c) {
 }
 
 extern "C" int gbt_run(gbt_ctx* c, const uint8_t* const* frames, const int64_t* pitches, int32_t location) {
+  LK_ONLY(pk_run(c->pk, frames, pitches, location));
   if (!c || !frames) return GBT_E_INVALID;
   CKO(cudaSetDevice(c->device));
   for (size_t k = 0; k < c->g.size(); k++) {
@@ -1714,6 +1786,7 @@ extern "C" int gbt_run(gbt_ctx* c, const uint8_t* const* frames, const int64_t* 
 }
 
 extern "C" int gbt_sync(gbt_ctx* c) {
+  LK_ONLY(pk_sync(c->pk));
   if (!c) return GBT_E_INVALID;
   int first = GBT_OK;
   for (Group* g : c->g) {
@@ -1725,6 +1798,7 @@ extern "C" int gbt_sync(gbt_ctx* c) {
 }
 
 extern "C" int gbt_kernel_launches(gbt_ctx* c, int64_t* total) {
+  LK_ONLY(pk_kernel_launches(c->pk, total));
   if (!c || !total) return GBT_E_INVALID;
   int64_t t = 0;
   for (Group* g : c->g) {
@@ -1737,6 +1811,7 @@ extern "C" int gbt_kernel_launches(gbt_ctx* c, int64_t* total) {
 }
 
 extern "C" int gbt_kernels_per_frame(gbt_ctx* c, int32_t* n) {
+  LK_ONLY(pk_kernels_per_frame(c->pk, n));
   if (!c || !n) return GBT_E_INVALID;
   int32_t t = 0;
   for (Group* g : c->g) {
@@ -1755,46 +1830,79 @@ extern "C" int gbt_kernels_per_frame(gbt_ctx* c, int32_t* n) {
   return adopt(c, g, call_with_local)
 
 extern "C" int gbt_set_param(gbt_ctx* c, int32_t stream, int32_t scale, int32_t key, int32_t value) {
+  LK_ONLY(pk_set_param(c->pk, stream, scale, key, value));
   DISPATCH(grp_set_param(g, ls, scale, key, value));
 }
 
 extern "C" int gbt_get_param(gbt_ctx* c, int32_t stream, int32_t scale, int32_t key, int32_t* value) {
+  LK_ONLY(pk_get_param(c->pk, stream, scale, key, value));
   DISPATCH(grp_get_param(g, ls, scale, key, value));
 }
 
 extern "C" int gbt_nparticles(gbt_ctx* c, int32_t stream, int32_t scale, int32_t* n) {
+  LK_ONLY(pk_nparticles(c->pk, stream, scale, n));
   DISPATCH(grp_nparticles(g, ls, scale, n));
 }
 
 extern "C" int gbt_frame_count(gbt_ctx* c, int32_t stream, int32_t scale, int32_t* n) {
+  LK_ONLY(pk_frame_count(c->pk, stream, scale, n));
   DISPATCH(grp_frame_count(g, ls, scale, n));
 }
 
 extern "C" int gbt_get_particles(gbt_ctx* c, int32_t stream, int32_t scale, float* speed, int16_t* pos,
                                  uint16_t* age, uint8_t* features, int32_t* matches, int32_t* nmatches,
                                  int32_t* compact_has_run) {
+  if (c && c->pk) {  // integral positions (i_int2 truncation), no features
+    int32_t n = 0;
+    int r = pk_adopt(c, pk_nparticles(c->pk, stream, scale, &n));
+    if (r) return r;
+    std::vector<float> p(2 * (size_t)n);
+    r = pk_adopt(c, pk_get_particles(c->pk, stream, scale, p.data(), speed, age, matches, nmatches, compact_has_run));
+    if (r) return r;
+    for (size_t i = 0; pos && i < p.size(); i++) pos[i] = (int16_t)(int)p[i];
+    if (features) memset(features, 0, 16 * (size_t)n);
+    return GBT_OK;
+  }
   DISPATCH(grp_get_particles(g, ls, scale, speed, pos, age, features, matches, nmatches, compact_has_run));
+}
+
+extern "C" int gbt_get_particles_f(gbt_ctx* c, int32_t stream, int32_t scale, float* pos, float* speed, uint16_t* age,
+                                   int32_t* matches, int32_t* nmatches, int32_t* compact_has_run) {
+  LK_ONLY(pk_get_particles(c->pk, stream, scale, pos, speed, age, matches, nmatches, compact_has_run));
+  int32_t n = 0;
+  int r = gbt_nparticles(c, stream, scale, &n);
+  if (r) return r;
+  std::vector<int16_t> p(2 * (size_t)n);
+  r = gbt_get_particles(c, stream, scale, speed, p.data(), age, nullptr, matches, nmatches, compact_has_run);
+  if (r) return r;
+  for (size_t i = 0; pos && i < p.size(); i++) pos[i] = (float)p[i];
+  return GBT_OK;
 }
 
 extern "C" int gbt_get_trajectories(gbt_ctx* c, int32_t stream, int32_t scale, int16_t* xy, uint8_t* len,
                                     int32_t* n, int32_t* history) {
+  LK_NOT("device-side trajectories");
   DISPATCH(grp_get_trajectories(g, ls, scale, xy, len, n, history));
 }
 
 extern "C" int gbt_bins(gbt_ctx* c, int32_t stream, int32_t scale, int32_t* rows, int32_t* cols) {
+  LK_NOT("flow bins");
   DISPATCH(grp_bins(g, ls, scale, rows, cols));
 }
 
 extern "C" int gbt_get_bins(gbt_ctx* c, int32_t stream, int32_t scale, float* flow, uint32_t* count,
                             int32_t* stat_n, int32_t* stat_speed) {
+  LK_NOT("flow bins");
   DISPATCH(grp_get_bins(g, ls, scale, flow, count, stat_n, stat_speed));
 }
 
 extern "C" int gbt_get_stage(gbt_ctx* c, int32_t stream, int32_t scale, int32_t stage, int32_t border, void* out) {
+  LK_ONLY(pk_get_stage(c->pk, stream, scale, stage, border, out));
   DISPATCH(grp_get_stage(g, ls, scale, stage, border, out));
 }
 
 extern "C" int gbt_read_counts(gbt_ctx* c, int32_t* counts, int32_t n) {
+  LK_ONLY(pk_read_counts(c->pk, counts, n, false));
   if (!c || !counts || n < c->nunits) return GBT_E_INVALID;
   for (size_t k = 0; k < c->g.size(); k++) {
     Group* g = c->g[k];
@@ -1808,6 +1916,7 @@ extern "C" int gbt_read_counts(gbt_ctx* c, int32_t* counts, int32_t n) {
 }
 
 extern "C" int gbt_read_counts_async(gbt_ctx* c, int32_t* counts, int32_t n) {
+  LK_ONLY(pk_read_counts(c->pk, counts, n, true));
   if (!c || !counts || n < c->nunits) return GBT_E_INVALID;
   CKO(cudaSetDevice(c->device));
   for (size_t k = 0; k < c->g.size(); k++) {
@@ -1833,6 +1942,7 @@ struct CkgHeader {
 }  // namespace
 
 extern "C" int gbt_checkpoint_size(gbt_ctx* c, size_t* bytes) {
+  LK_NOT("checkpointing");
   if (!c || !bytes) return GBT_E_INVALID;
   size_t b = sizeof(CkgHeader) + c->grp.size() * sizeof(int32_t) + c->g.size() * sizeof(uint64_t);
   for (Group* g : c->g) {
@@ -1846,6 +1956,7 @@ extern "C" int gbt_checkpoint_size(gbt_ctx* c, size_t* bytes) {
 }
 
 extern "C" int gbt_checkpoint_save(gbt_ctx* c, void* buf, size_t cap, size_t* written) {
+  LK_NOT("checkpointing");
   if (!c || !buf) return GBT_E_INVALID;
   size_t need = 0;
   int r = gbt_checkpoint_size(c, &need);
@@ -1878,6 +1989,7 @@ extern "C" int gbt_checkpoint_save(gbt_ctx* c, void* buf, size_t cap, size_t* wr
 }
 
 extern "C" int gbt_checkpoint_load(gbt_ctx* c, const void* buf, size_t len) {
+  LK_NOT("checkpointing");
   if (!c || !buf || len < sizeof(CkgHeader)) return GBT_E_INVALID;
   const uint8_t* p = (const uint8_t*)buf;
   const uint8_t* end = p + len;
@@ -1918,6 +2030,7 @@ extern "C" int gbt_checkpoint_load(gbt_ctx* c, const void* buf, size_t len) {
 }
 
 extern "C" int gbt_profile_enable(gbt_ctx* c, int32_t enable) {
+  LK_NOT("per-kernel profiling");
   if (!c) return GBT_E_INVALID;
   for (Group* g : c->g) {
     int r = grp_profile_enable(g, enable);
@@ -1929,6 +2042,7 @@ extern "C" int gbt_profile_enable(gbt_ctx* c, int32_t enable) {
 
 // Per-kernel entries of all groups, merged by kernel name (first-seen order).
 extern "C" int gbt_profile_read(gbt_ctx* c, int32_t i, char* name, size_t len, double* total_ms, int32_t* launches) {
+  LK_NOT("per-kernel profiling");
   if (!c) return -1;
   std::vector<std::string> names;
   std::vector<double> ms;

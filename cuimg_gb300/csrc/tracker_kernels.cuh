@@ -1098,52 +1098,14 @@ __global__ void __launch_bounds__(256) k_pmask_dilate(const Unit* __restrict__ u
   u.pmask[local] = h | (h << 8) | (h >> 8) | (hu >> 56) | (hd << 56);
 }
 
-// fast::compute_saliency without branches, for a pixel P of a shared tile
-// with compile-time row length LD.  A ring pixel is "strong" when it differs
-// from the centre by more than th (bright: above, dark: below); the reference
-// scans the ring for the longest run of strong pixels of one sign, wrapping
-// around (fast_detector.hpp:95-146), and scores max(sum bright, sum dark) over
-// all strong pixels (stored as gl8u).  Here the runs are tested on 16-bit
-// masks doubled to 32 bits (so a run may wrap): a run of n_ exists iff the AND
-// of the mask shifted by 0..n_-1 is non-zero.  The reference's pre-test on
-// ring pixels 0, 4, 8, 12 only rejects pixels the full test rejects too (a run
-// of n_ >= 9 covers two cyclically adjacent ones of them, n_ >= 12 three), so
-// it is left out.  th >= 0 (the context rejects negative thresholds).
+// fast::compute_saliency for a pixel P of a shared tile with compile-time row
+// length LD (the score itself: fast_score in gbt_device.cuh).
 template <int LD>
 __device__ __forceinline__ int fast_saliency_bf(const uint8_t* P, int n_, int th) {
-  const int vp = P[0];
-  unsigned B = 0, D = 0;
-  int sb = 0, sd = 0;
+  int ring[16];
 #pragma unroll
-  for (int i = 0; i < 16; i++) {
-    const int d = (int)P[circle16_r(i) * LD + circle16_c(i)] - vp;
-    const bool br = d > th, dk = -d > th;
-    B |= (unsigned)br << i;
-    D |= (unsigned)dk << i;
-    sb += br ? d : 0;
-    sd += dk ? -d : 0;
-  }
-  if (n_ > 16) return 0;
-  const unsigned MB = B | (B << 16), MD = D | (D << 16);
-  unsigned xb, xd;
-  if (n_ == 9) {  // runs of 2, 4, 8, then 9
-    xb = MB & (MB >> 1);
-    xd = MD & (MD >> 1);
-    xb &= xb >> 2;
-    xd &= xd >> 2;
-    xb &= xb >> 4;
-    xd &= xd >> 4;
-    xb &= MB >> 8;
-    xd &= MD >> 8;
-  } else {
-    xb = MB;
-    xd = MD;
-    for (int k = 1; k < n_; k++) {
-      xb &= MB >> k;
-      xd &= MD >> k;
-    }
-  }
-  return (xb | xd) ? ((sb > sd ? sb : sd) & 255) : 0;
+  for (int i = 0; i < 16; i++) ring[i] = P[circle16_r(i) * LD + circle16_c(i)];
+  return fast_score(ring, P[0], n_, th);
 }
 
 // A necessary condition of the FAST run test for n_ >= 8: any 8 cyclically

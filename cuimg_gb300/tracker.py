@@ -22,6 +22,7 @@ from ._native import GbtError, check, cuda_lib, gbt_config
 
 GBT_FRAMES_HOST, GBT_FRAMES_DEVICE, GBT_FRAMES_HOST_RGB, GBT_FRAMES_DEVICE_RGB = 0, 1, 2, 3
 GBT_RGB_CHANNEL0, GBT_RGB_BT601 = 0, 1
+GBT_MATCHER_BC2S, GBT_MATCHER_LK = 0, 1
 STAGES = dict(input=0, s1=1, s2=2, contrast=3, saliency=4, mask=5, sparse=6)
 
 
@@ -182,6 +183,8 @@ class BatchTracker:
         and k) of `stream` (every stream when None), through gbt_set_param
         once the context runs."""
         pid, upward = PARAMS[key]
+        if key == "k" and self._cfgs[0].matcher == GBT_MATCHER_LK:
+            upward = False  # pyrlk_cpu::set_k sets its own scale only (pyrlk_tracker.h:44)
         streams = range(self.nstreams) if stream is None else [stream]
         for s in streams:
             L = self._cfgs[s].nscales
@@ -305,7 +308,28 @@ class BatchTracker:
         check(self._lib.gbt_nparticles(self._ensure(), stream, scale, ctypes.byref(n)), self._ctx)
         return n.value
 
+    def is_lk(self):
+        """True for a context of the LK matcher (gbt_config.matcher == GBT_MATCHER_LK)."""
+        return self._cfgs[0].matcher == GBT_MATCHER_LK
+
+    def particles_f(self, stream, scale):
+        """Particle state with float positions and speeds (gbt_get_particles_f)."""
+        ctx = self._ensure()
+        n = self.nparticles(stream, scale)
+        pos = np.zeros((n, 2), np.float32)
+        speed = np.zeros((n, 2), np.float32)
+        age = np.zeros(n, np.uint16)
+        nm, comp = ctypes.c_int32(), ctypes.c_int32()
+        check(self._lib.gbt_get_particles_f(ctx, stream, scale, None, None, None, None, ctypes.byref(nm),
+                                            ctypes.byref(comp)), ctx)
+        matches = np.zeros(max(nm.value, 1), np.int32)
+        check(self._lib.gbt_get_particles_f(ctx, stream, scale, pos.ctypes.data, speed.ctypes.data, age.ctypes.data,
+                                            matches.ctypes.data, ctypes.byref(nm), ctypes.byref(comp)), ctx)
+        return dict(pos=pos, speed=speed, age=age, matches=matches[: nm.value], compact=bool(comp.value))
+
     def _particles(self, stream, scale):
+        if self.is_lk():
+            return self.particles_f(stream, scale)
         ctx = self._ensure()
         n = self.nparticles(stream, scale)
         speed = np.zeros((n, 2), np.float32)
@@ -411,11 +435,12 @@ class BatchTracker:
 
 
 class Tracker(BatchTracker):
-    """Single-stream tracker with the reference's tracker<F> interface."""
+    """Single-stream tracker with the reference's tracker<F> interface.
+    matcher="lk" selects the pyramidal LK tracker strategy (pyrlk_cpu)."""
 
-    def __init__(self, domain, nscales, device=0, graphs=False, **settings):
+    def __init__(self, domain, nscales, device=0, graphs=False, matcher="bc2s", **settings):
         rows, cols = domain
-        cfg = dict(rows=rows, cols=cols, nscales=nscales)
+        cfg = dict(rows=rows, cols=cols, nscales=nscales, matcher={"bc2s": GBT_MATCHER_BC2S, "lk": GBT_MATCHER_LK}[matcher])
         cfg.update(settings)
         super().__init__([cfg], device=device, graphs=graphs)
 

@@ -50,7 +50,25 @@ typedef struct {
   int32_t detector;             /* GBT_DETECTOR_*: the strategy's detector (default FAST) */
   int32_t detector_step;        /* regular_detector::set_step (default 1) */
   int32_t detector_grad_th;     /* regular_detector::set_grad_th (default 1) */
+  int32_t matcher;              /* GBT_MATCHER_*: the strategy's matcher (default BC2S) */
 } gbt_config;
+
+/* Matchers.  GBT_MATCHER_BC2S is the generic strategy's BC2S feature descent
+ * (bc2s_fast_gradient_cpu and the other detectors above).  GBT_MATCHER_LK is
+ * the reference's pyramidal LK tracker strategy,
+ * pyrlk_cpu<fast_detector<cpu>, iterative_lk_match_5x5>
+ * (cuimg/tracking2/pyrlk_tracker.h:16-82, pyrlk_tracker.hpp:772-1063):
+ * sub-pixel particles (gbt_get_particles_f) matched by LK with an 11x11
+ * window, the 25 strongest gradients, 30 iterations and the coarse-to-fine
+ * prediction of get_flow_at, FAST births, compaction and merge; no BC2S
+ * features or flow bins.  All streams of a context use the same matcher.  LK
+ * contexts take gray frames (GBT_FRAMES_HOST / GBT_FRAMES_DEVICE) and keep the
+ * stages INPUT (the strategy's image, border up to 3), SALIENCY, MASK and
+ * SPARSE; input slots, graphs, tuning, trajectories, checkpoints, flow bins,
+ * profiling and RGB input return GBT_E_INVALID for them.  The FAST detector
+ * is the only detector of the LK strategy. */
+#define GBT_MATCHER_BC2S 0
+#define GBT_MATCHER_LK 1
 
 /* Detectors of the reference's generic strategy (tracking_strategies.h):
  * bc2s_fast_gradient_cpu (fast_detector), bc2s_regular_gradient_cpu
@@ -201,6 +219,15 @@ int gbt_nparticles(gbt_ctx* ctx, int32_t stream, int32_t scale, int32_t* n);
 int gbt_get_particles(gbt_ctx* ctx, int32_t stream, int32_t scale, float* speed, int16_t* pos,
                       uint16_t* age, uint8_t* features, int32_t* matches, int32_t* nmatches,
                       int32_t* compact_has_run);
+
+/* The particle set with sub-pixel positions: pos and speed as 2 floats
+ * (row, col) per slot, the rest as gbt_get_particles.  For the LK matcher the
+ * positions are the particle_f<translation_transform> positions
+ * (particle_container.h:45-57); gbt_get_particles gives them truncated to
+ * int16 (the reference's i_int2 conversion) and zero features.  For the BC2S
+ * matcher they are the integral positions as floats. */
+int gbt_get_particles_f(gbt_ctx* ctx, int32_t stream, int32_t scale, float* pos, float* speed, uint16_t* age,
+                        int32_t* matches, int32_t* nmatches, int32_t* compact_has_run);
 
 /* Stage images of (stream, scale) after the last frame, for checks and
  * debugging.  Sizes: level rows x cols (+2*border for the bordered ones). */

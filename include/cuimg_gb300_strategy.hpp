@@ -1,15 +1,22 @@
 /*
- * cuimg_gb300_strategy.hpp -- the GB300 path as a strategy of cuimg's
+ * cuimg_gb300_strategy.hpp -- the GB300 path as strategies of cuimg's
  * unchanged tracker<F> (cuimg/tracking2/tracker.h:10-47).
  *
  * tracker<F> builds one strategy object per scale and, every frame, calls
  * update(input, pset) on each scale, coarsest first (tracker.hpp:83-91).
- * bc2s_fast_gradient_gb300 satisfies the strategy concept of
- * generic_strategy (cuimg/tracking2/tracking_strategies.h:28-107): the types
- * input / particles_type / particle_type / architecture, construction from
- * the scale's obox2d, set_upper, init, update, clear, border_needed,
- * detector() with set_n / set_fast_threshold (fast_detector.hpp:170-193),
- * and the frequency / k / merge setters, which take effect at any time.
+ * Two strategies:
+ *   bc2s_fast_gradient_gb300 -- bc2s_fast_gradient_cpu
+ *     (cuimg/tracking2/tracking_strategies.h:138-151): the strategy concept of
+ *     generic_strategy (:28-107);
+ *   pyrlk_gb300 -- pyrlk_cpu<fast_detector<cpu>, iterative_lk_match_5x5>
+ *     (cuimg/tracking2/pyrlk_tracker.h:16-82): sub-pixel particle_f particles
+ *     tracked by pyramidal LK.
+ * Both provide the types input / particles_type / particle_type /
+ * architecture, construction from the scale's obox2d, set_upper, upper, init,
+ * update, clear, border_needed, detector() with set_n / set_fast_threshold
+ * (fast_detector.hpp:170-193), and the frequency / k / merge setters, which
+ * take effect at any time with the reference's scope (pyrlk_cpu's set_k sets
+ * its own scale only; generic_strategy's forwards to the coarser scales).
  *
  * The scales share one GPU context.  The finest scale's update() uploads the
  * frame and advances every scale in one gbt_run; the coarser scales' update()
@@ -24,7 +31,10 @@
  * Use: include the cuimg headers as usual, then this file; change the
  * strategy name, e.g. in samples/tracking/main.cc:101
  *     typedef tracker<tracking_strategies::bc2s_fast_gradient_gb300> T1;
- * and link libcuimg_gb300.so.  Nothing else in the caller changes.
+ * and link libcuimg_gb300.so.  Nothing else in the caller changes.  (pyrlk_gb300's
+ * particle set has the reference's particle_f<translation_transform>
+ * particles and an empty feature of its own, gb300::no_feature, in place of
+ * pyrlk_tracker.h's dummy_feature, so that this header needs no Eigen.)
  *
  * The host pyramid that tracker<F>::update_input still builds
  * (tracker.hpp:53-69) is not used by the GPU path.
@@ -162,6 +172,88 @@ void load_pset(const scale_state& st, PS& pset) {
   pset.tick();
 }
 
+// The LK matcher's particles: sub-pixel positions and speeds.
+struct lk_scale_state {
+  std::vector<float> pos, speed;  // 2 per slot (row, col)
+  std::vector<uint16_t> age;
+  std::vector<int32_t> matches;
+  bool compacted = false;
+  int rows = 0, cols = 0;
+  std::vector<uint32_t> sparse;
+};
+
+inline void read_scale_state(gbt_ctx* ctx, int stream, int scale, int rows, int cols, lk_scale_state& st) {
+  int32_t n = 0, nm = 0, comp = 0;
+  check(gbt_nparticles(ctx, stream, scale, &n), ctx, "gbt_nparticles");
+  check(gbt_get_particles_f(ctx, stream, scale, nullptr, nullptr, nullptr, nullptr, &nm, &comp), ctx,
+        "gbt_get_particles_f");
+  st.pos.resize(2 * (size_t)n);
+  st.speed.resize(2 * (size_t)n);
+  st.age.resize(n);
+  st.matches.resize(nm);
+  check(gbt_get_particles_f(ctx, stream, scale, st.pos.data(), st.speed.data(), st.age.data(), st.matches.data(),
+                            &nm, &comp),
+        ctx, "gbt_get_particles_f");
+  st.matches.resize(nm);
+  st.compacted = comp != 0;
+  st.rows = rows;
+  st.cols = cols;
+  st.sparse.resize((size_t)rows * cols);
+  check(gbt_get_stage(ctx, stream, scale, GBT_STAGE_SPARSE, 0, st.sparse.data()), ctx, "gbt_get_stage");
+}
+
+// The empty feature of pyrlk_gb300's particle set (pyrlk_tracker.h:13-17's
+// dummy_feature, restated so that this header needs no Eigen).
+struct no_feature {
+  typedef int value_type;
+  int operator()(i_int2) const { return 0; }
+};
+
+// load_pset for particle_f particles (particle_container.h:45-57), the same
+// compaction replay.
+template <typename PS>
+void load_pset(const lk_scale_state& st, PS& pset) {
+  typedef typename PS::particle_type P;
+  typedef typename PS::feature_type FV;
+  const size_t n = st.age.size();
+  auto particle_of = [&](size_t j) {
+    P p;
+    p.speed = i_float2(st.speed[2 * j], st.speed[2 * j + 1]);
+    p.pos = i_float2(st.pos[2 * j], st.pos[2 * j + 1]);
+    p.age = st.age[j];
+    return p;
+  };
+  pset.before_matching();
+  auto& parts = pset.dense_particles();
+  auto& feats = pset.features();
+  if (st.compacted) {
+    const size_t m = st.matches.size();
+    parts.assign(m, P());
+    feats.assign(m, FV());
+    for (size_t i = 0; i < m; i++) {
+      const int j = st.matches[i];
+      if (j < 0) continue;
+      if ((size_t)j >= n) throw std::runtime_error("cuimg_gb300: compaction map points past the particles");
+      parts[i] = particle_of(j);
+      parts[i].age = 1;  // alive through the compaction; final age below
+    }
+    pset.compact();
+    if (parts.size() != n) throw std::runtime_error("cuimg_gb300: compaction map does not match the particles");
+    for (size_t j = 0; j < n; j++) parts[j].age = st.age[j];
+  } else {
+    parts.resize(n);
+    feats.assign(n, FV());
+    for (size_t j = 0; j < n; j++) parts[j] = particle_of(j);
+    auto& mv = pset.matches();
+    mv.resize(st.matches.size());
+    for (size_t i = 0; i < st.matches.size(); i++) mv[i] = (unsigned)st.matches[i];
+  }
+  auto& sp = pset.sparse_particles();
+  for (int r = 0; r < st.rows; r++)
+    for (int c = 0; c < st.cols; c++) sp(r, c) = st.sparse[(size_t)r * st.cols + c];
+  pset.tick();
+}
+
 // Per-scale settings, as generic_strategy and fast_detector hold them.
 struct scale_params {
   int threshold = 20;  // fast_detector's threshold (the reference leaves it unset until set_fast_threshold)
@@ -179,7 +271,7 @@ struct engine {
   std::vector<obox2d> domains;
   gbt_ctx* ctx = nullptr;
   int device = 0;
-  scale_state tmp;
+  int matcher = GBT_MATCHER_BC2S;
 
   ~engine() {
     if (ctx) gbt_destroy(ctx);
@@ -217,6 +309,7 @@ struct engine {
     c.filtering_frequency = p0.filtering_frequency;
     c.k = p0.k;
     c.with_merge = p0.with_merge;
+    c.matcher = matcher;
     check(gbt_create(&c, 1, device, &ctx), nullptr, "gbt_create");
     static const int keys[] = {GBT_PARAM_DETECTOR_THRESHOLD, GBT_PARAM_DETECTOR_N, GBT_PARAM_DETECTOR_FREQUENCY,
                                GBT_PARAM_FILTERING_FREQUENCY, GBT_PARAM_K, GBT_PARAM_WITH_MERGE};
@@ -255,27 +348,52 @@ class gb300_fast_detector {
   int border_needed() const { return 3; }
 
  private:
-  friend struct bc2s_fast_gradient_gb300;
+  template <typename T>
+  friend class basic_gb300_strategy;
   gb300::engine* eng_ = nullptr;
   int scale_ = 0;
 };
 
-struct bc2s_fast_gradient_gb300 {
- public:
-  typedef bc2s_fast_gradient_gb300 self;
-  typedef host_image2d<gl8u> input;
+namespace gb300 {
+
+// bc2s_fast_gradient_cpu's types and scopes.
+struct bc2s_traits {
   typedef particle_container<bc2s_feature<cpu>, particle, cpu> particles_type;
-  typedef particles_type::particle_type particle_type;
+  typedef scale_state state_type;
+  static constexpr int matcher = GBT_MATCHER_BC2S;
+  static constexpr int border = 6;        // bc2s_feature's 6 (bc2s_feature.h:85) > fast_detector's 3
+  static constexpr bool k_forwards = true;  // generic_strategy::set_k (tracking_strategies.hpp:66-74)
+};
+
+// pyrlk_cpu<fast_detector<cpu>, iterative_lk_match_5x5>'s.
+struct pyrlk_traits {
+  typedef particle_container<no_feature, particle_f<translation_transform>, cpu> particles_type;
+  typedef lk_scale_state state_type;
+  static constexpr int matcher = GBT_MATCHER_LK;
+  static constexpr int border = 3;          // pyrlk_cpu::border_needed: the detector's (pyrlk_tracker.hpp:822-827)
+  static constexpr bool k_forwards = false;  // pyrlk_cpu::set_k (pyrlk_tracker.h:44)
+};
+
+}  // namespace gb300
+
+template <typename T>
+class basic_gb300_strategy {
+ public:
+  typedef basic_gb300_strategy<T> self;
+  typedef host_image2d<gl8u> input;
+  typedef typename T::particles_type particles_type;
+  typedef typename particles_type::particle_type particle_type;
   typedef cpu architecture;
   typedef gb300_fast_detector detector_t;
 
-  explicit bc2s_fast_gradient_gb300(const obox2d& d) : eng_(std::make_shared<gb300::engine>()) {
+  explicit basic_gb300_strategy(const obox2d& d) : eng_(std::make_shared<gb300::engine>()) {
     eng_->params.resize(1);
     eng_->psets.assign(1, nullptr);
     eng_->domains.assign(1, d);
+    eng_->matcher = T::matcher;
     bind();
   }
-  bc2s_fast_gradient_gb300(const self&) = delete;
+  basic_gb300_strategy(const self&) = delete;
   self& operator=(const self&) = delete;
 
   // tracker<F> links scale s to scale s + 1 after building the coarser
@@ -296,9 +414,9 @@ struct bc2s_fast_gradient_gb300 {
   self* upper() { return upper_; }
   void init() {}
 
-  // generic_strategy's setters: the frequencies and k apply to this scale and
-  // every coarser one (tracking_strategies.hpp:56-82), with_merge to this
-  // scale (:41-45).
+  // The frequencies apply to this scale and every coarser one
+  // (tracking_strategies.hpp:56-82, pyrlk_tracker.hpp:795-815), with_merge to
+  // this scale, k as the traits say.
   self& set_detector_frequency(unsigned nframe) {
     eng_->set(scale_, (int)eng_->params.size(), GBT_PARAM_DETECTOR_FREQUENCY, (int)nframe);
     return *this;
@@ -308,7 +426,7 @@ struct bc2s_fast_gradient_gb300 {
     return *this;
   }
   self& set_k(int k) {
-    eng_->set(scale_, (int)eng_->params.size(), GBT_PARAM_K, k);
+    eng_->set(scale_, T::k_forwards ? (int)eng_->params.size() : scale_ + 1, GBT_PARAM_K, k);
     return *this;
   }
   void set_with_merge(bool b) { eng_->set(scale_, scale_ + 1, GBT_PARAM_WITH_MERGE, b ? 1 : 0); }
@@ -316,7 +434,7 @@ struct bc2s_fast_gradient_gb300 {
   void set_device(int device) { eng_->device = device; }
 
   detector_t& detector() { return detector_; }
-  int border_needed() const { return 6; }  // bc2s_feature's 6 (bc2s_feature.h:85) > fast_detector's 3
+  int border_needed() const { return T::border; }
 
   void update(const input& in, particles_type& pset) {
     gb300::engine& e = *eng_;
@@ -328,8 +446,8 @@ struct bc2s_fast_gradient_gb300 {
     gb300::check(gbt_run(e.ctx, &frame, &pitch, GBT_FRAMES_HOST), e.ctx, "gbt_run");
     for (size_t s = 0; s < e.params.size(); s++) {
       if (!e.psets[s]) continue;
-      gb300::read_scale_state(e.ctx, 0, (int)s, e.domains[s].nrows(), e.domains[s].ncols(), e.tmp);
-      gb300::load_pset(e.tmp, *(particles_type*)e.psets[s]);
+      gb300::read_scale_state(e.ctx, 0, (int)s, e.domains[s].nrows(), e.domains[s].ncols(), state_);
+      gb300::load_pset(state_, *(particles_type*)e.psets[s]);
     }
   }
 
@@ -354,7 +472,11 @@ struct bc2s_fast_gradient_gb300 {
   self* upper_ = nullptr;
   self* lower_ = nullptr;
   detector_t detector_;
+  typename T::state_type state_;
 };
+
+typedef basic_gb300_strategy<gb300::bc2s_traits> bc2s_fast_gradient_gb300;
+typedef basic_gb300_strategy<gb300::pyrlk_traits> pyrlk_gb300;
 
 }  // namespace tracking_strategies
 }  // namespace cuimg

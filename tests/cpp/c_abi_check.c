@@ -29,6 +29,7 @@ int main(void) {
   FIELD(gbt_config, detector);
   FIELD(gbt_config, detector_step);
   FIELD(gbt_config, detector_grad_th);
+  FIELD(gbt_config, matcher);
   printf("sizeof.gbt_lk_params %zu\n", sizeof(gbt_lk_params));
   FIELD(gbt_lk_params, window);
   FIELD(gbt_lk_params, npix);
@@ -37,9 +38,9 @@ int main(void) {
   FIELD(gbt_lk_params, max_err);
   FIELD(gbt_lk_params, warps_per_block);
   gbt_config_default(&c, 480, 640, 3);
-  printf("default %d %d %d %d %d %d %d %d %d %d %d %d\n", c.rows, c.cols, c.nscales, c.detector_threshold,
+  printf("default %d %d %d %d %d %d %d %d %d %d %d %d %d\n", c.rows, c.cols, c.nscales, c.detector_threshold,
          c.detector_n, c.detector_frequency, c.filtering_frequency, c.k, c.with_merge, c.detector, c.detector_step,
-         c.detector_grad_th);
+         c.detector_grad_th, c.matcher);
   gbt_lk_params_default(&p);
   printf("lk_default %d %d %d %.9g %.9g %d\n", p.window, p.npix, p.max_iter, p.eps, p.max_err, p.warps_per_block);
   printf("sizes_ok %d %d %d\n", gbt_sizes_ok(1080, 1920, 4), gbt_sizes_ok(97, 131, 3), gbt_sizes_ok(8, 8, 1));
