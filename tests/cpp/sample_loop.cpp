@@ -27,6 +27,12 @@
 
 #include "cuimg_gb300_strategy.hpp"
 
+// The GB300 strategy the loop runs (bc2s_fast_gradient_gb300 unless the build
+// names another, e.g. -DSAMPLE_STRATEGY=pyrlk_gb300).
+#ifndef SAMPLE_STRATEGY
+#define SAMPLE_STRATEGY bc2s_fast_gradient_gb300
+#endif
+
 using namespace cuimg;
 
 struct trajectory {
@@ -41,7 +47,7 @@ void update_trajectories(std::vector<trajectory>& v, TR& pset) {
   for (unsigned i = 0; i < v.size(); i++) {
     v[i].alive = parts[i].age > 0;
     if (parts[i].age > 0) {
-      v[i].history.push_back(i_int2(parts[i].pos));
+      v[i].history.push_back(i_int2(parts[i].pos));  // i_int2 of a float position truncates, as in the sample
       if (v[i].history.size() > 20) v[i].history.pop_front();
     } else {
       v[i].history.clear();
@@ -67,7 +73,7 @@ int main(int argc, char** argv) {
   host_image2d<gl8u> frame_gl(domain);
   try {
     // Tracker definition: the only line that differs from the sample.
-    typedef tracker<tracking_strategies::bc2s_fast_gradient_gb300> T1;
+    typedef tracker<tracking_strategies::SAMPLE_STRATEGY> T1;
     T1 tr1(domain, NSCALES);
 
     // Tracker settings, as the sample makes them.
@@ -88,7 +94,7 @@ int main(int argc, char** argv) {
         std::fprintf(out, "frame %d scale %d n %d compact %d longest %zu\n", t, s, tr1.scale(s).pset().size(),
                      (int)tr1.scale(s).pset().compact_has_run(), longest);
         for (size_t i = 0; i < parts.size(); i++)
-          std::fprintf(out, "%d %d %d\n", parts[i].pos.x, parts[i].pos.y, parts[i].age);
+          std::fprintf(out, "%g %g %d\n", (double)parts[i].pos.x, (double)parts[i].pos.y, parts[i].age);
       }
     }
     std::printf("ok frames=%d particles=%u\n", nframes, tr1.nparticles());

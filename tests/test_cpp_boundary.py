@@ -4,8 +4,9 @@
   layouts and host-only calls agree with the ctypes mirror.
 * include/cuimg_gb300_strategy.hpp compiles against the reference's own
   headers: the sample's tracking loop with tracker<bc2s_fast_gradient_gb300>
-  builds and links against libcuimg_gb300.so, and the strategy's particle-set
-  loader reproduces the reference tracker's pset() of every scale on every
+  and with tracker<pyrlk_gb300> builds and links against libcuimg_gb300.so,
+  and the strategies' particle-set loaders reproduce the reference trackers'
+  pset() (bc2s_fast_gradient_cpu's and pyrlk_cpu's) of every scale on every
   frame, bit for bit (particles, features, matches, compact_has_run, the
   sparse index, the sample's trajectories through sync_attributes).
 
@@ -110,13 +111,30 @@ def test_strategy_loader_reproduces_the_reference_psets(tmp_path, rows, cols, L,
 
 
 @needs_ref
-def test_sample_loop_with_the_gb300_strategy_builds_and_links(tmp_path):
+@pytest.mark.parametrize("rows,cols,L,det,n,seed", [(320, 480, 3, 3, 16, 5), (256, 384, 2, 1, 10, 6)])
+def test_lk_strategy_loader_reproduces_the_reference_psets(tmp_path, rows, cols, L, det, n, seed):
+    from oracle_lib import black_margin_frames
+    exe = str(tmp_path / "pyrlk_load_check")
+    _compile(["g++"] + REF_FLAGS + [os.path.join(CPP, "pyrlk_load_check.cpp"),
+                                    os.path.join(ROOT, "oracle", "_build", "liboracle.so"),
+                                    "-Wl,-rpath," + os.path.join(ROOT, "oracle", "_build"), "-o", exe] + LINK_GBT)
+    raw = str(tmp_path / "clip.raw")
+    np.ascontiguousarray(black_margin_frames(seed, rows, cols, n, 16 << (L - 1))).tofile(raw)
+    r = _run(exe, rows, cols, L, det, n, raw)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert r.stdout.startswith("ok"), r.stdout
+
+
+@needs_ref
+@pytest.mark.parametrize("strategy", ["bc2s", "pyrlk"])
+def test_sample_loop_with_the_gb300_strategy_builds_and_links(tmp_path, strategy):
     """The sample's loop compiles unchanged but for the strategy name, links
     against libcuimg_gb300.so and reaches the C ABI.  Without a GPU the first
     frame's gbt_create fails and the strategy throws, as the reference throws on
     a CUDA error; with one, the run tracks."""
     exe = str(tmp_path / "sample_loop")
-    _compile(["g++"] + REF_FLAGS + [os.path.join(CPP, "sample_loop.cpp"), "-o", exe] + LINK_GBT)
+    extra = ["-DSAMPLE_STRATEGY=pyrlk_gb300"] if strategy == "pyrlk" else []
+    _compile(["g++"] + REF_FLAGS + extra + [os.path.join(CPP, "sample_loop.cpp"), "-o", exe] + LINK_GBT)
     rows, cols, L, n = 120, 160, 3, 6
     raw = str(tmp_path / "clip.raw")
     _clip(rows, cols, n, 1).tofile(raw)
