@@ -636,7 +636,56 @@ def measure_extras(args, dev, local, peak):
     torch.cuda.empty_cache()
     out["batched_uneven_64"] = measure_uneven(dev, local)
     out["combined_4k"] = measure_combined_4k(dev)
+    out["lk_tracker"] = measure_lk_tracker(dev)
     return out
+
+
+def measure_lk_tracker(dev, cases=((480, 640, 3, 16), (1080, 1920, 4, 4)), pre=40, timed=20):
+    """The pyramidal LK tracker strategy (gbt_config.matcher = GBT_MATCHER_LK):
+    B streams of one size, `pre` frames untimed, then `timed` frames timed
+    with CUDA events on the context stream; frames resident in HBM."""
+    import numpy as np
+    import torch
+
+    from cuimg_gb300 import BatchTracker
+    from cuimg_gb300._native import check, cuda_lib
+    lib = cuda_lib()
+    res = {}
+    for rows, cols, L, B in cases:
+        vids = gen_clips([(900 + i, rows, cols, pre + timed) for i in range(B)])
+        dv = [torch.from_numpy(v).to(dev) for v in vids]
+        bt = BatchTracker([dict(rows=rows, cols=cols, nscales=L, matcher=1, detector_threshold=THRESHOLD,
+                                detector_frequency=DET_FREQ, filtering_frequency=FILT_FREQ)] * B,
+                          device=dev.index or 0)
+        bt._ensure()
+        cst = torch.cuda.ExternalStream(bt.cuda_stream(), device=dev)
+        ptrs = (ctypes.c_void_p * B)()
+        pit = (ctypes.c_int64 * B)(*([cols] * B))
+
+        def step(t):
+            for s in range(B):
+                ptrs[s] = dv[s][t].data_ptr()
+            check(lib.gbt_run(bt._ctx, ptrs, pit, 1), bt._ctx)
+
+        for t in range(pre):
+            step(t)
+        bt.sync()
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(timed + 1)]
+        ev[0].record(cst)
+        for t in range(timed):
+            step(pre + t)
+            ev[t + 1].record(cst)
+        ev[-1].synchronize()
+        ms = ev[0].elapsed_time(ev[-1]) / timed
+        live = float(np.mean([sum(int((bt.particles_f(s, l)["age"] > 0).sum()) for l in range(L)) for s in range(B)]))
+        bt.close()
+        del dv
+        res["%dx%d_x%d" % (cols, rows, B)] = {
+            "streams": B, "scales": L, "ms_per_step": round(ms, 3), "frames_per_s": round(B / (ms / 1000), 1),
+            "mpix_per_s": round(B * rows * cols / (ms / 1000) / 1e6, 1), "live_particles_per_stream_end": round(live)}
+    res["note"] = ("pyrlk_cpu on the GPU: 11x11 window, 25 strongest gradients, 30 iterations, detector every 10 "
+                   "frames; %d frames untimed, %d timed (CUDA events)" % (pre, timed))
+    return res
 
 
 def measure_uneven(dev, local, nstreams=64, nf=60, timed=20):
@@ -827,6 +876,30 @@ def _case_tracker(nstreams, frames, det_freq, blur_rows=None):
     bt.close()
 
 
+def _case_steady(nstreams, det_freq, frames, lk=False, rows=ROWS, cols=COLS, nscales=NSCALES, preroll=PREROLL):
+    """`nstreams` streams in one group, `preroll` frames untimed, then `frames`
+    frames between cudaProfilerStart / Stop: with ncu --profile-from-start off
+    only the steady-state frames are captured."""
+    import torch
+
+    from cuimg_gb300 import BatchTracker
+    cfg = [dict(rows=rows, cols=cols, nscales=nscales, detector_threshold=THRESHOLD, detector_frequency=det_freq,
+                matcher=1 if lk else 0)]
+    vids = gen_clips([(1000 + i, rows, cols, preroll + frames) for i in range(nstreams)])
+    bt = BatchTracker(cfg * nstreams, graphs=False, groups=1)  # one launch per stage over every stream
+    if not lk:
+        bt.set_tuning(1, 32)
+    for t in range(preroll):
+        bt.run([v[t] for v in vids])
+    bt.sync()
+    torch.cuda.profiler.start()
+    for t in range(preroll, preroll + frames):
+        bt.run([v[t] for v in vids])
+    bt.sync()
+    torch.cuda.profiler.stop()
+    bt.close()
+
+
 PROFILE_CASES = {
     "gaussian": _case_gaussian,
     "lk": _case_lk,
@@ -834,6 +907,10 @@ PROFILE_CASES = {
     "tracker": lambda: _case_tracker(4, 6, 10),        # 4 streams of 1920x1080, 6 frames
     "tracker_det": lambda: _case_tracker(4, 8, 3),     # the same with the detector every third frame
     "tracker16": lambda: _case_tracker(16, 4, 10, 32),  # 16 streams in one group, 32-row blur strips
+    # steady state (120 frames before the captured ones):
+    "tracker16_steady": lambda: _case_steady(16, DET_FREQ, 10),  # the benchmark's streams, one detector period
+    "tracker4_steady": lambda: _case_steady(4, 3, 3),             # 4 streams, detector every third frame
+    "lk_tracker_steady": lambda: _case_steady(2, DET_FREQ, 2, lk=True, preroll=30),  # LK strategy, 2 x 1080p
 }
 
 
