@@ -460,10 +460,11 @@ def bench_ours(args):
             if pipelined:
                 consume((n - 1) & 1)
 
-        rates = []
+        rates, counts = [], []
         for rep_ in range(E2E_REPEATS):
             if pg:
                 pg.barrier()
+            seen0 = seen[0]
             t0 = time.perf_counter()
             block(rep_ * e2e_steps, e2e_steps)
             el = time.perf_counter() - t0
@@ -472,13 +473,14 @@ def bench_ours(args):
                 pg.all_reduce(tt, op=pg.ReduceOp.MAX)
                 el = float(tt.item())
             rates.append(B * world * e2e_steps / el)
+            counts.append((seen[0] - seen0) / (e2e_steps * B))
         bt_.close()
-        return sorted(rates)[len(rates) // 2], rates
+        return sorted(rates)[len(rates) // 2], rates, counts
 
     host = [torch.from_numpy(f).pin_memory() for f in frames]
     gray_index = lambda t: pal(W0 + t, nfr)  # noqa: E731  (continues the clip after the pre-roll)
-    e2e, e2e_all = timed_e2e(host, gray_index, COLS, 0, True)
-    e2e_block, _ = timed_e2e(host, gray_index, COLS, 0, False)
+    e2e, e2e_all, e2e_counts = timed_e2e(host, gray_index, COLS, 0, True)
+    e2e_block, _, _ = timed_e2e(host, gray_index, COLS, 0, False)
     del host
     # RGB frames: 3 bytes per pixel go to the device and the pyramid kernel
     # makes them gray (channel 0, as the reference's sample).  The RGB clip is
@@ -486,7 +488,7 @@ def bench_ours(args):
     nrgb = max(1, min(40, nfr - W0))
     host_rgb = [torch.from_numpy(np.ascontiguousarray(np.repeat(frames[s][W0:W0 + nrgb, :, :, None], 3,
                                                                 axis=3))).pin_memory() for s in range(B)]
-    e2e_rgb, _ = timed_e2e(host_rgb, lambda t: pal(t, nrgb), COLS * 3, 2, True)
+    e2e_rgb, _, _ = timed_e2e(host_rgb, lambda t: pal(t, nrgb), COLS * 3, 2, True)
     del host_rgb
 
     extras = {} if args.no_extras else measure_extras(args, dev, local, peak)
@@ -537,9 +539,11 @@ def bench_ours(args):
             "e2e": {"value": round(e2e, 2), "unit": UNIT, "h2d_bytes_per_step": B * ROWS * COLS,
                     "d2h_bytes_per_step": 4 * nunits, "steps": e2e_steps, "repeats": E2E_REPEATS,
                     "all": [round(x, 1) for x in e2e_all],
+                    "particles_per_stream": [round(x) for x in e2e_counts],
                     "note": "gbt_run from pinned host frames continuing the clip after the pre-roll (palindromic "
-                            "order); each step's per-unit counts read with gbt_read_counts_async while the next "
-                            "step runs",
+                            "order), three blocks of consecutive frames; each step's per-unit counts read with "
+                            "gbt_read_counts_async while the next step runs (particles_per_stream: their mean per "
+                            "block, all scales, slots before compaction included)",
                     "blocking": round(e2e_block, 2)},
             "cpu_baseline": cpu,
             "tuning": {autotune.KNOBS[int(k)][0]: v for k, v in tuning.items()},
