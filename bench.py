@@ -416,79 +416,72 @@ def bench_ours(args):
     frame_gbs = frame_bytes * args.steps / (ms / 1000.0) / 1e9
 
     # End to end through the C ABI: pinned host frames in, every step's
-    # per-unit particle counts out, H2D and D2H inside the timed region.
-    # "e2e" reads step t's counts while step t + 1 runs (gbt_read_counts_async
-    # into pinned memory, an event per step); "blocking" waits for each step's
-    # counts before queuing the next.  Each context first runs the pre-roll
-    # from resident frames; the timed steps continue the same clip in
-    # palindromic order.  Host clock, max over ranks; the median of three
-    # timed blocks (the host shares its cores with other work).
+    # per-unit particle counts out, H2D and D2H inside the timed region, on
+    # the frames the resident rate is timed on.  "e2e" reads step t's counts
+    # while step t + 1 runs (gbt_read_counts_async into pinned memory, an
+    # event per step); "blocking" waits for each step's counts before queuing
+    # the next.  Every repeat makes a fresh context, runs the pre-roll from
+    # resident frames (untimed), then times frames W0 .. W0 + steps - 1 from
+    # the host.  Host clock, max over ranks; the median of the repeats (the
+    # host shares its cores with other work).
     nunits = B * NSCALES
-    e2e_steps = max(args.steps, 100)
-    E2E_REPEATS = 3
+    E2E_REPEATS = 5
 
-    def timed_e2e(host_frames, frame_index, pitch_bytes, location, pipelined):
-        bt_ = make(B)
-        preroll(bt_, B, W0)
-        stream = torch.cuda.ExternalStream(bt_.cuda_stream(), device=dev)
+    def timed_e2e(host_frames, pitch_bytes, location, pipelined):
         ptrs_ = (ctypes.c_void_p * B)()
         pitch_ = (ctypes.c_int64 * B)(*([pitch_bytes] * B))
         outs = [torch.zeros(nunits, dtype=torch.int32).pin_memory() for _ in range(2)]
         evs = [torch.cuda.Event() for _ in range(2)]
-        seen = [0]
+        rates = []
+        for rep_ in range(E2E_REPEATS):
+            bt_ = make(B)
+            preroll(bt_, B, W0)
+            stream = torch.cuda.ExternalStream(bt_.cuda_stream(), device=dev)
+            seen = [0]
 
-        def consume(k):
-            evs[k].synchronize()
-            seen[0] += int(outs[k].sum())
-
-        def run(t, k):
-            for s_ in range(B):
-                ptrs_[s_] = host_frames[s_][frame_index(t)].data_ptr()
-            check(lib.gbt_run(bt_._ctx, ptrs_, pitch_, location), bt_._ctx)
-            if pipelined:
-                check(lib.gbt_read_counts_async(bt_._ctx, outs[k].data_ptr(), nunits), bt_._ctx)
-                evs[k].record(stream)
-            else:
-                check(lib.gbt_read_counts(bt_._ctx, outs[k].data_ptr(), nunits), bt_._ctx)
+            def consume(k):
+                evs[k].synchronize()
                 seen[0] += int(outs[k].sum())
 
-        def block(t0_, n):
-            for t in range(n):
-                run(t0_ + t, t & 1)
+            def run(t, k):
+                for s_ in range(B):
+                    ptrs_[s_] = host_frames[s_][t].data_ptr()
+                check(lib.gbt_run(bt_._ctx, ptrs_, pitch_, location), bt_._ctx)
+                if pipelined:
+                    check(lib.gbt_read_counts_async(bt_._ctx, outs[k].data_ptr(), nunits), bt_._ctx)
+                    evs[k].record(stream)
+                else:
+                    check(lib.gbt_read_counts(bt_._ctx, outs[k].data_ptr(), nunits), bt_._ctx)
+                    seen[0] += int(outs[k].sum())
+
+            if pg:
+                pg.barrier()
+            t0 = time.perf_counter()
+            for t in range(args.steps):
+                run(t, t & 1)
                 if pipelined and t > 0:
                     consume((t - 1) & 1)
             if pipelined:
-                consume((n - 1) & 1)
-
-        rates, counts = [], []
-        for rep_ in range(E2E_REPEATS):
-            if pg:
-                pg.barrier()
-            seen0 = seen[0]
-            t0 = time.perf_counter()
-            block(rep_ * e2e_steps, e2e_steps)
+                consume((args.steps - 1) & 1)
             el = time.perf_counter() - t0
             if pg:
                 tt = torch.tensor([el], device=dev)
                 pg.all_reduce(tt, op=pg.ReduceOp.MAX)
                 el = float(tt.item())
-            rates.append(B * world * e2e_steps / el)
-            counts.append((seen[0] - seen0) / (e2e_steps * B))
-        bt_.close()
-        return sorted(rates)[len(rates) // 2], rates, counts
+            rates.append(B * world * args.steps / el)
+            bt_.close()
+        return sorted(rates)[len(rates) // 2], rates
 
-    host = [torch.from_numpy(f).pin_memory() for f in frames]
-    gray_index = lambda t: pal(W0 + t, nfr)  # noqa: E731  (continues the clip after the pre-roll)
-    e2e, e2e_all, e2e_counts = timed_e2e(host, gray_index, COLS, 0, True)
-    e2e_block, _, _ = timed_e2e(host, gray_index, COLS, 0, False)
+    host = [torch.from_numpy(np.ascontiguousarray(frames[s][W0:W0 + args.steps])).pin_memory() for s in range(B)]
+    e2e, e2e_all = timed_e2e(host, COLS, 0, True)
+    e2e_block, _ = timed_e2e(host, COLS, 0, False)
     del host
-    # RGB frames: 3 bytes per pixel go to the device and the pyramid kernel
-    # makes them gray (channel 0, as the reference's sample).  The RGB clip is
-    # the (at most 40) frames that follow the pre-roll, played back and forth.
-    nrgb = max(1, min(40, nfr - W0))
-    host_rgb = [torch.from_numpy(np.ascontiguousarray(np.repeat(frames[s][W0:W0 + nrgb, :, :, None], 3,
+    # RGB frames of the same timed frames: 3 bytes per pixel go to the device
+    # and the pyramid kernel makes them gray (channel 0, as the reference's
+    # sample).
+    host_rgb = [torch.from_numpy(np.ascontiguousarray(np.repeat(frames[s][W0:W0 + args.steps, :, :, None], 3,
                                                                 axis=3))).pin_memory() for s in range(B)]
-    e2e_rgb, _, _ = timed_e2e(host_rgb, lambda t: pal(t, nrgb), COLS * 3, 2, True)
+    e2e_rgb, _ = timed_e2e(host_rgb, COLS * 3, 2, True)
     del host_rgb
 
     extras = {} if args.no_extras else measure_extras(args, dev, local, peak)
@@ -533,17 +526,15 @@ def bench_ours(args):
                              "relative_to_value": round(traj_fps / value, 3)},
             "clocks": clocks,
             "e2e_rgb": {"value": round(e2e_rgb, 2), "unit": UNIT, "h2d_bytes_per_step": B * ROWS * COLS * 3,
-                        "d2h_bytes_per_step": nunits * 4, "steps": e2e_steps, "repeats": E2E_REPEATS,
-                        "note": "pinned RGB host frames (the %d frames after the pre-roll, back and forth), gray "
-                                "made on the GPU; results read one step behind" % nrgb},
+                        "d2h_bytes_per_step": nunits * 4, "steps": args.steps, "repeats": E2E_REPEATS,
+                        "note": "pinned RGB host frames of the timed frames, gray made on the GPU; results read "
+                                "one step behind"},
             "e2e": {"value": round(e2e, 2), "unit": UNIT, "h2d_bytes_per_step": B * ROWS * COLS,
-                    "d2h_bytes_per_step": 4 * nunits, "steps": e2e_steps, "repeats": E2E_REPEATS,
+                    "d2h_bytes_per_step": 4 * nunits, "steps": args.steps, "repeats": E2E_REPEATS,
                     "all": [round(x, 1) for x in e2e_all],
-                    "particles_per_stream": [round(x) for x in e2e_counts],
-                    "note": "gbt_run from pinned host frames continuing the clip after the pre-roll (palindromic "
-                            "order), three blocks of consecutive frames; each step's per-unit counts read with "
-                            "gbt_read_counts_async while the next step runs (particles_per_stream: their mean per "
-                            "block, all scales, slots before compaction included)",
+                    "note": "gbt_run from pinned host frames: the frames the resident rate is timed on, after the "
+                            "same untimed pre-roll, in a fresh context per repeat; each step's per-unit counts "
+                            "read with gbt_read_counts_async while the next step runs",
                     "blocking": round(e2e_block, 2)},
             "cpu_baseline": cpu,
             "tuning": {autotune.KNOBS[int(k)][0]: v for k, v in tuning.items()},

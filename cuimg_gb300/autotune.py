@@ -20,7 +20,7 @@ KNOBS = {
     0: ("matcher", (0, 1, 2, 3), ("k_match", "k_match_warp", "k_match_tiled", "k_mt_count", "k_mt_scan",
                                   "k_mt_scatter")),
     1: ("blur_rows", (16, 32, 64), ("k_blur",)),
-    2: ("match_tile", (0, 1, 2, 3), ("k_match_tiled",)),
+    2: ("match_tile", (0, 1, 2, 3, 4, 5, 6), ("k_match_tiled",)),
 }
 DEFAULT_CACHE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "_build", "autotune.json")
 

@@ -87,6 +87,7 @@ struct Group {
   long long mt_list_cap = 0;
   int* d_mt_prefix = nullptr;
   int* d_mt_cnt = nullptr;
+  unsigned long long* d_mt_fallback = nullptr;  // particles the slim-margin tiled matcher finished from global memory
   int* d_mt_off = nullptr;
   int* d_mt_list = nullptr;
   int2* d_mt_key = nullptr;  // per slot: (tile, rank in the tile) of the count pass
@@ -108,7 +109,7 @@ struct Group {
   int front_launches = 0;       // kernels in a captured front-end graph
   long long kernels_total = 0;  // kernels launched by this context, graph nodes included
   int match_variant = 0;  // GBT_TUNE_MATCHER
-  int mt_shape = 3;       // GBT_TUNE_MATCH_TILE: tiled matcher threads and particle assignment
+  int mt_shape = 6;       // GBT_TUNE_MATCH_TILE: tiled matcher threads, particle assignment and margins
   int withhold_tiles = 0; // test hook: the tiled matcher's tile copies are not issued
   int fm_grid = 0;        // k_filter_merge CTAs: the ones all SMs hold at once
   // TMA descriptors of every unit's s1 and s2 for the tiled matcher, parity 0
@@ -255,9 +256,10 @@ typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t,
                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
 
 // 2-D uint8 maps over the bordered s1 / s2 (FIXED_FPITCH bytes by H + 2 RB
-// rows, row stride FIXED_FPITCH) with the matcher's staged box (MT_SC bytes
-// by MT_SR rows).  Leaves d_tmaps null when the entry point or an encoding is
-// unavailable.
+// rows, row stride FIXED_FPITCH) with the matcher's staged boxes: the full
+// margins' (MT_SC bytes by MT_SR rows) at d_tmaps[((0 * 2 + par) * nunits +
+// unit) * 2 + image], the slim margins' after them (geometry 1).  Leaves
+// d_tmaps null when the entry point or an encoding is unavailable.
 static int encode_tile_maps(Group* ctx) {
   void* fn = nullptr;
   cudaDriverEntryPointQueryResult q;
@@ -268,21 +270,23 @@ static int encode_tile_maps(Group* ctx) {
   }
   const EncodeTiledFn encode = (EncodeTiledFn)fn;
   const size_t nunits = ctx->units.size();
-  std::vector<CUtensorMap> maps(2 * nunits * 2);
-  for (int par = 0; par < 2; par++)
-    for (size_t ui = 0; ui < nunits; ui++) {
-      const Unit v = unit_view(ctx, ui, par);
-      const cuuint64_t dims[2] = {(cuuint64_t)FIXED_FPITCH, (cuuint64_t)(v.H + 2 * RB)};
-      const cuuint64_t strides[1] = {(cuuint64_t)FIXED_FPITCH};
-      const cuuint32_t box[2] = {(cuuint32_t)MT_SC, (cuuint32_t)MT_SR};
-      const cuuint32_t estr[2] = {1, 1};
-      uint8_t* img[2] = {v.s1, v.s2};
-      for (int k = 0; k < 2; k++)
-        if (encode(&maps[(par * nunits + ui) * 2 + k], CU_TENSOR_MAP_DATA_TYPE_UINT8, 2, img[k], dims, strides, box,
-                   estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
-                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
-          return GBT_OK;
-    }
+  std::vector<CUtensorMap> maps(2 * 2 * nunits * 2);
+  for (int geom = 0; geom < 2; geom++)
+    for (int par = 0; par < 2; par++)
+      for (size_t ui = 0; ui < nunits; ui++) {
+        const Unit v = unit_view(ctx, ui, par);
+        const cuuint64_t dims[2] = {(cuuint64_t)FIXED_FPITCH, (cuuint64_t)(v.H + 2 * RB)};
+        const cuuint64_t strides[1] = {(cuuint64_t)FIXED_FPITCH};
+        const cuuint32_t box[2] = {(cuuint32_t)(geom ? MT_C + 2 * MT_MC_SLIM : MT_SC),
+                                   (cuuint32_t)(geom ? MT_R + 2 * MT_MR_SLIM : MT_SR)};
+        const cuuint32_t estr[2] = {1, 1};
+        uint8_t* img[2] = {v.s1, v.s2};
+        for (int k = 0; k < 2; k++)
+          if (encode(&maps[((geom * 2 + par) * nunits + ui) * 2 + k], CU_TENSOR_MAP_DATA_TYPE_UINT8, 2, img[k], dims,
+                     strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                     CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+            return GBT_OK;
+      }
   int r;
   if ((r = dalloc_t(ctx, &ctx->d_tmaps, maps.size(), false))) return r;
   CK(cudaMemcpy(ctx->d_tmaps, maps.data(), maps.size() * sizeof(CUtensorMap), cudaMemcpyHostToDevice));
@@ -437,6 +441,7 @@ static int build(Group* ctx, const gbt_config* cfgs, int nstreams) {
   if ((r = dalloc_t(ctx, &ctx->d_counts, nunits))) return r;
   if ((r = dalloc_t(ctx, &ctx->d_pre, nunits + 1))) return r;
   if ((r = dalloc_t(ctx, &ctx->d_mt_cnt, ctx->mt_tiles + 1))) return r;
+  if ((r = dalloc_t(ctx, &ctx->d_mt_fallback, 1))) return r;
   if ((r = dalloc_t(ctx, &ctx->d_mt_off, ctx->mt_tiles + 1))) return r;
   if ((r = dalloc_t(ctx, &ctx->d_mt_list, ctx->mt_list_cap))) return r;
   if ((r = dalloc_t(ctx, &ctx->d_mt_key, ctx->mt_list_cap))) return r;
@@ -714,17 +719,25 @@ static int enqueue_back(Group* ctx, bool any_det, bool any_filt, int par, int& n
     { PROF("k_mt_count"); k_mt_bin<0><<<pgrid, CHUNK, 0, st>>>(du, ctx->d_state, ctx->d_pre, nunits, ctx->d_mt_cnt, ctx->d_mt_key, nullptr, nullptr); }
     { PROF("k_mt_scan"); k_mt_scan<<<1, 1024, 0, st>>>(ctx->d_mt_cnt, ctx->mt_tiles, ctx->d_mt_off); }
     { PROF("k_mt_scatter"); k_mt_bin<1><<<pgrid, CHUNK, 0, st>>>(du, ctx->d_state, ctx->d_pre, nunits, nullptr, ctx->d_mt_key, ctx->d_mt_off, ctx->d_mt_list); }
-    PROF("k_match_tiled");
-    const CUtensorMap* tm = ctx->d_tmaps ? ctx->d_tmaps + (size_t)par * nunits * 2 : nullptr;
+    const bool slim = ctx->mt_shape >= 4;
+    const CUtensorMap* tm = ctx->d_tmaps ? ctx->d_tmaps + ((size_t)(slim ? 2 : 0) + par) * nunits * 2 : nullptr;
     int* err = &ctx->d_frame->err;
-    if (ctx->mt_shape == 1)
-      k_match_tiled<128, true, 8><<<ctx->mt_tiles, 128, 0, st>>>(du, ctx->d_state, ctx->d_frame, ctx->d_mt_prefix, nunits, ctx->d_mt_off, ctx->d_mt_list, tm, err, ctx->withhold_tiles);
-    else if (ctx->mt_shape == 2)
-      k_match_tiled<64, true, 10><<<ctx->mt_tiles, 64, 0, st>>>(du, ctx->d_state, ctx->d_frame, ctx->d_mt_prefix, nunits, ctx->d_mt_off, ctx->d_mt_list, tm, err, ctx->withhold_tiles);
-    else if (ctx->mt_shape == 3)
-      k_match_tiled<256, true, 4><<<ctx->mt_tiles, 256, 0, st>>>(du, ctx->d_state, ctx->d_frame, ctx->d_mt_prefix, nunits, ctx->d_mt_off, ctx->d_mt_list, tm, err, ctx->withhold_tiles);
-    else
-      k_match_tiled<MT_THREADS, false, 4><<<ctx->mt_tiles, MT_THREADS, 0, st>>>(du, ctx->d_state, ctx->d_frame, ctx->d_mt_prefix, nunits, ctx->d_mt_off, ctx->d_mt_list, tm, err, ctx->withhold_tiles);
+    unsigned long long* fb = ctx->d_mt_fallback;
+#define GBT_MT_ARGS du, ctx->d_state, ctx->d_frame, ctx->d_mt_prefix, nunits, ctx->d_mt_off, ctx->d_mt_list, tm, err, ctx->withhold_tiles, fb
+    constexpr int FR = MT_MR, FC = MT_MC, SR_ = MT_MR_SLIM, SC_ = MT_MC_SLIM;
+    {
+    PROF("k_match_tiled");
+    switch (ctx->mt_shape) {
+      case 1: k_match_tiled<128, true, 8, FR, FC><<<ctx->mt_tiles, 128, 0, st>>>(GBT_MT_ARGS); break;
+      case 2: k_match_tiled<64, true, 10, FR, FC><<<ctx->mt_tiles, 64, 0, st>>>(GBT_MT_ARGS); break;
+      case 3: k_match_tiled<256, true, 4, FR, FC><<<ctx->mt_tiles, 256, 0, st>>>(GBT_MT_ARGS); break;
+      case 4: k_match_tiled<128, true, 7, SR_, SC_><<<ctx->mt_tiles, 128, 0, st>>>(GBT_MT_ARGS); break;
+      case 5: k_match_tiled<256, true, 4, SR_, SC_><<<ctx->mt_tiles, 256, 0, st>>>(GBT_MT_ARGS); break;
+      case 6: k_match_tiled<192, true, 5, SR_, SC_><<<ctx->mt_tiles, 192, 0, st>>>(GBT_MT_ARGS); break;
+      default: k_match_tiled<MT_THREADS, false, 4, FR, FC><<<ctx->mt_tiles, MT_THREADS, 0, st>>>(GBT_MT_ARGS); break;
+    }
+    }
+#undef GBT_MT_ARGS
     n += 4;
   } else if (ctx->match_variant == 1) {
     PROF("k_match_warp");
@@ -861,7 +874,7 @@ static int grp_set_tuning(Group* ctx, int32_t knob, int32_t value) {
     ctx->blur_tiles = ctx->blur_tiles_v[v];
     return GBT_OK;
   }
-  if (knob == GBT_TUNE_MATCH_TILE && value >= 0 && value <= 3) {
+  if (knob == GBT_TUNE_MATCH_TILE && value >= 0 && value <= 6) {
     if (ctx->mt_shape != value) drop_graphs(ctx);
     ctx->mt_shape = value;
     return GBT_OK;
@@ -1740,6 +1753,23 @@ extern "C" int gbt_test_withhold_tile_copies(gbt_ctx* c, int32_t enable) {
     int r = grp_test_withhold_tile_copies(g, enable);
     if (r) return adopt(c, g, r);
   }
+  return GBT_OK;
+}
+
+extern "C" int gbt_test_tile_fallbacks(gbt_ctx* c, int64_t* count) {
+  LK_NOT("gbt_test_tile_fallbacks");
+  if (!c || !count) return GBT_E_INVALID;
+  int64_t total = 0;
+  for (Group* g : c->g) {
+    if (cudaSetDevice(g->device) != cudaSuccess) return adopt(c, g, set_err(g, GBT_E_CUDA, "cudaSetDevice failed"));
+    int r = sync_all(g);
+    if (r) return adopt(c, g, r);
+    unsigned long long n = 0;
+    if (cudaMemcpy(&n, g->d_mt_fallback, sizeof n, cudaMemcpyDeviceToHost) != cudaSuccess)
+      return adopt(c, g, set_err(g, GBT_E_CUDA, "reading the tiled matcher's fallback count failed"));
+    total += (int64_t)n;
+  }
+  *count = total;
   return GBT_OK;
 }
 

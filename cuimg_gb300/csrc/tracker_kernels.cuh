@@ -1,6 +1,8 @@
 // Tracker kernels: one launch per stage processes every (stream, scale) unit.
 // Each kernel cites the reference functor whose semantics it reproduces.
 #pragma once
+#include <type_traits>
+
 #include "gbt_device.cuh"
 
 namespace gbt {
@@ -266,6 +268,7 @@ struct Feat {
   const uint8_t* s1;
   const uint8_t* s2;
   int o1[8], o2[8];
+  __device__ __forceinline__ static constexpr bool safe(int, int) { return true; }  // the whole bordered image
   __device__ __forceinline__ void init(const Unit& u) {
     s1 = fptr(u.s1, u.fpitch, 0, 0);
     s2 = fptr(u.s2, u.fpitch, 0, 0);
@@ -349,6 +352,23 @@ struct FeatFP {
     const uint8_t* a = s1 + (r * P + c);
     return (int)(__vsadu4(word<1, 0>(a), f.x) + __vsadu4(word<1, 4>(a), f.y));
   }
+  // Whether a descent may continue around (r, c): always, since the whole
+  // bordered image (or a tile with a full-descent margin) is readable.
+  __device__ __forceinline__ static constexpr bool safe(int, int) { return true; }
+};
+
+// FeatFP over a staged tile whose margins do not cover the longest descent:
+// rows lo_r - 7 .. lo_r - 7 + SR - 1 and columns lo_c - 7 .. lo_c - 7 + SC - 1
+// of s1 / s2 are staged at pitch SC.  A descent centred at (r, c) reads its
+// candidates (r +- 1, c +- 1) and their ring taps (6 pixels further at most),
+// so it may continue there only when (r, c) is at least 7 pixels inside the
+// staged rectangle.
+template <int SC, int SR>
+struct FeatTile : FeatFP<SC> {
+  int lo_r, lo_c;
+  __device__ __forceinline__ bool safe(int r, int c) const {
+    return (unsigned)(r - lo_r) < (unsigned)(SR - 14) && (unsigned)(c - lo_c) < (unsigned)(SC - 14);
+  }
 };
 
 // gradient_descent_match (tracking2/gradient_descent_matcher.hpp:9-76): greedy
@@ -390,12 +410,16 @@ __device__ __forceinline__ int c8_dc(int i) { return (int)((c8_pack(true) >> (2 
 // s1+s2 one -- and leaves as the distance at the match.  Every candidate's
 // distance is computed whole: stopping at a partial sum that already reaches
 // the best would give the same descent, but the branches serialise the 8 or 16
-// independent gathers, which costs more than the loads saved.
+// independent gathers, which costs more than the loads saved.  Returns false,
+// with nothing written, when the descent moves to a centre where F cannot
+// serve the next sweep (F.safe), so the caller can redo the match from the
+// images in global memory; true otherwise.  (pr, pc) itself must be safe.
 template <bool WITH_S1, class FeatT>
-__device__ __forceinline__ void gd_match(const Unit& u, const FeatT& F, const uint4& f, int pr, int pc, int& best,
+__device__ __forceinline__ bool gd_match(const Unit& u, const FeatT& F, const uint4& f, int pr, int pc, int& best,
                                          int& dr, int& dc) {
   int predr = pr, predc = pc, mr = pr, mc = pc;
   int mi = 8;
+  bool ok = true;
   for (int search = 0; search < 10; search++) {
     const int i0 = sweep_first(mi), n = sweep_len(mi);
     for (int j = 0; j < n; j++) {
@@ -412,11 +436,16 @@ __device__ __forceinline__ void gd_match(const Unit& u, const FeatT& F, const ui
       }
     }
     if ((predr == mr && predc == mc) || !in_dom(u, mr, mc)) break;
+    if (!F.safe(mr, mc)) {
+      ok = false;
+      break;
+    }
     predr = mr;
     predc = mc;
   }
   dr = mr - pr;
   dc = mc - pc;
+  return ok;
 }
 
 // contrast_kernel (tracking_strategies.hpp:101-135), clamped level reads.
@@ -459,8 +488,10 @@ template <class FeatT>
 __device__ __forceinline__ void match_finish(const Unit& u, const FeatT& F, int f, int b, int i, unsigned short age,
                                              short2 pos, int pr, int pc, const uint4& feat, int dr, int dc);
 
+// Returns false, with nothing written, when a descent left the area F can
+// serve (see gd_match).
 template <class FeatT>
-__device__ __forceinline__ void match_one(const Unit& u, const FeatT& F, int f, int b, int i, unsigned short age,
+__device__ __forceinline__ bool match_one(const Unit& u, const FeatT& F, int f, int b, int i, unsigned short age,
                                           short2 pos, int pr, int pc, const uint4& feat) {
   int d1r, d1c, d2r, d2c;
   // Step 1 compares s2-only candidates against the s1+s2 distance at the
@@ -470,10 +501,13 @@ __device__ __forceinline__ void match_one(const Unit& u, const FeatT& F, int f, 
   // ended with plus the s1 part there.
   const int init = F.dist(feat, pr, pc, u.fpitch, true);
   int best = init;
-  gd_match<false>(u, F, feat, pr, pc, best, d1r, d1c);
-  best = (d1r != 0 || d1c != 0) ? best + F.s1_part(feat, pr + d1r, pc + d1c, u.fpitch) : init;
-  gd_match<true>(u, F, feat, pr + d1r, pc + d1c, best, d2r, d2c);
-  match_finish(u, F, f, b, i, age, pos, pr, pc, feat, d1r + d2r, d1c + d2c);
+  bool ok = gd_match<false>(u, F, feat, pr, pc, best, d1r, d1c);
+  if (ok) {
+    best = (d1r != 0 || d1c != 0) ? best + F.s1_part(feat, pr + d1r, pc + d1c, u.fpitch) : init;
+    ok = gd_match<true>(u, F, feat, pr + d1r, pc + d1c, best, d2r, d2c);
+  }
+  if (ok) match_finish(u, F, f, b, i, age, pos, pr, pc, feat, d1r + d2r, d1c + d2c);
+  return ok;
 }
 
 // The match's acceptance and the particle update (kernel_particle_container::
@@ -543,20 +577,27 @@ __global__ void __launch_bounds__(MATCH_BLOCK) k_match(const Unit* __restrict__ 
 // ---------------------------------------------------------------------------
 // Tiled matcher.  Live particles are binned by their prediction into tiles of
 // MT_R x MT_C pixels (count, scan, scatter); one CTA per non-empty tile stages
-// the tile's s1 / s2 neighbourhood in shared memory with 16-byte cp.async
-// copies and matches its particles from there.  A descent moves at most 10
+// the tile's s1 / s2 neighbourhood in shared memory (TMA, or 16-byte cp.async
+// copies) and matches its particles from there.  A descent moves at most 10
 // pixels per step in each axis (two steps) and the BC2S taps reach 6 pixels
-// further, so with margins of 26 rows and 32 columns every sample a particle
-// of the tile can touch is staged.  Particles are independent (each writes
-// only its own slot; the sparse index keeps the highest slot with atomicMax),
-// so the order inside a tile does not change any result.
+// further, so with the full margins (26 rows, 32 columns) every sample a
+// particle of the tile can touch is staged.  The slim margins (14 rows, 16
+// columns) stage 34% fewer bytes, so that more CTAs fit on an SM; a particle
+// whose descent would read outside them (about 0.1% of them on 1080p video:
+// most descents end within a few pixels, and only particles near a tile edge
+// can reach the margin) is matched again from the images in global memory,
+// with the same result.  Particles are independent (each writes only its own slot;
+// the sparse index keeps the highest slot with atomicMax), so the order inside
+// a tile does not change any result.
 constexpr int MT_R = 64, MT_C = 128;                // tile
-constexpr int MT_MR = 26, MT_MC = 32;              // staged margins
+constexpr int MT_MR = 26, MT_MC = 32;              // full staged margins
 constexpr int MT_SR = MT_R + 2 * MT_MR;            // staged rows (116)
 constexpr int MT_SC = MT_C + 2 * MT_MC;            // staged columns (192), 16-byte chunks
+constexpr int MT_MR_SLIM = 14, MT_MC_SLIM = 16;    // slim staged margins: 92 rows x 160 columns
 constexpr int MT_THREADS = 256;
-static_assert(MT_MR >= 2 * 10 + 6 && MT_MC >= 2 * 10 + 6, "staged margins cover a full descent");
-static_assert(MT_SC % 16 == 0 && MT_MC % 16 == 0, "16-byte staging");
+static_assert(MT_MR >= 2 * 10 + 6 && MT_MC >= 2 * 10 + 6, "full staged margins cover a full descent");
+static_assert(MT_MR_SLIM >= 7 && MT_MC_SLIM >= 7, "the prediction's own sweep is always staged");
+static_assert(MT_SC % 16 == 0 && MT_MC % 16 == 0 && MT_MC_SLIM % 16 == 0, "16-byte staging");
 
 __device__ __forceinline__ int mt_tile(const Unit& u, int pr, int pc) {
   return u.mt_base + (pr / MT_R) * u.MTC + pc / MT_C;
@@ -651,13 +692,16 @@ __device__ __forceinline__ void cp_async16(void* sdst, const void* gsrc) {
   asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(gsrc) : "memory");
 }
 
-// Stages rows R0s .. R0s + MT_SR - 1 and columns C0s .. C0s + MT_SC - 1 of s1
-// and s2, skipping chunks outside the bordered images (never sampled: the taps
-// stay within 6 pixels of the domain, inside the zero border).
-// The same tile by two TMA copies (one per image) that complete on an
-// mbarrier.  The staged region starts at byte column C0s + CB of the bordered
-// rows, a multiple of 16 (C0s = 128 k - 32, CB = 16); rows above or below the
-// bordered image read zeros.  Thread 0 issues; mt_tma_wait waits.
+// Stages rows R0s .. R0s + SR - 1 and columns C0s .. C0s + SC - 1 of s1 and
+// s2 (mt_stage_issue, below), skipping chunks outside the bordered images
+// (never sampled: the taps stay within 6 pixels of the domain, inside the zero
+// border).  mt_tma_issue stages the same tile by two TMA copies (one per
+// image) that complete on an mbarrier.  The staged region starts at byte
+// column C0s + CB of the bordered rows, a multiple of 16 (C0s = 128 k - MC
+// with a margin MC of 32 or 16 columns, CB = 16); rows above or below the
+// bordered image, and columns right of it, read zeros.  Thread 0 issues;
+// mt_tma_wait waits.
+template <int SR, int SC>
 __device__ __forceinline__ void mt_tma_issue(const CUtensorMap* m1, const CUtensorMap* m2, int R0s, int C0s,
                                              uint8_t* ts1, uint8_t* ts2, unsigned long long* mbar, bool copies) {
   const unsigned bar = (unsigned)__cvta_generic_to_shared(mbar);
@@ -668,7 +712,7 @@ __device__ __forceinline__ void mt_tma_issue(const CUtensorMap* m1, const CUtens
   __syncthreads();
   if (threadIdx.x == 0) {
     const int x = C0s + CB, y = R0s + RB;
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(bar), "r"(2 * MT_SR * MT_SC)
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(bar), "r"(2 * SR * SC)
                  : "memory");
     if (!copies) return;  // test hook: the barrier is armed but nothing will complete it
     asm volatile(
@@ -742,16 +786,17 @@ __device__ __forceinline__ bool mt_tma_wait_cta(unsigned long long* mbar, bool c
   return *verdict != 0;
 }
 
+template <int SR, int SC>
 __device__ __forceinline__ void mt_stage_issue(const Unit& u, int R0s, int C0s, uint8_t* ts1, uint8_t* ts2) {
-  constexpr int CPR = MT_SC / 16;
-  for (int v = threadIdx.x; v < MT_SR * CPR; v += blockDim.x) {
+  constexpr int CPR = SC / 16;
+  for (int v = threadIdx.x; v < SR * CPR; v += blockDim.x) {
     const int row = v / CPR, ck = v % CPR;
     const int gr = R0s + row;                    // image row
     const int gb = C0s + CB + 16 * ck;           // byte offset inside the bordered row
     if (gr < -RB || gr >= u.H + RB || gb < 0 || gb + 16 > FIXED_FPITCH) continue;
     const size_t go = (size_t)(gr + RB) * FIXED_FPITCH + gb;
-    cp_async16(&ts1[row * MT_SC + 16 * ck], u.s1 + go);
-    cp_async16(&ts2[row * MT_SC + 16 * ck], u.s2 + go);
+    cp_async16(&ts1[row * SC + 16 * ck], u.s1 + go);
+    cp_async16(&ts2[row * SC + 16 * ck], u.s2 + go);
   }
   asm volatile("cp.async.commit_group;\n" ::: "memory");
 }
@@ -763,8 +808,11 @@ __device__ __forceinline__ void mt_stage_issue(const Unit& u, int R0s, int C0s, 
 // next particle) instead of every THREADS-th one.  A tile whose wait gives up
 // sets ERR_TIMEOUT in *err and leaves its particles unmatched (and
 // ERR_COPY_INFLIGHT if its copies never landed); `withhold` (a test hook) arms
-// the barrier without issuing the copies, so that the wait gives up.
-template <int THREADS, bool DYN, int MINB>
+// the barrier without issuing the copies, so that the wait gives up.  MR x MC
+// are the staged margins: the full ones, or the slim ones, with which a
+// particle whose descent leaves the staged area is matched again by its thread
+// from the bordered images in global memory (counted in *fallbacks).
+template <int THREADS, bool DYN, int MINB, int MR, int MC>
 __global__ void __launch_bounds__(THREADS, MINB) k_match_tiled(const Unit* __restrict__ units,
                                                                const UState* __restrict__ st,
                                                                const Frame* __restrict__ fr,
@@ -772,9 +820,12 @@ __global__ void __launch_bounds__(THREADS, MINB) k_match_tiled(const Unit* __res
                                                                const int* __restrict__ off,
                                                                const int* __restrict__ list,
                                                                const CUtensorMap* __restrict__ tmaps,
-                                                               int* __restrict__ err, int withhold) {
-  __shared__ __align__(128) uint8_t ts1[MT_SR * MT_SC];
-  __shared__ __align__(128) uint8_t ts2[MT_SR * MT_SC];
+                                                               int* __restrict__ err, int withhold,
+                                                               unsigned long long* __restrict__ fallbacks) {
+  constexpr int SR = MT_R + 2 * MR, SC = MT_C + 2 * MC;
+  constexpr bool FULL = MR >= MT_MR && MC >= MT_MC;  // every sample of every descent is staged
+  __shared__ __align__(128) uint8_t ts1[SR * SC];
+  __shared__ __align__(128) uint8_t ts2[SR * SC];
   __shared__ __align__(8) unsigned long long mbar;
   __shared__ int next;
   __shared__ int tile_ok;
@@ -784,12 +835,12 @@ __global__ void __launch_bounds__(THREADS, MINB) k_match_tiled(const Unit* __res
   const int ui = find_unit(tile_prefix, nunits, t);
   const Unit& u = units[ui];
   const int local = t - tile_prefix[ui];
-  const int R0s = (local / u.MTC) * MT_R - MT_MR, C0s = (local % u.MTC) * MT_C - MT_MC;
+  const int R0s = (local / u.MTC) * MT_R - MR, C0s = (local % u.MTC) * MT_C - MC;
   if (DYN && threadIdx.x == 0) next = n0 + THREADS;
   if (tmaps)
-    mt_tma_issue(tmaps + 2 * ui, tmaps + 2 * ui + 1, R0s, C0s, ts1, ts2, &mbar, !withhold);
+    mt_tma_issue<SR, SC>(tmaps + 2 * ui, tmaps + 2 * ui + 1, R0s, C0s, ts1, ts2, &mbar, !withhold);
   else
-    mt_stage_issue(u, R0s, C0s, ts1, ts2);
+    mt_stage_issue<SR, SC>(u, R0s, C0s, ts1, ts2);
   // The thread's first particle is read while the tile arrives.
   const int f = fr->f;
   const int b = st[ui].cur;
@@ -811,13 +862,24 @@ __global__ void __launch_bounds__(THREADS, MINB) k_match_tiled(const Unit* __res
     asm volatile("cp.async.wait_group 0;\n" ::: "memory");
     __syncthreads();
   }
-  FeatFP<MT_SC> F;
-  F.s1 = ts1 - (R0s * MT_SC + C0s);  // F.s1 + (r * MT_SC + c) is staged pixel (r, c)
-  F.s2 = ts2 - (R0s * MT_SC + C0s);
+  typename std::conditional<FULL, FeatFP<SC>, FeatTile<SC, SR>>::type F;
+  F.s1 = ts1 - (R0s * SC + C0s);  // F.s1 + (r * SC + c) is staged pixel (r, c)
+  F.s2 = ts2 - (R0s * SC + C0s);
+  if constexpr (!FULL) {
+    F.lo_r = R0s + 7;
+    F.lo_c = C0s + 7;
+  }
   while (k < n1) {
     int pr, pc;
     predict(age, pos, spd, pr, pc);
-    match_one(u, F, f, b, i, age, pos, pr, pc, feat);
+    if (!match_one(u, F, f, b, i, age, pos, pr, pc, feat)) {
+      // The descent left the staged area (slim margins only): the same match
+      // from the bordered images in global memory.
+      FeatFP<FIXED_FPITCH> G;
+      G.init(u);
+      match_one(u, G, f, b, i, age, pos, pr, pc, feat);
+      atomicAdd(fallbacks, 1ull);
+    }
     k = DYN ? atomicAdd(&next, 1) : k + THREADS;
     if (k < n1) {
       i = list[k];

@@ -284,6 +284,13 @@ class BatchTracker:
         check(self._lib.gbt_get_tuning(self._ensure(), knob, ctypes.byref(v)), self._ctx)
         return v.value
 
+    def tile_fallbacks(self):
+        """Particles the slim-margin tiled matcher matched again from global
+        memory, over the frames run so far (test and diagnostic hook)."""
+        v = ctypes.c_int64()
+        check(self._lib.gbt_test_tile_fallbacks(self._ensure(), ctypes.byref(v)), self._ctx)
+        return v.value
+
     def kernels_per_frame(self):
         n = ctypes.c_int32()
         check(self._lib.gbt_kernels_per_frame(self._ensure(), ctypes.byref(n)), self._ctx)

@@ -169,6 +169,12 @@ int gbt_sync(gbt_ctx* ctx);
  * by TMA (another matcher variant, or no tensor maps). */
 int gbt_test_withhold_tile_copies(gbt_ctx* ctx, int32_t enable);
 
+/* Test hook (no reference counterpart): the number of particles the tiled
+ * matcher with slim margins (GBT_TUNE_MATCH_TILE 4..6) has matched again from
+ * global memory because their descent would have left the staged tile, summed
+ * over the context's frames so far; waits for queued work. */
+int gbt_test_tile_fallbacks(gbt_ctx* ctx, int64_t* count);
+
 /* The CUDA stream (cudaStream_t) that follows the context's work: after every
  * call that queues work it waits for all of that work, so an event recorded
  * on it (or work queued on it) comes after the frames queued so far, and input
@@ -296,12 +302,16 @@ int gbt_checkpoint_load(gbt_ctx* ctx, const void* buf, size_t len);
  * GBT_TUNE_BLUR_ROWS: height of the strip one warp walks in the BC2S blur.
  * GBT_TUNE_MATCH_TILE (matcher 0 only): 0 = 256 threads per tile CTA, each
  * taking every 256th particle of the tile; 1 / 2 / 3 = 128 / 64 / 256 threads
- * taking the tile's particles one at a time from a shared counter.  The package's
- * autotuner (cuimg_gb300/autotune.py) times the settings on the caller's
- * workload and caches the winner. */
+ * taking the tile's particles one at a time from a shared counter; 4 / 5 / 6 =
+ * 128 / 256 / 192 threads likewise, with the tile staged with slim margins (14
+ * rows and 16 columns instead of 26 and 32, so more CTAs fit on an SM; the few
+ * particles whose descent would leave the staged area are matched again from
+ * global memory); 6 is the default.  The package's autotuner
+ * (cuimg_gb300/autotune.py) times the settings on the caller's workload and
+ * caches the winner. */
 #define GBT_TUNE_MATCHER 0
 #define GBT_TUNE_BLUR_ROWS 1   /* rows per warp strip of the BC2S blur: 16, 32 or 64 */
-#define GBT_TUNE_MATCH_TILE 2  /* tiled matcher CTA shape: 0..3 */
+#define GBT_TUNE_MATCH_TILE 2  /* tiled matcher CTA shape and staged margins: 0..6 */
 int gbt_set_tuning(gbt_ctx* ctx, int32_t knob, int32_t value);
 int gbt_get_tuning(gbt_ctx* ctx, int32_t knob, int32_t* value);
 

@@ -46,14 +46,18 @@ def test_gpu_matches_reference_golden(case):
     tr.close()
 
 
-def _compare_run(rows, cols, L, n, seed, detf=10, filtf=1, graphs=False, matcher=None, blur_rows=None):
+def _compare_run(rows, cols, L, n, seed, detf=10, filtf=1, graphs=False, matcher=None, blur_rows=None,
+                 match_tile=None, frames=None, stats=None):
     from cuimg_gb300 import synth
-    frames = synth.frames(seed, rows, cols, n)
+    if frames is None:
+        frames = synth.frames(seed, rows, cols, n)
     tr = _gpu_tracker(rows, cols, L, 20, detf, filtf, graphs)
     if matcher is not None:
         tr.set_tuning(0, matcher)
     if blur_rows is not None:
         tr.set_tuning(1, blur_rows)
+    if match_tile is not None:
+        tr.set_tuning(2, match_tile)
     o = tracker_oracle(rows, cols, L, 20, detf, filtf)
     for t in range(n):
         tr.run(frames[t])
@@ -61,6 +65,8 @@ def _compare_run(rows, cols, L, n, seed, detf=10, filtf=1, graphs=False, matcher
         bad = diff_snapshots(snapshot(o, L), tr.snapshot(), detector_frame=(t % detf == 0))
         assert not bad, "frame %d: %s" % (t, bad)
     total = tr.nparticles()
+    if stats is not None:
+        stats["fallbacks"] = tr.tile_fallbacks()
     tr.close()
     o.destroy()
     return total
@@ -120,6 +126,41 @@ def test_gpu_matches_oracle_1080p():
 @pytest.mark.parametrize("matcher", [0, 1, 2, 3])
 def test_matcher_variants_match_oracle(matcher):
     _compare_run(480, 640, 3, 14, 6, detf=5, matcher=matcher)
+
+
+@pytest.mark.parametrize("match_tile", range(7))
+def test_tile_shapes_match_oracle(match_tile):
+    # Every CTA shape of the tiled matcher, with full (0..3) and slim (4..6)
+    # staged margins.
+    stats = {}
+    _compare_run(480, 640, 3, 12, 6, detf=5, matcher=0, match_tile=match_tile, stats=stats)
+    if match_tile < 4:
+        assert stats["fallbacks"] == 0
+
+
+def _jittered_frames(seed, rows, cols, n, amp):
+    """A synthetic scene shifted by a random offset of up to `amp` pixels in
+    each axis on every frame, so that predictions miss and descents run long."""
+    from cuimg_gb300 import synth
+    base = synth.frames(seed, rows + 2 * amp, cols + 2 * amp, 1)[0]
+    rng = np.random.default_rng(seed)
+    out = np.empty((n, rows, cols), np.uint8)
+    for t in range(n):
+        dy, dx = rng.integers(0, 2 * amp + 1, size=2)
+        out[t] = base[dy:dy + rows, dx:dx + cols]
+    return out
+
+
+@pytest.mark.parametrize("match_tile", [4, 5, 6])
+def test_slim_tile_fallbacks_match_oracle(match_tile):
+    # Long descents: the particles whose descent leaves the slim staged margins
+    # are matched again from global memory, with the oracle's results.
+    rows, cols, L, n = 480, 640, 3, 10
+    stats = {}
+    frames = _jittered_frames(41, rows, cols, n, 9)
+    assert _compare_run(rows, cols, L, n, 41, detf=2, matcher=0, match_tile=match_tile, frames=frames,
+                        stats=stats) > 0
+    assert stats["fallbacks"] > 0
 
 
 @pytest.mark.parametrize("blur_rows", [16, 32, 64])
