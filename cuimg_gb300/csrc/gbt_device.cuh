@@ -89,6 +89,9 @@ struct Unit {
 // Frame ingest of one stream for the next frame: mode 0 = the gray frame is
 // already in level 0; 1 = interleaved RGB at `rgb`, track channel 0 (get_x,
 // dsl/get_comp.h:105); 2 = the same, BT.601 luma (77 R + 150 G + 29 B + 128) / 256.
+// How k_pyramid gets a stream's level 0: mode 0 = already in the unit's image;
+// 1 / 2 = from interleaved RGB at `rgb` (channel 0 / BT.601 luma); 3 = from a
+// gray frame in device memory at `rgb` (the name covers both sources).
 struct Ingest {
   const uint8_t* rgb;
   long long pitch;

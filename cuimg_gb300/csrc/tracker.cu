@@ -72,7 +72,13 @@ struct Group {
   int* d_bin_prefix = nullptr;
   int* d_cap_table = nullptr;  // particle-capacity chunks per unit (trajectories)
   Ingest* d_ingest = nullptr;   // per stream: how k_pyramid gets level 0
-  Ingest* h_ingest = nullptr;   // pinned host copy of what d_ingest holds
+  // Pinned host tables for d_ingest, INGEST_RING of them: a changed table is
+  // written into the next one, whose upload to d_ingest has completed (its
+  // event), so that per-frame source pointers need no host synchronisation.
+  Ingest* h_ingest_ring = nullptr;
+  Ingest* h_ingest = nullptr;   // the table being edited / last uploaded
+  int ingest_slot = 0;
+  cudaEvent_t ingest_ev[4] = {};
   bool ingest_dirty = true;
   int rgb_mode = GBT_RGB_CHANNEL0;
   int traj_T = 0;              // trajectory history length, 0 = off
@@ -218,7 +224,9 @@ static void free_ctx(Group* ctx) {
   for (void* p : ctx->allocs) cudaFree(p);
   for (auto& s : ctx->streams)
     if (s.pinned) cudaFreeHost(s.pinned);
-  if (ctx->h_ingest) cudaFreeHost(ctx->h_ingest);
+  if (ctx->h_ingest_ring) cudaFreeHost(ctx->h_ingest_ring);
+  for (cudaEvent_t e : ctx->ingest_ev)
+    if (e) cudaEventDestroy(e);
   for (cudaEvent_t e : {ctx->ev_front, ctx->ev_back[0], ctx->ev_back[1]})
     if (e) cudaEventDestroy(e);
   if (ctx->pre) cudaStreamDestroy(ctx->pre);
@@ -502,8 +510,10 @@ static int build(Group* ctx, const gbt_config* cfgs, int nstreams) {
     CK(cudaMallocHost((void**)&s.pinned, s.pinned_bytes));
   }
   if ((r = dalloc_t(ctx, &ctx->d_ingest, nstreams))) return r;
-  CK(cudaMallocHost((void**)&ctx->h_ingest, sizeof(Ingest) * nstreams));
-  memset(ctx->h_ingest, 0, sizeof(Ingest) * nstreams);
+  CK(cudaMallocHost((void**)&ctx->h_ingest_ring, sizeof(Ingest) * nstreams * 4));
+  memset(ctx->h_ingest_ring, 0, sizeof(Ingest) * nstreams * 4);
+  ctx->h_ingest = ctx->h_ingest_ring;
+  for (cudaEvent_t& e : ctx->ingest_ev) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
   CK(cudaDeviceSynchronize());
   return GBT_OK;
 }
@@ -899,20 +909,26 @@ static int grp_get_tuning(Group* ctx, int32_t knob, int32_t* value) {
   return GBT_E_INVALID;
 }
 
-// Uploads the per-stream ingest modes when they changed (ordered on the
-// context stream before the frame's kernels).
-static int set_ingest(Group* ctx, size_t s, int mode) {
-  StreamInfo& si = ctx->streams[s];
-  Ingest want{mode ? si.d_rgb : nullptr, mode ? si.rgb_pitch : 0, mode, 0};
-  Ingest& have = ctx->h_ingest[s];
-  if (have.rgb != want.rgb || have.pitch != want.pitch || have.mode != want.mode) {
-    if (!ctx->ingest_dirty) {  // h_ingest may feed a copy in flight, d_ingest a pyramid
-      int r = sync_all(ctx);
-      if (r) return r;
-    }
-    have = want;
+// Sets stream s's ingest (mode, and the source for modes 1 - 3) for the next
+// frame.  d_ingest is rewritten on the front stream before the frame's
+// kernels, after every earlier frame's pyramid, so only the host table needs
+// care: once uploaded it may still feed a copy in flight, so a change after an
+// upload goes into the next table of the ring.
+static int set_ingest(Group* ctx, size_t s, int mode, const uint8_t* src, int64_t pitch) {
+  const Ingest want{src, mode ? (long long)pitch : 0, mode, 0};
+  const Ingest& cur = ctx->h_ingest[s];
+  if (cur.rgb == want.rgb && cur.pitch == want.pitch && cur.mode == want.mode) return GBT_OK;
+  if (!ctx->ingest_dirty) {
+    const size_t n = ctx->streams.size();
+    const int next = (ctx->ingest_slot + 1) % 4;
+    CK(cudaEventSynchronize(ctx->ingest_ev[next]));  // its last upload (long done, as a rule)
+    Ingest* t = ctx->h_ingest_ring + (size_t)next * n;
+    memcpy(t, ctx->h_ingest, sizeof(Ingest) * n);
+    ctx->h_ingest = t;
+    ctx->ingest_slot = next;
     ctx->ingest_dirty = true;
   }
+  ctx->h_ingest[s] = want;
   return GBT_OK;
 }
 
@@ -920,6 +936,7 @@ static int flush_ingest(Group* ctx) {
   if (ctx->ingest_dirty) {
     CK(cudaMemcpyAsync(ctx->d_ingest, ctx->h_ingest, sizeof(Ingest) * ctx->streams.size(), cudaMemcpyHostToDevice,
                        front_stream(ctx)));
+    CK(cudaEventRecord(ctx->ingest_ev[ctx->ingest_slot], front_stream(ctx)));
     ctx->ingest_dirty = false;
   }
   return GBT_OK;
@@ -967,7 +984,7 @@ static int grp_run_resident(Group* ctx, cudaEvent_t user) {
   if (r0) return r0;
   if (user) CK(cudaStreamWaitEvent(front_stream(ctx), user, 0));
   for (size_t s = 0; s < ctx->streams.size(); s++) {
-    int r = set_ingest(ctx, s, 0);
+    int r = set_ingest(ctx, s, 0, nullptr, 0);
     if (r) return r;
   }
   int r = flush_ingest(ctx);
@@ -986,11 +1003,16 @@ static int grp_run(Group* ctx, const uint8_t* const* frames, const int64_t* pitc
     const Unit u = unit_view(ctx, si.unit0, ctx->host_frame & 1);
     const uint8_t* src = frames[s];
     int mode = 0;
+    const uint8_t* isrc = nullptr;  // the pyramid's source for modes 1 - 3
+    int64_t ipitch = 0;
     if (!src) return set_err(ctx, GBT_E_INVALID, "frame %zu is NULL", s);
     if (location == GBT_FRAMES_DEVICE) {
       int64_t p = pitches ? pitches[s] : u.W;
       if (p < u.W) return set_err(ctx, GBT_E_INVALID, "pitch %lld < cols %d", (long long)p, u.W);
-      CK(cudaMemcpy2DAsync(u.img, u.ipitch, src, p, u.W, u.H, cudaMemcpyDeviceToDevice, in));
+      // Read by the frame's pyramid kernel straight from the caller's buffer.
+      mode = 3;
+      isrc = src;
+      ipitch = p;
     } else if (location == GBT_FRAMES_HOST) {
       int64_t p = pitches ? pitches[s] : u.W;
       if (p < u.W) return set_err(ctx, GBT_E_INVALID, "pitch %lld < cols %d", (long long)p, u.W);
@@ -1009,14 +1031,16 @@ static int grp_run(Group* ctx, const uint8_t* const* frames, const int64_t* pitc
       const int64_t row = (int64_t)u.W * 3;
       int64_t p = pitches ? pitches[s] : row;
       if (p < row) return set_err(ctx, GBT_E_INVALID, "pitch %lld too small for RGB", (long long)p);
-      if (!si.d_rgb) {
-        si.rgb_pitch = (row + 15) / 16 * 16;
-        int r = dalloc(ctx, (void**)&si.d_rgb, (size_t)si.rgb_pitch * u.H, false);
-        if (r) return r;
-      }
       if (location == GBT_FRAMES_DEVICE_RGB) {
-        CK(cudaMemcpy2DAsync(si.d_rgb, si.rgb_pitch, src, p, row, u.H, cudaMemcpyDeviceToDevice, in));
+        // Read by the frame's pyramid kernel straight from the caller's buffer.
+        isrc = src;
+        ipitch = p;
       } else {
+        if (!si.d_rgb) {
+          si.rgb_pitch = (row + 15) / 16 * 16;
+          int r = dalloc(ctx, (void**)&si.d_rgb, (size_t)si.rgb_pitch * u.H, false);
+          if (r) return r;
+        }
         cudaPointerAttributes at;
         bool pinned = cudaPointerGetAttributes(&at, src) == cudaSuccess && at.type == cudaMemoryTypeHost;
         cudaGetLastError();
@@ -1028,12 +1052,14 @@ static int grp_run(Group* ctx, const uint8_t* const* frames, const int64_t* pitc
           p = row;
         }
         CK(cudaMemcpy2DAsync(si.d_rgb, si.rgb_pitch, src, p, row, u.H, cudaMemcpyHostToDevice, in));
+        isrc = si.d_rgb;
+        ipitch = si.rgb_pitch;
       }
       mode = ctx->rgb_mode == GBT_RGB_BT601 ? 2 : 1;
     } else {
       return set_err(ctx, GBT_E_INVALID, "bad frame location %d", location);
     }
-    int r = set_ingest(ctx, s, mode);
+    int r = set_ingest(ctx, s, mode, isrc, ipitch);
     if (r) return r;
   }
   int r = flush_ingest(ctx);

@@ -68,7 +68,31 @@ __global__ void __launch_bounds__(256) k_pyramid(const Unit* __restrict__ units,
   const int tw = (B.W + PYR_TC - 1) / PYR_TC;
   const int R0 = (local / tw) * PYR_TR, C0 = (local % tw) * PYR_TC;
 
-  if (in.mode != 0) {
+  if (in.mode == 3) {
+    // Fused ingest of a gray frame in device memory: level 0 copied into the
+    // unit's image and the shared tile (16 bytes at a time where the source
+    // chunk is aligned).
+    for (int v = threadIdx.x; v < PYR_TR * (PYR_TC / 16); v += blockDim.x) {
+      const int r = v / (PYR_TC / 16), c16 = (v % (PYR_TC / 16)) * 16;
+      const int gr = R0 + r, gc = C0 + c16;
+      uint8_t* d = &sm[0][r * PYR_TC + c16];
+      const uint8_t* src = in.rgb + (size_t)gr * in.pitch + gc;
+      uint8_t* dst = B.img + (size_t)gr * B.ipitch + gc;
+      if (gr < B.H && gc + 16 <= B.W && ((uintptr_t)src & 15) == 0) {
+        const uint4 x = *(const uint4*)src;
+        *(uint4*)d = x;
+        *(uint4*)dst = x;
+      } else {
+        for (int j = 0; j < 16; j++) {
+          const bool in_img = gr < B.H && gc + j < B.W;
+          const uint8_t g = in_img ? src[j] : 0;
+          d[j] = g;
+          if (in_img) dst[j] = g;
+        }
+      }
+    }
+    if (nlev <= 0) return;
+  } else if (in.mode != 0) {
     // Fused ingest: RGB -> gray into level 0 and the shared tile.
     for (int v = threadIdx.x; v < PYR_TR * PYR_TC; v += blockDim.x) {
       const int r = v / PYR_TC, c = v % PYR_TC, gr = R0 + r, gc = C0 + c;

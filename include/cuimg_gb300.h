@@ -116,7 +116,11 @@ int gbt_last_error(gbt_ctx* ctx, char* buf, size_t len);
 /* Frame input.  `frames[i]` is stream i's gray uint8 frame with row pitch
  * `pitches[i]` bytes; `location` says where the pointers live.  With
  * GBT_FRAMES_HOST the frames are staged through the context's pinned buffers
- * (host copy + one H2D copy per stream, ordered on the context stream).
+ * (host copy + one H2D copy per stream, ordered on the context stream).  With
+ * GBT_FRAMES_DEVICE (and GBT_FRAMES_DEVICE_RGB) the frame's first kernel reads
+ * the caller's buffers directly, with no copy: they must hold the frame when
+ * the context's streams reach it and stay unchanged until the frame is done
+ * (gbt_sync, or an event recorded on gbt_stream after this call).
  * Replaces tracker<F>::run(const I& in) (tracker.hpp:72-80). */
 #define GBT_FRAMES_HOST 0
 #define GBT_FRAMES_DEVICE 1
