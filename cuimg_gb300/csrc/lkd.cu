@@ -324,6 +324,21 @@ struct Grid {
   __device__ __forceinline__ bool holds(const Bil& s) const {
     return s.y0 >= y0 && s.y0 + s.dy < y0 + GH && s.x0 >= x0 && s.x0 + s.dx < x0 + GW;
   }
+  // Adds v00 .. v11 at the sample's four taps.
+  __device__ __forceinline__ void add4(float* img, const Bil& s, float v00, float v10, float v01, float v11) const {
+    if (holds(s)) {
+      float* b = c + (s.y0 - y0) * GW + (s.x0 - x0);
+      atomicAdd(b, v00);
+      atomicAdd(b + s.dy * GW, v10);
+      atomicAdd(b + s.dx, v01);
+      atomicAdd(b + s.dy * GW + s.dx, v11);
+    } else {
+      atomicAdd(img + stride * s.i00, v00);
+      atomicAdd(img + stride * s.i10, v10);
+      atomicAdd(img + stride * s.i01, v01);
+      atomicAdd(img + stride * s.i11, v11);
+    }
+  }
   __device__ __forceinline__ void add(float* img, const Bil& s, float v) const {
     if (holds(s)) {
       float* b = c + (s.y0 - y0) * GW + (s.x0 - x0);
@@ -458,6 +473,25 @@ __global__ void __launch_bounds__(32 * WARPS, BW_MINB) k_lkd_backward(const Lvl*
     float dg0[PPL], dg1[PPL], dT[PPL];
 #pragma unroll
     for (int k = 0; k < PPL; k++) dg0[k] = dg1[k] = dT[k] = 0.f;
+    // The residual samples' adjoint goes to dB at each step's window taps.
+    // Every window pixel of a step shares the centre's integer position, and
+    // the iterates converge, so consecutive steps mostly share their taps:
+    // the four tap contributions of each window pixel are summed in registers
+    // (acc) while the window's integer position stays (wacc), and scattered
+    // once when it changes and after the last step.
+    Win wacc;
+    wacc.y0 = INT_MIN;
+    float acc00[PPL], acc10[PPL], acc01[PPL], acc11[PPL];
+    auto scatter_acc = [&]() {
+#pragma unroll
+      for (int kk = 0; kk < PPL; kk++) {
+        const int i = lane + 32 * kk;
+        if (i < n) {
+          const Bil sb = bil_win(e.H, e.W, wacc, i / ws - hws, i % ws - hws);
+          gB.add4(e.dB, sb, acc00[kk], acc10[kk], acc01[kk], acc11[kk]);
+        }
+      }
+    };
     for (int k = K - 1; k >= 0; k--) {
       const float4 vk = hist[l * HS + k];  // v_k and b_k of the forward
       const float d0 = dv0, d1 = dv1;                       // adjoint of v_{k+1}
@@ -465,6 +499,12 @@ __global__ void __launch_bounds__(32 * WARPS, BW_MINB) k_lkd_backward(const Lvl*
       const float b0 = vk.z, b1 = vk.w;
       float pv0 = 0.f, pv1 = 0.f;
       const Win wk = win_at(e.H, e.W, vk.x, vk.y, hws);
+      if (wk.y0 != wacc.y0 || wk.x0 != wacc.x0) {  // warp-uniform
+        if (wacc.y0 != INT_MIN) scatter_acc();
+        wacc = wk;
+#pragma unroll
+        for (int kk = 0; kk < PPL; kk++) acc00[kk] = acc10[kk] = acc01[kk] = acc11[kk] = 0.f;
+      }
 #pragma unroll
       for (int kk = 0; kk < PPL; kk++) {
         const int i = lane + 32 * kk;
@@ -477,7 +517,10 @@ __global__ void __launch_bounds__(32 * WARPS, BW_MINB) k_lkd_backward(const Lvl*
           dg0[kk] += res * db0;
           dg1[kk] += res * db1;
           dT[kk] += dres;
-          gB.add(e.dB, sb, -dres);
+          acc00[kk] -= wk.w00 * dres;
+          acc10[kk] -= wk.w10 * dres;
+          acc01[kk] -= wk.w01 * dres;
+          acc11[kk] -= wk.w11 * dres;
           pv0 -= dres * gb.x;
           pv1 -= dres * gb.y;
         }
@@ -489,6 +532,7 @@ __global__ void __launch_bounds__(32 * WARPS, BW_MINB) k_lkd_backward(const Lvl*
       dM10 += d1 * b0;
       dM11 += d1 * b1;
     }
+    if (wacc.y0 != INT_MIN) scatter_acc();
     // dG = -M dM M (M symmetric); then dg += (dG + dG^T) g.
     const float t00 = dM00 * S.M00 + dM01 * S.M01, t01 = dM00 * S.M01 + dM01 * S.M11;
     const float t10 = dM10 * S.M00 + dM11 * S.M01, t11 = dM10 * S.M01 + dM11 * S.M11;
