@@ -156,8 +156,10 @@ struct __align__(8) WarpSmem {
 // iterative_lk_match_5x5::match (pyrlk_tracker.hpp:165-334) at level u of the
 // point p with prediction transform ptr, by the whole warp.  Returns false
 // when the matcher rejects (tr = (-1, -1), err = 1000 as the reference).  The
-// final error is computed only when `want_err` (get_flow_at ignores it).
-__device__ bool lk_match(const PUnit& u, int par, WarpSmem& S, float py, float px, float ptr_y, float ptr_x,
+// final error is computed only when `want_err` (get_flow_at ignores it).  Not
+// inlined: k_pk_match calls it for the upper scales and for the particle's
+// own, and one copy of its long exact-order body keeps the kernel's code small.
+__device__ __noinline__ bool lk_match(const PUnit& u, int par, WarpSmem& S, float py, float px, float ptr_y, float ptr_x,
                          bool want_err, float& tr_y, float& tr_x, float& err) {
   const int lane = threadIdx.x & 31;
   const int prev = par ^ 1;
@@ -387,7 +389,7 @@ __global__ void k_pk_prefix(const PState* __restrict__ st, int nunits, int* __re
 }
 
 // pyrlk_match_particles_kernel (:677-769) for every slot, a warp per slot.
-__global__ void __launch_bounds__(32 * MW) k_pk_match(PUnit* __restrict__ units, PState* __restrict__ st, int nunits,
+__global__ void __launch_bounds__(32 * MW, 3) k_pk_match(PUnit* __restrict__ units, PState* __restrict__ st, int nunits,
                                                      const int* __restrict__ prefix, int par) {
   __shared__ WarpSmem smem[MW];
   WarpSmem& S = smem[threadIdx.x >> 5];
