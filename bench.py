@@ -220,6 +220,50 @@ def run_cpu_streams(nstreams, steps, preroll):
     return workers * steps / wall, wall, workers, float(np.mean([r[2] for r in res]))
 
 
+def _cpu_pyrlk_worker(i, rows, cols, nscales, preroll, nframes, barrier, out):
+    """One stream of the oracle's LK tracker (one thread) in its own process:
+    `preroll` frames untimed, then `nframes` timed, started together by a
+    barrier shared by all streams; reports the time of the timed calls."""
+    os.environ["OMP_NUM_THREADS"] = "1"
+    sys.path.insert(0, ROOT)
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from cuimg_gb300 import synth
+    from oracle_lib import PyrlkLib
+    frames = synth.frames(900 + i, rows, cols, preroll + nframes)  # the GPU row's clips (gen_clips, seeds 900 + i)
+    o = PyrlkLib("oracle", rows, cols, nscales, THRESHOLD, DET_FREQ, FILT_FREQ)
+    for t in range(preroll):
+        o.run(frames[t])
+    barrier.wait()
+    t0 = time.perf_counter()
+    for t in range(preroll, preroll + nframes):
+        o.run(frames[t])
+    dt = time.perf_counter() - t0
+    barrier.wait()
+    out.put((i, dt))
+    o.destroy()
+
+
+def run_cpu_pyrlk_streams(nstreams, rows, cols, nscales, preroll, steps):
+    """The oracle's LK tracker on `nstreams` streams at once, one process
+    and core per stream; returns frames/s over all streams, the slowest
+    stream's timed seconds and the cores used."""
+    import multiprocessing as mp
+    subprocess.check_call(["make", "-s", "-C", os.path.join(ROOT, "oracle")])
+    workers = max(1, min(nstreams, os.cpu_count() or 1))
+    ctx = mp.get_context("spawn")
+    barrier = ctx.Barrier(workers)
+    out = ctx.Queue()
+    procs = [ctx.Process(target=_cpu_pyrlk_worker, args=(i, rows, cols, nscales, preroll, steps, barrier, out))
+             for i in range(workers)]
+    for pr in procs:
+        pr.start()
+    res = [out.get() for _ in procs]
+    for pr in procs:
+        pr.join()
+    wall = max(r[1] for r in res)
+    return workers * steps / wall, wall, workers
+
+
 def dist_setup():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -637,6 +681,15 @@ def measure_extras(args, dev, local, peak):
     out["batched_uneven_64"] = measure_uneven(dev, local)
     out["combined_4k"] = measure_combined_4k(dev)
     out["lk_tracker"] = measure_lk_tracker(dev)
+    if local == 0 and not args.no_cpu:
+        # The same 640x480 streams through the oracle's LK tracker (a
+        # restatement of pyrlk_cpu, bit-exact with it), one process and core
+        # per stream: 40 frames untimed, then one detector period timed.
+        fps, wall, cores = run_cpu_pyrlk_streams(16, 480, 640, 3, 40, DET_FREQ)
+        out["lk_tracker"]["640x480_x16"]["cpu_baseline"] = {
+            "frames_per_s": round(fps, 2), "cores": cores, "kind": "port", "cpu": cpu_model(),
+            "sample": "%d frames of each of %d streams after 40 untimed frames (%.1f s wall), one process and core "
+                      "per stream" % (DET_FREQ, cores, wall)}
     return out
 
 
