@@ -472,6 +472,18 @@ __device__ __forceinline__ bool gd_match(const Unit& u, const FeatT& F, const ui
   return ok;
 }
 
+// Asks L1 for the level-image rows r - 3 .. r + 3 around column c (clamped
+// into the image): the contrast test of a match near (r, c) then reads L1
+// instead of waiting on L2.  A hint only; it changes no result.
+__device__ __forceinline__ void prefetch_contrast(const Unit& u, int r, int c) {
+  const int cc = clampi(c, 0, u.W - 1);
+#pragma unroll
+  for (int d = -3; d <= 3; d++) {
+    const uint8_t* a = u.img + (size_t)clampi(r + d, 0, u.H - 1) * u.ipitch + cc;
+    asm volatile("prefetch.global.L1 [%0];" ::"l"(a));
+  }
+}
+
 // contrast_kernel (tracking_strategies.hpp:101-135), clamped level reads.
 __device__ __forceinline__ int contrast_at(const Unit& u, int r, int c) {
   const int d = 2;
@@ -527,6 +539,7 @@ __device__ __forceinline__ bool match_one(const Unit& u, const FeatT& F, int f, 
   int best = init;
   bool ok = gd_match<false>(u, F, feat, pr, pc, best, d1r, d1c);
   if (ok) {
+    prefetch_contrast(u, pr + d1r, pc + d1c);  // step 2 rarely moves far from step 1's match
     best = (d1r != 0 || d1c != 0) ? best + F.s1_part(feat, pr + d1r, pc + d1c, u.fpitch) : init;
     ok = gd_match<true>(u, F, feat, pr + d1r, pc + d1c, best, d2r, d2c);
   }
