@@ -316,7 +316,10 @@ __global__ void __launch_bounds__(32 * WARPS) k_lkd_forward(const Lvl* __restric
 // (atomics there), added to the level image once at the end; samples whose
 // taps fall outside the box go to the image directly.
 constexpr int GRID_CELLS = 1024;
-constexpr int BW_MINB = 5;  // backward CTAs per SM the registers are sized for
+// Backward CTAs per SM the registers are sized for: five (96 registers) for
+// small windows, four (128) from 9 x 9 up, where 96 registers spill the
+// per-pixel accumulators of the window's three pixels per lane.
+constexpr int bw_minb(int ws) { return ws >= 9 ? 4 : 5; }
 struct Grid {
   float* c;        // cells, row-major GW per row
   int y0, x0, GH, GW;
@@ -382,8 +385,72 @@ __device__ __forceinline__ void grid_flush(const Grid& g, float* img, int W) {
   __syncwarp();
 }
 
+// Vector reductions (sm_90 and later): four or two consecutive floats in one
+// L2 operation; the address must be 16- / 8-byte aligned.
+__device__ __forceinline__ void red_add_v4(float* p, float a, float b, float c, float d) {
+  asm volatile("red.global.add.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(p), "f"(a), "f"(b), "f"(c), "f"(d) : "memory");
+}
+__device__ __forceinline__ void red_add_v2(float* p, float a, float b) {
+  asm volatile("red.global.add.v2.f32 [%0], {%1, %2};" ::"l"(p), "f"(a), "f"(b) : "memory");
+}
+
+// The box's cell (row, col), zero outside the box.
+__device__ __forceinline__ float grid_cell(const Grid& g, int row, int col) {
+  return (col >= 0 && col < g.GW) ? g.c[row * g.GW + col] : 0.f;
+}
+
+// grid_flush of a one-float-per-pixel image (stride 1) with one red.v4 per
+// 16-byte-aligned run of four pixels of a box row (cells outside the box add
+// zero; runs of four zeros are skipped): about a third of the reductions of
+// one per cell.  Images whose rows or base are not 16-byte aligned take
+// grid_flush.
+__device__ __forceinline__ void grid_flush_v4(const Grid& g, float* img, int W) {
+  if ((W & 3) != 0 || (((unsigned long long)img) & 15) != 0) {
+    grid_flush(g, img, W);
+    return;
+  }
+  __syncwarp();
+  const int q0 = g.x0 >> 2, nq = ((g.x0 + g.GW - 1) >> 2) - q0 + 1;
+  for (int it = threadIdx.x & 31; it < g.GH * nq; it += 32) {
+    const int row = it / nq, x = 4 * (q0 + it % nq), col = x - g.x0;
+    const float a = grid_cell(g, row, col), b = grid_cell(g, row, col + 1);
+    const float c = grid_cell(g, row, col + 2), d = grid_cell(g, row, col + 3);
+    if (a != 0.f || b != 0.f || c != 0.f || d != 0.f) red_add_v4(img + (size_t)(g.y0 + row) * W + x, a, b, c, d);
+  }
+  __syncwarp();
+}
+
+// Both components of a float2 image (gx: .x, gy: .y, the same box) in one
+// pass: one red.v4 per 16-byte-aligned pair of pixels, or one red.v2 per
+// pixel where the image's rows or base allow only 8-byte alignment.
+__device__ __forceinline__ void grid_flush_pair(const Grid& gx, const Grid& gy, float2* img, int W) {
+  const unsigned long long a = (unsigned long long)img;
+  if ((a & 7) != 0) {
+    grid_flush(gx, (float*)img, W);
+    grid_flush(gy, (float*)img + 1, W);
+    return;
+  }
+  __syncwarp();
+  if ((W & 1) == 0 && (a & 15) == 0) {
+    const int p0 = gx.x0 >> 1, np = ((gx.x0 + gx.GW - 1) >> 1) - p0 + 1;
+    for (int it = threadIdx.x & 31; it < gx.GH * np; it += 32) {
+      const int row = it / np, x = 2 * (p0 + it % np), col = x - gx.x0;
+      const float u0 = grid_cell(gx, row, col), v0 = grid_cell(gy, row, col);
+      const float u1 = grid_cell(gx, row, col + 1), v1 = grid_cell(gy, row, col + 1);
+      if (u0 != 0.f || v0 != 0.f || u1 != 0.f || v1 != 0.f)
+        red_add_v4((float*)(img + (size_t)(gx.y0 + row) * W + x), u0, v0, u1, v1);
+    }
+  } else {
+    for (int k = threadIdx.x & 31; k < gx.GH * gx.GW; k += 32) {
+      const float u = gx.c[k], v = gy.c[k];
+      if (u != 0.f || v != 0.f) red_add_v2((float*)(img + (size_t)(gx.y0 + k / gx.GW) * W + gx.x0 + k % gx.GW), u, v);
+    }
+  }
+  __syncwarp();
+}
+
 template <int WS, bool TAPE>
-__global__ void __launch_bounds__(32 * WARPS, BW_MINB) k_lkd_backward(const Lvl* __restrict__ levels, int L, int /*window: WS*/, int K,
+__global__ void __launch_bounds__(32 * WARPS, bw_minb(WS)) k_lkd_backward(const Lvl* __restrict__ levels, int L, int /*window: WS*/, int K,
                                                              int npairs, int npts, const float* __restrict__ pts,
                                                              const float* __restrict__ u0,
                                                              const float* __restrict__ dloss, float* __restrict__ du0,
@@ -551,10 +618,9 @@ __global__ void __launch_bounds__(32 * WARPS, BW_MINB) k_lkd_backward(const Lvl*
         gA.add(e.dA, st, dT[kk]);
       }
     }
-    grid_flush(gA, e.dA, e.W);
-    grid_flush(gS0, (float*)e.dS, e.W);
-    grid_flush(gS1, (float*)e.dS + 1, e.W);
-    grid_flush(gB, e.dB, e.W);
+    grid_flush_v4(gA, e.dA, e.W);
+    grid_flush_pair(gS0, gS1, e.dS, e.W);
+    grid_flush_v4(gB, e.dB, e.W);
     // v_0 = q + d_init: the adjoint of d_init is dv.
     if (l + 1 < L) {
       dv0 *= 2.f;  // d_init(l) = 2 (v_K(l+1) - q(l+1))
