@@ -123,6 +123,37 @@ __device__ __forceinline__ float2 bil_grad(const float* img, const Bil& s) {
   float v00 = img[s.i00], v10 = img[s.i10], v01 = img[s.i01], v11 = img[s.i11];
   return make_float2((1.f - s.b) * (v10 - v00) + s.b * (v11 - v01), (1.f - s.a) * (v01 - v00) + s.a * (v11 - v10));
 }
+// The taps of a whole window: tap (i, j) = img(clamp(y0 - h + i),
+// clamp(x0 - h + j)) for i, j in [0, ws], staged once per window in the
+// warp's shared buffer tg (row-major, ws + 1 per row) by row loads.  Window
+// pixel (r, c) (0-based) then reads its four taps at tg[r (ws + 1) + c ..]:
+// they are the taps bil_win gives it, since bil_win clamps each tap
+// coordinate on its own.  A window of ws x ws samples needs (ws + 1)^2
+// distinct taps, not 4 ws^2 scattered loads.
+template <int WS>
+__device__ __forceinline__ void stage_taps(const float* img, int H, int W, const Win& w, float* tg) {
+  constexpr int TW = WS + 1, NT = TW * TW, h = WS / 2;
+  __syncwarp();  // every lane is done with the previous window's taps
+#pragma unroll
+  for (int k = 0; k < (NT + 31) / 32; k++) {
+    const int t = (threadIdx.x & 31) + 32 * k;
+    if (t < NT) {
+      int y = w.y0 - h + t / TW, x = w.x0 - h + t % TW;
+      if (!w.inner) {
+        y = min(max(y, 0), H - 1);
+        x = min(max(x, 0), W - 1);
+      }
+      tg[t] = img[(size_t)y * W + x];
+    }
+  }
+  __syncwarp();
+}
+// bil_val of the sample whose four taps start at p (row pitch TW).
+template <int TW>
+__device__ __forceinline__ float tap_val(const float* p, const Win& s) {
+  return s.w00 * p[0] + s.w10 * p[TW] + s.w01 * p[1] + s.w11 * p[TW + 1];
+}
+
 __device__ __forceinline__ void bil_scatter(float* img, const Bil& s, float v) {
   atomicAdd(img + s.i00, s.w00 * v);
   atomicAdd(img + s.i10, s.w10 * v);
@@ -196,19 +227,21 @@ __device__ __forceinline__ void level_setup(const Tmpl<PPL>& T, int n, float& M0
 }
 
 // One Gauss-Newton right-hand side b = sum g (T - B(v + o)).
+// tg: the warp's tap buffer ((ws + 1)^2 floats, stage_taps).
 template <int WS>
 __device__ __forceinline__ void rhs(const Lvl& e, int /*window: WS*/, const Tmpl<ppl_of(WS)>& T, float v0, float v1, float& b0,
-                                    float& b1) {
+                                    float& b1, float* tg) {
   constexpr int ws = WS, PPL = (WS * WS + 31) / 32;
   const int lane = threadIdx.x & 31, hws = ws / 2, n = ws * ws;
   b0 = 0.f;
   b1 = 0.f;
   const Win wv = win_at(e.H, e.W, v0, v1, hws);
+  stage_taps<WS>(e.B, e.H, e.W, wv, tg);
 #pragma unroll
   for (int k = 0; k < PPL; k++) {
     const int i = lane + 32 * k;
     if (i < n) {
-      const float res = T.a[k] - bil_val(e.B, bil_win(e.H, e.W, wv, i / ws - hws, i % ws - hws));
+      const float res = T.a[k] - tap_val<WS + 1>(tg + (i / ws) * (ws + 1) + i % ws, wv);
       b0 += T.g[k].x * res;
       b1 += T.g[k].y * res;
     }
@@ -220,7 +253,7 @@ __device__ __forceinline__ void rhs(const Lvl& e, int /*window: WS*/, const Tmpl
 // Forward of one point; fills the per-level setup and the iterate history.
 template <int WS>
 __device__ float point_forward(const Lvl* lv, int L, int /*window: WS*/, int K, float p0, float p1, float u0, float u1,
-                               Setup* su, float4* hist, int hs, float& vf0, float& vf1) {
+                               Setup* su, float4* hist, int hs, float& vf0, float& vf1, float* tg) {
   constexpr int ws = WS, PPL = (WS * WS + 31) / 32;
   const int n = ws * ws;
   const float top = level_scale(L - 1);
@@ -238,7 +271,7 @@ __device__ float point_forward(const Lvl* lv, int L, int /*window: WS*/, int K, 
     v1 = q1 + d1;
     for (int k = 0; k < K; k++) {
       float b0, b1;
-      rhs<WS>(e, ws, T, v0, v1, b0, b1);
+      rhs<WS>(e, ws, T, v0, v1, b0, b1, tg);
       if (hist) hist[l * hs + k] = make_float4(v0, v1, b0, b1);  // iterate and its right-hand side
       v0 += M00 * b0 + M01 * b1;
       v1 += M01 * b0 + M11 * b1;
@@ -291,6 +324,7 @@ __global__ void __launch_bounds__(32 * WARPS) k_lkd_forward(const Lvl* __restric
                                                             const float* __restrict__ u0, float* __restrict__ loss,
                                                             float* __restrict__ vfinal, void* __restrict__ tape) {
   constexpr int ws = WS;
+  __shared__ float tg_all[WARPS][(WS + 1) * (WS + 1)];  // each warp's window taps (stage_taps)
   const long long g = (long long)blockIdx.x * WARPS + (threadIdx.x >> 5);
   if (g >= (long long)npairs * npts) return;
   const int pair = (int)(g / npts);
@@ -300,7 +334,7 @@ __global__ void __launch_bounds__(32 * WARPS) k_lkd_forward(const Lvl* __restric
   TapeView t{nullptr, nullptr, nullptr};
   if (tape) t = tape_at(tape, g, L, K);
   float l = point_forward<WS>(levels + (size_t)pair * L, L, ws, K, pts[2 * g], pts[2 * g + 1], u0[2 * g],
-                               u0[2 * g + 1], t.su, t.hist, K + 1, vf0, vf1);
+                               u0[2 * g + 1], t.su, t.hist, K + 1, vf0, vf1, tg_all[threadIdx.x >> 5]);
   if ((threadIdx.x & 31) == 0) {
     loss[g] = l;
     vfinal[2 * g] = vf0;
@@ -460,7 +494,9 @@ __global__ void __launch_bounds__(32 * WARPS, bw_minb(WS)) k_lkd_backward(const 
   extern __shared__ float4 hist_dyn[];  // WARPS x L x (K + 1): the iterate history
   __shared__ float gB_all[WARPS][GRID_CELLS];                       // dB over the level's residual samples
   __shared__ float gT_all[WARPS][3][(MAXW + 1) * (MAXW + 1)];      // dA, dS.x, dS.y over the template
+  __shared__ float tg_all[WARPS][(WS + 1) * (WS + 1)];              // window taps of the replayed forward
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  float* tg = tg_all[warp];
   const long long gidx = (long long)blockIdx.x * WARPS + warp;
   if (gidx >= (long long)npairs * npts) return;
   const int pair = (int)(gidx / npts);
@@ -478,7 +514,7 @@ __global__ void __launch_bounds__(32 * WARPS, bw_minb(WS)) k_lkd_backward(const 
     vf0 = t.vf[0];
     vf1 = t.vf[1];
   } else {
-    point_forward<WS>(lv, L, ws, K, p0, p1, u0[2 * gidx], u0[2 * gidx + 1], su, hist, HS, vf0, vf1);
+    point_forward<WS>(lv, L, ws, K, p0, p1, u0[2 * gidx], u0[2 * gidx + 1], su, hist, HS, vf0, vf1, tg);
   }
   __syncwarp();
   const float w = dloss[gidx];
@@ -576,10 +612,11 @@ __global__ void __launch_bounds__(32 * WARPS, bw_minb(WS)) k_lkd_backward(const 
       for (int kk = 0; kk < PPL; kk++) {
         const int i = lane + 32 * kk;
         if (i < n) {
-          Bil sb = bil_win(e.H, e.W, wk, i / ws - hws, i % ws - hws);
-          const float2 g = T.g[kk];
-          const float res = T.a[kk] - bil_val(e.B, sb);
+          const Bil sb = bil_win(e.H, e.W, wk, i / ws - hws, i % ws - hws);
+          const float bv = bil_val(e.B, sb);
           const float2 gb = bil_grad(e.B, sb);
+          const float2 g = T.g[kk];
+          const float res = T.a[kk] - bv;
           const float dres = g.x * db0 + g.y * db1;
           dg0[kk] += res * db0;
           dg1[kk] += res * db1;
