@@ -692,11 +692,11 @@ static int enqueue_front(Group* ctx, int par, cudaStream_t st, int& n) {
   const int nstreams = (int)ctx->streams.size();
   const Unit* du = ctx->d_units_v[par];
   n = 0;
-  { PROF("k_pyramid"); k_pyramid<<<ctx->pyr_tiles[0], 256, 0, st>>>(du, ctx->d_stream_unit0, ctx->d_pyr_prefix[0], nstreams, 0, ctx->d_ingest); }
+  { PROF("k_pyramid"); k_pyramid<<<ctx->pyr_tiles[0], PYR_THREADS, 0, st>>>(du, ctx->d_stream_unit0, ctx->d_pyr_prefix[0], nstreams, 0, ctx->d_ingest); }
   n++;
   if (ctx->pyr_tiles[1] > 0) {
     PROF("k_pyramid5");
-    k_pyramid<<<ctx->pyr_tiles[1], 256, 0, st>>>(du, ctx->d_stream_unit0, ctx->d_pyr_prefix[1], nstreams, 5, ctx->d_ingest);
+    k_pyramid<<<ctx->pyr_tiles[1], PYR_THREADS, 0, st>>>(du, ctx->d_stream_unit0, ctx->d_pyr_prefix[1], nstreams, 5, ctx->d_ingest);
     n++;
   }
   {

@@ -35,10 +35,15 @@ __device__ __forceinline__ int block_prefix(bool pred, int* warp_tot, int& total
 
 // ---------------------------------------------------------------------------
 // Pyramid: mipmap_kernel (cuimg/gpu/mipmap.h:24-49) applied level after level,
-// out(p) = (a + b + c + d) / 4 over the 2x2 block at 2p.  One CTA turns a
-// 32 x 128 tile of level `base` into up to five coarser levels held in shared
-// memory, so each frame is read from HBM once.
-constexpr int PYR_TR = 32, PYR_TC = 128;
+// out(p) = (a + b + c + d) / 4 over the 2x2 block at 2p.  One CTA of 256
+// threads turns a 64 x 128 tile of level `base` into up to five coarser levels
+// held in shared memory, so each frame is read from HBM once.  A thread loads
+// two 16-byte chunks of the tile, both issued before either is stored, so that
+// twice the bytes are in flight while the CTA waits on memory; eight CTAs fit
+// on an SM (32 registers a thread).
+constexpr int PYR_TR = 64, PYR_TC = 128, PYR_THREADS = 256;
+constexpr int PYR_CPR = PYR_TC / 16, PYR_NCH = PYR_TR * PYR_CPR / PYR_THREADS;  // chunks per row / per thread
+static_assert(PYR_TR * PYR_CPR % PYR_THREADS == 0, "whole chunks per thread");
 
 // Four outputs (a + b + c + d) / 4 from 8 pixels of two rows (a, b: the upper
 // and lower rows' bytes).  The even and odd bytes of each 32-bit half go to
@@ -52,7 +57,7 @@ __device__ __forceinline__ uint32_t pyr_mean4(uint2 a, uint2 b) {
   return __byte_perm(pyr_mean2(a.x, b.x), pyr_mean2(a.y, b.y), 0x6420);
 }
 
-__global__ void __launch_bounds__(256) k_pyramid(const Unit* __restrict__ units,
+__global__ void __launch_bounds__(PYR_THREADS, 8) k_pyramid(const Unit* __restrict__ units,
                                                  const int* __restrict__ stream_unit0,
                                                  const int* __restrict__ tile_prefix, int nstreams, int base,
                                                  const Ingest* __restrict__ ingest) {
@@ -72,16 +77,26 @@ __global__ void __launch_bounds__(256) k_pyramid(const Unit* __restrict__ units,
     // Fused ingest of a gray frame in device memory: level 0 copied into the
     // unit's image and the shared tile (16 bytes at a time where the source
     // chunk is aligned).
-    for (int v = threadIdx.x; v < PYR_TR * (PYR_TC / 16); v += blockDim.x) {
-      const int r = v / (PYR_TC / 16), c16 = (v % (PYR_TC / 16)) * 16;
+    uint4 x[PYR_NCH];
+    bool vec[PYR_NCH];
+#pragma unroll
+    for (int k = 0; k < PYR_NCH; k++) {
+      const int v = threadIdx.x + PYR_THREADS * k, gr = R0 + v / PYR_CPR, gc = C0 + (v % PYR_CPR) * 16;
+      const uint8_t* src = in.rgb + (size_t)gr * in.pitch + gc;
+      vec[k] = gr < B.H && gc + 16 <= B.W && ((uintptr_t)src & 15) == 0;
+      if (vec[k]) x[k] = *(const uint4*)src;
+    }
+#pragma unroll
+    for (int k = 0; k < PYR_NCH; k++) {
+      const int v = threadIdx.x + PYR_THREADS * k;
+      const int r = v / PYR_CPR, c16 = (v % PYR_CPR) * 16;
       const int gr = R0 + r, gc = C0 + c16;
       uint8_t* d = &sm[0][r * PYR_TC + c16];
       const uint8_t* src = in.rgb + (size_t)gr * in.pitch + gc;
       uint8_t* dst = B.img + (size_t)gr * B.ipitch + gc;
-      if (gr < B.H && gc + 16 <= B.W && ((uintptr_t)src & 15) == 0) {
-        const uint4 x = *(const uint4*)src;
-        *(uint4*)d = x;
-        *(uint4*)dst = x;
+      if (vec[k]) {
+        *(uint4*)d = x[k];
+        *(uint4*)dst = x[k];
       } else {
         for (int j = 0; j < 16; j++) {
           const bool in_img = gr < B.H && gc + j < B.W;
@@ -107,12 +122,20 @@ __global__ void __launch_bounds__(256) k_pyramid(const Unit* __restrict__ units,
     if (nlev <= 0) return;
   } else {
     // Load the level-`base` tile.
-    for (int v = threadIdx.x; v < PYR_TR * (PYR_TC / 16); v += blockDim.x) {
-      int r = v / (PYR_TC / 16), c16 = (v % (PYR_TC / 16)) * 16;
-      int gr = R0 + r, gc = C0 + c16;
+    uint4 x[PYR_NCH];
+#pragma unroll
+    for (int k = 0; k < PYR_NCH; k++) {
+      const int v = threadIdx.x + PYR_THREADS * k, gr = R0 + v / PYR_CPR, gc = C0 + (v % PYR_CPR) * 16;
+      if (gr < B.H && gc + 16 <= B.W) x[k] = *(const uint4*)(B.img + (size_t)gr * B.ipitch + gc);
+    }
+#pragma unroll
+    for (int k = 0; k < PYR_NCH; k++) {
+      const int v = threadIdx.x + PYR_THREADS * k;
+      const int r = v / PYR_CPR, c16 = (v % PYR_CPR) * 16;
+      const int gr = R0 + r, gc = C0 + c16;
       uint8_t* d = &sm[0][r * PYR_TC + c16];
       if (gr < B.H && gc + 16 <= B.W) {
-        *(uint4*)d = *(const uint4*)(B.img + (size_t)gr * B.ipitch + gc);
+        *(uint4*)d = x[k];
       } else {
         for (int j = 0; j < 16; j++) d[j] = (gr < B.H && gc + j < B.W) ? B.img[(size_t)gr * B.ipitch + gc + j] : 0;
       }
