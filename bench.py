@@ -45,12 +45,13 @@ PER_PARTICLE_BYTES = 84  # state read/write, template read/write, sparse index
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one launch per
 # 1080p stream (4 scales), measured by ncu on launches over four 1080p streams
 # at steady state (k_match_tiled with its default 192-thread, slim-margin
-# tiles: 81.2 and 89.1 MB for two consecutive frames after 120 untimed ones;
+# tiles: 81.1 and 88.9 MB for two consecutive frames after 120 untimed ones;
 # k_match: 76.8 MB); a launch's traffic grows with the streams it covers.
 DRAM_BYTES_PER_STREAM = {"k_match_tiled": 21.3e6, "k_match": 19.2e6}
 # The unit that limits the tiled matcher and its utilisation in the same ncu
-# capture (l1tex__data_pipe_lsu_wavefronts: shared-memory byte gathers).
-LIMITER = {"k_match_tiled": ("L1 / shared-memory data pipe (byte gathers at the ring offsets)", 0.65)}
+# capture (l1tex__data_pipe_lsu_wavefronts: shared-memory byte gathers; 61.9%
+# and 70.1% of peak for the two frames).
+LIMITER = {"k_match_tiled": ("L1 / shared-memory data pipe (byte gathers at the ring offsets)", 0.66)}
 
 
 def pal(t, n):
