@@ -79,6 +79,7 @@ def _declare(lib):
     lib.gbt_input_slot.argtypes = [P, I32, ctypes.POINTER(P), ctypes.POINTER(ctypes.c_int64)]
     lib.gbt_use_graphs.argtypes = [P, I32]
     lib.gbt_test_withhold_tile_copies.argtypes = [P, I32]
+    lib.gbt_test_tile_capacity.argtypes = [P, I32]
     lib.gbt_test_tile_fallbacks.argtypes = [P, ctypes.POINTER(ctypes.c_int64)]
     lib.gbt_sync.argtypes = [P]
     lib.gbt_stream.argtypes = [P, ctypes.POINTER(P)]

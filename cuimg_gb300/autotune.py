@@ -17,8 +17,7 @@ from ._native import check, cuda_lib
 
 KNOBS = {
     # knob id: (name, settings, kernel names whose time decides)
-    0: ("matcher", (0, 1, 2, 3), ("k_match", "k_match_warp", "k_match_tiled", "k_mt_count", "k_mt_scan",
-                                  "k_mt_scatter")),
+    0: ("matcher", (0, 1, 2, 3), ("k_match", "k_match_warp", "k_match_tiled", "k_mt_list", "k_match_overflow")),
     1: ("blur_rows", (16, 32, 64), ("k_blur",)),
     2: ("match_tile", (0, 1, 2, 3, 4, 5, 6), ("k_match_tiled",)),
 }

@@ -78,7 +78,6 @@ struct Unit {
   // matcher tiles (k_match_tiled)
   int MTR, MTC;       // tiles per column / row
   int mt_base;        // first tile of this unit in the context-wide tile arrays
-  int mt_pbase;       // first slot of this unit in the context-wide per-particle bin keys
   // trajectories (k_traj; null until enabled): position k of slot j's history
   // ring at tpos[b][k * cap + j], next write at thead, length tlen
   short2* tpos[2];

@@ -94,9 +94,9 @@ struct Group {
   int* d_mt_prefix = nullptr;
   int* d_mt_cnt = nullptr;
   unsigned long long* d_mt_fallback = nullptr;  // particles the slim-margin tiled matcher finished from global memory
-  int* d_mt_off = nullptr;
-  int* d_mt_list = nullptr;
-  int2* d_mt_key = nullptr;  // per slot: (tile, rank in the tile) of the count pass
+  int* d_mt_list = nullptr;  // mt_tiles lists of MT_LIST_CAP slots (k_mt_list)
+  int2* d_mt_ovf = nullptr;  // (unit, slot) of the particles beyond a tile's list capacity
+  int mt_cap = MT_LIST_CAP;  // list capacity in use (test hook: smaller, to force the overflow path)
   int* d_post = nullptr;
   // bulk buffers cleared per frame
   void* occ_all = nullptr;
@@ -421,7 +421,6 @@ static int build(Group* ctx, const gbt_config* cfgs, int nstreams) {
     u.MTC = (u.W + MT_C - 1) / MT_C;
     u.mt_base = ctx->mt_tiles;
     ctx->mt_tiles += u.MTR * u.MTC;
-    u.mt_pbase = (int)ctx->mt_list_cap;
     ctx->mt_list_cap += u.cap;
     for (int b = 0; b < 2; b++) {
       if ((r = dalloc_t(ctx, &u.pos[b], u.cap))) return r;
@@ -450,9 +449,8 @@ static int build(Group* ctx, const gbt_config* cfgs, int nstreams) {
   if ((r = dalloc_t(ctx, &ctx->d_pre, nunits + 1))) return r;
   if ((r = dalloc_t(ctx, &ctx->d_mt_cnt, ctx->mt_tiles + 1))) return r;
   if ((r = dalloc_t(ctx, &ctx->d_mt_fallback, 1))) return r;
-  if ((r = dalloc_t(ctx, &ctx->d_mt_off, ctx->mt_tiles + 1))) return r;
-  if ((r = dalloc_t(ctx, &ctx->d_mt_list, ctx->mt_list_cap))) return r;
-  if ((r = dalloc_t(ctx, &ctx->d_mt_key, ctx->mt_list_cap))) return r;
+  if ((r = dalloc_t(ctx, &ctx->d_mt_list, (size_t)ctx->mt_tiles * MT_LIST_CAP, false))) return r;
+  if ((r = dalloc_t(ctx, &ctx->d_mt_ovf, ctx->mt_list_cap, false))) return r;
   if ((r = dalloc_t(ctx, &ctx->d_post, nunits + 1))) return r;
 
   // Static tables.
@@ -725,15 +723,17 @@ static int enqueue_back(Group* ctx, bool any_det, bool any_filt, int par, int& n
   n = 0;
   CK(cudaMemsetAsync(ctx->occ_all, 0, ctx->occ_bytes, st));
   if (ctx->match_variant == 0 && ctx->fixed_fpitch) {
-    CK(cudaMemsetAsync(ctx->d_mt_cnt, 0, (size_t)ctx->mt_tiles * sizeof(int), st));
-    { PROF("k_mt_count"); k_mt_bin<0><<<pgrid, CHUNK, 0, st>>>(du, ctx->d_state, ctx->d_pre, nunits, ctx->d_mt_cnt, ctx->d_mt_key, nullptr, nullptr); }
-    { PROF("k_mt_scan"); k_mt_scan<<<1, 1024, 0, st>>>(ctx->d_mt_cnt, ctx->mt_tiles, ctx->d_mt_off); }
-    { PROF("k_mt_scatter"); k_mt_bin<1><<<pgrid, CHUNK, 0, st>>>(du, ctx->d_state, ctx->d_pre, nunits, nullptr, ctx->d_mt_key, ctx->d_mt_off, ctx->d_mt_list); }
+    CK(cudaMemsetAsync(ctx->d_mt_cnt, 0, (size_t)(ctx->mt_tiles + 1) * sizeof(int), st));  // + the overflow count
+    {
+      PROF("k_mt_list");
+      k_mt_list<<<pgrid, CHUNK, 0, st>>>(du, ctx->d_state, ctx->d_pre, nunits, ctx->d_mt_cnt, ctx->mt_tiles,
+                                         ctx->mt_cap, ctx->d_mt_list, ctx->d_mt_ovf);
+    }
     const bool slim = ctx->mt_shape >= 4;
     const CUtensorMap* tm = ctx->d_tmaps ? ctx->d_tmaps + ((size_t)(slim ? 2 : 0) + par) * nunits * 2 : nullptr;
     int* err = &ctx->d_frame->err;
     unsigned long long* fb = ctx->d_mt_fallback;
-#define GBT_MT_ARGS du, ctx->d_state, ctx->d_frame, ctx->d_mt_prefix, nunits, ctx->d_mt_off, ctx->d_mt_list, tm, err, ctx->withhold_tiles, fb
+#define GBT_MT_ARGS du, ctx->d_state, ctx->d_frame, ctx->d_mt_prefix, nunits, ctx->d_mt_cnt, ctx->mt_cap, ctx->d_mt_list, tm, err, ctx->withhold_tiles, fb
     constexpr int FR = MT_MR, FC = MT_MC, SR_ = MT_MR_SLIM, SC_ = MT_MC_SLIM;
     {
     PROF("k_match_tiled");
@@ -748,7 +748,12 @@ static int enqueue_back(Group* ctx, bool any_det, bool any_filt, int par, int& n
     }
     }
 #undef GBT_MT_ARGS
-    n += 4;
+    {
+      PROF("k_match_overflow");
+      k_match_overflow<<<ctx->nsm, 256, 0, st>>>(du, ctx->d_state, ctx->d_frame, ctx->d_mt_cnt + ctx->mt_tiles,
+                                                  ctx->d_mt_ovf);
+    }
+    n += 3;
   } else if (ctx->match_variant == 1) {
     PROF("k_match_warp");
     k_match_warp<<<ctx->nsm * 4, 32 * MW_WARPS, 0, st>>>(du, ctx->d_state, ctx->d_frame, ctx->d_pre, nunits);
@@ -967,6 +972,13 @@ static int grp_test_withhold_tile_copies(Group* ctx, int32_t enable) {
     return set_err(ctx, GBT_E_INVALID, "the tiled matcher does not stage its tiles by TMA in this context");
   if (ctx->withhold_tiles != (enable != 0)) drop_graphs(ctx);
   ctx->withhold_tiles = enable != 0;
+  return GBT_OK;
+}
+
+static int grp_test_tile_capacity(Group* ctx, int32_t cap) {
+  if (!ctx || cap < 1 || cap > MT_LIST_CAP) return GBT_E_INVALID;
+  if (ctx->mt_cap != cap) drop_graphs(ctx);
+  ctx->mt_cap = cap;
   return GBT_OK;
 }
 
@@ -1777,6 +1789,16 @@ extern "C" int gbt_test_withhold_tile_copies(gbt_ctx* c, int32_t enable) {
   if (!c) return GBT_E_INVALID;
   for (Group* g : c->g) {
     int r = grp_test_withhold_tile_copies(g, enable);
+    if (r) return adopt(c, g, r);
+  }
+  return GBT_OK;
+}
+
+extern "C" int gbt_test_tile_capacity(gbt_ctx* c, int32_t cap) {
+  LK_NOT("gbt_test_tile_capacity");
+  if (!c) return GBT_E_INVALID;
+  for (Group* g : c->g) {
+    int r = grp_test_tile_capacity(g, cap);
     if (r) return adopt(c, g, r);
   }
   return GBT_OK;

@@ -636,7 +636,8 @@ __global__ void __launch_bounds__(MATCH_BLOCK) k_match(const Unit* __restrict__ 
 
 // ---------------------------------------------------------------------------
 // Tiled matcher.  Live particles are binned by their prediction into tiles of
-// MT_R x MT_C pixels (count, scan, scatter); one CTA per non-empty tile stages
+// MT_R x MT_C pixels (k_mt_list: fixed-capacity tile lists, the rare excess in
+// an overflow list matched from global memory); one CTA per non-empty tile stages
 // the tile's s1 / s2 neighbourhood in shared memory (TMA, or 16-byte cp.async
 // copies) and matches its particles from there.  A descent moves at most 10
 // pixels per step in each axis (two steps) and the BC2S taps reach 6 pixels
@@ -655,6 +656,10 @@ constexpr int MT_SR = MT_R + 2 * MT_MR;            // staged rows (116)
 constexpr int MT_SC = MT_C + 2 * MT_MC;            // staged columns (192), 16-byte chunks
 constexpr int MT_MR_SLIM = 14, MT_MC_SLIM = 16;    // slim staged margins: 92 rows x 160 columns
 constexpr int MT_THREADS = 256;
+// Particles a tile's list holds (k_mt_list); the rest of a fuller tile is
+// matched by k_match_overflow.  Steady-state 1080p video puts at most about
+// 640 particles in one tile (the oracle over 40 frames, any level).
+constexpr int MT_LIST_CAP = 1024;
 static_assert(MT_MR >= 2 * 10 + 6 && MT_MC >= 2 * 10 + 6, "full staged margins cover a full descent");
 static_assert(MT_MR_SLIM >= 7 && MT_MC_SLIM >= 7, "the prediction's own sweep is always staged");
 static_assert(MT_SC % 16 == 0 && MT_MC % 16 == 0 && MT_MC_SLIM % 16 == 0, "16-byte staging");
@@ -663,27 +668,24 @@ __device__ __forceinline__ int mt_tile(const Unit& u, int pr, int pc) {
   return u.mt_base + (pr / MT_R) * u.MTC + pc / MT_C;
 }
 
-// Pass 0 counts live particles per tile, remembering each particle's tile and
-// rank in it (and removes those predicted outside the domain, as the matcher
-// does); pass 1 places every binned slot at its tile's offset + rank.
-template <int PASS>
-__global__ void __launch_bounds__(CHUNK) k_mt_bin(const Unit* __restrict__ units, const UState* __restrict__ st,
-                                                  const int* __restrict__ table, int nunits, int* __restrict__ cnt,
-                                                  int2* __restrict__ key, const int* __restrict__ off,
-                                                  int* __restrict__ list) {
+// One pass bins the live particles by the tile of their prediction (and
+// removes those predicted outside the domain, as the matcher does): a
+// particle's rank in its tile comes from the tile's counter, and the particle
+// goes to slot rank of the tile's fixed-capacity list (tile t's list starts at
+// t * cap).  A particle ranked at or beyond cap goes to the overflow list
+// instead ((unit, slot) pairs, counted in cnt[ntiles]), which k_match_overflow
+// matches from global memory.  The order within a tile or the overflow list is
+// the order of the atomics; it changes no result (particles are independent).
+__global__ void __launch_bounds__(CHUNK) k_mt_list(const Unit* __restrict__ units, const UState* __restrict__ st,
+                                                   const int* __restrict__ table, int nunits, int* __restrict__ cnt,
+                                                   int ntiles, int cap, int* __restrict__ list,
+                                                   int2* __restrict__ ovf) {
   const int total = table[nunits];
   for (int g = blockIdx.x; g < total; g += gridDim.x) {
     ChunkCursor cc = chunk_of(table, nunits, g);
     const Unit& u = units[cc.unit];
     const UState s = st[cc.unit];
     const int i = cc.chunk * CHUNK + threadIdx.x;
-    int2* k = key + u.mt_pbase + i;
-    if (PASS == 1) {
-      if (i >= s.n) continue;
-      const int2 tr = *k;
-      if (tr.x >= 0) list[off[tr.x] + tr.y] = i;
-      continue;
-    }
     if ((i & ~31) >= s.n) continue;  // whole warp past the slots
     const int b = s.cur;
     int tile = -1;
@@ -700,51 +702,21 @@ __global__ void __launch_bounds__(CHUNK) k_mt_bin(const Unit* __restrict__ units
     }
     // Slots follow birth order, which is raster order within a detector
     // frame, so a warp's particles mostly share a few tiles: one atomic per
-    // distinct tile of the warp (ranks within a tile are in any order).
+    // distinct tile of the warp.
     const int lane = threadIdx.x & 31;
     const unsigned peers = __match_any_sync(0xffffffffu, tile);
     const int leader = __ffs(peers) - 1;
     int base = 0;
     if (tile >= 0 && lane == leader) base = atomicAdd(&cnt[tile], __popc(peers));
     base = __shfl_sync(0xffffffffu, base, leader);
-    if (i < s.n) *k = tile >= 0 ? make_int2(tile, base + __popc(peers & ((1u << lane) - 1u))) : make_int2(-1, 0);
-  }
-}
-
-// Exclusive scan of the tile counts into offsets (off[ntiles] = total): each
-// thread scans a contiguous run of counts, the block scans the run totals.
-__global__ void __launch_bounds__(1024) k_mt_scan(const int* __restrict__ cnt, int ntiles, int* __restrict__ off) {
-  __shared__ int wt[65];
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  const int per = (ntiles + 1023) / 1024, k0 = threadIdx.x * per, k1 = min(k0 + per, ntiles);
-  int run = 0;
-  for (int k = k0; k < k1; k++) run += cnt[k];
-  int x = run;
-#pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
-    const int y = __shfl_up_sync(0xffffffffu, x, o);
-    if (lane >= o) x += y;
-  }
-  if (lane == 31) wt[wid] = x;
-  __syncthreads();
-  if (wid == 0) {
-    const int w = wt[lane];
-    int z = w;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      const int y = __shfl_up_sync(0xffffffffu, z, o);
-      if (lane >= o) z += y;
+    if (tile >= 0) {
+      const int rank = base + __popc(peers & ((1u << lane) - 1u));
+      if (rank < cap)
+        list[(size_t)tile * cap + rank] = i;
+      else
+        ovf[atomicAdd(&cnt[ntiles], 1)] = make_int2(cc.unit, i);
     }
-    wt[32 + lane] = z - w;
-    if (lane == 31) wt[64] = z;
   }
-  __syncthreads();
-  int e = wt[32 + wid] + x - run;
-  for (int k = k0; k < k1; k++) {
-    off[k] = e;
-    e += cnt[k];
-  }
-  if (threadIdx.x == 0) off[ntiles] = wt[64];
 }
 
 __device__ __forceinline__ void cp_async16(void* sdst, const void* gsrc) {
@@ -877,7 +849,7 @@ __global__ void __launch_bounds__(THREADS, MINB) k_match_tiled(const Unit* __res
                                                                const UState* __restrict__ st,
                                                                const Frame* __restrict__ fr,
                                                                const int* __restrict__ tile_prefix, int nunits,
-                                                               const int* __restrict__ off,
+                                                               const int* __restrict__ cnt, int cap,
                                                                const int* __restrict__ list,
                                                                const CUtensorMap* __restrict__ tmaps,
                                                                int* __restrict__ err, int withhold,
@@ -890,7 +862,7 @@ __global__ void __launch_bounds__(THREADS, MINB) k_match_tiled(const Unit* __res
   __shared__ int next;
   __shared__ int tile_ok;
   const int t = blockIdx.x;
-  const int n0 = off[t], n1 = off[t + 1];
+  const int n0 = t * cap, n1 = n0 + min(cnt[t], cap);  // the tile's list (k_mt_list)
   if (n0 == n1) return;
   const int ui = find_unit(tile_prefix, nunits, t);
   const Unit& u = units[ui];
@@ -948,6 +920,28 @@ __global__ void __launch_bounds__(THREADS, MINB) k_match_tiled(const Unit* __res
       spd = u.spd[b][i];
       feat = u.feat[b][i];
     }
+  }
+}
+
+// The particles k_mt_list could not place in their tile's list (more than
+// `cap` in one tile), matched from the bordered images in global memory like
+// k_match; a thread per entry, any order (particles are independent).  The
+// list is usually empty and the CTAs return at once.
+__global__ void __launch_bounds__(256) k_match_overflow(const Unit* __restrict__ units, const UState* __restrict__ st,
+                                                        const Frame* __restrict__ fr, const int* __restrict__ nov,
+                                                        const int2* __restrict__ ovf) {
+  const int f = fr->f, n = *nov;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+    const int2 e = ovf[k];
+    const Unit& u = units[e.x];
+    const int b = st[e.x].cur, i = e.y;
+    const unsigned short age = u.age[b][i];
+    const short2 pos = u.pos[b][i];
+    int pr, pc;
+    predict(age, pos, u.spd[b][i], pr, pc);  // inside the domain: k_mt_list removed the others
+    FeatFP<FIXED_FPITCH> G;
+    G.init(u);
+    match_one(u, G, f, b, i, age, pos, pr, pc, u.feat[b][i]);
   }
 }
 

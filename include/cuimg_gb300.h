@@ -173,6 +173,13 @@ int gbt_sync(gbt_ctx* ctx);
  * by TMA (another matcher variant, or no tensor maps). */
 int gbt_test_withhold_tile_copies(gbt_ctx* ctx, int32_t enable);
 
+/* Test hook (no reference counterpart): the tiled matcher bins each frame's
+ * particles into a fixed-capacity list per 64 x 128 tile (1024 particles) and
+ * matches the particles beyond a full tile's capacity from global memory in a
+ * second kernel; this sets a smaller capacity (1 .. 1024) so that the
+ * overflow path carries most particles.  Results do not change. */
+int gbt_test_tile_capacity(gbt_ctx* ctx, int32_t cap);
+
 /* Test hook (no reference counterpart): the number of particles the tiled
  * matcher with slim margins (GBT_TUNE_MATCH_TILE 4..6) has matched again from
  * global memory because their descent would have left the staged tile, summed

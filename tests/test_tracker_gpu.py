@@ -47,11 +47,14 @@ def test_gpu_matches_reference_golden(case):
 
 
 def _compare_run(rows, cols, L, n, seed, detf=10, filtf=1, graphs=False, matcher=None, blur_rows=None,
-                 match_tile=None, frames=None, stats=None):
+                 match_tile=None, frames=None, stats=None, tile_cap=None):
     from cuimg_gb300 import synth
+    from cuimg_gb300._native import cuda_lib
     if frames is None:
         frames = synth.frames(seed, rows, cols, n)
     tr = _gpu_tracker(rows, cols, L, 20, detf, filtf, graphs)
+    if tile_cap is not None:
+        assert cuda_lib().gbt_test_tile_capacity(tr._ensure(), tile_cap) == 0
     if matcher is not None:
         tr.set_tuning(0, matcher)
     if blur_rows is not None:
@@ -161,6 +164,23 @@ def test_slim_tile_fallbacks_match_oracle(match_tile):
     assert _compare_run(rows, cols, L, n, 41, detf=2, matcher=0, match_tile=match_tile, frames=frames,
                         stats=stats) > 0
     assert stats["fallbacks"] > 0
+
+
+@pytest.mark.parametrize("tile_cap,graphs", [(1, False), (4, True), (64, False)])
+def test_tile_list_overflow_matches_oracle(tile_cap, graphs):
+    # Tile lists of 1, 4 or 64 particles: the particles beyond a tile's list
+    # are matched by the overflow kernel from global memory, bit-exactly.
+    assert _compare_run(480, 640, 3, 12, 7, detf=3, graphs=graphs, tile_cap=tile_cap) > 0
+
+
+def test_tile_capacity_hook_rejects_bad_values():
+    from cuimg_gb300._native import cuda_lib
+    tr = _gpu_tracker(120, 160, 3)
+    lib = cuda_lib()
+    assert lib.gbt_test_tile_capacity(tr._ensure(), 0) != 0
+    assert lib.gbt_test_tile_capacity(tr._ensure(), 1025) != 0
+    assert lib.gbt_test_tile_capacity(tr._ensure(), 1024) == 0
+    tr.close()
 
 
 @pytest.mark.parametrize("blur_rows", [16, 32, 64])
