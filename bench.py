@@ -858,8 +858,8 @@ def measure_combined_4k(dev, nf=300, every=10):
 # Each runs its kernels a few times on inputs larger than L2 but a few GB at
 # most on the device, so a capture of one or two launches ends quickly.
 
-def _case_gaussian(reps=3):
-    """8 fp32 1920x1080 images, sigma 4."""
+def _case_gaussian(reps=3, sigma=4.0):
+    """8 fp32 1920x1080 images, sigma 4 (or `sigma`)."""
     import torch
 
     from cuimg_gb300 import synth
@@ -870,7 +870,7 @@ def _case_gaussian(reps=3):
     y = torch.empty_like(x)
     for _ in range(reps):
         check(lib.gbt_gaussian_f32_batch(x.data_ptr(), COLS * 4, ROWS * COLS * 4, y.data_ptr(), COLS * 4,
-                                         ROWS * COLS * 4, ROWS, COLS, n, ctypes.c_float(4.0), None))
+                                         ROWS * COLS * 4, ROWS, COLS, n, ctypes.c_float(sigma), None))
     torch.cuda.synchronize()
 
 
@@ -956,6 +956,7 @@ def _case_steady(nstreams, det_freq, frames, lk=False, rows=ROWS, cols=COLS, nsc
 
 PROFILE_CASES = {
     "gaussian": _case_gaussian,
+    "gaussian_s2": lambda: _case_gaussian(sigma=2.0),
     "lk": _case_lk,
     "adjoint": _case_adjoint,
     "tracker": lambda: _case_tracker(4, 6, 10),        # 4 streams of 1920x1080, 6 frames
