@@ -1738,12 +1738,14 @@ __device__ __forceinline__ unsigned merge_dirs(const Unit& u, const UState& s, i
 // when it survives, finds its qualifying directions.  Actives are counted per
 // warp of 32 slots (act_cnt[i / 32]) and their candidates stored at their slot
 // (act_cand[8 i ..]) for k_merge_unit.
-// Quarter-chunk CTAs (256 threads) for the merge passes: their register
-// footprint allows six CTAs per SM, where 1024-thread CTAs get one.
+// Quarter-chunk CTAs (256 threads) for the merge passes, compiled for five
+// CTAs per SM (at most 48 registers a thread; with no bound the kernel takes
+// 60 and four fit): the pass waits on dependent global loads, so more
+// resident threads keep more of them in flight.
 constexpr int FM_THREADS = 256;
 constexpr int FM_SUB = CHUNK / FM_THREADS;
 
-__global__ void __launch_bounds__(FM_THREADS) k_filter_merge(const Unit* __restrict__ units,
+__global__ void __launch_bounds__(FM_THREADS, 5) k_filter_merge(const Unit* __restrict__ units,
                                                              const UState* __restrict__ st,
                                                              const Frame* __restrict__ fr,
                                                              const int* __restrict__ table, int nunits) {
