@@ -471,7 +471,7 @@ def bench_ours(args):
     # frames W0 .. W0 + steps - 1 from the host.  Host clock, max over ranks;
     # the median of the repeats (the host shares its cores with other work).
     nunits = B * NSCALES
-    E2E_REPEATS = 7
+    E2E_REPEATS = 15
 
     def timed_e2e(host_frames, pitch_bytes, location, pipelined):
         ptrs_ = (ctypes.c_void_p * B)()
