@@ -19,7 +19,7 @@ KNOBS = {
     # knob id: (name, settings, kernel names whose time decides)
     0: ("matcher", (0, 1, 2, 3), ("k_match", "k_match_warp", "k_match_tiled", "k_mt_list", "k_match_overflow")),
     1: ("blur_rows", (16, 32, 64), ("k_blur",)),
-    2: ("match_tile", (0, 1, 2, 3, 4, 5, 6), ("k_match_tiled",)),
+    2: ("match_tile", (0, 1, 2, 3, 4, 5, 6, 7), ("k_match_tiled",)),
 }
 DEFAULT_CACHE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "_build", "autotune.json")
 

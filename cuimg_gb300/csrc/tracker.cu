@@ -115,7 +115,7 @@ struct Group {
   int front_launches = 0;       // kernels in a captured front-end graph
   long long kernels_total = 0;  // kernels launched by this context, graph nodes included
   int match_variant = 0;  // GBT_TUNE_MATCHER
-  int mt_shape = 6;       // GBT_TUNE_MATCH_TILE: tiled matcher threads, particle assignment and margins
+  int mt_shape = 7;       // GBT_TUNE_MATCH_TILE: tiled matcher threads, particle assignment and margins
   int withhold_tiles = 0; // test hook: the tiled matcher's tile copies are not issued
   int fm_grid = 0;        // k_filter_merge CTAs: the ones all SMs hold at once
   // TMA descriptors of every unit's s1 and s2 for the tiled matcher, parity 0
@@ -744,6 +744,7 @@ static int enqueue_back(Group* ctx, bool any_det, bool any_filt, int par, int& n
       case 4: k_match_tiled<128, true, 7, SR_, SC_><<<ctx->mt_tiles, 128, 0, st>>>(GBT_MT_ARGS); break;
       case 5: k_match_tiled<256, true, 4, SR_, SC_><<<ctx->mt_tiles, 256, 0, st>>>(GBT_MT_ARGS); break;
       case 6: k_match_tiled<192, true, 5, SR_, SC_><<<ctx->mt_tiles, 192, 0, st>>>(GBT_MT_ARGS); break;
+      case 7: k_match_tiled<160, true, 6, SR_, SC_><<<ctx->mt_tiles, 160, 0, st>>>(GBT_MT_ARGS); break;
       default: k_match_tiled<MT_THREADS, false, 4, FR, FC><<<ctx->mt_tiles, MT_THREADS, 0, st>>>(GBT_MT_ARGS); break;
     }
     }
@@ -889,7 +890,7 @@ static int grp_set_tuning(Group* ctx, int32_t knob, int32_t value) {
     ctx->blur_tiles = ctx->blur_tiles_v[v];
     return GBT_OK;
   }
-  if (knob == GBT_TUNE_MATCH_TILE && value >= 0 && value <= 6) {
+  if (knob == GBT_TUNE_MATCH_TILE && value >= 0 && value <= 7) {
     if (ctx->mt_shape != value) drop_graphs(ctx);
     ctx->mt_shape = value;
     return GBT_OK;

@@ -181,7 +181,7 @@ int gbt_test_withhold_tile_copies(gbt_ctx* ctx, int32_t enable);
 int gbt_test_tile_capacity(gbt_ctx* ctx, int32_t cap);
 
 /* Test hook (no reference counterpart): the number of particles the tiled
- * matcher with slim margins (GBT_TUNE_MATCH_TILE 4..6) has matched again from
+ * matcher with slim margins (GBT_TUNE_MATCH_TILE 4..7) has matched again from
  * global memory because their descent would have left the staged tile, summed
  * over the context's frames so far; waits for queued work. */
 int gbt_test_tile_fallbacks(gbt_ctx* ctx, int64_t* count);
@@ -317,12 +317,13 @@ int gbt_checkpoint_load(gbt_ctx* ctx, const void* buf, size_t len);
  * 128 / 256 / 192 threads likewise, with the tile staged with slim margins (14
  * rows and 16 columns instead of 26 and 32, so more CTAs fit on an SM; the few
  * particles whose descent would leave the staged area are matched again from
- * global memory); 6 is the default.  The package's autotuner
+ * global memory); 7 = 160 threads likewise, compiled for six CTAs per SM (the
+ * same 30 warps as 6 in smaller CTAs), the default.  The package's autotuner
  * (cuimg_gb300/autotune.py) times the settings on the caller's workload and
  * caches the winner. */
 #define GBT_TUNE_MATCHER 0
 #define GBT_TUNE_BLUR_ROWS 1   /* rows per warp strip of the BC2S blur: 16, 32 or 64 */
-#define GBT_TUNE_MATCH_TILE 2  /* tiled matcher CTA shape and staged margins: 0..6 */
+#define GBT_TUNE_MATCH_TILE 2  /* tiled matcher CTA shape and staged margins: 0..7 */
 int gbt_set_tuning(gbt_ctx* ctx, int32_t knob, int32_t value);
 int gbt_get_tuning(gbt_ctx* ctx, int32_t knob, int32_t* value);
 

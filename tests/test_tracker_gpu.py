@@ -131,7 +131,7 @@ def test_matcher_variants_match_oracle(matcher):
     _compare_run(480, 640, 3, 14, 6, detf=5, matcher=matcher)
 
 
-@pytest.mark.parametrize("match_tile", range(7))
+@pytest.mark.parametrize("match_tile", range(8))
 def test_tile_shapes_match_oracle(match_tile):
     # Every CTA shape of the tiled matcher, with full (0..3) and slim (4..6)
     # staged margins.
@@ -154,7 +154,7 @@ def _jittered_frames(seed, rows, cols, n, amp):
     return out
 
 
-@pytest.mark.parametrize("match_tile", [4, 5, 6])
+@pytest.mark.parametrize("match_tile", [4, 5, 6, 7])
 def test_slim_tile_fallbacks_match_oracle(match_tile):
     # Long descents: the particles whose descent leaves the slim staged margins
     # are matched again from global memory, with the oracle's results.
