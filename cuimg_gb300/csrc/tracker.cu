@@ -90,7 +90,7 @@ struct Group {
   int* d_pre = nullptr;
   // tiled matcher: tiles over all units, per-tile counts / offsets, binned slots
   int mt_tiles = 0;
-  long long mt_list_cap = 0;
+  long long mt_list_cap = 0;  // particle slots of all units: the overflow list never needs more
   int* d_mt_prefix = nullptr;
   int* d_mt_cnt = nullptr;
   unsigned long long* d_mt_fallback = nullptr;  // particles the slim-margin tiled matcher finished from global memory
