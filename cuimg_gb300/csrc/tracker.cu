@@ -88,7 +88,7 @@ struct Group {
   int* d_btable = nullptr;
   // dynamic chunk tables
   int* d_pre = nullptr;
-  // tiled matcher: tiles over all units, per-tile counts / offsets, binned slots
+  // tiled matcher: tiles over all units, per-tile counts (then the overflow count), tile lists
   int mt_tiles = 0;
   long long mt_list_cap = 0;  // particle slots of all units: the overflow list never needs more
   int* d_mt_prefix = nullptr;
