@@ -571,12 +571,13 @@ __device__ __forceinline__ int block_scan(int v, int* wsum, int* total) {
 // Births in raster order (particle_container::add, particle_container.hpp:
 // 370-387) and the stable compaction (compact(cpu), :215-252), then the
 // sparse index of the survivors (the last survivor at a pixel wins).  One CTA
-// per detector unit.
+// per unit; the CTAs of units that do not detect in frame f return at once.
 __global__ void __launch_bounds__(SCAN_T) k_pk_births_compact(PUnit* __restrict__ units, PState* __restrict__ st,
-                                                               const int* __restrict__ det_units, int* __restrict__ err) {
+                                                               int f, int* __restrict__ err) {
   __shared__ int wsum[32];
-  const int ui = det_units[blockIdx.x];
+  const int ui = blockIdx.x;
   const PUnit& u = units[ui];
+  if (!det_frame(u, f)) return;  // uniform per CTA
   PState s = st[ui];
   const int b = s.cur, nitems = 3 * u.TH * u.TW;
   int nb = 0, total;
@@ -664,12 +665,13 @@ __global__ void k_pk_merge_cand(PUnit* __restrict__ units, const PState* __restr
 }
 
 // Step 2: one warp per unit replays the slots with candidates in slot order
-// with the current ages, as the reference's loop does.
-__global__ void k_pk_merge_replay(PUnit* __restrict__ units, const PState* __restrict__ st,
-                                  const int* __restrict__ merge_units) {
+// with the current ages, as the reference's loop does (the warps of units that
+// do not merge in frame f return at once).
+__global__ void k_pk_merge_replay(PUnit* __restrict__ units, const PState* __restrict__ st, int f) {
   constexpr int C8R[8] = {-1, 0, 1, -1, 1, -1, 0, 1}, C8C[8] = {1, 1, 1, 0, 0, -1, -1, -1};
-  const int ui = merge_units[blockIdx.x];
+  const int ui = blockIdx.x;
   const PUnit& u = units[ui];
+  if (!merge_frame(u, f)) return;
   const PState s = st[ui];
   const int b = s.cur, lane = threadIdx.x & 31;
   for (int base = 0; base < s.n; base += 32) {
@@ -731,8 +733,6 @@ struct PkTracker {
   int* d_prefix = nullptr;
   int* d_err = nullptr;
   int* d_scale_units = nullptr;  // per scale: the unit of every stream (-1 when the stream has fewer scales)
-  int* d_det_units = nullptr;    // this frame's detector units
-  int* d_merge_units = nullptr;  // this frame's merge units
   int maxL = 0;
   int frame = 0;
   int64_t launches = 0;
@@ -857,8 +857,7 @@ int pk_create(const gbt_config* cfgs, int nstreams, int device, PkTracker** out,
     for (int l = 0; l < t->streams[s].cfg.nscales; l++) su[(size_t)l * nstreams + s] = t->streams[s].unit0 + l;
   if ((r = pk_alloc(t, &t->d_units, (size_t)nu)) || (r = pk_alloc(t, &t->d_state, (size_t)nu)) ||
       (r = pk_alloc(t, &t->d_prefix, (size_t)nu + 1)) || (r = pk_alloc(t, &t->d_err, 1)) ||
-      (r = pk_alloc(t, &t->d_scale_units, su.size())) || (r = pk_alloc(t, &t->d_det_units, (size_t)nu)) ||
-      (r = pk_alloc(t, &t->d_merge_units, (size_t)nu)))
+      (r = pk_alloc(t, &t->d_scale_units, su.size())))
     return fail(r);
   if (cudaMemcpy(t->d_scale_units, su.data(), su.size() * sizeof(int), cudaMemcpyHostToDevice) != cudaSuccess ||
       (r = pk_upload_units(t)))
@@ -896,17 +895,15 @@ int pk_run(PkTracker* t, const uint8_t* const* frames, const int64_t* pitches, i
       PCK(cudaMemcpy2DAsync(u.lvl, u.W, frames[s], pitches[s], u.W, u.H, cudaMemcpyDeviceToDevice, t->stream));
     }
   }
-  // Which units detect / merge this frame.
-  std::vector<int> det, mer;
+  // Whether any unit detects / merges this frame (each kernel's CTAs check
+  // their own unit, so no per-frame list goes to the device and the host
+  // queues frames without waiting for the GPU).
+  bool any_det = false, any_mer = false;
   for (int i = 0; i < nu; i++) {
     const PUnit& u = t->units[i];
-    if (f % u.det_freq == 0) det.push_back(i);
-    if (f % u.filt_freq == 0 && u.with_merge) mer.push_back(i);
+    any_det |= f % u.det_freq == 0;
+    any_mer |= f % u.filt_freq == 0 && u.with_merge;
   }
-  if (!det.empty())
-    PCK(cudaMemcpyAsync(t->d_det_units, det.data(), det.size() * sizeof(int), cudaMemcpyHostToDevice, t->stream));
-  if (!mer.empty())
-    PCK(cudaMemcpyAsync(t->d_merge_units, mer.data(), mer.size() * sizeof(int), cudaMemcpyHostToDevice, t->stream));
   int maxpx = 0;
   for (const PUnit& u : t->units) maxpx = std::max(maxpx, (u.H + 2 * MB) * u.mpitch);
   const int pxblocks = std::min(1024, std::max(1, (maxpx + 255) / 256));
@@ -924,22 +921,20 @@ int pk_run(PkTracker* t, const uint8_t* const* frames, const int64_t* pitches, i
     k_pk_match<<<t->nsm * 6, 32 * MW, 0, t->stream>>>(t->d_units, t->d_state, nu, t->d_prefix, par);
     launches += 2;
   }
-  if (!det.empty()) {
+  if (any_det) {
     k_pk_mask<<<slot_grid, 256, 0, t->stream>>>(t->d_units, t->d_state, nu, t->d_prefix, f);
     k_pk_saliency<<<dim3(pxblocks, nu), 256, 0, t->stream>>>(t->d_units, nu, f, par);
     k_pk_nms<<<dim3(pxblocks, nu), 256, 0, t->stream>>>(t->d_units, nu, f);
-    k_pk_births_compact<<<(unsigned)det.size(), SCAN_T, 0, t->stream>>>(t->d_units, t->d_state, t->d_det_units,
-                                                                        t->d_err);
+    k_pk_births_compact<<<nu, SCAN_T, 0, t->stream>>>(t->d_units, t->d_state, f, t->d_err);
     k_pk_prefix<<<1, 32, 0, t->stream>>>(t->d_state, nu, t->d_prefix);
     launches += 5;
   }
-  if (!mer.empty()) {
+  if (any_mer) {
     k_pk_merge_cand<<<slot_grid, 256, 0, t->stream>>>(t->d_units, t->d_state, nu, t->d_prefix, f);
-    k_pk_merge_replay<<<(unsigned)mer.size(), 32, 0, t->stream>>>(t->d_units, t->d_state, t->d_merge_units);
+    k_pk_merge_replay<<<nu, 32, 0, t->stream>>>(t->d_units, t->d_state, f);
     launches += 2;
   }
   PCK(cudaGetLastError());
-  if (!det.empty() || !mer.empty()) PCK(cudaStreamSynchronize(t->stream));  // the unit lists are host vectors
   t->frame++;
   t->launches += launches;
   t->last_launches = launches;
